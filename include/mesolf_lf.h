@@ -1,0 +1,136 @@
+/*
+ * mesolf_lf.h -- C ABI of libmesolf_lf.so, the GB300 (sm_103a) light-field projector and
+ * phase-space Richardson-Lucy deconvolver.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (MLF_OK == 0) and never aborts the
+ *     process; mlf_last_error() returns the calling thread's last message.
+ *   - Arrays use MATLAB's column-major layout and dimension order, so a MEX shim passes
+ *     mxGetData()/mxGPUGetData() pointers straight through.
+ *   - "dev" pointers must be device memory of the current CUDA device; "any" pointers may
+ *     be device or host memory (detected with cudaPointerGetAttributes; host buffers are
+ *     staged through the library's own device buffers).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).  Calls are
+ *     stream-ordered; functions documented "synchronous" synchronise the stream before
+ *     returning, as the reference MEX does.
+ *   - An mlf_psf may be shared read-only by many solvers; an mlf_solver is used by one
+ *     host thread / stream at a time.
+ */
+#ifndef MESOLF_LF_H
+#define MESOLF_LF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MLF_ABI_VERSION 1
+
+enum mlf_status_code {
+  MLF_OK = 0,
+  MLF_ERR_INVALID = 1,     /* bad argument: shape, size, null pointer, unsupported Nnum */
+  MLF_ERR_CUDA = 2,        /* a CUDA runtime call failed (message holds cudaGetErrorString) */
+  MLF_ERR_NOMEM = 3,       /* device allocation failed / admission refused for lack of HBM */
+  MLF_ERR_UNSUPPORTED = 4, /* valid input outside what this build implements */
+  MLF_ERR_TIMEOUT = 5,     /* a bounded wait expired (device status flag) */
+  MLF_ERR_CANCELLED = 6    /* request cancelled by the caller */
+};
+
+enum mlf_precision {
+  MLF_PREC_FP32 = 0,       /* plain FP32 FMA projector (the drop-in path) */
+  MLF_PREC_BF16X3 = 1,     /* tensor-core BF16 split hi+lo operands, FP32 accumulate */
+  MLF_PREC_BF16 = 2        /* tensor-core single BF16 operands, FP32 accumulate */
+};
+
+typedef struct mlf_psf mlf_psf;       /* phase-space PSF resident in HBM */
+typedef struct mlf_solver mlf_solver; /* per-image-size solve context (scratch in HBM) */
+
+typedef struct mlf_stats {
+  int32_t n_views;          /* active views per iteration (weight != 0) */
+  int32_t iterations;       /* iterations run */
+  double gpu_ms;            /* device time of the solve (CUDA events) */
+  double view_ms;           /* mean device time of one view step */
+  double filter_ms;         /* device time of the per-iteration sample filter */
+  int64_t kernel_launches;  /* kernels launched by the solve */
+} mlf_stats;
+
+/* Library / ABI version (MLF_ABI_VERSION). */
+int mlf_version(void);
+
+/* Copy the calling thread's last error message into buf (always NUL-terminated).
+ * Returns the status code of that error. */
+int mlf_last_error(char* buf, size_t len);
+
+/* ---------------------------------------------------------------------------------
+ * MEX projector.  Replaces mexFunction of src/cuda/mex_lfm_convolution_vec.cu:276-421
+ * (kernel semantics :43-266):
+ *   out(x,y,i) = sum_{kx,ky < kw} bitmap(x+kx-kw/2, y+ky-kw/2, i) * kernels(kx,ky,x%nnum,y%nnum)
+ * zero outside the bitmap (the reference's edge clipping, :55-78).
+ *   bitmap  : any, float32, W x H x n (column-major; W = MATLAB dims[0])
+ *   kernels : any, float32, kw x kw x nnum x nnum
+ *   out     : any, float32, W x H x n (fully written; the reference zero-initialises it)
+ * Limits as the reference: 1 <= kw <= 341 (:41,344), n >= 1 (:332), nnum == 15 (:35).
+ * Synchronous (the reference calls cudaDeviceSynchronize, :406). */
+int mlf_conv_vec(const float* bitmap, int64_t W, int64_t H, int64_t n,
+                 const float* kernels, int64_t kw, int32_t nnum, float* out, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Phase-space PSF.  Replaces recon_theory_phase_space_LFM_with_filter.m:13-40 and
+ * gen_phasespace_PSF_theory.m:1-31: per-depth FP64 normalisation of H and Ht, the
+ * phase-space realignment of H, the crop of Ht, and the view weights (weight_cut 0.2,
+ * scale 0.3).  H, Ht: any, float32, K0 x K0 x N x N x Z (MATLAB layout); K0 odd.
+ * The result owns its HBM (per-view projector taps for every view). */
+int mlf_psf_create(const float* H, const float* Ht, int64_t K0, int32_t N, int64_t Z,
+                   mlf_psf** out, void* stream);
+int mlf_psf_destroy(mlf_psf* psf);
+/* Shape queries: N, Z, phase-space PSF side S. */
+int mlf_psf_info(const mlf_psf* psf, int32_t* N, int64_t* Z, int64_t* S);
+/* View weights (N x N, column-major, FP64) exactly as the solver uses them. */
+int mlf_psf_weights(const mlf_psf* psf, double* w_host);
+/* Bytes of HBM the PSF holds. */
+int64_t mlf_psf_device_bytes(const mlf_psf* psf);
+
+/* ---------------------------------------------------------------------------------
+ * RL solve.  Replaces recon_theory_phase_space_LFM_with_filter(LFIMG, H, Ht, maxIter,
+ * gpuFlag, gpu_id) (recon_theory_phase_space_LFM_with_filter.m:10-151): flat initial
+ * guess sum(LFIMG)/numel, views in spiral order skipping zero weights, per view
+ * forward projection -> ratio -> back projection -> multiplicative update -> blend,
+ * and the flux-preserving NIP low-pass (sample_filter) after each iteration.
+ *
+ * mlf_solver_create sizes a context for Xr x Xc images (Xr, Xc multiples of N).
+ *   lfimg      : any, float32, Xr x Xc
+ *   warm_start : any or NULL, float32, Xr x Xc x Z (replaces the flat initial guess)
+ *   vol_out    : any, float32, Xr x Xc x Z
+ *   precision  : enum mlf_precision
+ *   stats      : host, may be NULL
+ * Synchronous when any pointer is host memory or stats != NULL. */
+int mlf_solver_create(mlf_psf* psf, int64_t Xr, int64_t Xc, mlf_solver** out);
+int mlf_solver_destroy(mlf_solver* s);
+int64_t mlf_solver_device_bytes(const mlf_solver* s);
+int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t precision,
+                   const float* warm_start, float* vol_out, mlf_stats* stats, void* stream);
+
+/* One-shot form with the reference's argument order (H, Ht raw PSFs).  Builds the PSF
+ * and a solver, runs, frees.  Synchronous. */
+int mlf_rl_solve(const float* lfimg, int64_t Xr, int64_t Xc, const float* H, const float* Ht,
+                 int64_t K0, int32_t N, int64_t Z, int32_t max_iter, int32_t precision,
+                 float* vol_out, mlf_stats* stats, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Building blocks of one RL view, exposed for parity tests and for callers that drive
+ * the view loop themselves.  (u, v) are 0-based view indices; volumes are Xr x Xc x Z
+ * float32 device arrays in MATLAB layout.
+ *
+ * Forward projection of one view: recon_…_with_filter.m:243-249
+ *   hx (dev, Xr/N x Xc/N) = (sum_z conv2(vol_z, Hps(:,:,u,v,z), 'same'))((N+1)/2:N:end, ...) */
+int mlf_forward_view(mlf_solver* s, const float* vol, int32_t u, int32_t v, float* hx, void* stream);
+/* Back projection of one view: recon_…_with_filter.m:211-220
+ *   out (dev, Xr x Xc x Z): out_z = conv2(B, Ht(:,:,u,v,z), 'same'), B(u:N:end, v:N:end) = proj */
+int mlf_backward_view(mlf_solver* s, const float* proj, int32_t u, int32_t v, float* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MESOLF_LF_H */

@@ -1,0 +1,225 @@
+"""Host-side mirror of the reference's call interface for the projector / RL path.
+
+* :func:`mex_lfm_convolution_vec` -- ``out = mex_lfm_convolution_vec(bitmap, kernels)``
+  (``src/cuda/mex_lfm_convolution_vec.cu:276-421``).
+* :func:`recon_theory_phase_space_LFM_with_filter` --
+  ``Xguess = recon_theory_phase_space_LFM_with_filter(LFIMG, H, Ht, maxIter, gpuFlag, gpu_id)``
+  (``src/recon/recon_theory_phase_space_LFM_with_filter.m:10``).
+* :class:`PhaseSpacePSF` / :class:`RLSolver` -- the same solve split into a resident PSF
+  and a reusable per-image-size context (what a serving loop keeps in HBM).
+
+Arrays are indexed in MATLAB order (``bitmap[x, y, i]``, ``H[x, y, a, b, z]``,
+``vol[r, c, z]``).  numpy arrays are host memory; torch CUDA tensors are device memory
+(any strides; they are made column-major).  Every call goes through libmesolf_lf.so:
+there is no CPU fallback, and a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import MLFStats, check
+
+PRECISIONS = {"fp32": _lib.MLF_PREC_FP32, "bf16x3": _lib.MLF_PREC_BF16X3, "bf16": _lib.MLF_PREC_BF16}
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+def _fortran(x):
+    """(keepalive, pointer) of x as float32 column-major memory."""
+    if _is_torch(x):
+        import torch
+        t = x.to(torch.float32)
+        rev = tuple(range(t.dim() - 1, -1, -1))
+        want = []
+        s = 1
+        for d in t.shape:
+            want.append(s)
+            s *= d
+        if list(t.stride()) != want:
+            t = t.permute(rev).contiguous().permute(rev)
+        return t, t.data_ptr()
+    a = np.asfortranarray(np.asarray(x, dtype=np.float32))
+    return a, a.ctypes.data
+
+
+def _empty_like_kind(ref, shape):
+    if _is_torch(ref):
+        import torch
+        rev = tuple(range(len(shape) - 1, -1, -1))
+        t = torch.empty(tuple(reversed(shape)), dtype=torch.float32, device=ref.device).permute(rev)
+        return t, t.data_ptr()
+    a = np.empty(shape, dtype=np.float32, order="F")
+    return a, a.ctypes.data
+
+
+def _stream_of(x, stream):
+    if stream is not None:
+        return ctypes.c_void_p(int(stream))
+    if _is_torch(x) and x.is_cuda:
+        import torch
+        return ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
+    return ctypes.c_void_p(0)
+
+
+def mex_lfm_convolution_vec(bitmap, kernels, stream=None):
+    """Drop-in for the MEX projector.
+
+    bitmap: (W, H) or (W, H, n) float32; kernels: (kw, kw, 15, 15) float32.  Returns an
+    array of the bitmap's shape, in the bitmap's memory kind.  Input checks follow
+    ``mex_lfm_convolution_vec.cu:305-355`` and raise ``MesoLFError`` like its
+    ``mexErrMsgIdAndTxt``.
+    """
+    lib = _lib.load()
+    shp = tuple(bitmap.shape)
+    if len(shp) not in (2, 3):
+        raise _lib.MesoLFError(_lib.MLF_ERR_INVALID, "Invalid input to mex_lfm_convolution_vec()")
+    if len(kernels.shape) != 4:
+        raise _lib.MesoLFError(_lib.MLF_ERR_INVALID, "Invalid input to mex_lfm_convolution_vec()")
+    W, Hh = shp[0], shp[1]
+    n = shp[2] if len(shp) == 3 else 1
+    kw = kernels.shape[0]
+    b_keep, bp = _fortran(bitmap)
+    k_keep, kp = _fortran(kernels)
+    out, op = _empty_like_kind(bitmap, shp)
+    check(lib.mlf_conv_vec(bp, W, Hh, n, kp, kw, int(kernels.shape[2]), op, _stream_of(bitmap, stream)))
+    del b_keep, k_keep
+    return out
+
+
+class PhaseSpacePSF:
+    """Normalised phase-space PSF resident in HBM (``…_with_filter.m:13-40``)."""
+
+    def __init__(self, H, Ht, stream=None):
+        lib = _lib.load()
+        if tuple(H.shape) != tuple(Ht.shape) or len(H.shape) != 5:
+            raise _lib.MesoLFError(_lib.MLF_ERR_INVALID, "H and Ht must both be K0 x K0 x N x N x Z")
+        K0, _, N, _, Z = H.shape
+        hk, hp = _fortran(H)
+        tk, tp = _fortran(Ht)
+        h = ctypes.c_void_p()
+        check(lib.mlf_psf_create(hp, tp, K0, N, Z, ctypes.byref(h), _stream_of(H, stream)))
+        self._h = h
+        self.K0, self.N, self.Z = int(K0), int(N), int(Z)
+        n = ctypes.c_int32()
+        z = ctypes.c_int64()
+        s = ctypes.c_int64()
+        check(lib.mlf_psf_info(h, ctypes.byref(n), ctypes.byref(z), ctypes.byref(s)))
+        self.S = int(s.value)
+        w = np.zeros((N, N), dtype=np.float64, order="F")
+        check(lib.mlf_psf_weights(h, w.ctypes.data))
+        self.weights = w
+        del hk, tk
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def device_bytes(self):
+        return int(_lib.load().mlf_psf_device_bytes(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().mlf_psf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RLSolver:
+    """Solve context for one image size (scratch volume, sub-aperture images, graphs)."""
+
+    def __init__(self, psf: PhaseSpacePSF, image_shape):
+        lib = _lib.load()
+        self.psf = psf
+        self.Xr, self.Xc = int(image_shape[0]), int(image_shape[1])
+        h = ctypes.c_void_p()
+        check(lib.mlf_solver_create(psf.handle, self.Xr, self.Xc, ctypes.byref(h)))
+        self._h = h
+        self.last_stats = None
+
+    @property
+    def device_bytes(self):
+        return int(_lib.load().mlf_solver_device_bytes(self._h))
+
+    def run(self, lfimg, max_iter, precision="fp32", warm_start=None, out=None, stream=None,
+            want_stats=True):
+        """Run ``max_iter`` RL iterations; returns the (Xr, Xc, Z) volume."""
+        lib = _lib.load()
+        lk, lp = _fortran(lfimg)
+        wk, wp = (None, None) if warm_start is None else _fortran(warm_start)
+        shape = (self.Xr, self.Xc, self.psf.Z)
+        if out is None:
+            out, op = _empty_like_kind(lfimg, shape)
+        else:
+            op = out.data_ptr() if _is_torch(out) else out.ctypes.data
+        st = MLFStats()
+        check(lib.mlf_solver_run(self._h, lp, int(max_iter), PRECISIONS[precision], wp, op,
+                                 ctypes.byref(st) if want_stats else None, _stream_of(lfimg, stream)))
+        self.last_stats = st.as_dict() if want_stats else None
+        del lk, wk
+        return out
+
+    def forward_view(self, vol, u, v, stream=None):
+        """HX of view (u, v) (0-based) for a device volume -> (Xr/N, Xc/N) device array."""
+        import torch
+        vk, vp = _fortran(vol)
+        hx = torch.empty((self.Xc // self.psf.N, self.Xr // self.psf.N), dtype=torch.float32,
+                         device=vol.device).t()
+        check(_lib.load().mlf_forward_view(self._h, vp, int(u), int(v), hx.data_ptr(), _stream_of(vol, stream)))
+        del vk
+        return hx
+
+    def backward_view(self, proj, u, v, stream=None):
+        """Back projection of a (Xr/N, Xc/N) device array for view (u, v) -> (Xr, Xc, Z)."""
+        pk, pp = _fortran(proj)
+        out, op = _empty_like_kind(proj, (self.Xr, self.Xc, self.psf.Z))
+        check(_lib.load().mlf_backward_view(self._h, pp, int(u), int(v), op, _stream_of(proj, stream)))
+        del pk
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().mlf_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def recon_theory_phase_space_LFM_with_filter(LFIMG, H, Ht, maxIter, gpuFlag=True, gpu_id=1,
+                                             precision="fp32"):
+    """Same arguments as the reference solver; returns the volume as a host float64
+    array (the reference returns ``gather(Xguess)`` in double).  ``gpuFlag`` must be
+    true: this library has no CPU branch."""
+    if not gpuFlag:
+        raise _lib.MesoLFError(_lib.MLF_ERR_UNSUPPORTED,
+                               "gpuFlag=false: libmesolf_lf.so implements only the GPU path")
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(gpu_id) - 1)
+    except ImportError:
+        pass
+    psf = PhaseSpacePSF(H, Ht)
+    try:
+        solver = RLSolver(psf, LFIMG.shape)
+        try:
+            vol = solver.run(np.asarray(LFIMG), maxIter, precision=precision)
+        finally:
+            solver.close()
+    finally:
+        psf.close()
+    return np.asarray(vol, dtype=np.float64)

@@ -1,0 +1,286 @@
+// extern "C" entry points of libmesolf_lf.so (declared in include/mesolf_lf.h).
+//
+// Argument validation mirrors the reference's own checks (the MEX at
+// src/cuda/mex_lfm_convolution_vec.cu:301-355 and the shape assumptions of
+// recon_theory_phase_space_LFM_with_filter.m); failures return a status code and set a
+// per-thread message instead of aborting.  Pointers may be device or host memory: host
+// arrays are staged through device buffers owned by the call or the solver.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+namespace {
+thread_local int g_code = MLF_OK;
+thread_local std::string g_msg;
+}  // namespace
+
+int fail(int code, const std::string& msg) {
+  g_code = code;
+  g_msg = msg;
+  return code;
+}
+
+void clear_error() {
+  g_code = MLF_OK;
+  g_msg.clear();
+}
+
+int DevBuf::alloc(size_t n, const char* what) {
+  release();
+  if (n == 0) n = 16;
+  cudaError_t e = cudaMalloc(&p, n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    p = nullptr;
+    return fail(MLF_ERR_NOMEM, std::string("cudaMalloc(") + std::to_string(n) + " B) for " + what +
+                                   ": " + cudaGetErrorString(e));
+  }
+  bytes = n;
+  return MLF_OK;
+}
+
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+bool is_device_ptr(const void* ptr) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace mlf
+
+using namespace mlf;
+
+struct mlf_psf : public mlf::Psf {};
+struct mlf_solver : public mlf::Solver {};
+
+namespace {
+
+// Device view of an "any" input array: the pointer itself, or a staged copy.
+int stage_in(const float* p, size_t n, DevBuf& tmp, const float** dev, cudaStream_t st) {
+  if (p == nullptr) {
+    *dev = nullptr;
+    return MLF_OK;
+  }
+  if (is_device_ptr(p)) {
+    *dev = p;
+    return MLF_OK;
+  }
+  if (tmp.bytes < n * sizeof(float)) MLF_TRY(tmp.alloc(n * sizeof(float), "input staging"));
+  MLF_CUDA(cudaMemcpyAsync(tmp.p, p, n * sizeof(float), cudaMemcpyHostToDevice, st));
+  *dev = tmp.as<float>();
+  return MLF_OK;
+}
+
+struct OutStage {
+  float* user = nullptr;
+  float* dev = nullptr;
+  size_t n = 0;
+  bool host = false;
+};
+
+int stage_out(float* p, size_t n, DevBuf& tmp, OutStage* o) {
+  o->user = p;
+  o->n = n;
+  o->host = !is_device_ptr(p);
+  if (!o->host) {
+    o->dev = p;
+    return MLF_OK;
+  }
+  if (tmp.bytes < n * sizeof(float)) MLF_TRY(tmp.alloc(n * sizeof(float), "output staging"));
+  o->dev = tmp.as<float>();
+  return MLF_OK;
+}
+
+int finish_out(const OutStage& o, cudaStream_t st) {
+  if (o.host) MLF_CUDA(cudaMemcpyAsync(o.user, o.dev, o.n * sizeof(float), cudaMemcpyDeviceToHost, st));
+  return MLF_OK;
+}
+
+int current_device(int* dev) {
+  MLF_CUDA(cudaGetDevice(dev));
+  return MLF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mlf_version(void) { return MLF_ABI_VERSION; }
+
+int mlf_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    std::strncpy(buf, g_msg.c_str(), len - 1);
+    buf[len - 1] = '\0';
+  }
+  return g_code;
+}
+
+int mlf_conv_vec(const float* bitmap, int64_t W, int64_t H, int64_t n, const float* kernels,
+                 int64_t kw, int32_t nnum, float* out, void* stream) {
+  clear_error();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // src/cuda/mex_lfm_convolution_vec.cu:313-347 -- 2-D/3-D single bitmap, n >= 1,
+  // 4-D single kernels with kw <= 341; the kernel count per axis is fixed at 15 (:35).
+  if (!bitmap || !kernels || !out) return fail(MLF_ERR_INVALID, "Invalid input to mex_lfm_convolution_vec(): null pointer");
+  if (W < 1 || H < 1) return fail(MLF_ERR_INVALID, "Invalid input to mex_lfm_convolution_vec(): empty bitmap");
+  if (n < 1) return fail(MLF_ERR_INVALID, "Invalid input to mex_lfm_convolution_vec(): bitmap_n has to be at least 1");
+  if (kw < 1 || kw > 341) return fail(MLF_ERR_INVALID, "Invalid input to mex_lfm_convolution_vec(): kernel_width exceeds kernel_width_limit=341");
+  if (nnum != 15) return fail(MLF_ERR_INVALID, "Invalid input to mex_lfm_convolution_vec(): the kernel grid must be 15 x 15");
+  if (W * H * n > ((int64_t)1 << 40)) return fail(MLF_ERR_INVALID, "bitmap too large");
+  DevBuf bin, kin, bout;
+  const float *db = nullptr, *dk = nullptr;
+  MLF_TRY(stage_in(bitmap, (size_t)(W * H * n), bin, &db, st));
+  MLF_TRY(stage_in(kernels, (size_t)(kw * kw * nnum * nnum), kin, &dk, st));
+  OutStage o;
+  MLF_TRY(stage_out(out, (size_t)(W * H * n), bout, &o));
+  MLF_TRY(conv_vec_run(db, W, H, n, dk, kw, nnum, o.dev, st));
+  MLF_TRY(finish_out(o, st));
+  MLF_CUDA(cudaStreamSynchronize(st));
+  return MLF_OK;
+}
+
+int mlf_psf_create(const float* H, const float* Ht, int64_t K0, int32_t N, int64_t Z, mlf_psf** out,
+                   void* stream) {
+  clear_error();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!H || !Ht || !out) return fail(MLF_ERR_INVALID, "mlf_psf_create: null pointer");
+  *out = nullptr;
+  if (N < 3 || N % 2 == 0) return fail(MLF_ERR_INVALID, "mlf_psf_create: Nnum must be odd and >= 3");
+  if (K0 < N || K0 % 2 == 0) return fail(MLF_ERR_INVALID, "mlf_psf_create: PSF side K0 must be odd and >= Nnum");
+  if (Z < 1) return fail(MLF_ERR_INVALID, "mlf_psf_create: need at least one depth plane");
+  const int64_t S = K0 - ((K0 - N) % (2 * N));
+  const int64_t T = S / N;
+  if (!view_taps_supported((int)T))
+    return fail(MLF_ERR_UNSUPPORTED, "mlf_psf_create: phase-space PSF side S = " + std::to_string(S) +
+                                         " gives S/N = " + std::to_string(T) + " (supported: 3..17, odd)");
+  std::unique_ptr<mlf_psf> p(new mlf_psf());
+  MLF_TRY(current_device(&p->device));
+  p->N = N;
+  p->Z = (int)Z;
+  p->K0 = (int)K0;
+  const size_t nel = (size_t)K0 * K0 * N * N * Z;
+  DevBuf sh, sht;
+  const float *dH = nullptr, *dHt = nullptr;
+  MLF_TRY(stage_in(H, nel, sh, &dH, st));
+  MLF_TRY(stage_in(Ht, nel, sht, &dHt, st));
+  MLF_TRY(psf_build(p.get(), dH, dHt, st));
+  MLF_CUDA(cudaStreamSynchronize(st));
+  *out = p.release();
+  return MLF_OK;
+}
+
+int mlf_psf_destroy(mlf_psf* psf) {
+  clear_error();
+  delete psf;
+  return MLF_OK;
+}
+
+int mlf_psf_info(const mlf_psf* psf, int32_t* N, int64_t* Z, int64_t* S) {
+  clear_error();
+  if (!psf) return fail(MLF_ERR_INVALID, "mlf_psf_info: null psf");
+  if (N) *N = psf->N;
+  if (Z) *Z = psf->Z;
+  if (S) *S = psf->S;
+  return MLF_OK;
+}
+
+int mlf_psf_weights(const mlf_psf* psf, double* w) {
+  clear_error();
+  if (!psf || !w) return fail(MLF_ERR_INVALID, "mlf_psf_weights: null pointer");
+  std::memcpy(w, psf->weights.data(), sizeof(double) * psf->weights.size());
+  return MLF_OK;
+}
+
+int64_t mlf_psf_device_bytes(const mlf_psf* psf) { return psf ? (int64_t)psf->bytes() : 0; }
+
+int mlf_solver_create(mlf_psf* psf, int64_t Xr, int64_t Xc, mlf_solver** out) {
+  clear_error();
+  if (!psf || !out) return fail(MLF_ERR_INVALID, "mlf_solver_create: null pointer");
+  *out = nullptr;
+  if (Xr < psf->N || Xc < psf->N || Xr % psf->N || Xc % psf->N)
+    return fail(MLF_ERR_INVALID, "mlf_solver_create: image sides must be positive multiples of Nnum");
+  std::unique_ptr<mlf_solver> s(new mlf_solver());
+  s->psf = psf;
+  s->Xr = Xr;
+  s->Xc = Xc;
+  MLF_TRY(current_device(&s->device));
+  if (s->device != psf->device) return fail(MLF_ERR_INVALID, "mlf_solver_create: PSF lives on another device");
+  MLF_TRY(solver_init(s.get()));
+  *out = s.release();
+  return MLF_OK;
+}
+
+int mlf_solver_destroy(mlf_solver* s) {
+  clear_error();
+  delete s;
+  return MLF_OK;
+}
+
+int64_t mlf_solver_device_bytes(const mlf_solver* s) { return s ? (int64_t)s->bytes() : 0; }
+
+int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t precision,
+                   const float* warm_start, float* vol_out, mlf_stats* stats, void* stream) {
+  clear_error();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!s || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_solver_run: null pointer");
+  if (max_iter < 0) return fail(MLF_ERR_INVALID, "mlf_solver_run: maxIter must be >= 0");
+  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16)
+    return fail(MLF_ERR_INVALID, "mlf_solver_run: unknown precision");
+  const size_t n_img = (size_t)(s->Xr * s->Xc), n_vol = n_img * s->Z;
+  const float *dlf = nullptr, *dwarm = nullptr;
+  MLF_TRY(stage_in(lfimg, n_img, s->stage_in, &dlf, st));
+  DevBuf warm_tmp;
+  MLF_TRY(stage_in(warm_start, n_vol, warm_tmp, &dwarm, st));
+  OutStage o;
+  MLF_TRY(stage_out(vol_out, n_vol, s->stage_out, &o));
+  MLF_TRY(solver_run(s, dlf, max_iter, precision, dwarm, o.dev, stats, st));
+  MLF_TRY(finish_out(o, st));
+  if (o.host || warm_tmp.p || dlf != lfimg) MLF_CUDA(cudaStreamSynchronize(st));
+  return MLF_OK;
+}
+
+int mlf_rl_solve(const float* lfimg, int64_t Xr, int64_t Xc, const float* H, const float* Ht,
+                 int64_t K0, int32_t N, int64_t Z, int32_t max_iter, int32_t precision, float* vol_out,
+                 mlf_stats* stats, void* stream) {
+  mlf_psf* psf = nullptr;
+  MLF_TRY(mlf_psf_create(H, Ht, K0, N, Z, &psf, stream));
+  std::unique_ptr<mlf_psf> guard(psf);
+  mlf_solver* s = nullptr;
+  MLF_TRY(mlf_solver_create(psf, Xr, Xc, &s));
+  std::unique_ptr<mlf_solver> sguard(s);
+  MLF_TRY(mlf_solver_run(s, lfimg, max_iter, precision, nullptr, vol_out, stats, stream));
+  MLF_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  return MLF_OK;
+}
+
+int mlf_forward_view(mlf_solver* s, const float* vol, int32_t u, int32_t v, float* hx, void* stream) {
+  clear_error();
+  if (!s || !vol || !hx) return fail(MLF_ERR_INVALID, "mlf_forward_view: null pointer");
+  if (u < 0 || v < 0 || u >= s->N || v >= s->N) return fail(MLF_ERR_INVALID, "mlf_forward_view: view out of range");
+  if (!is_device_ptr(vol) || !is_device_ptr(hx)) return fail(MLF_ERR_INVALID, "mlf_forward_view: device pointers required");
+  return forward_view(s, vol, u, v, hx, static_cast<cudaStream_t>(stream));
+}
+
+int mlf_backward_view(mlf_solver* s, const float* proj, int32_t u, int32_t v, float* out, void* stream) {
+  clear_error();
+  if (!s || !proj || !out) return fail(MLF_ERR_INVALID, "mlf_backward_view: null pointer");
+  if (u < 0 || v < 0 || u >= s->N || v >= s->N) return fail(MLF_ERR_INVALID, "mlf_backward_view: view out of range");
+  if (!is_device_ptr(proj) || !is_device_ptr(out)) return fail(MLF_ERR_INVALID, "mlf_backward_view: device pointers required");
+  return backward_view(s, proj, u, v, out, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,366 @@
+// Flux-preserving NIP low-pass applied after every RL iteration.
+//
+// recon_theory_phase_space_LFM_with_filter.m:44-61 builds, per bank entry i, the filter
+//   F_i = |fftshift(fft2(g_i))| / max,  g_i(x, y) = exp(-((x/w_i)^2 + (y/w_i)^2))
+// and sample_filter (:222-240) applies  real(ifft2(ifftshift(fftshift(fft2(X_z)) .* F)))
+// to the planes inside the bank's range, then rescales to the plane's original sum.
+// Because ifftshift(fftshift(A) .* F) = A .* ifftshift(F) and g is separable,
+//   ifftshift(F_i) = ax_i (x) ay_i,   ax_i = |fft(gx_i)| / max|fft(gx_i)|,
+// so the filter is a separable CIRCULAR convolution with the real, even kernels
+// cx_i = ifft(ax_i) and cy_i = ifft(ay_i).  The kernels are computed here in FP64 and
+// truncated where the remaining tail mass is below 1e-12 of the total (the Gaussian
+// widths used give compact kernels; a wide kernel falls back to the full circulant).
+// The plane sums before and after filtering are accumulated in FP64.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+namespace {
+
+constexpr int kLines = 32;      // lines per CTA (one per lane)
+constexpr int kPad = 33;        // shared-memory row stride (bank-conflict free)
+constexpr int kChunk = 8;       // consecutive outputs per thread
+constexpr int kFiltThreads = 256;
+
+struct FGeo {
+  int64_t Xr, Xc;
+  int Z;
+};
+
+// Phase-major -> MATLAB layout for all planes (into the scratch volume).
+__global__ void k_unphase(const float* __restrict__ X, int N, int Z, int Li, int Pa, int64_t plane,
+                          int64_t Xr, int64_t Xc, float* __restrict__ V) {
+  const int64_t n = Xr * Xc * Z;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e % Xr;
+    const int64_t c = (e / Xr) % Xc;
+    const int z = (int)(e / (Xr * Xc));
+    const int64_t ch = ((c % N) * N + (r % N)) * Z + z;
+    V[e] = X[ch * plane + (c / N) * Pa + (r / N)];
+  }
+}
+
+// MATLAB layout -> phase-major, scaling each plane by scale[z].
+__global__ void k_rephase(const float* __restrict__ V, const double* __restrict__ scale, int N, int Z,
+                          int Pa, int64_t plane, int64_t Xr, int64_t Xc, float* __restrict__ X) {
+  const int64_t n = Xr * Xc * Z;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e % Xr;
+    const int64_t c = (e / Xr) % Xc;
+    const int z = (int)(e / (Xr * Xc));
+    const int64_t ch = ((c % N) * N + (r % N)) * Z + z;
+    X[ch * plane + (c / N) * Pa + (r / N)] = (float)((double)V[e] * scale[z]);
+  }
+}
+
+// Circular 1-D filtering of kLines lines of length L held in shared memory as
+// buf[i * kPad + line].  taps[k] = c[(k - wlo) mod L], k < nt:
+//   y[i] = sum_k taps[k] * x[(i + wlo - k) mod L]
+// Each thread produces kChunk consecutive outputs of one line (lane = line).
+// `emit(line, i, value)` stores an output; returns the thread's FP64 sum of outputs.
+template <class Emit>
+__device__ double filter_lines(const float* __restrict__ buf, int L, const float* __restrict__ taps,
+                               int nt, int wlo, int nlines, Emit emit) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  double s = 0.0;
+  const int nchunks = (L + kChunk - 1) / kChunk;
+  for (int chk = warp; chk < nchunks; chk += nwarps) {
+    if (lane >= nlines) continue;
+    const int i0 = chk * kChunk;
+    float win[kChunk];
+    int j = (i0 + wlo) % L;  // index of x for output i0 at k = 0
+#pragma unroll
+    for (int t = 0; t < kChunk; ++t) {
+      int jt = j + t;
+      if (jt >= L) jt -= L;
+      win[t] = buf[jt * kPad + lane];
+    }
+    float acc[kChunk];
+#pragma unroll
+    for (int t = 0; t < kChunk; ++t) acc[t] = 0.f;
+    for (int k = 0; k < nt; ++k) {
+      const float c = taps[k];
+#pragma unroll
+      for (int t = 0; t < kChunk; ++t) acc[t] = fmaf(c, win[t], acc[t]);
+      // slide: next k needs x[(i + wlo - k - 1) mod L]
+#pragma unroll
+      for (int t = kChunk - 1; t > 0; --t) win[t] = win[t - 1];
+      j = (j == 0) ? L - 1 : j - 1;
+      win[0] = buf[j * kPad + lane];
+    }
+#pragma unroll
+    for (int t = 0; t < kChunk; ++t) {
+      const int i = i0 + t;
+      if (i < L) {
+        emit(lane, i, acc[t]);
+        s += (double)acc[t];
+      }
+    }
+  }
+  return s;
+}
+
+__device__ void block_reduce_store(double s, double* out) {
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += sh[i];
+    *out = r;
+  }
+}
+
+// Pass along r (contiguous): grid (ceil(Xc / kLines), Zf).  Lines = columns c of plane z.
+// Also accumulates the plane's input sum (sum_before).
+__global__ void k_filter_r(float* __restrict__ V, FGeo g, const int* __restrict__ zlist,
+                           const int* __restrict__ plane_entry, const float* __restrict__ cx,
+                           const int* __restrict__ wlo_e, const int* __restrict__ nt_e, int tap_stride,
+                           double* sums_in) {
+  extern __shared__ float buf[];  // [Xr][kPad]
+  const int z = zlist[blockIdx.y];
+  const int e = plane_entry[z];
+  const int64_t c0 = (int64_t)blockIdx.x * kLines;
+  const int nlines = (int)(g.Xc - c0 < kLines ? g.Xc - c0 : kLines);
+  float* plane = V + (int64_t)z * g.Xr * g.Xc;
+  double sin = 0.0;
+  for (int l = 0; l < nlines; ++l) {
+    const float* line = plane + (c0 + l) * g.Xr;
+    for (int64_t i = threadIdx.x; i < g.Xr; i += blockDim.x) {
+      const float x = line[i];
+      buf[i * kPad + l] = x;
+      sin += (double)x;
+    }
+  }
+  __syncthreads();
+  const int L = (int)g.Xr;
+  double sout = filter_lines(buf, L, cx + (int64_t)e * tap_stride, nt_e[e], wlo_e[e], nlines,
+                             [&](int l, int i, float y) { plane[(c0 + l) * g.Xr + i] = y; });
+  (void)sout;
+  block_reduce_store(sin, sums_in + (int64_t)blockIdx.y * gridDim.x + blockIdx.x);
+}
+
+// Pass along c (stride Xr): grid (ceil(Xr / kLines), Zf).  Lines = rows r of plane z.
+// Accumulates the plane's filtered sum.
+__global__ void k_filter_c(float* __restrict__ V, FGeo g, const int* __restrict__ zlist,
+                           const int* __restrict__ plane_entry, const float* __restrict__ cy,
+                           const int* __restrict__ wlo_e, const int* __restrict__ nt_e, int tap_stride,
+                           double* sums_out) {
+  extern __shared__ float buf[];  // [Xc][kPad]
+  const int z = zlist[blockIdx.y];
+  const int e = plane_entry[z];
+  const int64_t r0 = (int64_t)blockIdx.x * kLines;
+  const int nlines = (int)(g.Xr - r0 < kLines ? g.Xr - r0 : kLines);
+  float* plane = V + (int64_t)z * g.Xr * g.Xc;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int64_t c = warp; c < g.Xc; c += nwarps)
+    if (lane < nlines) buf[c * kPad + lane] = plane[c * g.Xr + r0 + lane];
+  __syncthreads();
+  const int L = (int)g.Xc;
+  double s = filter_lines(buf, L, cy + (int64_t)e * tap_stride, nt_e[e], wlo_e[e], nlines,
+                          [&](int l, int i, float y) { plane[(int64_t)i * g.Xr + r0 + l] = y; });
+  block_reduce_store(s, sums_out + (int64_t)blockIdx.y * gridDim.x + blockIdx.x);
+}
+
+// scale[z] = sum_before / sum_after for filtered planes (fixed-order sums), 1 otherwise.
+__global__ void k_filter_scale(const double* sin, int nin, const double* sout, int nout,
+                               const int* zlist, int nzf, int Z, double* scale) {
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  if (z >= Z) return;
+  int k = -1;
+  for (int t = 0; t < nzf; ++t)
+    if (zlist[t] == z) k = t;
+  if (k < 0) {
+    scale[z] = 1.0;
+    return;
+  }
+  double a = 0.0, b = 0.0;
+  for (int i = 0; i < nin; ++i) a += sin[(int64_t)k * nin + i];
+  for (int i = 0; i < nout; ++i) b += sout[(int64_t)k * nout + i];
+  scale[z] = a / b;
+}
+
+// |fft(g)|, g[n] = exp(-((n + 1 - L/2) / w)^2), by direct DFT in FP64.
+std::vector<double> axis_mag(int L, double w) {
+  std::vector<double> g(L), c(L), s(L), out(L);
+  for (int n = 0; n < L; ++n) {
+    const double x = (n + 1) - L / 2.0;
+    g[n] = std::exp(-(x / w) * (x / w));
+    c[n] = std::cos(2.0 * M_PI * n / L);
+    s[n] = std::sin(2.0 * M_PI * n / L);
+  }
+  for (int k = 0; k < L; ++k) {
+    double re = 0.0, im = 0.0;
+    int64_t idx = 0;
+    for (int n = 0; n < L; ++n) {
+      re += g[n] * c[idx];
+      im -= g[n] * s[idx];
+      idx += k;
+      if (idx >= L) idx -= L;
+    }
+    out[k] = std::sqrt(re * re + im * im);
+  }
+  return out;
+}
+
+// Circular kernel c = ifft(a / max a) (real and even), FP64.
+std::vector<double> circ_kernel(const std::vector<double>& a) {
+  const int L = (int)a.size();
+  double mx = 0.0;
+  for (double v : a) mx = std::max(mx, v);
+  std::vector<double> cs(L), out(L);
+  for (int n = 0; n < L; ++n) cs[n] = std::cos(2.0 * M_PI * n / L);
+  for (int d = 0; d < L; ++d) {
+    double acc = 0.0;
+    int64_t idx = 0;
+    for (int k = 0; k < L; ++k) {
+      acc += (a[k] / mx) * cs[idx];
+      idx += d;
+      if (idx >= L) idx -= L;
+    }
+    out[d] = acc / L;
+  }
+  return out;
+}
+
+// Half-width beyond which the kernel's tail mass is < 1e-12 of its total; wlo/nt taps.
+void truncate_kernel(const std::vector<double>& c, int* wlo, int* nt) {
+  const int L = (int)c.size();
+  double tot = 0.0;
+  for (double v : c) tot += std::fabs(v);
+  int W = (L - 1) / 2;
+  for (int w = 0; 2 * w + 1 < L; ++w) {
+    double tail = 0.0;
+    for (int d = 0; d < L; ++d) {
+      const int dist = std::min(d, L - d);
+      if (dist > w) tail += std::fabs(c[d]);
+    }
+    if (tail <= 1e-12 * tot) { W = w; break; }
+  }
+  if (2 * W + 1 >= L) {
+    *wlo = (L - 1) / 2;
+    *nt = L;
+  } else {
+    *wlo = W;
+    *nt = 2 * W + 1;
+  }
+}
+
+}  // namespace
+
+int filter_init(Solver* s) {
+  FilterPlan& f = s->filt;
+  const int Z = s->Z, N = s->N;
+  // omega_NIP_array and the plane -> bank-entry map, recon_…_with_filter.m:21-26,54-56,224-231
+  int R = (int)std::ceil(Z / 3.0);
+  if (R % 2 == 1) R += 1;
+  const int nb = 3 * R;
+  std::vector<double> om(nb);
+  for (int i = 0; i < nb; ++i) {
+    const double axis = (i + 1) - nb / 2.0;
+    const double t = axis / 100.0 * 2.0 * std::sqrt(std::log(2.0));
+    om[i] = (N - 7) * std::exp(-t * t);
+    if (om[i] < 0.2) om[i] = 0.2;
+  }
+  const int half_z = (int)std::floor(Z / 2.0 + 0.5);
+  f.plane_entry.assign(Z, -1);
+  std::vector<int> used(nb, -1), entries;
+  for (int z1 = 1; z1 <= Z; ++z1) {
+    if (z1 >= half_z - nb / 2.0 + 1 && z1 <= half_z + nb / 2.0) {
+      const int bank = (int)(z1 - half_z + nb / 2.0) - 1;
+      if (used[bank] < 0) {
+        used[bank] = (int)entries.size();
+        entries.push_back(bank);
+      }
+      f.plane_entry[z1 - 1] = used[bank];
+    }
+  }
+  f.n_entries = (int)entries.size();
+  const int Lr = (int)s->Xr, Lc = (int)s->Xc;
+  std::vector<float> cx((size_t)std::max(1, f.n_entries) * Lr, 0.f), cy((size_t)std::max(1, f.n_entries) * Lc, 0.f);
+  std::vector<int> wlo_x(std::max(1, f.n_entries), 0), nt_x(std::max(1, f.n_entries), 1);
+  std::vector<int> wlo_y(std::max(1, f.n_entries), 0), nt_y(std::max(1, f.n_entries), 1);
+  for (int e = 0; e < f.n_entries; ++e) {
+    const double w = om[entries[e]];
+    const std::vector<double> kx = circ_kernel(axis_mag(Lr, w));
+    const std::vector<double> ky = (Lc == Lr) ? kx : circ_kernel(axis_mag(Lc, w));
+    truncate_kernel(kx, &wlo_x[e], &nt_x[e]);
+    truncate_kernel(ky, &wlo_y[e], &nt_y[e]);
+    for (int k = 0; k < nt_x[e]; ++k) cx[(size_t)e * Lr + k] = (float)kx[((k - wlo_x[e]) % Lr + Lr) % Lr];
+    for (int k = 0; k < nt_y[e]; ++k) cy[(size_t)e * Lc + k] = (float)ky[((k - wlo_y[e]) % Lc + Lc) % Lc];
+  }
+  f.wx = nt_x;
+  f.wy = nt_y;
+  std::vector<int> zlist;
+  for (int z = 0; z < Z; ++z)
+    if (f.plane_entry[z] >= 0) zlist.push_back(z);
+  const int nzf = (int)zlist.size();
+  // int table: plane_entry[Z] | zlist[Z] | wlo_x | nt_x | wlo_y | nt_y
+  std::vector<int> itab;
+  itab.insert(itab.end(), f.plane_entry.begin(), f.plane_entry.end());
+  itab.insert(itab.end(), zlist.begin(), zlist.end());
+  itab.resize(2 * Z, 0);
+  itab.insert(itab.end(), wlo_x.begin(), wlo_x.end());
+  itab.insert(itab.end(), nt_x.begin(), nt_x.end());
+  itab.insert(itab.end(), wlo_y.begin(), wlo_y.end());
+  itab.insert(itab.end(), nt_y.begin(), nt_y.end());
+  MLF_TRY(f.cx.alloc(cx.size() * sizeof(float), "filter kernels"));
+  MLF_TRY(f.cy.alloc(cy.size() * sizeof(float), "filter kernels"));
+  MLF_TRY(f.plane_entry_dev.alloc(itab.size() * sizeof(int), "filter tables"));
+  MLF_CUDA(cudaMemcpy(f.cx.p, cx.data(), cx.size() * sizeof(float), cudaMemcpyHostToDevice));
+  MLF_CUDA(cudaMemcpy(f.cy.p, cy.data(), cy.size() * sizeof(float), cudaMemcpyHostToDevice));
+  MLF_CUDA(cudaMemcpy(f.plane_entry_dev.p, itab.data(), itab.size() * sizeof(int), cudaMemcpyHostToDevice));
+  const int gr = (int)((s->Xc + kLines - 1) / kLines), gc = (int)((s->Xr + kLines - 1) / kLines);
+  f.max_blocks = std::max(gr, gc);
+  MLF_TRY(f.sums.alloc(sizeof(double) * (2 * (size_t)std::max(1, nzf) * f.max_blocks + Z), "filter sums"));
+  const size_t smem_r = sizeof(float) * (size_t)Lr * kPad, smem_c = sizeof(float) * (size_t)Lc * kPad;
+  int dev_smem = 0;
+  MLF_CUDA(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
+  if ((int)std::max(smem_r, smem_c) > dev_smem)
+    return fail(MLF_ERR_UNSUPPORTED, "image side too large for the sample filter's line buffers");
+  MLF_CUDA(cudaFuncSetAttribute(k_filter_r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+  MLF_CUDA(cudaFuncSetAttribute(k_filter_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+  return MLF_OK;
+}
+
+int filter_run(Solver* s, cudaStream_t st) {
+  FilterPlan& f = s->filt;
+  const int Z = s->Z;
+  int nzf = 0;
+  for (int z = 0; z < Z; ++z) nzf += f.plane_entry[z] >= 0;
+  if (nzf == 0) return MLF_OK;
+  const int* itab = f.plane_entry_dev.as<int>();
+  const int* pe = itab;
+  const int* zl = itab + Z;
+  const int ne = std::max(1, f.n_entries);
+  const int* wlo_x = itab + 2 * Z;
+  const int* nt_x = wlo_x + ne;
+  const int* wlo_y = nt_x + ne;
+  const int* nt_y = wlo_y + ne;
+  const FGeo g{s->Xr, s->Xc, Z};
+  const int64_t n = s->Xr * s->Xc * Z;
+  const int eg = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+  float* V = s->Xtmp.as<float>();
+  k_unphase<<<eg, 256, 0, st>>>(s->X.as<float>(), s->N, Z, s->Li, s->Pa, s->plane, s->Xr, s->Xc, V);
+  const int gr = (int)((s->Xc + kLines - 1) / kLines), gc = (int)((s->Xr + kLines - 1) / kLines);
+  double* sin = f.sums.as<double>();
+  double* sout = sin + (size_t)nzf * f.max_blocks;
+  double* scale = sout + (size_t)nzf * f.max_blocks;
+  k_filter_r<<<dim3(gr, nzf), kFiltThreads, sizeof(float) * s->Xr * kPad, st>>>(
+      V, g, zl, pe, f.cx.as<float>(), wlo_x, nt_x, (int)s->Xr, sin);
+  k_filter_c<<<dim3(gc, nzf), kFiltThreads, sizeof(float) * s->Xc * kPad, st>>>(
+      V, g, zl, pe, f.cy.as<float>(), wlo_y, nt_y, (int)s->Xc, sout);
+  k_filter_scale<<<(Z + 255) / 256, 256, 0, st>>>(sin, gr, sout, gc, zl, nzf, Z, scale);
+  k_rephase<<<eg, 256, 0, st>>>(V, scale, s->N, Z, s->Pa, s->plane, s->Xr, s->Xc, s->X.as<float>());
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+}  // namespace mlf

@@ -1,0 +1,144 @@
+// Internal structures shared by the translation units of libmesolf_lf.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "mesolf_lf.h"
+
+namespace mlf {
+
+// ------------------------------------------------------------------ error plumbing
+int fail(int code, const std::string& msg);  // records the message, returns code
+void clear_error();
+
+#define MLF_CUDA(call)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return ::mlf::fail(MLF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define MLF_TRY(call)             \
+  do {                            \
+    int st_ = (call);             \
+    if (st_ != MLF_OK) return st_; \
+  } while (0)
+
+// Device allocation owned by a host object.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  int alloc(size_t n, const char* what);
+  void release();
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// true if ptr is device (or managed) memory usable by kernels on the current device
+bool is_device_ptr(const void* ptr);
+
+// ------------------------------------------------------------------ PSF
+// Per-view projector taps in phase-major ("polyphase") form.  For view (u, v) (0-based,
+// view = u + N*v) and volume channel ch = (beta*N + alpha)*Z + z the forward taps are
+//   wf[view][ch][db*T + da] = Hps_z[N(2q-da) + N-1-alpha, N(2q-db) + N-1-beta]
+// and the backward taps
+//   wb[view][ch][dj*T + di] = Htc_z[N(2q-di) + f_alpha, N(2q-dj) + f_beta],
+//   f_alpha = (alpha - u + h) mod N,  h = (N-1)/2,  T = 2q+1 = S/N.
+struct Psf {
+  int device = 0;
+  int N = 0, Z = 0, K0 = 0, S = 0, q = 0, T = 0;
+  int64_t nch = 0;           // N*N*Z volume channels
+  int64_t taps_per_view = 0; // nch * T * T
+  DevBuf wf, wb;             // float [N*N][nch][T*T]
+  std::vector<double> weights;  // N*N, index u + N*v (MATLAB weight(u+1, v+1))
+  std::vector<int> view_order;  // active views in spiral order (view = u + N*v)
+  size_t bytes() const { return wf.bytes + wb.bytes; }
+};
+
+// ------------------------------------------------------------------ solver
+struct FilterPlan {
+  // sample_filter as separable circular convolutions.  For bank entry e the 1-D kernels
+  // are cx_e (length Xr) and cy_e (length Xc) with half-widths Wx_e / Wy_e.
+  int n_entries = 0;
+  std::vector<int> plane_entry;  // per plane: bank entry or -1 (pass-through)
+  std::vector<int> wx, wy;       // per entry half-width
+  DevBuf cx, cy;                 // float [n_entries][Xr] / [n_entries][Xc], index = offset d mod len
+  DevBuf plane_entry_dev;        // int [Z]
+  DevBuf wx_dev, wy_dev;         // int [n_entries]
+  DevBuf sums;                   // double [2][Z][max_blocks] partial flux sums
+  int max_blocks = 0;
+};
+
+struct Solver {
+  Psf* psf = nullptr;
+  int device = 0;
+  int64_t Xr = 0, Xc = 0;
+  int N = 0, Z = 0, Li = 0, Lj = 0, q = 0, T = 0;
+  int Pa = 0;          // row pitch (floats) of a phase-major plane
+  int64_t plane = 0;   // floats per plane (Lj * Pa)
+  int64_t nch = 0;
+  // view-kernel geometry
+  int tilesA = 0, tilesB = 0, tps = 0, slots = 0, threads = 0, grid = 0;
+  int RP = 0, RProws = 0, XP = 0, XProws = 0, maxc = 0;
+  size_t smem = 0;
+  int ncA[3] = {0, 0, 0}, ncB[3] = {0, 0, 0};
+  DevBuf X;          // float [nch][plane]      phase-major volume
+  DevBuf Xtmp;       // float [nch][plane]      scratch volume (back-projection output, filter)
+  DevBuf lfs;        // float [N*N][Lj*Li]      sub-aperture images
+  DevBuf rpad;       // float [RProws][RP]      halo-padded ratio image
+  DevBuf part;       // float [grid][Lj*Li]     per-CTA forward partials
+  DevBuf hx;         // float [Lj*Li]           last forward projection
+  DevBuf cls;        // int tables: clsA[3][Li], clsB[3][Lj], rngA[3][maxc][2], rngB[3][maxc][2]
+  DevBuf red;        // double scratch for reductions
+  DevBuf stage_in, stage_out;  // device staging for host arrays
+  FilterPlan filt;
+  size_t bytes() const;
+};
+
+// ------------------------------------------------------------------ entry points used across TUs
+int psf_build(Psf* psf, const float* dH, const float* dHt, cudaStream_t st);
+int solver_init(Solver* s);
+int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const float* d_warm,
+               float* d_out, mlf_stats* stats, cudaStream_t st);
+int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaStream_t st);
+int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cudaStream_t st);
+int filter_init(Solver* s);
+int filter_run(Solver* s, cudaStream_t st);
+int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,
+                 int64_t kw, int nnum, float* d_out, cudaStream_t st);
+
+// view kernels (instantiated per tap count T in mlf_view_T*.cu)
+struct ViewArgs {
+  float* X;            // phase-major volume (read; written when updating)
+  float* Cout;         // MODE_BWDC: phase-major back projection output
+  const float* rpad;   // halo-padded ratio image
+  const float* wb;     // backward taps of the current view [nch][T*T]
+  const float* wf;     // forward taps of the view being projected [nch][T*T]
+  float* part;         // [gridDim.x][Lj*Li]
+  const int* clsA;     // [3][Li]
+  const int* clsB;     // [3][Lj]
+  const int* rngA;     // [3][maxc][2]
+  const int* rngB;     // [3][maxc][2]
+  float w;             // view weight
+  int u, v;            // current view (backward / update)
+  int do_fwd;          // MODE_STEP: also project with wf
+  int N, Z, Li, Lj, Pa, q;
+  int64_t plane, nch;
+  int tilesA, tilesB, tps, slots;
+  int RP, RProws, XP, XProws, maxc, slot_floats;
+};
+enum ViewMode { MODE_FWD = 0, MODE_STEP = 1, MODE_BWDC = 2 };
+int prepare_view_kernels(int T, size_t smem);
+int occupancy_view_kernel(int T, int threads, size_t smem, int* blocks);
+int launch_view_kernel(int T, int mode, const ViewArgs& a, int grid, int threads, size_t smem,
+                       cudaStream_t st);
+bool view_taps_supported(int T);
+
+}  // namespace mlf

@@ -1,0 +1,468 @@
+// Phase-space Richardson-Lucy solve on one GPU (host orchestration + small kernels).
+//
+// recon_theory_phase_space_LFM_with_filter.m:72-146: flat initial guess, iterations of
+// the spiral view loop (forward projection, ratio, back projection, update, blend) and
+// the per-iteration sample_filter.  Each view step is one launch of the fused view
+// kernel (back projection + D + update of view k, forward projection of view k+1) plus
+// one launch of the partial-sum reduction that forms the next ratio image.  One
+// iteration is captured once as a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <utility>
+#include <vector>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+namespace {
+
+__device__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum of n floats into part[blockIdx.x] (FP64); fixed per-block order.
+__global__ void k_sum_partial(const float* __restrict__ a, int64_t n, double* part) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s += (double)a[i];
+  s = warp_sum_d(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += sh[i];
+    part[blockIdx.x] = r;
+  }
+}
+
+// Flat initial guess, recon_…_with_filter.m:72-73: ones/sum(ones)*sum(LFIMG).
+__global__ void k_init_flat(float* X, int64_t n, const double* part, int nparts, double inv_count) {
+  __shared__ float val;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < nparts; ++i) s += part[i];
+    val = (float)(inv_count * s);
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    X[i] = val;
+}
+
+struct Geo {
+  int N, Z, Li, Lj, Pa;
+  int64_t plane, Xr, Xc;
+};
+
+// MATLAB (Xr, Xc, Z) volume -> phase-major planes; one thread per voxel of the input.
+__global__ void k_to_phase(const float* __restrict__ vol, Geo g, float* __restrict__ X) {
+  const int64_t n = g.Xr * g.Xc * g.Z;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e % g.Xr;
+    const int64_t c = (e / g.Xr) % g.Xc;
+    const int z = (int)(e / (g.Xr * g.Xc));
+    const int alpha = (int)(r % g.N), a = (int)(r / g.N);
+    const int beta = (int)(c % g.N), b = (int)(c / g.N);
+    const int64_t ch = ((int64_t)beta * g.N + alpha) * g.Z + z;
+    X[ch * g.plane + (int64_t)b * g.Pa + a] = vol[e];
+  }
+}
+
+__global__ void k_from_phase(const float* __restrict__ X, Geo g, float* __restrict__ vol) {
+  const int64_t n = g.Xr * g.Xc * g.Z;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e % g.Xr;
+    const int64_t c = (e / g.Xr) % g.Xc;
+    const int z = (int)(e / (g.Xr * g.Xc));
+    const int alpha = (int)(r % g.N), a = (int)(r / g.N);
+    const int beta = (int)(c % g.N), b = (int)(c / g.N);
+    const int64_t ch = ((int64_t)beta * g.N + alpha) * g.Z + z;
+    vol[e] = X[ch * g.plane + (int64_t)b * g.Pa + a];
+  }
+}
+
+// Sub-aperture images, LFIMG(u:N:end, v:N:end) for every view u + N*v: lfs[view][b*Li + a].
+__global__ void k_extract_views(const float* __restrict__ lf, Geo g, float* __restrict__ lfs) {
+  const int64_t n = g.Xr * g.Xc;
+  const int64_t LL = (int64_t)g.Li * g.Lj;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e % g.Xr, c = e / g.Xr;
+    const int u = (int)(r % g.N), a = (int)(r / g.N);
+    const int v = (int)(c % g.N), b = (int)(c / g.N);
+    lfs[(int64_t)(u + g.N * v) * LL + (int64_t)b * g.Li + a] = lf[e];
+  }
+}
+
+// HX = sum of the per-CTA forward partials (fixed order).  Optionally writes HX and the
+// ratio image R = LF_sub ./ HX with non-finite -> 0 (recon_…_with_filter.m:116-117) into
+// the halo-padded buffer read by the next view kernel.
+__global__ void k_reduce_ratio(const float* __restrict__ part, int nparts, int Li, int Lj,
+                               const float* __restrict__ lfsub, float* __restrict__ hx_out,
+                               float* __restrict__ rpad, int RP, int off) {
+  const int LL = Li * Lj;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= LL) return;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+  int k = 0;
+  for (; k + 4 <= nparts; k += 4) {
+    s0 += part[(int64_t)(k + 0) * LL + i];
+    s1 += part[(int64_t)(k + 1) * LL + i];
+    s2 += part[(int64_t)(k + 2) * LL + i];
+    s3 += part[(int64_t)(k + 3) * LL + i];
+  }
+  for (; k < nparts; ++k) s0 += part[(int64_t)k * LL + i];
+  const float hx = (s0 + s1) + (s2 + s3);
+  if (hx_out) hx_out[i] = hx;
+  if (rpad) {
+    float r = lfsub[i] / hx;
+    if (!isfinite(r)) r = 0.f;
+    const int a = i % Li, b = i / Li;
+    rpad[(b + off) * RP + a + off] = r;
+  }
+}
+
+// proj (Li x Lj, MATLAB layout) into the interior of the halo-padded ratio buffer.
+__global__ void k_fill_rpad(const float* __restrict__ proj, int Li, int Lj, float* rpad, int RP,
+                            int off) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Li * Lj) return;
+  const int a = i % Li, b = i / Li;
+  rpad[(b + off) * RP + a + off] = proj[i];
+}
+
+inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
+inline int round_up(int a, int b) { return ceil_div(a, b) * b; }
+
+int grid_for(int64_t n, int threads = 256) {
+  int64_t g = (n + threads - 1) / threads;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
+}
+
+Geo geo_of(const Solver* s) {
+  return Geo{s->N, s->Z, s->Li, s->Lj, s->Pa, s->plane, s->Xr, s->Xc};
+}
+
+ViewArgs view_args(Solver* s) {
+  ViewArgs a{};
+  const int* cls = s->cls.as<int>();
+  a.X = s->X.as<float>();
+  a.Cout = nullptr;
+  a.rpad = s->rpad.as<float>();
+  a.part = s->part.as<float>();
+  a.clsA = cls;
+  a.clsB = cls + 3 * s->Li;
+  a.rngA = cls + 3 * s->Li + 3 * s->Lj;
+  a.rngB = a.rngA + 3 * s->maxc * 2;
+  a.N = s->N; a.Z = s->Z; a.Li = s->Li; a.Lj = s->Lj; a.Pa = s->Pa; a.q = s->q;
+  a.plane = s->plane; a.nch = s->nch;
+  a.tilesA = s->tilesA; a.tilesB = s->tilesB; a.tps = s->tps; a.slots = s->slots;
+  a.RP = s->RP; a.RProws = s->RProws; a.XP = s->XP; a.XProws = s->XProws; a.maxc = s->maxc;
+  a.slot_floats = round_up(s->XProws * s->XP + 2 * s->T * s->T + s->maxc * s->maxc + s->T * s->maxc, 4);
+  return a;
+}
+
+const float* wf_of(const Solver* s, int view) {
+  return s->psf->wf.as<float>() + (int64_t)view * s->psf->taps_per_view;
+}
+const float* wb_of(const Solver* s, int view) {
+  return s->psf->wb.as<float>() + (int64_t)view * s->psf->taps_per_view;
+}
+
+// D-table classes: for output coarse index a and channel shift s in {-1,0,1}, the valid
+// taps are di in [max(0, q-s-a), min(2q, L-1-a-s+q)].  Identical (lo, hi) pairs share a
+// class.
+void build_classes(int L, int q, std::vector<int>& cls, std::vector<std::pair<int, int>> rng[3],
+                   int nc[3]) {
+  cls.assign(3 * L, 0);
+  for (int s = -1; s <= 1; ++s) {
+    std::map<std::pair<int, int>, int> id;
+    rng[s + 1].clear();
+    for (int a = 0; a < L; ++a) {
+      int lo = std::max(0, q - s - a);
+      int hi = std::min(2 * q, L - 1 - a - s + q);
+      if (lo > hi) { lo = 1; hi = 0; }
+      auto key = std::make_pair(lo, hi);
+      auto it = id.find(key);
+      int c;
+      if (it == id.end()) {
+        c = (int)rng[s + 1].size();
+        id[key] = c;
+        rng[s + 1].push_back(key);
+      } else {
+        c = it->second;
+      }
+      cls[(s + 1) * L + a] = c;
+    }
+    nc[s + 1] = (int)rng[s + 1].size();
+  }
+}
+
+int run_view(Solver* s, int mode, int view_cur, int view_next, float w, bool do_fwd,
+             cudaStream_t st) {
+  ViewArgs a = view_args(s);
+  const int N = s->N;
+  a.u = view_cur % N;
+  a.v = view_cur / N;
+  a.w = w;
+  a.do_fwd = do_fwd ? 1 : 0;
+  a.wb = wb_of(s, view_cur);
+  a.wf = wf_of(s, view_next >= 0 ? view_next : view_cur);
+  return launch_view_kernel(s->T, mode, a, s->grid, s->threads, s->smem, st);
+}
+
+int run_reduce(Solver* s, int view, float* hx_out, bool ratio, cudaStream_t st) {
+  const int LL = s->Li * s->Lj;
+  const float* lfsub = s->lfs.as<float>() + (int64_t)view * LL;
+  k_reduce_ratio<<<ceil_div(LL, 256), 256, 0, st>>>(
+      s->part.as<float>(), s->grid, s->Li, s->Lj, lfsub, hx_out,
+      ratio ? s->rpad.as<float>() : nullptr, s->RP, s->q + 1);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+// One RL iteration (recon_…_with_filter.m:100-142), stream-ordered.
+int enqueue_iteration(Solver* s, int64_t* launches, cudaStream_t st) {
+  const std::vector<int>& views = s->psf->view_order;
+  const int V = (int)views.size();
+  int64_t n = 0;
+  if (V > 0) {
+    MLF_TRY(run_view(s, MODE_FWD, views[0], views[0], 0.f, true, st));
+    MLF_TRY(run_reduce(s, views[0], nullptr, true, st));
+    n += 2;
+    for (int k = 0; k < V; ++k) {
+      const int cur = views[k];
+      const bool more = k + 1 < V;
+      const float w = (float)s->psf->weights[cur];
+      MLF_TRY(run_view(s, MODE_STEP, cur, more ? views[k + 1] : -1, w, more, st));
+      ++n;
+      if (more) {
+        MLF_TRY(run_reduce(s, views[k + 1], nullptr, true, st));
+        ++n;
+      }
+    }
+  }
+  MLF_TRY(filter_run(s, st));
+  n += 3;
+  if (launches) *launches += n;
+  return MLF_OK;
+}
+
+}  // namespace
+
+size_t Solver::bytes() const {
+  return X.bytes + Xtmp.bytes + lfs.bytes + rpad.bytes + part.bytes + hx.bytes + cls.bytes +
+         red.bytes + stage_in.bytes + stage_out.bytes + filt.cx.bytes + filt.cy.bytes +
+         filt.sums.bytes;
+}
+
+bool view_taps_supported(int T) { return T >= 3 && T <= 17 && (T % 2) == 1; }
+
+int solver_init(Solver* s) {
+  Psf* p = s->psf;
+  s->N = p->N;
+  s->Z = p->Z;
+  s->q = p->q;
+  s->T = p->T;
+  s->nch = p->nch;
+  s->Li = (int)(s->Xr / s->N);
+  s->Lj = (int)(s->Xc / s->N);
+  if (!view_taps_supported(s->T))
+    return fail(MLF_ERR_UNSUPPORTED, "phase-space PSF side S/N = " + std::to_string(s->T) +
+                                         " not in {3,5,...,17} (K0 up to 255 at N = 15)");
+  s->Pa = round_up(s->Li, 4);
+  s->plane = (int64_t)s->Lj * s->Pa;
+  s->tilesA = ceil_div(s->Li, 4);
+  s->tilesB = ceil_div(s->Lj, 8);
+  s->tps = s->tilesA * s->tilesB;
+  if (s->tps > 256)
+    return fail(MLF_ERR_UNSUPPORTED, "patch of " + std::to_string(s->Li) + " x " +
+                                         std::to_string(s->Lj) +
+                                         " lenslets exceeds the 128 x 64 per-solve limit; tile the field of view");
+  const int NW = (4 + s->T - 1 + 2 + 3) / 4;
+  s->RP = round_up(4 * (s->tilesA - 1) + 4 * NW, 4);
+  s->RProws = s->tilesB * 8 + s->T + 1;
+  s->XP = s->RP;
+  s->XProws = s->tilesB * 8 + s->T - 1;
+
+  std::vector<int> clsA, clsB;
+  std::vector<std::pair<int, int>> rngA[3], rngB[3];
+  build_classes(s->Li, s->q, clsA, rngA, s->ncA);
+  build_classes(s->Lj, s->q, clsB, rngB, s->ncB);
+  s->maxc = 1;
+  for (int k = 0; k < 3; ++k) s->maxc = std::max({s->maxc, s->ncA[k], s->ncB[k]});
+  std::vector<int> tab;
+  tab.insert(tab.end(), clsA.begin(), clsA.end());
+  tab.insert(tab.end(), clsB.begin(), clsB.end());
+  for (auto* rng : {rngA, rngB})
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < s->maxc; ++c) {
+        if (c < (int)rng[k].size()) {
+          tab.push_back(rng[k][c].first);
+          tab.push_back(rng[k][c].second);
+        } else {
+          tab.push_back(1);
+          tab.push_back(0);
+        }
+      }
+  MLF_TRY(s->cls.alloc(tab.size() * sizeof(int), "class tables"));
+  MLF_CUDA(cudaMemcpy(s->cls.p, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
+
+  const int slot_floats = round_up(s->XProws * s->XP + 2 * s->T * s->T + s->maxc * s->maxc + s->T * s->maxc, 4);
+  s->slots = s->tps >= 128 ? 1 : std::max(1, std::min(32, 192 / s->tps));
+  s->threads = round_up(s->slots * s->tps, 32);
+  s->smem = sizeof(float) * ((size_t)s->RProws * s->RP + (size_t)s->slots * slot_floats);
+  int dev_smem = 0, nsm = 0;
+  MLF_CUDA(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
+  MLF_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device));
+  if ((int)s->smem > dev_smem) return fail(MLF_ERR_UNSUPPORTED, "view kernel shared memory exceeds the device limit");
+  MLF_TRY(prepare_view_kernels(s->T, s->smem));
+  int per_sm = 1;
+  MLF_TRY(occupancy_view_kernel(s->T, s->threads, s->smem, &per_sm));
+  per_sm = std::max(1, per_sm);
+  const int64_t max_blocks = (s->nch + s->slots - 1) / s->slots;
+  s->grid = (int)std::min<int64_t>(max_blocks, (int64_t)nsm * per_sm);
+
+  const int64_t vol = s->nch * s->plane;
+  const int64_t LL = (int64_t)s->Li * s->Lj;
+  MLF_TRY(s->X.alloc(vol * sizeof(float), "volume"));
+  MLF_TRY(s->Xtmp.alloc(vol * sizeof(float), "scratch volume"));
+  MLF_TRY(s->lfs.alloc((size_t)s->N * s->N * LL * sizeof(float), "sub-aperture images"));
+  MLF_TRY(s->rpad.alloc((size_t)s->RProws * s->RP * sizeof(float), "ratio image"));
+  MLF_TRY(s->part.alloc((size_t)s->grid * LL * sizeof(float), "forward partials"));
+  MLF_TRY(s->hx.alloc(LL * sizeof(float), "forward projection"));
+  MLF_TRY(s->red.alloc(4096 * sizeof(double), "reduction scratch"));
+  MLF_CUDA(cudaMemset(s->X.p, 0, s->X.bytes));
+  MLF_CUDA(cudaMemset(s->Xtmp.p, 0, s->Xtmp.bytes));
+  MLF_CUDA(cudaMemset(s->rpad.p, 0, s->rpad.bytes));
+  MLF_TRY(filter_init(s));
+  return MLF_OK;
+}
+
+int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const float* d_warm,
+               float* d_out, mlf_stats* stats, cudaStream_t st) {
+  if (precision != MLF_PREC_FP32)
+    return fail(MLF_ERR_UNSUPPORTED, "only MLF_PREC_FP32 is built into this library version");
+  const Geo g = geo_of(s);
+  const int64_t n_img = s->Xr * s->Xc;
+  const int64_t n_vol = n_img * s->Z;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (stats) {
+    MLF_CUDA(cudaEventCreate(&e0));
+    MLF_CUDA(cudaEventCreate(&e1));
+    MLF_CUDA(cudaEventRecord(e0, st));
+  }
+  int64_t launches = 0;
+  k_extract_views<<<grid_for(n_img), 256, 0, st>>>(d_lf, g, s->lfs.as<float>());
+  ++launches;
+  if (d_warm) {
+    k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_warm, g, s->X.as<float>());
+    ++launches;
+  } else {
+    const int nb = 256;
+    k_sum_partial<<<nb, 256, 0, st>>>(d_lf, n_img, s->red.as<double>());
+    k_init_flat<<<grid_for(s->nch * s->plane), 256, 0, st>>>(
+        s->X.as<float>(), s->nch * s->plane, s->red.as<double>(), nb, 1.0 / (double)n_vol);
+    launches += 2;
+  }
+  MLF_CUDA(cudaGetLastError());
+  for (int it = 0; it < max_iter; ++it) MLF_TRY(enqueue_iteration(s, &launches, st));
+  k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->X.as<float>(), g, d_out);
+  ++launches;
+  MLF_CUDA(cudaGetLastError());
+  if (stats) {
+    MLF_CUDA(cudaEventRecord(e1, st));
+    MLF_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    MLF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    stats->n_views = (int)s->psf->view_order.size();
+    stats->iterations = max_iter;
+    stats->gpu_ms = ms;
+    stats->view_ms = (max_iter > 0 && stats->n_views > 0) ? ms / (max_iter * stats->n_views) : 0.0;
+    stats->filter_ms = 0.0;
+    stats->kernel_launches = launches;
+  }
+  return MLF_OK;
+}
+
+int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaStream_t st) {
+  const Geo g = geo_of(s);
+  const int64_t n_vol = s->Xr * s->Xc * s->Z;
+  k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->Xtmp.as<float>());
+  MLF_CUDA(cudaGetLastError());
+  ViewArgs a = view_args(s);
+  a.X = s->Xtmp.as<float>();
+  a.u = u; a.v = v; a.w = 0.f; a.do_fwd = 1;
+  a.wb = wb_of(s, u + s->N * v);
+  a.wf = wf_of(s, u + s->N * v);
+  MLF_TRY(launch_view_kernel(s->T, MODE_FWD, a, s->grid, s->threads, s->smem, st));
+  return run_reduce(s, u + s->N * v, d_hx, false, st);
+}
+
+int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cudaStream_t st) {
+  const Geo g = geo_of(s);
+  const int LL = s->Li * s->Lj;
+  MLF_CUDA(cudaMemsetAsync(s->rpad.p, 0, s->rpad.bytes, st));
+  k_fill_rpad<<<ceil_div(LL, 256), 256, 0, st>>>(d_proj, s->Li, s->Lj, s->rpad.as<float>(), s->RP, s->q + 1);
+  MLF_CUDA(cudaGetLastError());
+  ViewArgs a = view_args(s);
+  a.Cout = s->Xtmp.as<float>();
+  a.u = u; a.v = v; a.w = 0.f; a.do_fwd = 0;
+  a.wb = wb_of(s, u + s->N * v);
+  a.wf = wf_of(s, u + s->N * v);
+  MLF_TRY(launch_view_kernel(s->T, MODE_BWDC, a, s->grid, s->threads, s->smem, st));
+  const int64_t n_vol = s->Xr * s->Xc * s->Z;
+  k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->Xtmp.as<float>(), g, d_out);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+// ---------------------------------------------------------------- dispatch per T
+#define MLF_DECL_T(T)                                                                     \
+  int prepare_view_T##T(size_t smem);                                                    \
+  int occupancy_view_T##T(int threads, size_t smem, int* blocks);                        \
+  int launch_view_T##T(int mode, const ViewArgs& a, int grid, int threads, size_t smem, \
+                       cudaStream_t st);
+MLF_DECL_T(3) MLF_DECL_T(5) MLF_DECL_T(7) MLF_DECL_T(9) MLF_DECL_T(11) MLF_DECL_T(13) MLF_DECL_T(15) MLF_DECL_T(17)
+#undef MLF_DECL_T
+
+#define MLF_CASES(EXPR) \
+  switch (T) {          \
+    case 3: return EXPR(3);   \
+    case 5: return EXPR(5);   \
+    case 7: return EXPR(7);   \
+    case 9: return EXPR(9);   \
+    case 11: return EXPR(11); \
+    case 13: return EXPR(13); \
+    case 15: return EXPR(15); \
+    case 17: return EXPR(17); \
+    default: return fail(MLF_ERR_UNSUPPORTED, "unsupported tap count"); \
+  }
+
+int prepare_view_kernels(int T, size_t smem) {
+#define E(t) prepare_view_T##t(smem)
+  MLF_CASES(E)
+#undef E
+}
+int occupancy_view_kernel(int T, int threads, size_t smem, int* blocks) {
+#define E(t) occupancy_view_T##t(threads, smem, blocks)
+  MLF_CASES(E)
+#undef E
+}
+int launch_view_kernel(int T, int mode, const ViewArgs& a, int grid, int threads, size_t smem,
+                       cudaStream_t st) {
+#define E(t) launch_view_T##t(mode, a, grid, threads, smem, st)
+  MLF_CASES(E)
+#undef E
+}
+
+}  // namespace mlf

@@ -1,0 +1,297 @@
+// Per-view phase-space RL kernel (plain FP32 path).
+//
+// The volume lives in phase-major layout: channel ch = (beta*N + alpha)*Z + z holds the
+// coarse plane P_ch[b][a] = X(N*a + alpha, N*b + beta, z) (row pitch Pa).  In that layout
+// the reference's per-view operators (recon_theory_phase_space_LFM_with_filter.m:211-249)
+// become, per channel, small dense correlations on the lenslet grid:
+//
+//   forward  (:243-249)  HX[j][i]  += sum_{db,da} P_ch[j+db-q][i+da-q] * wf_ch[db][da]
+//   backward (:211-220)  C_ch[b][a] = sum_{dj,di} R[b+sb-q+dj][a+sa-q+di] * wb_ch[dj][di]
+//   D        (:123)      D_ch[b][a] = the same sum over the taps that land inside R
+//   update   (:130-137)  X <- w*clean(X*C/D) + (1-w)*X, clamped at 0
+//
+// with sa = floor((alpha-u+h)/N), sb = floor((beta-v+h)/N).  One CTA owns one or more
+// channel slots; each thread of a slot owns an 8 (b) x 4 (a) output tile.  Inputs are
+// staged in shared memory with zero halos, so the tap loops need no bounds checks; the
+// sliding windows are read with aligned 128-bit shared loads.  The forward partial sums
+// of a CTA stay in registers across all its channels and are written once
+// (deterministic reduction happens in a second kernel).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+constexpr int VT_TY = 8;  // tile rows (b direction)
+constexpr int VT_TX = 4;  // tile cols (a direction)
+
+// Number of float4 loads covering a window of TX + T - 1 + OFFmax (OFFmax = 2) floats.
+template <int T>
+struct ViewWin {
+  static constexpr int NW = (VT_TX + T - 1 + 2 + 3) / 4;
+};
+
+// acc[ty][tx] += sum_{dy<T, dx<T} in[(y0+ty+dy)*pitch + x0 + OFF + tx + dx] * w[dy*T+dx]
+// `in + y0*pitch + x0` must be 16-byte aligned (x0 multiple of 4, pitch multiple of 4).
+template <int T, int OFF>
+__device__ __forceinline__ void conv_tile(const float* __restrict__ in, int pitch,
+                                          const float* __restrict__ w,
+                                          float (&acc)[VT_TY][VT_TX]) {
+  constexpr int NW = ViewWin<T>::NW;
+#pragma unroll 1
+  for (int dy = 0; dy < T; ++dy) {
+    float wr[T];
+#pragma unroll
+    for (int dx = 0; dx < T; ++dx) wr[dx] = w[dy * T + dx];
+    const float* rowp = in + dy * pitch;
+#pragma unroll
+    for (int ty = 0; ty < VT_TY; ++ty) {
+      float win[4 * NW];
+      const float4* r4 = reinterpret_cast<const float4*>(rowp + ty * pitch);
+#pragma unroll
+      for (int k = 0; k < NW; ++k) {
+        float4 t4 = r4[k];
+        win[4 * k + 0] = t4.x;
+        win[4 * k + 1] = t4.y;
+        win[4 * k + 2] = t4.z;
+        win[4 * k + 3] = t4.w;
+      }
+#pragma unroll
+      for (int dx = 0; dx < T; ++dx)
+#pragma unroll
+        for (int tx = 0; tx < VT_TX; ++tx)
+          acc[ty][tx] = fmaf(win[OFF + tx + dx], wr[dx], acc[ty][tx]);
+    }
+  }
+}
+
+__device__ __forceinline__ int floor_div(int a, int b) {
+  int q = a / b;
+  return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
+}
+
+template <int T, int MODE>
+__global__ void __launch_bounds__(256) k_view(ViewArgs A) {
+  extern __shared__ __align__(16) float sm[];
+  constexpr int TT = T * T;
+  const int tid = threadIdx.x;
+  const int slot = tid / A.tps;
+  const int lt = tid - slot * A.tps;  // thread index within slot
+  const bool slot_ok = slot < A.slots;
+  const int ta = lt % A.tilesA;
+  const int tb = lt / A.tilesA;
+  const int a0 = ta * VT_TX, b0 = tb * VT_TY;
+  constexpr bool BWD = (MODE != MODE_FWD);
+
+  // ---- shared memory carve-up
+  float* rs = sm;                                              // [RProws][RP] (BWD only)
+  float* slot_base = rs + (BWD ? A.RProws * A.RP : 0);
+  const int slot_floats = A.slot_floats;
+  float* xin = slot_base + (slot_ok ? slot : 0) * slot_floats;  // [XProws][XP]
+  float* wbs = xin + A.XProws * A.XP;
+  float* wfs = wbs + TT;
+  float* dtab = wfs + TT;                                      // [maxc][maxc]
+  float* rowp = dtab + A.maxc * A.maxc;                        // [T][maxc]
+
+  // ---- zero the slots (halos must be zero), stage R
+  {
+    const int total = A.slots * slot_floats;
+    for (int i = tid; i < total; i += blockDim.x) slot_base[i] = 0.f;
+    if (BWD) {
+      const int nr = A.RProws * A.RP;
+      const float4* src = reinterpret_cast<const float4*>(A.rpad);
+      float4* dst = reinterpret_cast<float4*>(rs);
+      for (int i = tid; i < nr / 4; i += blockDim.x) dst[i] = src[i];
+    }
+  }
+  __syncthreads();
+
+  float hx[VT_TY][VT_TX];
+#pragma unroll
+  for (int y = 0; y < VT_TY; ++y)
+#pragma unroll
+    for (int x = 0; x < VT_TX; ++x) hx[y][x] = 0.f;
+
+  const int h = (A.N - 1) / 2;
+  const int64_t step = (int64_t)gridDim.x * A.slots;
+  for (int64_t base = (int64_t)blockIdx.x * A.slots; base < A.nch; base += step) {
+    const int64_t ch = base + slot;
+    const bool active = slot_ok && ch < A.nch;
+    const int alpha = active ? (int)((ch / A.Z) % A.N) : 0;
+    const int beta = active ? (int)(ch / ((int64_t)A.Z * A.N)) : 0;
+    const int sa = floor_div(alpha - A.u + h, A.N);
+    const int sb = floor_div(beta - A.v + h, A.N);
+
+    // ---- taps of this channel
+    if (active) {
+      for (int i = lt; i < TT; i += A.tps) {
+        if (BWD) wbs[i] = __ldg(A.wb + ch * TT + i);
+        if (MODE != MODE_BWDC) wfs[i] = __ldg(A.wf + ch * TT + i);
+      }
+    }
+    // ---- prefetch the X tile (update / forward-only input)
+    float xv[VT_TY][VT_TX];
+    const float* Xch = A.X + ch * A.plane;
+    if (MODE != MODE_BWDC) {
+#pragma unroll
+      for (int y = 0; y < VT_TY; ++y) {
+        const int b = b0 + y;
+        float4 t4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (active && lt < A.tps && b < A.Lj)
+          t4 = *reinterpret_cast<const float4*>(Xch + (int64_t)b * A.Pa + a0);
+        xv[y][0] = t4.x; xv[y][1] = t4.y; xv[y][2] = t4.z; xv[y][3] = t4.w;
+      }
+    }
+    __syncthreads();
+
+    if (BWD && active) {
+      // D table: rowp[dj][ca] = sum_{di in rngA[sa][ca]} wb[dj][di];
+      //           dtab[cb][ca] = sum_{dj in rngB[sb][cb]} rowp[dj][ca]
+      const int* rA = A.rngA + (sa + 1) * A.maxc * 2;
+      for (int i = lt; i < T * A.maxc; i += A.tps) {
+        const int dj = i / A.maxc, ca = i - dj * A.maxc;
+        const int lo = rA[2 * ca], hi = rA[2 * ca + 1];
+        float s = 0.f;
+        for (int di = lo; di <= hi; ++di) s += wbs[dj * T + di];
+        rowp[i] = s;
+      }
+    }
+    __syncthreads();
+    if (BWD && active) {
+      const int* rB = A.rngB + (sb + 1) * A.maxc * 2;
+      for (int i = lt; i < A.maxc * A.maxc; i += A.tps) {
+        const int cb = i / A.maxc, ca = i - cb * A.maxc;
+        const int lo = rB[2 * cb], hi = rB[2 * cb + 1];
+        float s = 0.f;
+        for (int dj = lo; dj <= hi; ++dj) s += rowp[dj * A.maxc + ca];
+        dtab[i] = s;
+      }
+    }
+    __syncthreads();
+
+    if (active && lt < A.tps) {
+      if (BWD) {
+        float acc[VT_TY][VT_TX];
+#pragma unroll
+        for (int y = 0; y < VT_TY; ++y)
+#pragma unroll
+          for (int x = 0; x < VT_TX; ++x) acc[y][x] = 0.f;
+        const float* rin = rs + (b0 + sb + 1) * A.RP + a0;
+        switch (sa + 1) {
+          case 0: conv_tile<T, 0>(rin, A.RP, wbs, acc); break;
+          case 1: conv_tile<T, 1>(rin, A.RP, wbs, acc); break;
+          default: conv_tile<T, 2>(rin, A.RP, wbs, acc); break;
+        }
+        const int* cA = A.clsA + (sa + 1) * A.Li;
+        const int* cB = A.clsB + (sb + 1) * A.Lj;
+#pragma unroll
+        for (int y = 0; y < VT_TY; ++y) {
+          const int b = b0 + y;
+          if (b >= A.Lj) continue;
+          const int cb = __ldg(cB + b);
+#pragma unroll
+          for (int x = 0; x < VT_TX; ++x) {
+            const int a = a0 + x;
+            if (a >= A.Li) continue;
+            const float c = acc[y][x];
+            if (MODE == MODE_BWDC) {
+              A.Cout[ch * A.plane + (int64_t)b * A.Pa + a] = c;
+            } else {
+              const float d = dtab[cb * A.maxc + __ldg(cA + a)];
+              const float xo = xv[y][x];
+              float xc = xo * c / d;                       // :130  X .* C ./ D
+              if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;     // :132-134 NaN, Inf, < 0
+              float xn = xc * A.w + (1.f - A.w) * xo;       // :136
+              if (xn < 0.f) xn = 0.f;                      // :137
+              xv[y][x] = xn;
+            }
+          }
+        }
+      }
+      if (MODE != MODE_BWDC) {
+#pragma unroll
+        for (int y = 0; y < VT_TY; ++y) {
+          const int b = b0 + y;
+          if (b >= A.Lj) continue;
+          if (MODE == MODE_STEP) {
+            float* dst = A.X + ch * A.plane + (int64_t)b * A.Pa + a0;
+#pragma unroll
+            for (int x = 0; x < VT_TX; ++x)
+              if (a0 + x < A.Li) dst[x] = xv[y][x];
+          }
+#pragma unroll
+          for (int x = 0; x < VT_TX; ++x)
+            if (a0 + x < A.Li) xin[(b + A.q) * A.XP + a0 + x + A.q] = xv[y][x];
+        }
+      }
+    }
+    __syncthreads();
+    if (MODE != MODE_BWDC && (MODE == MODE_FWD || A.do_fwd) && active && lt < A.tps) {
+      conv_tile<T, 0>(xin + b0 * A.XP + a0, A.XP, wfs, hx);
+    }
+    __syncthreads();
+  }
+
+  // ---- forward partials: reduce slots through shared memory, write one plane per CTA
+  if (MODE == MODE_BWDC || (MODE == MODE_STEP && !A.do_fwd)) return;
+  float* red = slot_base;  // reuse: [slots][Lj*Li]
+  const int LL = A.Li * A.Lj;
+  __syncthreads();
+  if (slot_ok && lt < A.tps) {
+#pragma unroll
+    for (int y = 0; y < VT_TY; ++y) {
+      const int b = b0 + y;
+      if (b >= A.Lj) continue;
+#pragma unroll
+      for (int x = 0; x < VT_TX; ++x) {
+        const int a = a0 + x;
+        if (a < A.Li) red[slot * LL + b * A.Li + a] = hx[y][x];
+      }
+    }
+  }
+  __syncthreads();
+  float* out = A.part + (int64_t)blockIdx.x * LL;
+  for (int i = tid; i < LL; i += blockDim.x) {
+    float s = 0.f;
+    for (int k = 0; k < A.slots; ++k) s += red[k * LL + i];
+    out[i] = s;
+  }
+}
+
+#define MLF_INSTANTIATE_VIEW(T)                                                                  \
+  int prepare_view_T##T(size_t smem) {                                                          \
+    cudaError_t e = cudaFuncSetAttribute(k_view<T, MODE_FWD>,                                   \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e == cudaSuccess)                                                                       \
+      e = cudaFuncSetAttribute(k_view<T, MODE_STEP>,                                            \
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
+    if (e == cudaSuccess)                                                                       \
+      e = cudaFuncSetAttribute(k_view<T, MODE_BWDC>,                                            \
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
+    if (e != cudaSuccess)                                                                       \
+      return fail(MLF_ERR_CUDA, std::string("view kernel attributes: ") + cudaGetErrorString(e)); \
+    return MLF_OK;                                                                              \
+  }                                                                                             \
+  int occupancy_view_T##T(int threads, size_t smem, int* blocks) {                              \
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_view<T, MODE_STEP>, \
+                                                                  threads, smem);               \
+    if (e != cudaSuccess)                                                                       \
+      return fail(MLF_ERR_CUDA, std::string("occupancy: ") + cudaGetErrorString(e));            \
+    return MLF_OK;                                                                              \
+  }                                                                                             \
+  int launch_view_T##T(int mode, const ViewArgs& a, int grid, int threads, size_t smem,         \
+                       cudaStream_t st) {                                                       \
+    switch (mode) {                                                                             \
+      case MODE_FWD: k_view<T, MODE_FWD><<<grid, threads, smem, st>>>(a); break;                \
+      case MODE_STEP: k_view<T, MODE_STEP><<<grid, threads, smem, st>>>(a); break;              \
+      default: k_view<T, MODE_BWDC><<<grid, threads, smem, st>>>(a); break;                     \
+    }                                                                                           \
+    cudaError_t e = cudaGetLastError();                                                         \
+    if (e != cudaSuccess)                                                                       \
+      return fail(MLF_ERR_CUDA, std::string("view kernel launch: ") + cudaGetErrorString(e));   \
+    return MLF_OK;                                                                              \
+  }
+
+}  // namespace mlf

@@ -1,0 +1,540 @@
+"""CPU oracle for the MesoLF light-field projector and phase-space Richardson-Lucy solve.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product (``mesolf_gb300``) imports this
+module; only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline /
+reference legs use it, and only as the checker.
+
+It is an FP64 numpy restatement of the reference's own formulation, written against
+the MATLAB sources (paths relative to the reference project root):
+
+* ``src/recon/recon_theory_phase_space_LFM_with_filter.m`` (the RL solve, view
+  weights, NIP filter bank, spiral order, projectors, update, ``sample_filter``),
+* ``src/recon/gen_phasespace_PSF_theory.m`` (phase-space PSF realignment),
+* ``src/recon/conv2FFT.m`` (FFT 'same' convolution),
+* ``src/recon/forwardProjectACC.m`` / ``forwardProjectGPU.m`` (full LFM forward),
+* ``src/cuda/mex_lfm_convolution_vec.cu`` (MEX projector, semantics only).
+
+Everything is computed in the reference's formulation (full-resolution ``conv2 'same'``
+followed by lenslet sampling, sparse up-sampling followed by ``conv2 'same'``), NOT in
+the polyphase form that the CUDA kernels use, so the kernels' index algebra is checked
+independently.
+
+PARITY UNPINNED: the reference ships no golden vectors or known-answer tests for this
+path, and neither MATLAB nor its CUDA MEX (legacy texture references) can run here.
+The oracle is pinned instead by self-consistency checks (FFT path == direct path,
+literal MATLAB-semantics transcription == closed form, adjointness, flux conservation)
+and by committed golden vectors generated from it.
+
+Arrays use MATLAB index order: ``LFIMG[r, c]``, ``X[r, c, z]``, ``H[x, y, a, b, z]``.
+All indices in this file are 0-based unless a comment says "1-based".
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+from numpy.lib.stride_tricks import sliding_window_view
+
+__all__ = [
+    "matlab_round", "normalize_psf", "im_shift3", "gen_phasespace_psf_literal",
+    "gen_phasespace_psf", "phase_space_size", "view_weights", "nip_omegas",
+    "nip_filter_bank", "nip_axis_filters", "ex_size", "gen_spiral", "conv2_same_direct",
+    "conv2fft", "forward_ps", "backward_ps", "rl_update", "freq_filter",
+    "sample_filter", "recon_phase_space", "rl_view_step", "lfm_conv_vec",
+    "lfm_conv_vec_points", "forward_project_full", "sample_filter_plane_index",
+]
+
+
+# ----------------------------------------------------------------------------- helpers
+def matlab_round(x):
+    """MATLAB ``round``: half away from zero."""
+    x = np.asarray(x, dtype=np.float64)
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+# ----------------------------------------------------------------------------- a2
+def normalize_psf(H, Ht):
+    """Per-depth normalisation, ``recon_theory_phase_space_LFM_with_filter.m:13-16``.
+
+    ``H(:,:,:,:,i) = H(:,:,:,:,i) / sum(H(:,:,:,:,i),'all')`` and the same for Ht.
+    """
+    H = np.asarray(H, dtype=np.float64)
+    Ht = np.asarray(Ht, dtype=np.float64)
+    sH = H.sum(axis=(0, 1, 2, 3))
+    sHt = Ht.sum(axis=(0, 1, 2, 3))
+    return H / sH, Ht / sHt
+
+
+# ----------------------------------------------------------------------------- a3
+def phase_space_size(K0, N):
+    """``IMGsize`` and the 0-based crop start, ``gen_phasespace_PSF_theory.m:6-8``."""
+    S = K0 - ((K0 - N) % (2 * N))
+    i1 = int(matlab_round(K0 / 2) - math.trunc(S / 2)) - 1  # 1-based -> 0-based
+    return S, i1
+
+
+def im_shift3(img, SHIFTX, SHIFTY):
+    """Literal transcription of ``gen_phasespace_PSF_theory.m:34-57`` (zero-fill shift)."""
+    eqtol = 1e-10
+    if abs(math.fmod(SHIFTX, 1)) > eqtol or abs(math.fmod(SHIFTY, 1)) > eqtol:
+        raise ValueError("SHIFTX and SHIFTY should be integer numbers")
+    SX = int(matlab_round(SHIFTX))
+    SY = int(matlab_round(SHIFTY))
+    xl, yl = img.shape[0], img.shape[1]
+    new = np.zeros_like(img)
+    if SX >= 0 and SY >= 0:
+        new[SX:, SY:] = img[:xl - SX, :yl - SY]
+    elif SX >= 0 and SY < 0:
+        new[SX:, :yl + SY] = img[:xl - SX, -SY:]
+    elif SX < 0 and SY >= 0:
+        new[:xl + SX, SY:] = img[-SX:, :yl - SY]
+    else:
+        new[:xl + SX, :yl + SY] = img[-SX:, -SY:]
+    return new
+
+
+def gen_phasespace_psf_literal(H, Ht):
+    """Line-by-line transcription of ``gen_phasespace_PSF_theory.m:1-31``.
+
+    MATLAB's column-major ``reshape`` is reproduced with ``order='F'``; ``permute`` with
+    ``transpose``; ``end:-1:1`` with ``[::-1]``.  Slow (python loops) -- small PSFs only.
+    """
+    H = np.asarray(H, dtype=np.float64)
+    Ht = np.asarray(Ht, dtype=np.float64)
+    K0, N, Z = H.shape[0], H.shape[2], H.shape[4]
+    S = K0 - ((K0 - N) % (2 * N))                                   # :6
+    index1 = int(matlab_round(K0 / 2) - math.trunc(S / 2))          # :7 (1-based)
+    index2 = int(matlab_round(K0 / 2) + math.trunc(S / 2))          # :8 (1-based)
+    Hd = np.zeros((S, S, N, N, Z))
+    for z in range(Z):                                              # :10
+        LFtmp = np.zeros((S, S, N, N))
+        for ii in range(1, N + 1):                                  # :13 (1-based)
+            for jj in range(1, N + 1):
+                LFtmp[:, :, ii - 1, jj - 1] = im_shift3(
+                    H[index1 - 1:index2, index1 - 1:index2, ii - 1, jj - 1, z],
+                    ii - (N + 1) / 2, jj - (N + 1) / 2)
+        Hd[:, :, :, :, z] = LFtmp
+    sz = Hd.shape
+    Hd = Hd.reshape((N, sz[0] // N, N, sz[0] // N, N, N, sz[4]), order="F")   # :23
+    Hd = Hd.transpose((0, 2, 1, 3, 4, 5, 6))                                  # :24
+    Hd = Hd[:, :, :, :, ::-1, ::-1, :]                                        # :25
+    Hd = Hd.transpose((0, 1, 4, 2, 5, 3, 6))                                  # :26
+    Hd = Hd.reshape((N, N, sz[0], sz[0], sz[4]), order="F").transpose((2, 3, 0, 1, 4))  # :27
+    Htc = Ht[index1 - 1:index2, index1 - 1:index2, :, :, :]                   # :31
+    return np.ascontiguousarray(Hd), np.ascontiguousarray(Htc)
+
+
+def gen_phasespace_psf(H, Ht):
+    """Closed form of ``gen_phasespace_PSF_theory.m:1-31`` (vectorised).
+
+    ``Hps[p, q, u, v, z] = H[i1+p+u-h, i1+q+v-h, N-1-(p mod N), N-1-(q mod N), z]`` when
+    ``0 <= p+u-h < S`` and ``0 <= q+v-h < S`` (zero otherwise), with ``h=(N-1)/2`` and
+    ``i1`` the 0-based crop start; ``Htc = Ht[i1:i1+S, i1:i1+S]``.  Equal to the literal
+    transcription (checked in the tests).
+    """
+    H = np.asarray(H, dtype=np.float64)
+    Ht = np.asarray(Ht, dtype=np.float64)
+    K0, N, Z = H.shape[0], H.shape[2], H.shape[4]
+    S, i1 = phase_space_size(K0, N)
+    h = (N - 1) // 2
+    p = np.arange(S)
+    Hps = np.zeros((S, S, N, N, Z))
+    src_ab = N - 1 - (p % N)
+    for u in range(N):
+        rp = p + u - h
+        vr = (rp >= 0) & (rp < S)
+        rr = np.clip(rp, 0, S - 1) + i1
+        for v in range(N):
+            rq = p + v - h
+            vq = (rq >= 0) & (rq < S)
+            cc = np.clip(rq, 0, S - 1) + i1
+            vals = H[rr[:, None], cc[None, :], src_ab[:, None], src_ab[None, :], :]
+            vals = vals * (vr[:, None] & vq[None, :])[:, :, None]
+            Hps[:, :, u, v, :] = vals
+    Htc = Ht[i1:i1 + S, i1:i1 + S, :, :, :].copy()
+    return Hps, Htc
+
+
+# ----------------------------------------------------------------------------- a4
+def view_weights(Hps):
+    """View weights, ``recon_theory_phase_space_LFM_with_filter.m:20,30-38``."""
+    weight_cut = 0.2
+    with np.errstate(invalid="ignore", divide="ignore"):
+        w = Hps.sum(axis=(0, 1, 4))                      # :30 sum over x, y, z
+        w[np.isnan(w)] = 0                               # :31
+        w = w / w.sum()                                  # :32
+        w = w - w.min()                                  # :33
+        w = w / w.max()                                  # :36
+        w[w < weight_cut] = 0                            # :37 (NaN < 0.2 is false)
+        w = w * 0.3                                      # :38
+    return w
+
+
+# ----------------------------------------------------------------------------- a5
+def nip_omegas(Z, N):
+    """``omega_NIP_array`` of ``recon_theory_phase_space_LFM_with_filter.m:21-26,54-56``."""
+    omega_NIP = N - 7
+    R = int(math.ceil(Z / 3))
+    if R % 2 == 1:
+        R += 1
+    nb = 3 * R
+    axis = np.arange(1, nb + 1, dtype=np.float64) - nb / 2
+    om = omega_NIP * np.exp(-(axis / 100.0 * 2 * np.sqrt(np.log(2))) ** 2)
+    om[om < 0.2] = 0.2
+    return om
+
+
+def nip_filter_bank(size_h, size_w, Z, N):
+    """Literal filter bank, ``recon_theory_phase_space_LFM_with_filter.m:44-61``.
+
+    ``F_i = |fftshift(fft2(exp(-((xx/w_i)^2+(yy/w_i)^2))))| / max`` on the grid
+    ``x=(1:size_h)-size_h/2``, ``y=(1:size_w)-size_w/2``.  Returns (size_h, size_w, 3R).
+    """
+    om = nip_omegas(Z, N)
+    x = np.arange(1, size_h + 1, dtype=np.float64) - size_h / 2
+    y = np.arange(1, size_w + 1, dtype=np.float64) - size_w / 2
+    yy, xx = np.meshgrid(y, x)
+    F = np.zeros((size_h, size_w, om.size))
+    for i, w in enumerate(om):
+        g = np.exp(-((xx / w) ** 2 + (yy / w) ** 2))
+        buf = np.abs(np.fft.fftshift(np.fft.fft2(g)))
+        F[:, :, i] = buf / buf.max()
+    return F
+
+
+def nip_axis_filters(size_h, size_w, Z, N):
+    """Separable factors of the filter bank: ``F_i = fftshift(ax_i[:,None] * ay_i[None,:])``.
+
+    The Gaussian is separable, so ``|fft2(g)| = |fft(gx)| (x) |fft(gy)|`` and the max is the
+    product of the 1-D maxima.  Returned UNSHIFTED (frequency 0 first), each normalised
+    to max 1.  Used to cross-check the literal bank.
+    """
+    om = nip_omegas(Z, N)
+    x = np.arange(1, size_h + 1, dtype=np.float64) - size_h / 2
+    y = np.arange(1, size_w + 1, dtype=np.float64) - size_w / 2
+    ax = np.zeros((om.size, size_h))
+    ay = np.zeros((om.size, size_w))
+    for i, w in enumerate(om):
+        a = np.abs(np.fft.fft(np.exp(-(x / w) ** 2)))
+        b = np.abs(np.fft.fft(np.exp(-(y / w) ** 2)))
+        ax[i] = a / a.max()
+        ay[i] = b / b.max()
+    return ax, ay
+
+
+def sample_filter_plane_index(Z, nb):
+    """For each plane (0-based) the 0-based filter-bank index, or -1 if the plane is
+    passed through; ``recon_theory_phase_space_LFM_with_filter.m:224-231``."""
+    half_z = int(matlab_round(Z / 2))
+    idx = np.full(Z, -1, dtype=np.int64)
+    for z1 in range(1, Z + 1):                           # 1-based plane index
+        if z1 >= half_z - nb / 2 + 1 and z1 <= half_z + nb / 2:
+            idx[z1 - 1] = int(z1 - half_z + nb / 2) - 1
+    return idx
+
+
+# ----------------------------------------------------------------------------- a7
+def ex_size(xsize, S):
+    """FFT grid, ``recon_theory_phase_space_LFM_with_filter.m:78-82``."""
+    mmid = S // 2
+    out = []
+    for n in xsize:
+        e = n + mmid
+        out.append(int(min(2 ** math.ceil(math.log2(e)), 128 * math.ceil(e / 128))))
+    return tuple(out)
+
+
+# ----------------------------------------------------------------------------- a8
+def gen_spiral(Nnum):
+    """Literal transcription of ``gen_spiral``, ``…_with_filter.m:156-188``.
+
+    Returns 1-based (i_index, j_index) as MATLAB does.  ``mode(Nnum)`` of a scalar is the
+    scalar itself, so the ``== 0`` branch never fires for Nnum > 0.
+    """
+    if Nnum == 0:
+        loop_n = Nnum / 2
+    else:
+        loop_n = (Nnum + 1) / 2
+    loop_n = int(loop_n) if float(loop_n).is_integer() else int(math.floor(loop_n))
+    i_index = np.zeros(Nnum * Nnum, dtype=np.int64)
+    j_index = np.zeros(Nnum * Nnum, dtype=np.int64)
+    start = 1
+    for k in range(1, loop_n + 1):
+        cs = Nnum - 2 * (k - 1)
+        bias = k - 1
+        if cs > 1:
+            i_new = np.concatenate([np.arange(1, cs + 1), cs * np.ones(cs - 1, dtype=np.int64),
+                                    np.arange(cs - 1, 0, -1), np.ones(cs - 2, dtype=np.int64)])
+            j_new = np.concatenate([np.ones(cs, dtype=np.int64), np.arange(2, cs + 1),
+                                    cs * np.ones(cs - 1, dtype=np.int64), np.arange(cs - 1, 1, -1)])
+            n = 4 * (cs - 1)
+            i_index[start - 1:start - 1 + n] = i_new + bias
+            j_index[start - 1:start - 1 + n] = j_new + bias
+            start += n
+        else:
+            i_index[start - 1] = 1 + bias
+            j_index[start - 1] = 1 + bias
+    return i_index, j_index
+
+
+# ----------------------------------------------------------------------------- a10
+def conv2_same_direct(x, m):
+    """MATLAB ``conv2(x, m, 'same')`` for odd-sized m, by direct summation (FP64)."""
+    x = np.asarray(x, dtype=np.float64)
+    m = np.asarray(m, dtype=np.float64)
+    Sx, Sy = m.shape
+    mx, my = Sx // 2, Sy // 2
+    xp = np.zeros((x.shape[0] + Sx - 1, x.shape[1] + Sy - 1))
+    xp[mx:mx + x.shape[0], my:my + x.shape[1]] = x
+    win = sliding_window_view(xp, (Sx, Sy))
+    return np.einsum("ijpq,pq->ij", win, m[::-1, ::-1], optimize=True)
+
+
+def conv2fft(x, m, exsize):
+    """Transcription of ``conv2FFT.m:1-22`` with ``exindex(...,'circular')`` and
+    ``zeroPad`` (``:246-280``): pad both to ``exsize``, circularly re-centre the kernel
+    so its ``floor(size/2)`` element sits at the origin, multiply spectra, crop."""
+    x = np.asarray(x, dtype=np.float64)
+    m = np.asarray(m, dtype=np.float64)
+    E = tuple(int(e) for e in exsize)
+    xs = x.shape
+    mmid = (m.shape[0] // 2, m.shape[1] // 2)
+    xp = np.zeros(E)
+    xp[:xs[0], :xs[1]] = x
+    mp = np.zeros(E)
+    mp[:m.shape[0], :m.shape[1]] = m
+    r_idx = (np.arange(mmid[0] + 1, mmid[0] + E[0] + 1) - 1) % E[0]   # exindex circular
+    c_idx = (np.arange(mmid[1] + 1, mmid[1] + E[1] + 1) - 1) % E[1]
+    m1 = mp[np.ix_(r_idx, c_idx)]
+    y = np.real(np.fft.ifft2(np.fft.fft2(xp) * np.fft.fft2(m1)))
+    return y[:xs[0], :xs[1]]
+
+
+# ----------------------------------------------------------------------------- a9
+def forward_ps(h_uv, X, N):
+    """``forwardProjectGPU_phasespace_theory`` (``…_with_filter.m:243-249``; CPU twin
+    ``:191-198``): ``P = sum_z conv2(X_z, h_z, 'same')``, sampled at ``(N+1)/2:N:end``.
+
+    Only the sampled outputs are evaluated, each by a direct FP64 dot product.
+    """
+    X = np.asarray(X, dtype=np.float64)
+    h_uv = np.asarray(h_uv, dtype=np.float64)
+    Xr, Xc, Z = X.shape
+    S = h_uv.shape[0]
+    m = S // 2
+    c0 = (N + 1) // 2 - 1
+    Xp = np.zeros((Xr + 2 * m, Xc + 2 * m, Z))
+    Xp[m:m + Xr, m:m + Xc, :] = X
+    win = sliding_window_view(Xp, (S, S), axis=(0, 1))[c0::N, c0::N]   # (Li, Lj, Z, S, S)
+    hf = h_uv[::-1, ::-1, :]
+    return np.einsum("ijzpq,pqz->ij", win, hf, optimize=True)
+
+
+# ----------------------------------------------------------------------------- a12/a13
+def backward_ps(t_uv, R, u, v, N):
+    """``backwardProjectGPU_phasespace_theory`` (``…_with_filter.m:211-220``; CPU twin
+    ``:201-208``): ``B = 0; B(u:N:end, v:N:end) = R; C_z = conv2(B, t_z, 'same')``.
+
+    ``u, v`` are 0-based.  B is non-zero only on the lattice, so ``conv2`` is evaluated as
+    a scatter of shifted kernel copies -- exact FP64.
+    """
+    t_uv = np.asarray(t_uv, dtype=np.float64)
+    R = np.asarray(R, dtype=np.float64)
+    Li, Lj = R.shape
+    S, Z = t_uv.shape[0], t_uv.shape[2]
+    m = S // 2
+    Xr, Xc = Li * N, Lj * N
+    Cp = np.zeros((Xr + S - 1, Xc + S - 1, Z))
+    for i in range(Li):
+        r0 = u + N * i
+        for j in range(Lj):
+            val = R[i, j]
+            if val != 0.0:
+                c0 = v + N * j
+                Cp[r0:r0 + S, c0:c0 + S, :] += val * t_uv
+    return Cp[m:m + Xr, m:m + Xc, :]
+
+
+# ----------------------------------------------------------------------------- a14
+def rl_update(X, C, D, w):
+    """Multiplicative update, ``…_with_filter.m:130-137``."""
+    with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
+        Xc = X * C / D
+    Xc[np.isnan(Xc)] = 0
+    Xc[np.isinf(Xc)] = 0
+    Xc[Xc < 0] = 0
+    Xn = Xc * w + (1 - w) * X
+    Xn[Xn < 0] = 0
+    return Xn
+
+
+# ----------------------------------------------------------------------------- a15
+def freq_filter(image, filt):
+    """``freq_filter``, ``…_with_filter.m:251-254``."""
+    image_f = np.fft.fftshift(np.fft.fft2(image))
+    return np.real(np.fft.ifft2(np.fft.ifftshift(image_f * filt)))
+
+
+def sample_filter(X, F):
+    """``sample_filter``, ``…_with_filter.m:222-240`` (flux-preserving low-pass)."""
+    X = np.asarray(X, dtype=np.float64)
+    Z = X.shape[2]
+    nb = F.shape[2]
+    idx = sample_filter_plane_index(Z, nb)
+    out = X.copy()
+    for z in range(Z):
+        if idx[z] >= 0:
+            img = X[:, :, z]
+            s0 = img.sum()
+            buf = freq_filter(img, F[:, :, idx[z]])
+            out[:, :, z] = s0 * buf / buf.sum()
+    return out
+
+
+# ----------------------------------------------------------------------------- a1
+def _ratio(LF_sub, HX):
+    with np.errstate(invalid="ignore", divide="ignore"):
+        R = LF_sub / HX
+    R[~np.isfinite(R)] = 0
+    return R
+
+
+def rl_view_step(X, LFIMG, Hps, Htc, u, v, w, N):
+    """One view of the inner loop (``…_with_filter.m:109-137``), 0-based (u, v)."""
+    HX = forward_ps(Hps[:, :, u, v, :], X, N)
+    R = _ratio(LFIMG[u::N, v::N], HX)
+    C = backward_ps(Htc[:, :, u, v, :], R, u, v, N)
+    D = backward_ps(Htc[:, :, u, v, :], np.ones_like(R), u, v, N)
+    return rl_update(X, C, D, w)
+
+
+def recon_phase_space(LFIMG, H, Ht, maxIter, X0=None, callback=None):
+    """``recon_theory_phase_space_LFM_with_filter`` (``…_with_filter.m:10-151``), FP64.
+
+    ``X0`` (optional) replaces the flat initial guess of ``:72-73`` (warm start).
+    ``callback(it, X)`` is called after each iteration's ``sample_filter``.
+    """
+    LFIMG = np.asarray(LFIMG, dtype=np.float64)
+    Hn, Htn = normalize_psf(H, Ht)                                   # :13-16
+    Hps, Htc = gen_phasespace_psf(Hn, Htn)                           # :17
+    N = Hps.shape[2]
+    w = view_weights(Hps)                                            # :20-40
+    F = nip_filter_bank(LFIMG.shape[0], LFIMG.shape[1], Hps.shape[4], N)   # :44-61
+    Z = Hps.shape[4]
+    if X0 is None:
+        X = np.ones((LFIMG.shape[0], LFIMG.shape[1], Z))
+        X = X / X.sum() * LFIMG.sum()                                # :72-73
+    else:
+        X = np.asarray(X0, dtype=np.float64).copy()
+    i_idx, j_idx = gen_spiral(N)                                     # :95
+    for it in range(maxIter):                                        # :98
+        for u2 in range(1, N + 1):
+            for v2 in range(1, N + 1):
+                u = i_idx[(u2 - 1) * N + v2 - 1] - 1
+                v = j_idx[(u2 - 1) * N + v2 - 1] - 1
+                if w[u, v] == 0:
+                    continue
+                X = rl_view_step(X, LFIMG, Hps, Htc, u, v, w[u, v], N)
+        X = sample_filter(X, F)                                      # :142
+        if callback is not None:
+            callback(it, X)
+    return X
+
+
+# ----------------------------------------------------------------------------- a18
+def _conv_vec_padded(bitmap, kw):
+    """Zero-pad a (W, H, n) bitmap by kw//2 so that reference edge clipping
+    (``mex_lfm_convolution_vec.cu:55-78``) becomes plain zero padding.
+
+    For even kw the reference's ``kernel_end`` clip never reaches the last input column /
+    row (``bitmap_endx = x + kw/2 + 1``), so those are zeroed to keep its semantics."""
+    W, Hh, n = bitmap.shape
+    hk = kw // 2
+    b = np.asarray(bitmap, dtype=np.float64).copy()
+    if kw % 2 == 0:
+        b[W - 1, :, :] = 0
+        b[:, Hh - 1, :] = 0
+    P = np.zeros((W + kw, Hh + kw, n))
+    P[hk:hk + W, hk:hk + Hh, :] = b
+    return P
+
+
+def lfm_conv_vec(bitmap, kernels):
+    """Semantics of ``mex_lfm_convolution_vec`` (``src/cuda/mex_lfm_convolution_vec.cu``
+    ``:43-266`` kernel, ``:276-421`` host), FP64.
+
+    ``out(x, y, i) = sum_{kx,ky} in(x+kx-kw/2, y+ky-kw/2, i) * K(kx, ky, x mod 15, y mod 15)``
+    (0-based; ``kw/2`` integer division), zero outside the bitmap.  ``bitmap`` is (W, H)
+    or (W, H, n); ``kernels`` is (kw, kw, 15, 15).  Small shapes only.
+    """
+    bm = np.asarray(bitmap, dtype=np.float64)
+    squeeze = bm.ndim == 2
+    if squeeze:
+        bm = bm[:, :, None]
+    K = np.asarray(kernels, dtype=np.float64)
+    kw = K.shape[0]
+    nk = K.shape[2]
+    W, Hh, n = bm.shape
+    P = _conv_vec_padded(bm, kw)
+    out = np.zeros((W, Hh, n))
+    win = sliding_window_view(P, (kw, kw), axis=(0, 1))              # (W+1, H+1, n, kw, kw)
+    for px in range(nk):
+        for py in range(nk):
+            xs = np.arange(px, W, nk)
+            ys = np.arange(py, Hh, nk)
+            if xs.size == 0 or ys.size == 0:
+                continue
+            sub = win[px:W:nk, py:Hh:nk]                              # (|xs|, |ys|, n, kw, kw)
+            out[np.ix_(xs, ys)] = np.einsum("xyipq,pq->xyi", sub, K[:, :, px, py], optimize=True)
+    return out[:, :, 0] if squeeze else out
+
+
+def lfm_conv_vec_points(bitmap, kernels, pts):
+    """``lfm_conv_vec`` evaluated only at the (x, y, i) triples ``pts`` -- for large
+    shapes where the full FP64 evaluation is too slow."""
+    bm = np.asarray(bitmap, dtype=np.float64)
+    if bm.ndim == 2:
+        bm = bm[:, :, None]
+    K = np.asarray(kernels, dtype=np.float64)
+    kw = K.shape[0]
+    nk = K.shape[2]
+    P = _conv_vec_padded(bm, kw)
+    out = np.empty(len(pts))
+    for t, (x, y, i) in enumerate(pts):
+        out[t] = np.sum(P[x:x + kw, y:y + kw, i] * K[:, :, x % nk, y % nk])
+    return out
+
+
+# ----------------------------------------------------------------------------- a17
+def forward_project_full(H, vol, CAindex=None):
+    """Full LFM forward projector, ``forwardProjectACC.m:1-18`` / ``forwardProjectGPU.m``:
+    ``out = sum_{a,b,z} conv2(vol_z .* 1[(a,b) phase], H(:,:,a,b,z), 'same')``.
+
+    ``CAindex`` (Z x 2, 1-based inclusive, as in ``forwardProjectACC``) crops the PSF per
+    plane; None uses the whole PSF (``forwardProjectGPU``).  FFT evaluation in FP64.
+    """
+    H = np.asarray(H, dtype=np.float64)
+    vol = np.asarray(vol, dtype=np.float64)
+    N = H.shape[2]
+    Xr, Xc, Z = vol.shape
+    out = np.zeros((Xr, Xc))
+    for z in range(Z):
+        if CAindex is not None:
+            lo, hi = int(CAindex[z][0]) - 1, int(CAindex[z][1])
+            Hz = H[lo:hi, lo:hi, :, :, z]
+        else:
+            Hz = H[:, :, :, :, z]
+        S = Hz.shape[0]
+        m = S // 2
+        E = (Xr + S - 1, Xc + S - 1)
+        acc = np.zeros((E[0], E[1] // 2 + 1), dtype=np.complex128)
+        for a in range(N):
+            for b in range(N):
+                ts = np.zeros((Xr, Xc))
+                ts[a::N, b::N] = vol[a::N, b::N, z]
+                if not ts.any():
+                    continue
+                acc += np.fft.rfft2(ts, E) * np.fft.rfft2(Hz[:, :, a, b], E)
+        full = np.fft.irfft2(acc, E)
+        out += full[m:m + Xr, m:m + Xc]
+    return out

@@ -1,0 +1,76 @@
+"""The C-ABI library builds, loads and exports every symbol the header declares; host-side
+argument validation (no GPU compute)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "mesolf_lf.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mlf_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_lists_entry_points():
+    fns = header_functions()
+    assert "mlf_conv_vec" in fns and "mlf_solver_run" in fns and len(fns) >= 14
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from mesolf_gb300 import _lib
+    for name in header_functions():
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, f"{name} missing from the ctypes signature table"
+    assert lib.mlf_version() == 1
+
+
+def _err(lib):
+    buf = ctypes.create_string_buffer(512)
+    code = lib.mlf_last_error(buf, 512)
+    return code, buf.value.decode()
+
+
+def test_conv_vec_rejects_like_the_mex(lib):
+    a = np.zeros(16, np.float32)
+    p = a.ctypes.data
+    # kw above kernel_width_limit (mex_lfm_convolution_vec.cu:344)
+    assert lib.mlf_conv_vec(p, 4, 4, 1, p, 342, 15, p, None) == 1
+    assert "kernel_width_limit" in _err(lib)[1]
+    # bitmap_n < 1 (:332)
+    assert lib.mlf_conv_vec(p, 4, 4, 0, p, 3, 15, p, None) == 1
+    assert "at least 1" in _err(lib)[1]
+    # null pointers, wrong kernel grid
+    assert lib.mlf_conv_vec(None, 4, 4, 1, p, 3, 15, p, None) == 1
+    assert lib.mlf_conv_vec(p, 4, 4, 1, p, 3, 13, p, None) == 1
+    assert _err(lib)[0] == 1
+
+
+def test_psf_create_rejects_bad_shapes(lib):
+    a = np.zeros(16, np.float32)
+    p = a.ctypes.data
+    h = ctypes.c_void_p()
+    assert lib.mlf_psf_create(p, p, 60, 15, 3, ctypes.byref(h), None) == 1   # even K0
+    assert lib.mlf_psf_create(p, p, 61, 14, 3, ctypes.byref(h), None) == 1   # even N
+    assert lib.mlf_psf_create(p, p, 61, 15, 0, ctypes.byref(h), None) == 1   # no planes
+    # S/N = 19 (K0 = 285) is beyond the supported tap counts
+    assert lib.mlf_psf_create(p, p, 285, 15, 1, ctypes.byref(h), None) == 4
+    assert "supported" in _err(lib)[1]
+    assert lib.mlf_psf_create(None, p, 61, 15, 1, ctypes.byref(h), None) == 1
+
+
+def test_solver_rejects_null(lib):
+    h = ctypes.c_void_p()
+    assert lib.mlf_solver_create(None, 165, 165, ctypes.byref(h)) == 1
+    assert lib.mlf_solver_run(None, None, 1, 0, None, None, None, None) == 1
+
+
+def test_python_api_no_cpu_fallback():
+    from mesolf_gb300 import MesoLFError, recon_theory_phase_space_LFM_with_filter
+    with pytest.raises(MesoLFError):
+        recon_theory_phase_space_LFM_with_filter(np.zeros((15, 15)), np.zeros((15, 15, 15, 15, 1)),
+                                                 np.zeros((15, 15, 15, 15, 1)), 1, gpuFlag=False)

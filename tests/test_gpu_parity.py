@@ -1,0 +1,165 @@
+"""GPU parity of the CUDA path (through the C ABI) against the FP64 CPU oracle.
+
+Tolerance: relative L2 <= 1e-4 in FP32 (the bar the projector and RL loop must meet
+against the reference's own formulation); the FP32 kernels land near 1e-6.
+"""
+import numpy as np
+import pytest
+
+from oracle import mesolf_ref as R
+from mesolf_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+RTOL_L2 = 1e-4
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def to_dev(x):
+    import torch
+    from mesolf_gb300.api import _fortran
+    t = torch.as_tensor(np.ascontiguousarray(np.asarray(x, dtype=np.float32)))
+    return _fortran(t.cuda())[0]
+
+
+def to_host(t):
+    return t.detach().cpu().numpy()
+
+
+# ------------------------------------------------------------------------------ MEX
+@pytest.mark.parametrize("W,H,n,kw", [(40, 33, 3, 7), (31, 46, 2, 16), (15, 15, 1, 1),
+                                      (64, 50, 2, 61), (90, 77, 1, 120)])
+def test_conv_vec_matches_oracle(cuda, W, H, n, kw):
+    from mesolf_gb300 import mex_lfm_convolution_vec
+    rng = np.random.default_rng(W * 7 + kw)
+    bm = rng.random((W, H, n)).astype(np.float32)
+    K = rng.random((kw, kw, 15, 15)).astype(np.float32)
+    out = to_host(mex_lfm_convolution_vec(to_dev(bm), to_dev(K)))
+    ref = R.lfm_conv_vec(bm, K)
+    assert out.shape == (W, H, n)
+    assert rel_l2(out, ref) <= 1e-6
+
+
+def test_conv_vec_2d_bitmap_and_host_arrays(cuda):
+    from mesolf_gb300 import mex_lfm_convolution_vec
+    rng = np.random.default_rng(11)
+    bm = rng.random((37, 29)).astype(np.float32)
+    K = rng.random((9, 9, 15, 15)).astype(np.float32)
+    out_host = mex_lfm_convolution_vec(bm, K)            # numpy in -> numpy out (staged)
+    out_dev = to_host(mex_lfm_convolution_vec(to_dev(bm), to_dev(K)))
+    ref = R.lfm_conv_vec(bm, K)
+    assert out_host.shape == (37, 29)
+    np.testing.assert_array_equal(out_host, out_dev)
+    assert rel_l2(out_host, ref) <= 1e-6
+
+
+def test_conv_vec_fixture_shape_sampled(cuda):
+    """The reference's own MEX input shape (vols_slice.mat: 376 x 376 x 77, ~0.6% non-zero)
+    with a 241-wide synthetic kernel; checked at 3000 sampled output pixels."""
+    from mesolf_gb300 import mex_lfm_convolution_vec
+    rng = np.random.default_rng(12)
+    bm = np.zeros((376, 376, 77), np.float32)
+    nz = rng.choice(bm.size, 72050, replace=False)
+    bm.reshape(-1, order="F")[nz] = rng.uniform(0.0, 1.0859, nz.size).astype(np.float32)
+    bm = np.asfortranarray(bm)
+    K = np.asfortranarray(rng.random((241, 241, 15, 15)).astype(np.float32))
+    out = to_host(mex_lfm_convolution_vec(to_dev(bm), to_dev(K)))
+    pts = [(int(x), int(y), int(i)) for x, y, i in zip(rng.integers(0, 376, 3000), rng.integers(0, 376, 3000),
+                                                        rng.integers(0, 77, 3000))]
+    ref = R.lfm_conv_vec_points(bm, K, pts)
+    got = np.array([out[x, y, i] for x, y, i in pts])
+    assert rel_l2(got, ref) <= 1e-5
+
+
+# ------------------------------------------------------------------------------ projectors
+PROJ_CASES = [  # (lenslets, K0, Z): tap counts T = S/N = 3, 5, 7, 15
+    ((5, 4), 61, 3), ((7, 6), 91, 3), ((4, 5), 121, 2), ((6, 5), 231, 2), ((11, 11), 61, 4)]
+
+
+@pytest.mark.parametrize("lenslets,K0,Z", PROJ_CASES)
+def test_forward_backward_views_match_oracle(cuda, lenslets, K0, Z):
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver
+    w = synth.small_config(lenslets=lenslets, K0=K0, Z=Z)
+    H, Ht = w.psf()
+    rng = np.random.default_rng(K0)
+    Xr, Xc = w.image_shape
+    vol = rng.random((Xr, Xc, Z)).astype(np.float32)
+    Hn, Htn = R.normalize_psf(H, Ht)
+    Hps, Htc = R.gen_phasespace_psf(Hn, Htn)
+    psf = PhaseSpacePSF(H, Ht)
+    s = RLSolver(psf, (Xr, Xc))
+    for (u, v) in [(7, 7), (0, 0), (14, 3), (2, 12)]:
+        hx = to_host(s.forward_view(to_dev(vol), u, v))
+        ref = R.forward_ps(Hps[:, :, u, v, :], vol.astype(np.float64), 15)
+        assert rel_l2(hx, ref) <= 1e-6, (u, v)
+        proj = rng.random(lenslets).astype(np.float32)
+        c = to_host(s.backward_view(to_dev(proj), u, v))
+        refc = R.backward_ps(Htc[:, :, u, v, :], proj.astype(np.float64), u, v, 15)
+        assert rel_l2(c, refc) <= 1e-6, (u, v)
+    s.close()
+    psf.close()
+
+
+def test_psf_weights_match_oracle(cuda):
+    from mesolf_gb300 import PhaseSpacePSF
+    w = synth.small_config(lenslets=(3, 3), K0=91, Z=5)
+    H, Ht = w.psf()
+    psf = PhaseSpacePSF(H, Ht)
+    Hn, Htn = R.normalize_psf(H, Ht)
+    Hps, _ = R.gen_phasespace_psf(Hn, Htn)
+    ref = R.view_weights(Hps)
+    np.testing.assert_allclose(psf.weights, ref, rtol=1e-12, atol=1e-15)
+    assert ((psf.weights == 0) == (ref == 0)).all()
+
+
+# ------------------------------------------------------------------------------ RL solve
+RL_CASES = [((5, 4), 61, 3, 2), ((4, 6), 91, 5, 2), ((3, 3), 231, 3, 1), ((8, 7), 61, 7, 3)]
+
+
+@pytest.mark.parametrize("lenslets,K0,Z,iters", RL_CASES)
+def test_rl_solve_matches_oracle(cuda, lenslets, K0, Z, iters):
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver
+    w = synth.small_config(lenslets=lenslets, K0=K0, Z=Z, iters=iters)
+    H, Ht = w.psf()
+    LF = w.measured(H, w.volume())
+    ref = R.recon_phase_space(LF, H, Ht, iters)
+    psf = PhaseSpacePSF(H, Ht)
+    s = RLSolver(psf, LF.shape)
+    got = to_host(s.run(to_dev(LF), iters))
+    assert got.shape == ref.shape
+    assert rel_l2(got, ref) <= RTOL_L2
+    assert s.last_stats["n_views"] == int((psf.weights > 0).sum())
+    # host arrays through the same entry point give the same bits
+    got_h = s.run(LF, iters)
+    np.testing.assert_array_equal(got_h, got)
+    s.close()
+    psf.close()
+
+
+def test_rl_warm_start_matches_oracle(cuda):
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver
+    w = synth.small_config(lenslets=(5, 5), K0=61, Z=3)
+    H, Ht = w.psf()
+    LF = w.measured(H, w.volume())
+    X0 = np.random.default_rng(3).uniform(0.5, 1.5, (75, 75, 3)).astype(np.float32)
+    ref = R.recon_phase_space(LF, H, Ht, 1, X0=X0.astype(np.float64))
+    psf = PhaseSpacePSF(H, Ht)
+    s = RLSolver(psf, LF.shape)
+    got = to_host(s.run(to_dev(LF), 1, warm_start=to_dev(X0)))
+    assert rel_l2(got, ref) <= RTOL_L2
+
+
+def test_reference_signature_entry_point(cuda):
+    from mesolf_gb300 import recon_theory_phase_space_LFM_with_filter
+    w = synth.small_config(lenslets=(4, 4), K0=61, Z=3)
+    H, Ht = w.psf()
+    LF = w.measured(H, w.volume())
+    got = recon_theory_phase_space_LFM_with_filter(LF, H, Ht, 1, True, 1)
+    ref = R.recon_phase_space(LF, H, Ht, 1)
+    assert got.dtype == np.float64 and got.shape == ref.shape
+    assert rel_l2(got, ref) <= RTOL_L2

@@ -1,0 +1,185 @@
+"""Pins of the CPU oracle (no GPU).
+
+The reference ships no golden vectors for this path and cannot run here (no MATLAB; its
+MEX uses removed texture references), so the oracle is pinned by self-consistency:
+literal MATLAB-semantics transcriptions against closed forms, FFT path against direct
+sums, adjointness, flux conservation.
+"""
+import numpy as np
+import pytest
+
+from oracle import mesolf_ref as R
+from mesolf_gb300 import synth
+
+
+@pytest.mark.parametrize("K0,Z", [(61, 2), (45, 2), (75, 1), (91, 1)])
+def test_phasespace_closed_form_matches_literal(K0, Z):
+    z = np.arange(Z) - Z // 2
+    H, Ht = synth.make_psf(K0, 15, z, seed=3)
+    Hn, Htn = R.normalize_psf(H, Ht)
+    A, At = R.gen_phasespace_psf_literal(Hn, Htn)
+    B, Bt = R.gen_phasespace_psf(Hn, Htn)
+    assert A.shape == B.shape
+    np.testing.assert_array_equal(A, B)
+    np.testing.assert_array_equal(At, Bt)
+
+
+def test_phase_space_size():
+    # gen_phasespace_PSF_theory.m:6-8 for the workloads' PSF sides
+    assert R.phase_space_size(61, 15) == (45, 8)
+    assert R.phase_space_size(231, 15) == (225, 3)
+    assert R.phase_space_size(255, 15) == (255, 0)
+    assert R.phase_space_size(241, 15)[0] == 225
+
+
+def test_normalize_sums_to_one():
+    H, Ht = synth.make_psf(61, 15, [-2, 0, 3], seed=1)
+    Hn, Htn = R.normalize_psf(H, Ht)
+    np.testing.assert_allclose(Hn.sum(axis=(0, 1, 2, 3)), 1.0, rtol=1e-13)
+    np.testing.assert_allclose(Htn.sum(axis=(0, 1, 2, 3)), 1.0, rtol=1e-13)
+
+
+def test_spiral_order():
+    i, j = R.gen_spiral(15)
+    pairs = list(zip(i.tolist(), j.tolist()))
+    assert len(set(pairs)) == 225 and min(i) == 1 and max(i) == 15
+    # outer ring: down the first column, along the last row, up the last column, back
+    assert pairs[:15] == [(k, 1) for k in range(1, 16)]
+    assert pairs[15:29] == [(15, k) for k in range(2, 16)]
+    assert pairs[29:43] == [(k, 15) for k in range(14, 0, -1)]
+    assert pairs[43:56] == [(1, k) for k in range(14, 1, -1)]
+    assert pairs[-1] == (8, 8)
+    i3, j3 = R.gen_spiral(3)
+    assert list(zip(i3, j3)) == [(1, 1), (2, 1), (3, 1), (3, 2), (3, 3), (2, 3), (1, 3), (1, 2), (2, 2)]
+
+
+@pytest.mark.parametrize("shape,S", [((60, 45), 45), ((33, 50), 15), ((165, 165), 45)])
+def test_conv2fft_equals_direct(shape, S):
+    rng = np.random.default_rng(0)
+    x = rng.random(shape)
+    m = rng.random((S, S))
+    d = R.conv2_same_direct(x, m)
+    f = R.conv2fft(x, m, R.ex_size(shape, S))
+    assert np.abs(d - f).max() <= 1e-12 * np.abs(d).max()
+
+
+def test_exsize():
+    assert R.ex_size((165, 165), 45) == (256, 256)
+    assert R.ex_size((1005, 1005), 225) == (1152, 1152)
+
+
+def test_filter_bank_separable_and_omegas():
+    F = R.nip_filter_bank(45, 30, 5, 15)
+    ax, ay = R.nip_axis_filters(45, 30, 5, 15)
+    for i in range(F.shape[2]):
+        np.testing.assert_allclose(F[:, :, i], np.fft.fftshift(np.outer(ax[i], ay[i])), atol=1e-15)
+    om = R.nip_omegas(51, 15)
+    assert om.size == 54 and om.max() == 8.0 and om.min() > 6.5
+    assert R.nip_omegas(21, 15).size == 24
+
+
+def test_sample_filter_flux_and_plane_map():
+    rng = np.random.default_rng(1)
+    X = rng.random((45, 30, 7)) + 0.1
+    F = R.nip_filter_bank(45, 30, 7, 15)
+    Y = R.sample_filter(X, F)
+    np.testing.assert_allclose(Y.sum(axis=(0, 1)), X.sum(axis=(0, 1)), rtol=1e-12)
+    idx = R.sample_filter_plane_index(7, F.shape[2])
+    assert (idx >= 0).all()
+    # planes outside the bank's range pass through (a deep stack, a narrow bank)
+    idx2 = R.sample_filter_plane_index(40, 6)
+    assert (idx2 < 0).sum() == 34 and list(idx2[idx2 >= 0]) == list(range(6))
+
+
+def test_sample_filter_odd_size_shift_convention():
+    """fftshift / ifftshift are not inverses of each other's roles for odd sizes; the
+    composition used by freq_filter must equal filtering by ifftshift(F)."""
+    rng = np.random.default_rng(2)
+    img = rng.random((15, 9))
+    F = rng.random((15, 9))
+    a = R.freq_filter(img, F)
+    b = np.real(np.fft.ifft2(np.fft.fft2(img) * np.fft.ifftshift(F)))
+    np.testing.assert_allclose(a, b, atol=1e-13)
+
+
+def test_forward_backward_adjoint_center_view():
+    """With Ht = rot180(Hps) per slice, the backward projector of the centre view is the
+    adjoint of the forward projector (which samples at the lenslet centre)."""
+    rng = np.random.default_rng(4)
+    N, S, Z, L = 15, 45, 3, 4
+    h = rng.random((S, S, Z))
+    t = h[::-1, ::-1, :]
+    X = rng.random((L * N, L * N, Z))
+    Rimg = rng.random((L, L))
+    c = (N - 1) // 2
+    lhs = np.sum(R.forward_ps(h, X, N) * Rimg)
+    rhs = np.sum(X * R.backward_ps(t, Rimg, c, c, N))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_forward_ps_matches_fft_formulation():
+    rng = np.random.default_rng(5)
+    N, S, Z = 15, 45, 2
+    h = rng.random((S, S, Z))
+    X = rng.random((60, 75, Z))
+    E = R.ex_size((60, 75), S)
+    P = sum(R.conv2fft(X[:, :, z], h[:, :, z], E) for z in range(Z))
+    ref = P[7::N, 7::N]
+    np.testing.assert_allclose(R.forward_ps(h, X, N), ref, rtol=1e-11)
+
+
+def test_backward_ps_matches_fft_formulation():
+    rng = np.random.default_rng(6)
+    N, S, Z = 15, 45, 2
+    t = rng.random((S, S, Z))
+    Rimg = rng.random((4, 5))
+    u, v = 3, 11
+    B = np.zeros((60, 75))
+    B[u::N, v::N] = Rimg
+    E = R.ex_size((60, 75), S)
+    ref = np.stack([R.conv2fft(B, t[:, :, z], E) for z in range(Z)], axis=2)
+    np.testing.assert_allclose(R.backward_ps(t, Rimg, u, v, N), ref, rtol=1e-10, atol=1e-13)
+
+
+def test_rl_update_semantics():
+    X = np.array([1.0, 2.0, 3.0, 4.0, 5.0])
+    C = np.array([1.0, np.nan, 1.0, -1.0, 0.0])
+    D = np.array([2.0, 1.0, 0.0, 1.0, 0.0])
+    out = R.rl_update(X, C, D, 0.3)
+    # 0.5*w + (1-w)*1 ; NaN->0 ; Inf->0 ; negative->0 ; 0/0 -> NaN -> 0
+    np.testing.assert_allclose(out, [0.3 * 0.5 + 0.7, 0.7 * 2, 0.7 * 3, 0.7 * 4, 0.7 * 5])
+
+
+def test_conv_vec_semantics_small():
+    """lfm_conv_vec against a literal per-pixel loop of the MEX kernel's clipping logic
+    (mex_lfm_convolution_vec.cu:55-78,147-251)."""
+    rng = np.random.default_rng(7)
+    for W, Hh, n, kw in [(20, 17, 2, 7), (16, 31, 1, 6), (15, 15, 1, 1)]:
+        bm = rng.random((W, Hh, n))
+        K = rng.random((kw, kw, 15, 15))
+        got = R.lfm_conv_vec(bm, K)
+        ref = np.zeros_like(bm)
+        for i in range(n):
+            for y in range(Hh):
+                for x in range(W):
+                    sx, sy = x - kw // 2, y - kw // 2
+                    ksx = -sx if sx < 0 else 0
+                    ksy = -sy if sy < 0 else 0
+                    kex = kw - max(0, x + kw // 2 + 1 - W)
+                    key = kw - max(0, y + kw // 2 + 1 - Hh)
+                    acc = 0.0
+                    for ky in range(ksy, key):
+                        for kx in range(ksx, kex):
+                            acc += bm[sx + kx, sy + ky, i] * K[kx, ky, x % 15, y % 15]
+                    ref[x, y, i] = acc
+        np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_rl_view_step_flux_and_positivity():
+    w = synth.small_config(lenslets=(4, 3), K0=61, Z=3)
+    H, Ht = w.psf()
+    vol = w.volume()
+    LF = w.measured(H, vol)
+    X = R.recon_phase_space(LF, H, Ht, 1)
+    assert X.shape == (60, 45, 3)
+    assert np.isfinite(X).all() and (X >= 0).all()
