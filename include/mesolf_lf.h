@@ -130,6 +130,16 @@ int mlf_forward_view(mlf_solver* s, const float* vol, int32_t u, int32_t v, floa
  *   out (dev, Xr x Xc x Z): out_z = conv2(B, Ht(:,:,u,v,z), 'same'), B(u:N:end, v:N:end) = proj */
 int mlf_backward_view(mlf_solver* s, const float* proj, int32_t u, int32_t v, float* out, void* stream);
 
+/* One view of the RL inner loop, recon_…_with_filter.m:109-137: forward projection of
+ * view (u, v), ratio with LFIMG(u:N:end, v:N:end), back projection, update with weight w.
+ *   lfimg (dev, Xr x Xc); vol (dev, Xr x Xc x Z) updated in place.
+ * Uses the solver's volume buffer as scratch. */
+int mlf_rl_view_step(mlf_solver* s, const float* lfimg, float* vol, int32_t u, int32_t v, double w,
+                     void* stream);
+/* The per-iteration flux-preserving NIP low-pass, sample_filter (recon_…_with_filter.m:222-240,
+ * filter bank :44-61), applied in place to vol (dev, Xr x Xc x Z). */
+int mlf_sample_filter(mlf_solver* s, float* vol, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

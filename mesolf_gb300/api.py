@@ -187,6 +187,19 @@ class RLSolver:
         del pk
         return out
 
+    def view_step(self, lfimg, vol, u, v, w, stream=None):
+        """One RL view update of a device volume in place (``…_with_filter.m:109-137``)."""
+        lk, lp = _fortran(lfimg)
+        check(_lib.load().mlf_rl_view_step(self._h, lp, vol.data_ptr(), int(u), int(v), float(w),
+                                           _stream_of(vol, stream)))
+        del lk
+        return vol
+
+    def sample_filter(self, vol, stream=None):
+        """The per-iteration flux-preserving low-pass on a device volume, in place."""
+        check(_lib.load().mlf_sample_filter(self._h, vol.data_ptr(), _stream_of(vol, stream)))
+        return vol
+
     def close(self):
         if getattr(self, "_h", None):
             _lib.load().mlf_solver_destroy(self._h)

@@ -283,4 +283,20 @@ int mlf_backward_view(mlf_solver* s, const float* proj, int32_t u, int32_t v, fl
   return backward_view(s, proj, u, v, out, static_cast<cudaStream_t>(stream));
 }
 
+int mlf_rl_view_step(mlf_solver* s, const float* lfimg, float* vol, int32_t u, int32_t v, double w,
+                     void* stream) {
+  clear_error();
+  if (!s || !lfimg || !vol) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: null pointer");
+  if (u < 0 || v < 0 || u >= s->N || v >= s->N) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: view out of range");
+  if (!is_device_ptr(lfimg) || !is_device_ptr(vol)) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: device pointers required");
+  return rl_view_step(s, lfimg, vol, u, v, w, static_cast<cudaStream_t>(stream));
+}
+
+int mlf_sample_filter(mlf_solver* s, float* vol, void* stream) {
+  clear_error();
+  if (!s || !vol) return fail(MLF_ERR_INVALID, "mlf_sample_filter: null pointer");
+  if (!is_device_ptr(vol)) return fail(MLF_ERR_INVALID, "mlf_sample_filter: device pointer required");
+  return sample_filter(s, vol, static_cast<cudaStream_t>(stream));
+}
+
 }  // extern "C"

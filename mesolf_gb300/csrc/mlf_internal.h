@@ -109,6 +109,8 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
                float* d_out, mlf_stats* stats, cudaStream_t st);
 int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaStream_t st);
 int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cudaStream_t st);
+int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, double w, cudaStream_t st);
+int sample_filter(Solver* s, float* d_vol, cudaStream_t st);
 int filter_init(Solver* s);
 int filter_run(Solver* s, cudaStream_t st);
 int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,

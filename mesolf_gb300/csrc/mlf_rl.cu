@@ -426,6 +426,32 @@ int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cu
   return MLF_OK;
 }
 
+int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, double w, cudaStream_t st) {
+  const Geo g = geo_of(s);
+  const int64_t n_img = s->Xr * s->Xc, n_vol = n_img * s->Z;
+  const int view = u + s->N * v;
+  k_extract_views<<<grid_for(n_img), 256, 0, st>>>(d_lf, g, s->lfs.as<float>());
+  k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->X.as<float>());
+  MLF_CUDA(cudaGetLastError());
+  MLF_TRY(run_view(s, MODE_FWD, view, view, 0.f, true, st));
+  MLF_TRY(run_reduce(s, view, nullptr, true, st));
+  MLF_TRY(run_view(s, MODE_STEP, view, -1, (float)w, false, st));
+  k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->X.as<float>(), g, d_vol);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+int sample_filter(Solver* s, float* d_vol, cudaStream_t st) {
+  const Geo g = geo_of(s);
+  const int64_t n_vol = s->Xr * s->Xc * s->Z;
+  k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->X.as<float>());
+  MLF_CUDA(cudaGetLastError());
+  MLF_TRY(filter_run(s, st));
+  k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->X.as<float>(), g, d_vol);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
 // ---------------------------------------------------------------- dispatch per T
 #define MLF_DECL_T(T)                                                                     \
   int prepare_view_T##T(size_t smem);                                                    \

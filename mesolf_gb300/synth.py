@@ -48,15 +48,22 @@ def make_psf(K0, N, z_idx, seed=0, plane_sides=None, shift_per_z=0.15,
     uu = np.arange(1, N + 1, dtype=np.float64) - (N + 1) / 2.0
     for k in range(Z):
         zi = z_idx[k]
-        sigma = (2.0 + 0.6 * abs(zi)) / 2.0
-        cu = ctr + uu * zi * shift_per_z                       # (N,)
-        g = np.exp(-((x[:, None] - cu[None, :]) ** 2) / (2 * sigma ** 2))   # (K0, N)
+        radius = 2.0 + 0.6 * abs(zi)
+        sigma = radius / 2.0
+        cu = ctr + uu * zi * shift_per_z                        # (N,) centres per source index
+        d2x = (x[:, None] - cu[None, :]) ** 2                   # (K0, N)
+        win = np.ones(K0, dtype=bool)
         if plane_sides is not None:
-            half = (int(plane_sides[k]) - 1) / 2.0
-            g = g * (np.abs(x - ctr) <= half)[:, None]
-        g = g / g.sum(axis=0, keepdims=True)
-        slab = np.einsum("xa,yb->xyab", g, g) * jit[None, None, :, :, k]
-        H[:, :, :, :, k] = slab.astype(dtype)
+            win = np.abs(x - ctr) <= (int(plane_sides[k]) - 1) / 2.0
+        # hard-edged disc of the given radius, Gaussian profile inside (zero outside)
+        lo = max(0, int(np.floor(cu.min() - radius)) - 1)
+        hi = min(K0, int(np.ceil(cu.max() + radius)) + 2)
+        sub = slice(lo, hi)
+        d2 = d2x[sub, None, :, None] + d2x[None, sub, None, :]  # (n, n, N, N)
+        g = np.exp(-d2 / (2 * sigma ** 2)) * (d2 <= radius * radius)
+        g = g * (win[sub, None] & win[None, sub])[:, :, None, None]
+        g = g / g.sum(axis=(0, 1), keepdims=True)
+        H[sub, sub, :, :, k] = (g * jit[None, None, :, :, k]).astype(dtype)
     Ht = np.asfortranarray(H[::-1, ::-1, :, :, :])
     return H, Ht
 

@@ -42,7 +42,7 @@ def test_conv_vec_matches_oracle(cuda, W, H, n, kw):
     out = to_host(mex_lfm_convolution_vec(to_dev(bm), to_dev(K)))
     ref = R.lfm_conv_vec(bm, K)
     assert out.shape == (W, H, n)
-    assert rel_l2(out, ref) <= 1e-6
+    assert rel_l2(out, ref) <= 1e-5
 
 
 def test_conv_vec_2d_bitmap_and_host_arrays(cuda):
@@ -55,7 +55,7 @@ def test_conv_vec_2d_bitmap_and_host_arrays(cuda):
     ref = R.lfm_conv_vec(bm, K)
     assert out_host.shape == (37, 29)
     np.testing.assert_array_equal(out_host, out_dev)
-    assert rel_l2(out_host, ref) <= 1e-6
+    assert rel_l2(out_host, ref) <= 1e-5
 
 
 def test_conv_vec_fixture_shape_sampled(cuda):
@@ -63,10 +63,11 @@ def test_conv_vec_fixture_shape_sampled(cuda):
     with a 241-wide synthetic kernel; checked at 3000 sampled output pixels."""
     from mesolf_gb300 import mex_lfm_convolution_vec
     rng = np.random.default_rng(12)
-    bm = np.zeros((376, 376, 77), np.float32)
-    nz = rng.choice(bm.size, 72050, replace=False)
-    bm.reshape(-1, order="F")[nz] = rng.uniform(0.0, 1.0859, nz.size).astype(np.float32)
-    bm = np.asfortranarray(bm)
+    flat = np.zeros(376 * 376 * 77, np.float32)
+    nz = rng.choice(flat.size, 72050, replace=False)
+    flat[nz] = rng.uniform(0.0, 1.0859, nz.size).astype(np.float32)
+    bm = flat.reshape((376, 376, 77), order="F")
+    assert np.count_nonzero(bm) == 72050
     K = np.asfortranarray(rng.random((241, 241, 15, 15)).astype(np.float32))
     out = to_host(mex_lfm_convolution_vec(to_dev(bm), to_dev(K)))
     pts = [(int(x), int(y), int(i)) for x, y, i in zip(rng.integers(0, 376, 3000), rng.integers(0, 376, 3000),
@@ -96,11 +97,11 @@ def test_forward_backward_views_match_oracle(cuda, lenslets, K0, Z):
     for (u, v) in [(7, 7), (0, 0), (14, 3), (2, 12)]:
         hx = to_host(s.forward_view(to_dev(vol), u, v))
         ref = R.forward_ps(Hps[:, :, u, v, :], vol.astype(np.float64), 15)
-        assert rel_l2(hx, ref) <= 1e-6, (u, v)
+        assert rel_l2(hx, ref) <= 1e-5, (u, v)
         proj = rng.random(lenslets).astype(np.float32)
         c = to_host(s.backward_view(to_dev(proj), u, v))
         refc = R.backward_ps(Htc[:, :, u, v, :], proj.astype(np.float64), u, v, 15)
-        assert rel_l2(c, refc) <= 1e-6, (u, v)
+        assert rel_l2(c, refc) <= 1e-5, (u, v)
     s.close()
     psf.close()
 
@@ -115,6 +116,40 @@ def test_psf_weights_match_oracle(cuda):
     ref = R.view_weights(Hps)
     np.testing.assert_allclose(psf.weights, ref, rtol=1e-12, atol=1e-15)
     assert ((psf.weights == 0) == (ref == 0)).all()
+
+
+# ------------------------------------------------------------------------------ RL pieces
+@pytest.mark.parametrize("lenslets,K0,Z", [((5, 4), 61, 3), ((4, 6), 91, 2), ((9, 8), 61, 2)])
+def test_view_step_matches_oracle(cuda, lenslets, K0, Z):
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver
+    w = synth.small_config(lenslets=lenslets, K0=K0, Z=Z)
+    H, Ht = w.psf()
+    LF = w.measured(H, w.volume())
+    Hn, Htn = R.normalize_psf(H, Ht)
+    Hps, Htc = R.gen_phasespace_psf(Hn, Htn)
+    rng = np.random.default_rng(1)
+    X = rng.uniform(0.5, 1.5, LF.shape + (Z,)).astype(np.float32)
+    psf = PhaseSpacePSF(H, Ht)
+    s = RLSolver(psf, LF.shape)
+    for (u, v) in [(7, 7), (0, 0), (14, 3), (2, 12)]:
+        ref = R.rl_view_step(X.astype(np.float64), LF.astype(np.float64), Hps, Htc, u, v, 0.3, 15)
+        got = to_host(s.view_step(to_dev(LF), to_dev(X), u, v, 0.3))
+        assert rel_l2(got, ref) <= 1e-5, (u, v, rel_l2(got, ref))
+
+
+@pytest.mark.parametrize("shape,Z", [((60, 45), 5), ((165, 165), 21), ((45, 90), 3)])
+def test_sample_filter_matches_oracle(cuda, shape, Z):
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver
+    w = synth.small_config(lenslets=(shape[0] // 15, shape[1] // 15), K0=61, Z=Z)
+    H, Ht = w.psf()
+    rng = np.random.default_rng(2)
+    X = rng.uniform(0.5, 1.5, shape + (Z,)).astype(np.float32)
+    psf = PhaseSpacePSF(H, Ht)
+    s = RLSolver(psf, shape)
+    got = to_host(s.sample_filter(to_dev(X)))
+    F = R.nip_filter_bank(shape[0], shape[1], Z, 15)
+    ref = R.sample_filter(X.astype(np.float64), F)
+    assert rel_l2(got, ref) <= 1e-6
 
 
 # ------------------------------------------------------------------------------ RL solve
