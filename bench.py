@@ -1,0 +1,299 @@
+"""Throughput benchmark of the phase-space RL deconvolution on GB300.
+
+One step = one complete solve (all RL iterations) of one synthetic light-field patch:
+Nnum 15, 67 x 67 lenslets (1005 x 1005 px), 51 planes, PSF side 231 (phase-space side
+225), 3 iterations, plain FP32 -- the "full single patch" workload.  `value` is
+deconvolved voxels/s with the image already in HBM; `e2e` is the same solve through the
+C ABI (mlf_solver_run) with pinned host buffers, the image copy in and the volume copy
+out inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: patches are independent (replicas); each rank solves its own patch, no
+collective on the data path; value = all ranks' voxels / max rank time.
+The reference arm (--impl reference) times the CPU restatement of the reference's
+algorithm (the oracle port; the MATLAB original cannot run here) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("deconvolved voxels/s, plain FP32 vs batched mixed-prec @≤1e-3 rel L2; p99 ms")
+WORKLOAD = "lf1005x1005x51_k231_it3"
+WORKLOAD_DESC = ("Nnum 15, 67x67 lenslets (1005x1005 px), 51 planes (0-200 um at 4 um), "
+                 "PSF 231 px (phase-space 225), 2000 somas, 2000-photon Poisson image, 3 RL iterations")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = [r.split(", ") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(device, rank):
+    import torch
+    from mesolf_gb300 import synth
+    w = synth.config2(seed=rank)
+    H, Ht = w.psf()
+    vol = w.volume()
+    lf = w.measured(H, vol, device=str(device))
+    return w, H, Ht, lf
+
+
+def algorithmic_flop_per_view(Xr, Xc, Z, S, N):
+    # forward (sampled outputs) + back projection (lattice-sparse input), 2 flop per MAC:
+    # 2 * [(Xr/N)(Xc/N) Z S^2 + Xr Xc Z S^2 / N^2] = 4 Xr Xc Z S^2 / N^2
+    return 4.0 * Xr * Xc * Z * S * S / (N * N)
+
+
+def cpu_baseline_sample(H, Ht, lf, planes=8, u=3, v=5):
+    """Time one RL view step of the FP64 oracle port on `planes` of the 51 planes."""
+    from oracle import mesolf_ref as R
+    Hn, Htn = R.normalize_psf(H[:, :, :, :, :planes], Ht[:, :, :, :, :planes])
+    Hps, Htc = R.gen_phasespace_psf(Hn, Htn)
+    X = np.full(lf.shape + (planes,), float(lf.sum()) / (lf.size * 51))
+    t0 = time.perf_counter()
+    R.rl_view_step(X, lf.astype(np.float64), Hps, Htc, u, v, 0.3, 15)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    """CPU arm: the oracle port of the reference's per-view RL step, on the host cores."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from mesolf_gb300 import synth
+    w = synth.config2()
+    H, Ht = w.psf()
+    rng = np.random.default_rng(0)
+    lf = rng.poisson(200.0, w.image_shape).astype(np.float64)
+    planes = 4
+    for _ in range(max(0, args.warmup if args.warmup < 1 else 1)):
+        cpu_baseline_sample(H, Ht, lf, planes=1)
+    ts = [cpu_baseline_sample(H, Ht, lf, planes=planes) for _ in range(args.steps)]
+    t_plane = float(np.mean(ts)) / planes
+    from oracle import mesolf_ref as R
+    Hn, Htn = R.normalize_psf(H[:, :, :, :, :1], Ht[:, :, :, :, :1])
+    n_views = 190
+    t_solve = t_plane * w.Z * n_views * w.iters
+    val = w.voxels / t_solve
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "voxels/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_solve * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "desc": WORKLOAD_DESC},
+            "cpu_baseline": {"value": val, "unit": "voxels/s", "cores": 1, "kind": "port",
+                             "sample": f"one RL view step (forward, ratio, back projection, D, update) on "
+                                       f"{planes} of 51 planes, FP64 numpy oracle, extrapolated linearly to "
+                                       f"51 planes x {n_views} views x 3 iterations"},
+            "e2e": {"value": val, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import __graft_entry__
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    __graft_entry__.build()
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver, _lib
+    from mesolf_gb300.api import _fortran
+
+    w, H, Ht, lf = make_workload(dev, rank)
+    Xr, Xc = w.image_shape
+    Z = w.Z
+    psf = PhaseSpacePSF(H, Ht)
+    solver = RLSolver(psf, (Xr, Xc))
+    lf_dev = _fortran(torch.as_tensor(np.ascontiguousarray(lf)).to(dev))[0]
+    out_dev = torch.empty((Z, Xc, Xr), dtype=torch.float32, device=dev).permute(2, 1, 0)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        solver.run(lf_dev, w.iters, precision=args.precision, out=out_dev, want_stats=False)
+    barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    launches = 0
+    vk_ms = 0.0
+    vk_n = 0
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        solver.run(lf_dev, w.iters, precision=args.precision, out=out_dev, want_stats=True)
+        st = solver.last_stats
+        launches += st["kernel_launches"]
+        vk_ms += st["view_kernel_ms"]
+        vk_n += st["view_kernel_launches"]
+    e1.record(stream)
+    barrier()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    n_views = st["n_views"]
+    value = ws * w.voxels / (ms * 1e-3)
+
+    # e2e: pinned host image in, pinned host volume out, through mlf_solver_run
+    lf_host = torch.empty((Xc, Xr), dtype=torch.float32, pin_memory=True).t()
+    lf_host.copy_(torch.as_tensor(np.ascontiguousarray(lf)))
+    out_host = torch.empty((Z, Xc, Xr), dtype=torch.float32, pin_memory=True).permute(2, 1, 0)
+    solver.run(lf_host, w.iters, precision=args.precision, out=out_host, want_stats=False)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        solver.run(lf_host, w.iters, precision=args.precision, out=out_host, want_stats=False)
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": ws * w.voxels / (e2e_ms * 1e-3), "unit": "voxels/s",
+           "h2d_bytes_per_step": int(Xr * Xc * 4), "d2h_bytes_per_step": int(Xr * Xc * Z * 4),
+           "ms_per_step": e2e_ms, "path": "mlf_solver_run, pinned host buffers"}
+
+    # roofline of the dominant kernel (the per-view projector/update kernel)
+    peak = ctypes_peak = None
+    import ctypes
+    pk = ctypes.c_double()
+    if _lib.load().mlf_probe_fp32_peak(200.0, ctypes.byref(pk), ctypes.c_void_p(stream.cuda_stream)) == 0:
+        ctypes_peak = pk.value
+    peak = ctypes_peak
+    flop_view = algorithmic_flop_per_view(Xr, Xc, Z, psf.S, psf.N)
+    mean_launch_ms = vk_ms / max(1, vk_n)
+    # the launches of one iteration do n_views views' worth of work in n_views + 1 launches
+    achieved = flop_view * n_views * w.iters * args.steps / (vk_ms * 1e-3) / 1e12
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "k_view_traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if peak else None, "traffic": traffic,
+                "kernel": "k_view (fused back projection + update + next forward projection)",
+                "flop_per_view": flop_view, "mean_launch_ms": mean_launch_ms,
+                "peak_source": "measured live: mlf_probe_fp32_peak (register-only FP32 FMA kernel)",
+                "hbm_peak_gbs_measured": _measured_hbm()}
+
+    line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, see mesolf_gb300/synth.py)",
+            "config": {"workload": WORKLOAD, "desc": WORKLOAD_DESC, "precision": args.precision,
+                       "views_per_iteration": n_views, "parallelism": f"replicas x{ws}",
+                       "l2": "inputs larger than L2 (projector taps 4.6 GB, volume 206 MB)"},
+            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks,
+            "impl": "ours"}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        rng = np.random.default_rng(0)
+        planes = 4
+        t = cpu_baseline_sample(H, Ht, lf.astype(np.float64), planes=planes)
+        t_solve = t / planes * Z * n_views * w.iters
+        line["cpu_baseline"] = {"value": w.voxels / t_solve, "unit": "voxels/s", "cores": 1, "kind": "port",
+                                "sample": f"one RL view step of the FP64 numpy oracle on {planes} of {Z} planes "
+                                          f"({t:.1f} s), extrapolated to {Z} planes x {n_views} views x {w.iters} iterations"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    solver.close()
+    psf.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _measured_hbm():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except Exception:
+        return None
+
+
+if __name__ == "__main__":
+    main()

@@ -48,16 +48,23 @@ typedef struct mlf_psf mlf_psf;       /* phase-space PSF resident in HBM */
 typedef struct mlf_solver mlf_solver; /* per-image-size solve context (scratch in HBM) */
 
 typedef struct mlf_stats {
-  int32_t n_views;          /* active views per iteration (weight != 0) */
-  int32_t iterations;       /* iterations run */
-  double gpu_ms;            /* device time of the solve (CUDA events) */
-  double view_ms;           /* mean device time of one view step */
-  double filter_ms;         /* device time of the per-iteration sample filter */
-  int64_t kernel_launches;  /* kernels launched by the solve */
+  int32_t n_views;              /* active views per iteration (weight != 0) */
+  int32_t iterations;           /* iterations run */
+  double gpu_ms;                /* device time of the solve (CUDA events) */
+  double view_ms;               /* gpu_ms / (iterations * n_views) */
+  double view_kernel_ms;        /* summed device time of the projector (view) kernel launches */
+  int64_t view_kernel_launches; /* number of projector kernel launches timed */
+  int64_t kernel_launches;      /* kernels launched by the solve */
 } mlf_stats;
 
 /* Library / ABI version (MLF_ABI_VERSION). */
 int mlf_version(void);
+
+/* Device characterisation: runs a register-only FP32 FMA kernel on the current device
+ * for about `ms` milliseconds and returns the achieved FP32 rate in TFLOP/s (the
+ * denominator the plain FP32 projector is judged against).  No counterpart in the
+ * reference. */
+int mlf_probe_fp32_peak(double ms, double* tflops, void* stream);
 
 /* Copy the calling thread's last error message into buf (always NUL-terminated).
  * Returns the status code of that error. */

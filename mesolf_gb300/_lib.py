@@ -25,6 +25,7 @@ _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
 SIGNATURES = {
     "mlf_version": (ctypes.c_int, []),
+    "mlf_probe_fp32_peak": (ctypes.c_int, [ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]),
     "mlf_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "mlf_conv_vec": (ctypes.c_int, [_vp, _i64, _i64, _i64, _vp, _i64, _i32, _vp, _vp]),
     "mlf_psf_create": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i64, ctypes.POINTER(_vp), _vp]),
@@ -46,8 +47,8 @@ SIGNATURES = {
 
 class MLFStats(ctypes.Structure):
     _fields_ = [("n_views", ctypes.c_int32), ("iterations", ctypes.c_int32), ("gpu_ms", ctypes.c_double),
-                ("view_ms", ctypes.c_double), ("filter_ms", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int64)]
+                ("view_ms", ctypes.c_double), ("view_kernel_ms", ctypes.c_double),
+                ("view_kernel_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

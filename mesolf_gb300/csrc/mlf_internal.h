@@ -99,6 +99,11 @@ struct Solver {
   DevBuf red;        // double scratch for reductions
   DevBuf stage_in, stage_out;  // device staging for host arrays
   FilterPlan filt;
+  // optional per-launch timing of the projector kernels (enabled when stats are requested)
+  std::vector<cudaEvent_t> tev;
+  int tev_used = 0;
+  bool timing = false;
+  ~Solver();
   size_t bytes() const;
 };
 

@@ -205,8 +205,23 @@ void build_classes(int L, int q, std::vector<int>& cls, std::vector<std::pair<in
   }
 }
 
+int timing_mark(Solver* s, cudaStream_t st) {
+  if (!s->timing) return MLF_OK;
+  if (s->tev_used >= (int)s->tev.size()) {
+    const size_t grow = std::max<size_t>(256, s->tev.size());
+    for (size_t k = 0; k < grow; ++k) {
+      cudaEvent_t e;
+      MLF_CUDA(cudaEventCreate(&e));
+      s->tev.push_back(e);
+    }
+  }
+  MLF_CUDA(cudaEventRecord(s->tev[s->tev_used++], st));
+  return MLF_OK;
+}
+
 int run_view(Solver* s, int mode, int view_cur, int view_next, float w, bool do_fwd,
              cudaStream_t st) {
+  MLF_TRY(timing_mark(s, st));
   ViewArgs a = view_args(s);
   const int N = s->N;
   a.u = view_cur % N;
@@ -215,7 +230,8 @@ int run_view(Solver* s, int mode, int view_cur, int view_next, float w, bool do_
   a.do_fwd = do_fwd ? 1 : 0;
   a.wb = wb_of(s, view_cur);
   a.wf = wf_of(s, view_next >= 0 ? view_next : view_cur);
-  return launch_view_kernel(s->T, mode, a, s->grid, s->threads, s->smem, st);
+  MLF_TRY(launch_view_kernel(s->T, mode, a, s->grid, s->threads, s->smem, st));
+  return timing_mark(s, st);
 }
 
 int run_reduce(Solver* s, int view, float* hx_out, bool ratio, cudaStream_t st) {
@@ -256,6 +272,10 @@ int enqueue_iteration(Solver* s, int64_t* launches, cudaStream_t st) {
 }
 
 }  // namespace
+
+Solver::~Solver() {
+  for (cudaEvent_t e : tev) cudaEventDestroy(e);
+}
 
 size_t Solver::bytes() const {
   return X.bytes + Xtmp.bytes + lfs.bytes + rpad.bytes + part.bytes + hx.bytes + cls.bytes +
@@ -360,6 +380,8 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     MLF_CUDA(cudaEventRecord(e0, st));
   }
   int64_t launches = 0;
+  s->timing = stats != nullptr;
+  s->tev_used = 0;
   k_extract_views<<<grid_for(n_img), 256, 0, st>>>(d_lf, g, s->lfs.as<float>());
   ++launches;
   if (d_warm) {
@@ -388,9 +410,18 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     stats->iterations = max_iter;
     stats->gpu_ms = ms;
     stats->view_ms = (max_iter > 0 && stats->n_views > 0) ? ms / (max_iter * stats->n_views) : 0.0;
-    stats->filter_ms = 0.0;
+    double vk = 0.0;
+    for (int k = 0; k + 1 < s->tev_used; k += 2) {
+      float t = 0.f;
+      MLF_CUDA(cudaEventElapsedTime(&t, s->tev[k], s->tev[k + 1]));
+      vk += t;
+    }
+    stats->view_kernel_ms = vk;
+    stats->view_kernel_launches = s->tev_used / 2;
     stats->kernel_launches = launches;
   }
+  s->timing = false;
+  s->tev_used = 0;
   return MLF_OK;
 }
 

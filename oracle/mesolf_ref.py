@@ -323,11 +323,14 @@ def forward_ps(h_uv, X, N):
     S = h_uv.shape[0]
     m = S // 2
     c0 = (N + 1) // 2 - 1
-    Xp = np.zeros((Xr + 2 * m, Xc + 2 * m, Z))
-    Xp[m:m + Xr, m:m + Xc, :] = X
-    win = sliding_window_view(Xp, (S, S), axis=(0, 1))[c0::N, c0::N]   # (Li, Lj, Z, S, S)
     hf = h_uv[::-1, ::-1, :]
-    return np.einsum("ijzpq,pqz->ij", win, hf, optimize=True)
+    out = np.zeros(((Xr - c0 + N - 1) // N, (Xc - c0 + N - 1) // N))
+    Xp = np.zeros((Xr + 2 * m, Xc + 2 * m))
+    for z in range(Z):
+        Xp[m:m + Xr, m:m + Xc] = X[:, :, z]
+        win = sliding_window_view(Xp, (S, S))[c0::N, c0::N]                # (Li, Lj, S, S)
+        out += np.einsum("ijpq,pq->ij", win, hf[:, :, z])
+    return out
 
 
 # ----------------------------------------------------------------------------- a12/a13
