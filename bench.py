@@ -161,6 +161,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one solve of --iters iterations and exit (for ncu captures)")
+    ap.add_argument("--iters", type=int, default=None)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -178,12 +181,19 @@ def main():
     from mesolf_gb300.api import _fortran
 
     w, H, Ht, lf = make_workload(dev, rank)
+    torch.cuda.empty_cache()
     Xr, Xc = w.image_shape
     Z = w.Z
     psf = PhaseSpacePSF(H, Ht)
     solver = RLSolver(psf, (Xr, Xc))
     lf_dev = _fortran(torch.as_tensor(np.ascontiguousarray(lf)).to(dev))[0]
     out_dev = torch.empty((Z, Xc, Xr), dtype=torch.float32, device=dev).permute(2, 1, 0)
+    if args.profile:
+        torch.cuda.synchronize()
+        solver.run(lf_dev, args.iters or w.iters, precision=args.precision, out=out_dev, want_stats=True)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": solver.last_stats}), flush=True)
+        return
 
     def barrier():
         if ws > 1:
