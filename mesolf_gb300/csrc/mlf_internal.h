@@ -142,6 +142,15 @@ struct ViewArgs {
   int RP, RProws, XP, XProws, maxc, slot_floats;
 };
 enum ViewMode { MODE_FWD = 0, MODE_STEP = 1, MODE_BWDC = 2 };
+
+// View-kernel tiling shared by host and device.  Each thread owns an 8 (b) x 4 (a)
+// output tile; the forward-input plane keeps its interior at column offset
+// view_qpad(q) = round_up(q, 4) (16-byte aligned for cp.async), so the window offset of the
+// forward correlation is view_qpad(q) - q; the back projection's is s_alpha + 1 in {0,1,2}.
+constexpr int view_qpad(int q) { return (q + 3) & ~3; }
+constexpr int view_offmax(int q) { return (view_qpad(q) - q) > 2 ? (view_qpad(q) - q) : 2; }
+// float4 loads per window row: 4 outputs + T - 1 taps + the largest offset
+constexpr int view_nw(int T) { return (4 + T - 1 + view_offmax((T - 1) / 2) + 3) / 4; }
 int prepare_view_kernels(int T, size_t smem);
 int occupancy_view_kernel(int T, int threads, size_t smem, int* blocks);
 int launch_view_kernel(int T, int mode, const ViewArgs& a, int grid, int threads, size_t smem,

@@ -40,8 +40,10 @@ __global__ void k_sum_partial(const float* __restrict__ a, int64_t n, double* pa
   }
 }
 
-// Flat initial guess, recon_…_with_filter.m:72-73: ones/sum(ones)*sum(LFIMG).
-__global__ void k_init_flat(float* X, int64_t n, const double* part, int nparts, double inv_count) {
+// Flat initial guess, recon_…_with_filter.m:72-73: ones/sum(ones)*sum(LFIMG).  Only the
+// valid positions of each plane are written (row padding stays zero).
+__global__ void k_init_flat(float* X, int Li, int Lj, int Pa, int64_t plane, int64_t nch,
+                            const double* part, int nparts, double inv_count) {
   __shared__ float val;
   if (threadIdx.x == 0) {
     double s = 0.0;
@@ -49,9 +51,13 @@ __global__ void k_init_flat(float* X, int64_t n, const double* part, int nparts,
     val = (float)(inv_count * s);
   }
   __syncthreads();
+  const int64_t n = nch * Li * Lj;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    X[i] = val;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ch = i / ((int64_t)Li * Lj);
+    const int rem = (int)(i - ch * Li * Lj);
+    X[ch * plane + (int64_t)(rem / Li) * Pa + rem % Li] = val;
+  }
 }
 
 struct Geo {
@@ -165,7 +171,7 @@ ViewArgs view_args(Solver* s) {
   a.plane = s->plane; a.nch = s->nch;
   a.tilesA = s->tilesA; a.tilesB = s->tilesB; a.tps = s->tps; a.slots = s->slots;
   a.RP = s->RP; a.RProws = s->RProws; a.XP = s->XP; a.XProws = s->XProws; a.maxc = s->maxc;
-  a.slot_floats = round_up(s->XProws * s->XP + 2 * s->T * s->T + s->maxc * s->maxc + s->T * s->maxc, 4);
+  a.slot_floats = round_up(s->XProws * s->XP + 4 * s->T * s->T + s->maxc * s->maxc + s->T * s->maxc, 4);
   return a;
 }
 
@@ -306,7 +312,7 @@ int solver_init(Solver* s) {
     return fail(MLF_ERR_UNSUPPORTED, "patch of " + std::to_string(s->Li) + " x " +
                                          std::to_string(s->Lj) +
                                          " lenslets exceeds the 128 x 64 per-solve limit; tile the field of view");
-  const int NW = (4 + s->T - 1 + 2 + 3) / 4;
+  const int NW = view_nw(s->T);
   s->RP = round_up(4 * (s->tilesA - 1) + 4 * NW, 4);
   s->RProws = s->tilesB * 8 + s->T + 1;
   s->XP = s->RP;
@@ -335,7 +341,7 @@ int solver_init(Solver* s) {
   MLF_TRY(s->cls.alloc(tab.size() * sizeof(int), "class tables"));
   MLF_CUDA(cudaMemcpy(s->cls.p, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
 
-  const int slot_floats = round_up(s->XProws * s->XP + 2 * s->T * s->T + s->maxc * s->maxc + s->T * s->maxc, 4);
+  const int slot_floats = round_up(s->XProws * s->XP + 4 * s->T * s->T + s->maxc * s->maxc + s->T * s->maxc, 4);
   s->slots = s->tps >= 128 ? 1 : std::max(1, std::min(32, 192 / s->tps));
   s->threads = round_up(s->slots * s->tps, 32);
   s->smem = sizeof(float) * ((size_t)s->RProws * s->RP + (size_t)s->slots * slot_floats);
@@ -391,7 +397,8 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     const int nb = 256;
     k_sum_partial<<<nb, 256, 0, st>>>(d_lf, n_img, s->red.as<double>());
     k_init_flat<<<grid_for(s->nch * s->plane), 256, 0, st>>>(
-        s->X.as<float>(), s->nch * s->plane, s->red.as<double>(), nb, 1.0 / (double)n_vol);
+        s->X.as<float>(), s->Li, s->Lj, s->Pa, s->plane, s->nch, s->red.as<double>(), nb,
+        1.0 / (double)n_vol);
     launches += 2;
   }
   MLF_CUDA(cudaGetLastError());

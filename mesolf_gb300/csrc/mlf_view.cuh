@@ -13,9 +13,10 @@
 // with sa = floor((alpha-u+h)/N), sb = floor((beta-v+h)/N).  One CTA owns one or more
 // channel slots; each thread of a slot owns an 8 (b) x 4 (a) output tile.  Inputs are
 // staged in shared memory with zero halos, so the tap loops need no bounds checks; the
-// sliding windows are read with aligned 128-bit shared loads.  The forward partial sums
-// of a CTA stay in registers across all its channels and are written once
-// (deterministic reduction happens in a second kernel).
+// sliding windows are read with aligned 128-bit shared loads.  The X tile of a channel is
+// copied with cp.async straight into the forward-input plane and updated there in place.
+// The forward partial sums of a CTA stay in registers across all its channels and are
+// written once (a second kernel reduces them in a fixed order).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -27,19 +28,14 @@ namespace mlf {
 constexpr int VT_TY = 8;  // tile rows (b direction)
 constexpr int VT_TX = 4;  // tile cols (a direction)
 
-// Number of float4 loads covering a window of TX + T - 1 + OFFmax (OFFmax = 2) floats.
-template <int T>
-struct ViewWin {
-  static constexpr int NW = (VT_TX + T - 1 + 2 + 3) / 4;
-};
-
-// acc[ty][tx] += sum_{dy<T, dx<T} in[(y0+ty+dy)*pitch + x0 + OFF + tx + dx] * w[dy*T+dx]
-// `in + y0*pitch + x0` must be 16-byte aligned (x0 multiple of 4, pitch multiple of 4).
+// acc[ty][tx] += sum_{dy<T, dx<T} in[(ty+dy)*pitch + OFF + tx + dx] * w[dy*T+dx]
+// `in` must be 16-byte aligned and pitch a multiple of 4.
 template <int T, int OFF>
 __device__ __forceinline__ void conv_tile(const float* __restrict__ in, int pitch,
                                           const float* __restrict__ w,
                                           float (&acc)[VT_TY][VT_TX]) {
-  constexpr int NW = ViewWin<T>::NW;
+  constexpr int NW = view_nw(T);
+  static_assert(OFF + VT_TX + T - 1 <= 4 * NW, "window too short");
 #pragma unroll 1
   for (int dy = 0; dy < T; ++dy) {
     float wr[T];
@@ -72,32 +68,42 @@ __device__ __forceinline__ int floor_div(int a, int b) {
   return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
 }
 
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 template <int T, int MODE>
-__global__ void __launch_bounds__(256) k_view(ViewArgs A) {
+__global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
   extern __shared__ __align__(16) float sm[];
   constexpr int TT = T * T;
+  constexpr int Q = (T - 1) / 2;
+  constexpr int QP = view_qpad(Q);      // column of the forward-input interior
+  constexpr bool BWD = (MODE != MODE_FWD);
+  constexpr bool XIN = (MODE != MODE_BWDC);
   const int tid = threadIdx.x;
   const int slot = tid / A.tps;
   const int lt = tid - slot * A.tps;  // thread index within slot
   const bool slot_ok = slot < A.slots;
+  const bool tile_ok = slot_ok && lt < A.tps;
   const int ta = lt % A.tilesA;
   const int tb = lt / A.tilesA;
   const int a0 = ta * VT_TX, b0 = tb * VT_TY;
-  constexpr bool BWD = (MODE != MODE_FWD);
 
   // ---- shared memory carve-up
   float* rs = sm;                                              // [RProws][RP] (BWD only)
   float* slot_base = rs + (BWD ? A.RProws * A.RP : 0);
-  const int slot_floats = A.slot_floats;
-  float* xin = slot_base + (slot_ok ? slot : 0) * slot_floats;  // [XProws][XP]
-  float* wbs = xin + A.XProws * A.XP;
-  float* wfs = wbs + TT;
-  float* dtab = wfs + TT;                                      // [maxc][maxc]
+  float* xin = slot_base + (slot_ok ? slot : 0) * A.slot_floats;  // [XProws][XP]
+  float* taps = xin + A.XProws * A.XP;                         // [2 buffers][wb | wf]
+  float* dtab = taps + 4 * TT;                                 // [maxc][maxc]
   float* rowp = dtab + A.maxc * A.maxc;                        // [T][maxc]
 
   // ---- zero the slots (halos must be zero), stage R
   {
-    const int total = A.slots * slot_floats;
+    const int total = A.slots * A.slot_floats;
     for (int i = tid; i < total; i += blockDim.x) slot_base[i] = 0.f;
     if (BWD) {
       const int nr = A.RProws * A.RP;
@@ -116,35 +122,34 @@ __global__ void __launch_bounds__(256) k_view(ViewArgs A) {
 
   const int h = (A.N - 1) / 2;
   const int64_t step = (int64_t)gridDim.x * A.slots;
-  for (int64_t base = (int64_t)blockIdx.x * A.slots; base < A.nch; base += step) {
+  const int64_t first = (int64_t)blockIdx.x * A.slots + slot;
+  // taps of the first channel into buffer 0
+  if (slot_ok && first < A.nch) {
+    for (int i = lt; i < TT; i += A.tps) {
+      if (BWD) taps[i] = __ldg(A.wb + first * TT + i);
+      if (XIN) taps[TT + i] = __ldg(A.wf + first * TT + i);
+    }
+  }
+  int buf = 0;
+  for (int64_t base = (int64_t)blockIdx.x * A.slots; base < A.nch; base += step, buf ^= 1) {
     const int64_t ch = base + slot;
     const bool active = slot_ok && ch < A.nch;
     const int alpha = active ? (int)((ch / A.Z) % A.N) : 0;
     const int beta = active ? (int)(ch / ((int64_t)A.Z * A.N)) : 0;
     const int sa = floor_div(alpha - A.u + h, A.N);
     const int sb = floor_div(beta - A.v + h, A.N);
+    const float* wbs = taps + buf * 2 * TT;
+    const float* wfs = wbs + TT;
 
-    // ---- taps of this channel
-    if (active) {
-      for (int i = lt; i < TT; i += A.tps) {
-        if (BWD) wbs[i] = __ldg(A.wb + ch * TT + i);
-        if (MODE != MODE_BWDC) wfs[i] = __ldg(A.wf + ch * TT + i);
-      }
-    }
-    // ---- prefetch the X tile (update / forward-only input)
-    float xv[VT_TY][VT_TX];
-    const float* Xch = A.X + ch * A.plane;
-    if (MODE != MODE_BWDC) {
+    // ---- X tile -> forward-input plane (interior at rows +Q, cols +QP), asynchronously
+    if (XIN && active && lt < A.tps) {
+      const float* Xch = A.X + ch * A.plane;
 #pragma unroll
       for (int y = 0; y < VT_TY; ++y) {
         const int b = b0 + y;
-        float4 t4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (active && lt < A.tps && b < A.Lj)
-          t4 = *reinterpret_cast<const float4*>(Xch + (int64_t)b * A.Pa + a0);
-        xv[y][0] = t4.x; xv[y][1] = t4.y; xv[y][2] = t4.z; xv[y][3] = t4.w;
+        if (b < A.Lj) cp_async16(xin + (b + Q) * A.XP + a0 + QP, Xch + (int64_t)b * A.Pa + a0);
       }
     }
-    __syncthreads();
 
     if (BWD && active) {
       // D table: rowp[dj][ca] = sum_{di in rngA[sa][ca]} wb[dj][di];
@@ -184,52 +189,59 @@ __global__ void __launch_bounds__(256) k_view(ViewArgs A) {
           case 1: conv_tile<T, 1>(rin, A.RP, wbs, acc); break;
           default: conv_tile<T, 2>(rin, A.RP, wbs, acc); break;
         }
-        const int* cA = A.clsA + (sa + 1) * A.Li;
-        const int* cB = A.clsB + (sb + 1) * A.Lj;
+        if (MODE == MODE_BWDC) {
 #pragma unroll
-        for (int y = 0; y < VT_TY; ++y) {
-          const int b = b0 + y;
-          if (b >= A.Lj) continue;
-          const int cb = __ldg(cB + b);
+          for (int y = 0; y < VT_TY; ++y) {
+            const int b = b0 + y;
+            if (b >= A.Lj) continue;
 #pragma unroll
-          for (int x = 0; x < VT_TX; ++x) {
-            const int a = a0 + x;
-            if (a >= A.Li) continue;
-            const float c = acc[y][x];
-            if (MODE == MODE_BWDC) {
-              A.Cout[ch * A.plane + (int64_t)b * A.Pa + a] = c;
-            } else {
+            for (int x = 0; x < VT_TX; ++x)
+              if (a0 + x < A.Li) A.Cout[ch * A.plane + (int64_t)b * A.Pa + a0 + x] = acc[y][x];
+          }
+        } else {
+          cp_async_wait_all();  // this thread's X tile has landed in xin
+          const int* cA = A.clsA + (sa + 1) * A.Li;
+          const int* cB = A.clsB + (sb + 1) * A.Lj;
+          float* Xch = A.X + ch * A.plane;
+#pragma unroll
+          for (int y = 0; y < VT_TY; ++y) {
+            const int b = b0 + y;
+            if (b >= A.Lj) continue;
+            const int cb = __ldg(cB + b);
+            float* xrow = xin + (b + Q) * A.XP + a0 + QP;
+#pragma unroll
+            for (int x = 0; x < VT_TX; ++x) {
+              const int a = a0 + x;
+              if (a >= A.Li) continue;
+              const float c = acc[y][x];
               const float d = dtab[cb * A.maxc + __ldg(cA + a)];
-              const float xo = xv[y][x];
+              const float xo = xrow[x];
               float xc = xo * c / d;                       // :130  X .* C ./ D
               if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;     // :132-134 NaN, Inf, < 0
               float xn = xc * A.w + (1.f - A.w) * xo;       // :136
               if (xn < 0.f) xn = 0.f;                      // :137
-              xv[y][x] = xn;
+              xrow[x] = xn;
+              Xch[(int64_t)b * A.Pa + a] = xn;
             }
           }
         }
-      }
-      if (MODE != MODE_BWDC) {
-#pragma unroll
-        for (int y = 0; y < VT_TY; ++y) {
-          const int b = b0 + y;
-          if (b >= A.Lj) continue;
-          if (MODE == MODE_STEP) {
-            float* dst = A.X + ch * A.plane + (int64_t)b * A.Pa + a0;
-#pragma unroll
-            for (int x = 0; x < VT_TX; ++x)
-              if (a0 + x < A.Li) dst[x] = xv[y][x];
-          }
-#pragma unroll
-          for (int x = 0; x < VT_TX; ++x)
-            if (a0 + x < A.Li) xin[(b + A.q) * A.XP + a0 + x + A.q] = xv[y][x];
-        }
+      } else {
+        cp_async_wait_all();
       }
     }
     __syncthreads();
-    if (MODE != MODE_BWDC && (MODE == MODE_FWD || A.do_fwd) && active && lt < A.tps) {
-      conv_tile<T, 0>(xin + b0 * A.XP + a0, A.XP, wfs, hx);
+    if (XIN && (MODE == MODE_FWD || A.do_fwd) && active && lt < A.tps)
+      conv_tile<T, QP - Q>(xin + b0 * A.XP + a0, A.XP, wfs, hx);
+    // taps of the next channel into the other buffer (read after the barrier below)
+    {
+      const int64_t nxt = ch + step;
+      float* nb = taps + (buf ^ 1) * 2 * TT;
+      if (slot_ok && nxt < A.nch) {
+        for (int i = lt; i < TT; i += A.tps) {
+          if (BWD) nb[i] = __ldg(A.wb + nxt * TT + i);
+          if (XIN) nb[TT + i] = __ldg(A.wf + nxt * TT + i);
+        }
+      }
     }
     __syncthreads();
   }
@@ -239,7 +251,7 @@ __global__ void __launch_bounds__(256) k_view(ViewArgs A) {
   float* red = slot_base;  // reuse: [slots][Lj*Li]
   const int LL = A.Li * A.Lj;
   __syncthreads();
-  if (slot_ok && lt < A.tps) {
+  if (tile_ok) {
 #pragma unroll
     for (int y = 0; y < VT_TY; ++y) {
       const int b = b0 + y;
