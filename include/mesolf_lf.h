@@ -147,6 +147,21 @@ int mlf_rl_view_step(mlf_solver* s, const float* lfimg, float* vol, int32_t u, i
  * filter bank :44-61), applied in place to vol (dev, Xr x Xc x Z). */
 int mlf_sample_filter(mlf_solver* s, float* vol, void* stream);
 
+/* Forward projection of one view that allocates no device memory (no counterpart in the
+ * reference; the regular form is mlf_forward_view).  For callers that cannot call
+ * cudaMalloc/cudaFree: a MEX function working inside MATLAB's GPU memory manager, or a
+ * frame callback of the acquisition loop that must not block on the device-wide
+ * synchronisation allocation can cause.  Same result as mlf_forward_view(u, v):
+ *   hx (dev, Xr/N x Xc/N) = (sum_z conv2(vol_z, Hps(:,:,u,v,z), 'same'))((N+1)/2:N:end, ...)
+ * for vol (dev, Xr x Xc x Z, MATLAB layout), with the PSF's resident taps.
+ * Scratch: a static device array of 2 Mi floats (8 MiB) that every GPU loading the
+ * library holds until exit; (Xr/N)*(Xc/N) must not exceed it (MLF_ERR_INVALID otherwise).
+ * The first call on a device looks the array up with that device current: make it before
+ * any stream capture.  Calls share the array, so calls whose kernels overlap on the GPU
+ * (other streams or threads) race and must be serialised by the caller. */
+int mlf_forward_view_static(const mlf_psf* psf, const float* vol, int64_t Xr, int64_t Xc, int32_t u,
+                            int32_t v, float* hx, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,6 +42,7 @@ SIGNATURES = {
     "mlf_backward_view": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
     "mlf_rl_view_step": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, ctypes.c_double, _vp]),
     "mlf_sample_filter": (ctypes.c_int, [_vp, _vp, _vp]),
+    "mlf_forward_view_static": (ctypes.c_int, [_vp, _vp, _i64, _i64, _i32, _i32, _vp, _vp]),
 }
 
 
