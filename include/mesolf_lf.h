@@ -41,7 +41,8 @@ enum mlf_status_code {
 enum mlf_precision {
   MLF_PREC_FP32 = 0,       /* plain FP32 FMA projector (the drop-in path) */
   MLF_PREC_BF16X3 = 1,     /* tensor-core BF16 split hi+lo operands, FP32 accumulate */
-  MLF_PREC_BF16 = 2        /* tensor-core single BF16 operands, FP32 accumulate */
+  MLF_PREC_BF16 = 2,       /* tensor-core single BF16 operands, FP32 accumulate */
+  MLF_PREC_BF16X2 = 3      /* tensor-core BF16, taps split hi+lo (2 passes), FP32 accumulate */
 };
 
 typedef struct mlf_psf mlf_psf;       /* phase-space PSF resident in HBM */
@@ -143,6 +144,12 @@ int mlf_backward_view(mlf_solver* s, const float* proj, int32_t u, int32_t v, fl
  * Uses the solver's volume buffer as scratch. */
 int mlf_rl_view_step(mlf_solver* s, const float* lfimg, float* vol, int32_t u, int32_t v, double w,
                      void* stream);
+/* The same view step and forward projection at a given enum mlf_precision (the
+ * tensor-core forms for MLF_PREC_BF16*). */
+int mlf_rl_view_step_prec(mlf_solver* s, const float* lfimg, float* vol, int32_t u, int32_t v, double w,
+                          int32_t precision, void* stream);
+int mlf_forward_view_prec(mlf_solver* s, const float* vol, int32_t u, int32_t v, int32_t precision,
+                          float* hx, void* stream);
 /* The per-iteration flux-preserving NIP low-pass, sample_filter (recon_…_with_filter.m:222-240,
  * filter bank :44-61), applied in place to vol (dev, Xr x Xc x Z). */
 int mlf_sample_filter(mlf_solver* s, float* vol, void* stream);

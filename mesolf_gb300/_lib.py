@@ -18,6 +18,7 @@ MLF_ERR_CANCELLED = 6
 MLF_PREC_FP32 = 0
 MLF_PREC_BF16X3 = 1
 MLF_PREC_BF16 = 2
+MLF_PREC_BF16X2 = 3
 
 #: Every symbol declared in include/mesolf_lf.h, with (restype, argtypes).
 _vp = ctypes.c_void_p
@@ -42,6 +43,8 @@ SIGNATURES = {
     "mlf_backward_view": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
     "mlf_rl_view_step": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, ctypes.c_double, _vp]),
     "mlf_sample_filter": (ctypes.c_int, [_vp, _vp, _vp]),
+    "mlf_rl_view_step_prec": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, ctypes.c_double, _i32, _vp]),
+    "mlf_forward_view_prec": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i32, _vp, _vp]),
     "mlf_forward_view_static": (ctypes.c_int, [_vp, _vp, _i64, _i64, _i32, _i32, _vp, _vp]),
 }
 

@@ -22,7 +22,8 @@ import numpy as np
 from . import _lib
 from ._lib import MLFStats, check
 
-PRECISIONS = {"fp32": _lib.MLF_PREC_FP32, "bf16x3": _lib.MLF_PREC_BF16X3, "bf16": _lib.MLF_PREC_BF16}
+PRECISIONS = {"fp32": _lib.MLF_PREC_FP32, "bf16x3": _lib.MLF_PREC_BF16X3, "bf16": _lib.MLF_PREC_BF16,
+              "bf16x2": _lib.MLF_PREC_BF16X2}
 
 
 def _is_torch(x):
@@ -169,13 +170,18 @@ class RLSolver:
         del lk, wk
         return out
 
-    def forward_view(self, vol, u, v, stream=None):
+    def forward_view(self, vol, u, v, stream=None, precision="fp32"):
         """HX of view (u, v) (0-based) for a device volume -> (Xr/N, Xc/N) device array."""
         import torch
         vk, vp = _fortran(vol)
         hx = torch.empty((self.Xc // self.psf.N, self.Xr // self.psf.N), dtype=torch.float32,
                          device=vol.device).t()
-        check(_lib.load().mlf_forward_view(self._h, vp, int(u), int(v), hx.data_ptr(), _stream_of(vol, stream)))
+        if precision == "fp32":
+            check(_lib.load().mlf_forward_view(self._h, vp, int(u), int(v), hx.data_ptr(),
+                                               _stream_of(vol, stream)))
+        else:
+            check(_lib.load().mlf_forward_view_prec(self._h, vp, int(u), int(v), PRECISIONS[precision],
+                                                    hx.data_ptr(), _stream_of(vol, stream)))
         del vk
         return hx
 
@@ -187,11 +193,11 @@ class RLSolver:
         del pk
         return out
 
-    def view_step(self, lfimg, vol, u, v, w, stream=None):
+    def view_step(self, lfimg, vol, u, v, w, stream=None, precision="fp32"):
         """One RL view update of a device volume in place (``…_with_filter.m:109-137``)."""
         lk, lp = _fortran(lfimg)
-        check(_lib.load().mlf_rl_view_step(self._h, lp, vol.data_ptr(), int(u), int(v), float(w),
-                                           _stream_of(vol, stream)))
+        check(_lib.load().mlf_rl_view_step_prec(self._h, lp, vol.data_ptr(), int(u), int(v), float(w),
+                                                PRECISIONS[precision], _stream_of(vol, stream)))
         del lk
         return vol
 

@@ -238,7 +238,7 @@ int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (!s || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_solver_run: null pointer");
   if (max_iter < 0) return fail(MLF_ERR_INVALID, "mlf_solver_run: maxIter must be >= 0");
-  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16)
+  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2)
     return fail(MLF_ERR_INVALID, "mlf_solver_run: unknown precision");
   const size_t n_img = (size_t)(s->Xr * s->Xc), n_vol = n_img * s->Z;
   const float *dlf = nullptr, *dwarm = nullptr;
@@ -285,11 +285,27 @@ int mlf_backward_view(mlf_solver* s, const float* proj, int32_t u, int32_t v, fl
 
 int mlf_rl_view_step(mlf_solver* s, const float* lfimg, float* vol, int32_t u, int32_t v, double w,
                      void* stream) {
+  return mlf_rl_view_step_prec(s, lfimg, vol, u, v, w, MLF_PREC_FP32, stream);
+}
+
+int mlf_rl_view_step_prec(mlf_solver* s, const float* lfimg, float* vol, int32_t u, int32_t v, double w,
+                          int32_t precision, void* stream) {
   clear_error();
   if (!s || !lfimg || !vol) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: null pointer");
   if (u < 0 || v < 0 || u >= s->N || v >= s->N) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: view out of range");
+  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: unknown precision");
   if (!is_device_ptr(lfimg) || !is_device_ptr(vol)) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: device pointers required");
-  return rl_view_step(s, lfimg, vol, u, v, w, static_cast<cudaStream_t>(stream));
+  return rl_view_step(s, lfimg, vol, u, v, w, precision, static_cast<cudaStream_t>(stream));
+}
+
+int mlf_forward_view_prec(mlf_solver* s, const float* vol, int32_t u, int32_t v, int32_t precision, float* hx,
+                          void* stream) {
+  clear_error();
+  if (!s || !vol || !hx) return fail(MLF_ERR_INVALID, "mlf_forward_view_prec: null pointer");
+  if (u < 0 || v < 0 || u >= s->N || v >= s->N) return fail(MLF_ERR_INVALID, "mlf_forward_view_prec: view out of range");
+  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2) return fail(MLF_ERR_INVALID, "mlf_forward_view_prec: unknown precision");
+  if (!is_device_ptr(vol) || !is_device_ptr(hx)) return fail(MLF_ERR_INVALID, "mlf_forward_view_prec: device pointers required");
+  return forward_view_prec(s, vol, u, v, precision, hx, static_cast<cudaStream_t>(stream));
 }
 
 int mlf_sample_filter(mlf_solver* s, float* vol, void* stream) {

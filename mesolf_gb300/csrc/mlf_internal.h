@@ -44,6 +44,11 @@ struct DevBuf {
 // true if ptr is device (or managed) memory usable by kernels on the current device
 bool is_device_ptr(const void* ptr);
 
+struct TcPsfState;     // tensor-core operands of a PSF (mlf_tc.cu)
+struct TcSolverState;  // tensor-core scratch of a solver (mlf_tc.cu)
+void tc_psf_free(TcPsfState* t);
+void tc_solver_free(TcSolverState* t);
+
 // ------------------------------------------------------------------ PSF
 // Per-view projector taps in phase-major ("polyphase") form.  For view (u, v) (0-based,
 // view = u + N*v) and volume channel ch = (beta*N + alpha)*Z + z the forward taps are
@@ -59,7 +64,9 @@ struct Psf {
   DevBuf wf, wb;             // float [N*N][nch][T*T]
   std::vector<double> weights;  // N*N, index u + N*v (MATLAB weight(u+1, v+1))
   std::vector<int> view_order;  // active views in spiral order (view = u + N*v)
-  size_t bytes() const { return wf.bytes + wb.bytes; }
+  TcPsfState* tc = nullptr;     // built on the first tensor-core solve
+  ~Psf() { tc_psf_free(tc); }
+  size_t bytes() const;
 };
 
 // ------------------------------------------------------------------ solver
@@ -103,6 +110,7 @@ struct Solver {
   std::vector<cudaEvent_t> tev;
   int tev_used = 0;
   bool timing = false;
+  TcSolverState* tc = nullptr;  // built on the first tensor-core solve
   ~Solver();
   size_t bytes() const;
 };
@@ -114,9 +122,22 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
                float* d_out, mlf_stats* stats, cudaStream_t st);
 int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaStream_t st);
 int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cudaStream_t st);
-int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, double w, cudaStream_t st);
+int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, double w, int precision,
+                 cudaStream_t st);
+int forward_view_prec(Solver* s, const float* d_vol, int u, int v, int precision, float* d_hx, cudaStream_t st);
 int sample_filter(Solver* s, float* d_vol, cudaStream_t st);
 int filter_init(Solver* s);
+int timing_mark(Solver* s, cudaStream_t st);
+// tensor-core path (mlf_tc.cu)
+int tc_psf_prepare(Psf* p, cudaStream_t st);
+int tc_solver_prepare(Solver* s, cudaStream_t st);
+int tc_enqueue_views(Solver* s, int precision, int64_t* launches, cudaStream_t st);
+int tc_pack_volume(Solver* s, int precision, cudaStream_t st);
+int tc_forward_view(Solver* s, int precision, int view, float* hx_out, cudaStream_t st);
+int tc_view_step(Solver* s, int precision, int view, float w, cudaStream_t st);
+int tc_check_error(Solver* s);
+size_t tc_psf_bytes(const Psf* p);
+size_t tc_solver_bytes(const Solver* s);
 int filter_run(Solver* s, cudaStream_t st);
 int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,
                  int64_t kw, int nnum, float* d_out, cudaStream_t st);

@@ -211,6 +211,8 @@ void build_classes(int L, int q, std::vector<int>& cls, std::vector<std::pair<in
   }
 }
 
+}  // namespace
+
 int timing_mark(Solver* s, cudaStream_t st) {
   if (!s->timing) return MLF_OK;
   if (s->tev_used >= (int)s->tev.size()) {
@@ -224,6 +226,8 @@ int timing_mark(Solver* s, cudaStream_t st) {
   MLF_CUDA(cudaEventRecord(s->tev[s->tev_used++], st));
   return MLF_OK;
 }
+
+namespace {
 
 int run_view(Solver* s, int mode, int view_cur, int view_next, float w, bool do_fwd,
              cudaStream_t st) {
@@ -251,11 +255,13 @@ int run_reduce(Solver* s, int view, float* hx_out, bool ratio, cudaStream_t st) 
 }
 
 // One RL iteration (recon_…_with_filter.m:100-142), stream-ordered.
-int enqueue_iteration(Solver* s, int64_t* launches, cudaStream_t st) {
+int enqueue_iteration(Solver* s, int precision, int64_t* launches, cudaStream_t st) {
   const std::vector<int>& views = s->psf->view_order;
   const int V = (int)views.size();
   int64_t n = 0;
-  if (V > 0) {
+  if (precision != MLF_PREC_FP32) {
+    MLF_TRY(tc_enqueue_views(s, precision, &n, st));
+  } else if (V > 0) {
     MLF_TRY(run_view(s, MODE_FWD, views[0], views[0], 0.f, true, st));
     MLF_TRY(run_reduce(s, views[0], nullptr, true, st));
     n += 2;
@@ -281,13 +287,16 @@ int enqueue_iteration(Solver* s, int64_t* launches, cudaStream_t st) {
 
 Solver::~Solver() {
   for (cudaEvent_t e : tev) cudaEventDestroy(e);
+  tc_solver_free(tc);
 }
 
 size_t Solver::bytes() const {
   return X.bytes + Xtmp.bytes + lfs.bytes + rpad.bytes + part.bytes + hx.bytes + cls.bytes +
          red.bytes + stage_in.bytes + stage_out.bytes + filt.cx.bytes + filt.cy.bytes +
-         filt.sums.bytes;
+         filt.sums.bytes + tc_solver_bytes(this);
 }
+
+size_t Psf::bytes() const { return wf.bytes + wb.bytes + tc_psf_bytes(this); }
 
 bool view_taps_supported(int T) { return T >= 3 && T <= 17 && (T % 2) == 1; }
 
@@ -374,8 +383,7 @@ int solver_init(Solver* s) {
 
 int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const float* d_warm,
                float* d_out, mlf_stats* stats, cudaStream_t st) {
-  if (precision != MLF_PREC_FP32)
-    return fail(MLF_ERR_UNSUPPORTED, "only MLF_PREC_FP32 is built into this library version");
+  if (precision != MLF_PREC_FP32) MLF_TRY(tc_solver_prepare(s, st));
   const Geo g = geo_of(s);
   const int64_t n_img = s->Xr * s->Xc;
   const int64_t n_vol = n_img * s->Z;
@@ -402,7 +410,7 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     launches += 2;
   }
   MLF_CUDA(cudaGetLastError());
-  for (int it = 0; it < max_iter; ++it) MLF_TRY(enqueue_iteration(s, &launches, st));
+  for (int it = 0; it < max_iter; ++it) MLF_TRY(enqueue_iteration(s, precision, &launches, st));
   k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->X.as<float>(), g, d_out);
   ++launches;
   MLF_CUDA(cudaGetLastError());
@@ -426,6 +434,7 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     stats->view_kernel_ms = vk;
     stats->view_kernel_launches = s->tev_used / 2;
     stats->kernel_launches = launches;
+    if (precision != MLF_PREC_FP32) MLF_TRY(tc_check_error(s));
   }
   s->timing = false;
   s->tev_used = 0;
@@ -446,6 +455,15 @@ int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaS
   return run_reduce(s, u + s->N * v, d_hx, false, st);
 }
 
+int forward_view_prec(Solver* s, const float* d_vol, int u, int v, int precision, float* d_hx, cudaStream_t st) {
+  if (precision == MLF_PREC_FP32) return forward_view(s, d_vol, u, v, d_hx, st);
+  const Geo g = geo_of(s);
+  const int64_t n_vol = s->Xr * s->Xc * s->Z;
+  k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->X.as<float>());
+  MLF_CUDA(cudaGetLastError());
+  return tc_forward_view(s, precision, u + s->N * v, d_hx, st);
+}
+
 int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cudaStream_t st) {
   const Geo g = geo_of(s);
   const int LL = s->Li * s->Lj;
@@ -464,16 +482,21 @@ int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cu
   return MLF_OK;
 }
 
-int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, double w, cudaStream_t st) {
+int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, double w, int precision,
+                 cudaStream_t st) {
   const Geo g = geo_of(s);
   const int64_t n_img = s->Xr * s->Xc, n_vol = n_img * s->Z;
   const int view = u + s->N * v;
   k_extract_views<<<grid_for(n_img), 256, 0, st>>>(d_lf, g, s->lfs.as<float>());
   k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->X.as<float>());
   MLF_CUDA(cudaGetLastError());
-  MLF_TRY(run_view(s, MODE_FWD, view, view, 0.f, true, st));
-  MLF_TRY(run_reduce(s, view, nullptr, true, st));
-  MLF_TRY(run_view(s, MODE_STEP, view, -1, (float)w, false, st));
+  if (precision != MLF_PREC_FP32) {
+    MLF_TRY(tc_view_step(s, precision, view, (float)w, st));
+  } else {
+    MLF_TRY(run_view(s, MODE_FWD, view, view, 0.f, true, st));
+    MLF_TRY(run_reduce(s, view, nullptr, true, st));
+    MLF_TRY(run_view(s, MODE_STEP, view, -1, (float)w, false, st));
+  }
   k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->X.as<float>(), g, d_vol);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;

@@ -1,0 +1,761 @@
+// Mixed-precision phase-space RL view step on the 5th-generation tensor cores (tcgen05).
+//
+// The per-view operators of recon_theory_phase_space_LFM_with_filter.m:109-137 are cast
+// as two GEMMs over the lenslet grid (positions p = b*Li + a), the volume channels
+// (ch = (beta*N + alpha)*Z + z) and the projector taps:
+//
+//   back projection   C[p, ch] = sum_t' AR[p, t'] * Wb'[ch, t']        (t' in a (T+2)^2 window)
+//   D = bwd(ones)     D[p, ch] = sum_t' A1[p, t'] * Wb'[ch, t']
+//   update            X[ch][p] <- w*clean(X*C/D) + (1-w)*X              (FP32, epilogue)
+//   forward (next v)  Y[p, t]  = sum_ch Xb[p, ch] * Wf[ch, t]           (split over ch)
+//                     HX[j][i] = sum_t Y[(j+db-q)*Li + (i+da-q), t=(db,da)]  (col2im)
+//
+// AR = im2col of the ratio image R (rows p, columns the 17x17 window around the lenslet,
+// absorbing the per-channel phase shift s_alpha, s_beta into zero-padded taps), A1 = the
+// same im2col of the all-ones image (0/1, exact in BF16).  Operands are BF16, optionally
+// split hi + lo (x = hi + lo, both BF16) with the products accumulated in FP32 in TMEM:
+//   MLF_PREC_BF16    C = ARh Wbh                 Y = Xh Wfh
+//   MLF_PREC_BF16X2  C = ARh (Wbh + Wbl)         Y = Xh (Wfh + Wfl)
+//   MLF_PREC_BF16X3  C = ARh Wbh + ARh Wbl + ARl Wbh, Y likewise
+// (D always uses Wbh + Wbl when the taps are split, so C/D is a weighted mean with the same
+// weights).  The ratio, the update, the depth sums (inside C, D, Y) and the sample filter
+// stay in FP32.
+//
+// Both GEMM kernels are warp-specialised: warp 0 issues TMA tile loads (128-byte swizzle)
+// into a 2-stage shared-memory ring, warp 1 issues tcgen05.mma from one thread into TMEM
+// accumulators, warp 2 owns the TMEM allocation, and all four warps run the epilogue
+// (tcgen05.ld, 32 TMEM lanes per warp).  Every wait is bounded; a timeout sets a device
+// error flag, drains in-flight copies and MMAs, frees TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "mlf_internal.h"
+#include "mlf_tc.cuh"
+
+namespace mlf {
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int BM = 128;           // positions per tile (TMEM lanes)
+constexpr int BK = 64;            // K per stage (one 128-byte swizzle row of BF16)
+constexpr int STAGES = 2;
+constexpr int TILE_A = BM * BK * 2;  // 16 KB
+constexpr uint32_t WAIT_LIMIT = 1u << 22;  // polls; ~0.3-1 s with the back-off sleep
+
+enum TcErr { TC_ERR_TIMEOUT_PRODUCER = 1, TC_ERR_TIMEOUT_MMA = 2, TC_ERR_TIMEOUT_EPILOGUE = 3 };
+
+__device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
+  return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+}
+
+__device__ __forceinline__ void split_bf16(float x, bf16& hi, bf16& lo) {
+  hi = __float2bfloat16_rn(x);
+  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+// ------------------------------------------------------------------ back projection + update
+struct TcBwdArgs {
+  float* X;
+  bf16* xb_hi;
+  bf16* xb_lo;
+  int* err;
+  int64_t plane;
+  float w;
+  int Li, Lj, Pa, LL, CHP, nch, KB, brow0;  // brow0 = view * CHP (row of this view in Wb')
+  int npass_c, npass_d;                     // MMA passes for C (1..3) and D (1..2)
+  int write_lo;                             // also emit the lo half of Xb
+};
+
+constexpr int BWD_BN = 128;  // channels per tile
+constexpr int BWD_OFF_AHI = 0, BWD_OFF_ALO = TILE_A, BWD_OFF_A1 = 2 * TILE_A;
+constexpr int BWD_OFF_BHI = 3 * TILE_A, BWD_OFF_BLO = 4 * TILE_A;
+constexpr int BWD_STAGE = 5 * TILE_A;  // 80 KB
+constexpr size_t BWD_SMEM = (size_t)STAGES * BWD_STAGE + 1024;
+
+__global__ void __launch_bounds__(128, 1)
+k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+         const __grid_constant__ CUtensorMap mA1, const __grid_constant__ CUtensorMap mBh,
+         const __grid_constant__ CUtensorMap mBl, TcBwdArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], accb;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BWD_BN;
+  const int KS = a.KB / BK;
+  const bool need_blo = a.npass_c >= 2 || a.npass_d >= 2;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(&accb, 1);
+    tc::fence_mbar_init();
+    abort_flag = 0;
+    tc::tma_prefetch_desc(&mAh);
+    tc::tma_prefetch_desc(&mA1);
+    tc::tma_prefetch_desc(&mBh);
+  }
+  if (warp == 2) tc::tmem_alloc(&tmem_base, 256);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tC = tmem_base, tD = tmem_base + 128;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    // Ah + A1 + Bh always; Al for three passes; Bl when the taps are split
+    const uint32_t bytes = 3 * TILE_A + (a.npass_c >= 3 ? TILE_A : 0) + (need_blo ? TILE_A : 0);
+    int issued = 0;
+    for (int ks = 0; ks < KS; ++ks) {
+      const int s = ks % STAGES;
+      const uint32_t ph = (ks / STAGES) & 1;
+      if (!tc::mbar_wait(&empty[s], ph ^ 1, WAIT_LIMIT)) {
+        abort_flag = 1;
+        atomicExch(a.err, TC_ERR_TIMEOUT_PRODUCER);
+        break;
+      }
+      uint8_t* st = smem + s * BWD_STAGE;
+      tc::mbar_arrive_expect_tx(&full[s], bytes);
+      tc::tma_load_2d(st + BWD_OFF_AHI, &mAh, &full[s], ks * BK, m0);
+      if (a.npass_c >= 3) tc::tma_load_2d(st + BWD_OFF_ALO, &mAl, &full[s], ks * BK, m0);
+      tc::tma_load_2d(st + BWD_OFF_A1, &mA1, &full[s], ks * BK, m0);
+      tc::tma_load_2d(st + BWD_OFF_BHI, &mBh, &full[s], ks * BK, a.brow0 + n0);
+      if (need_blo) tc::tma_load_2d(st + BWD_OFF_BLO, &mBl, &full[s], ks * BK, a.brow0 + n0);
+      ++issued;
+    }
+    // drain: every issued copy must have landed before the CTA can exit
+    for (int ks = std::max(0, issued - STAGES); ks < issued; ++ks)
+      tc::mbar_wait(&full[ks % STAGES], (ks / STAGES) & 1, WAIT_LIMIT);
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    const uint32_t idesc = tc::idesc_bf16_f32(BM, BWD_BN);
+    for (int ks = 0; ks < KS; ++ks) {
+      const int s = ks % STAGES;
+      const uint32_t ph = (ks / STAGES) & 1;
+      if (abort_flag || !tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
+        abort_flag = 1;
+        atomicExch(a.err, TC_ERR_TIMEOUT_MMA);
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t st = tc::smem_u32(smem + s * BWD_STAGE);
+#pragma unroll
+      for (int k = 0; k < BK / 16; ++k) {
+        const uint32_t acc = (ks > 0 || k > 0) ? 1u : 0u;
+        const uint64_t dah = tc::desc_kmajor_sw128(st + BWD_OFF_AHI + 32 * k);
+        const uint64_t da1 = tc::desc_kmajor_sw128(st + BWD_OFF_A1 + 32 * k);
+        const uint64_t dbh = tc::desc_kmajor_sw128(st + BWD_OFF_BHI + 32 * k);
+        tc::mma_bf16(tC, dah, dbh, idesc, acc);
+        tc::mma_bf16(tD, da1, dbh, idesc, acc);
+        if (need_blo) {
+          const uint64_t dbl = tc::desc_kmajor_sw128(st + BWD_OFF_BLO + 32 * k);
+          if (a.npass_c >= 2) tc::mma_bf16(tC, dah, dbl, idesc, 1u);
+          if (a.npass_d >= 2) tc::mma_bf16(tD, da1, dbl, idesc, 1u);
+        }
+        if (a.npass_c >= 3) {
+          const uint64_t dal = tc::desc_kmajor_sw128(st + BWD_OFF_ALO + 32 * k);
+          tc::mma_bf16(tC, dal, dbh, idesc, 1u);
+        }
+      }
+      tc::mma_commit(&empty[s]);
+    }
+    tc::mma_commit(&accb);  // always: completes once every issued MMA has finished
+  }
+  __syncwarp();
+
+  // ---------------- epilogue: update X, emit Xb (all 4 warps, 32 TMEM lanes each)
+  const bool ok = tc::mbar_wait(&accb, 0, WAIT_LIMIT);
+  tc::tc_fence_after();
+  if (!ok && lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
+  const int row = warp * 32 + lane;
+  const int pos = m0 + row;
+  const bool pos_ok = pos < a.LL;
+  const int b = pos_ok ? pos / a.Li : 0, aa = pos_ok ? pos - b * a.Li : 0;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  if (ok) {
+    for (int c = 0; c < BWD_BN / 16; ++c) {
+      float cv[16], dv[16];
+      tc::tmem_ld16(tC + lane_off + c * 16, cv);
+      tc::tmem_ld16(tD + lane_off + c * 16, dv);
+      if (abort_flag) continue;
+      __align__(16) bf16 hi[16];
+      __align__(16) bf16 lo[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int ch = n0 + c * 16 + j;
+        float xn = 0.f;
+        if (pos_ok && ch < a.nch) {
+          float* xp = a.X + (int64_t)ch * a.plane + (int64_t)b * a.Pa + aa;
+          const float xo = *xp;
+          float xc = xo * cv[j] / dv[j];                 // :130  X .* C ./ D
+          if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;        // :132-134
+          xn = xc * a.w + (1.f - a.w) * xo;               // :136
+          if (xn < 0.f) xn = 0.f;                         // :137
+          *xp = xn;
+        }
+        split_bf16(xn, hi[j], lo[j]);
+      }
+      uint4* dh = reinterpret_cast<uint4*>(a.xb_hi + (int64_t)pos * a.CHP + n0 + c * 16);
+      dh[0] = reinterpret_cast<uint4*>(hi)[0];
+      dh[1] = reinterpret_cast<uint4*>(hi)[1];
+      if (a.write_lo) {
+        uint4* dl = reinterpret_cast<uint4*>(a.xb_lo + (int64_t)pos * a.CHP + n0 + c * 16);
+        dl[0] = reinterpret_cast<uint4*>(lo)[0];
+        dl[1] = reinterpret_cast<uint4*>(lo)[1];
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 2) tc::tmem_dealloc(tmem_base, 256);
+}
+
+// ------------------------------------------------------------------ forward projection
+struct TcFwdArgs {
+  float* ypart;  // [split][MP][NB]
+  int* err;
+  int MP, NB, NH, nparts, ks_per_split, KS, frow0, npass;  // frow0 = view * NB
+};
+
+__global__ void __launch_bounds__(128, 1)
+k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+         const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, TcFwdArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], accb;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM;
+  const int split = blockIdx.y;
+  const int ks0 = split * a.ks_per_split;
+  const int ks1 = min(a.KS, ks0 + a.ks_per_split);
+  const int tileB = a.NB * 128;  // NB rows x 128 bytes
+  const int offAl = TILE_A, offBh = 2 * TILE_A, offBl = 2 * TILE_A + tileB;
+  const int stage_bytes = 2 * TILE_A + 2 * tileB;
+  const uint32_t tcols = a.NB > 256 ? 512u : 256u;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(&accb, 1);
+    tc::fence_mbar_init();
+    abort_flag = 0;
+    tc::tma_prefetch_desc(&mAh);
+    tc::tma_prefetch_desc(&mBh);
+  }
+  if (warp == 2) tc::tmem_alloc(&tmem_base, tcols);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tY = tmem_base;
+
+  if (warp == 0 && lane == 0) {
+    const uint32_t bytes = TILE_A * (a.npass >= 3 ? 2 : 1) + tileB * (a.npass >= 2 ? 2 : 1);
+    int issued = 0;
+    for (int ks = ks0; ks < ks1; ++ks) {
+      const int i = ks - ks0, s = i % STAGES;
+      const uint32_t ph = (i / STAGES) & 1;
+      if (!tc::mbar_wait(&empty[s], ph ^ 1, WAIT_LIMIT)) {
+        abort_flag = 1;
+        atomicExch(a.err, TC_ERR_TIMEOUT_PRODUCER);
+        break;
+      }
+      uint8_t* st = smem + s * stage_bytes;
+      tc::mbar_arrive_expect_tx(&full[s], bytes);
+      tc::tma_load_2d(st, &mAh, &full[s], ks * BK, m0);
+      if (a.npass >= 3) tc::tma_load_2d(st + offAl, &mAl, &full[s], ks * BK, m0);
+      for (int p = 0; p < a.nparts; ++p) {
+        tc::tma_load_2d(st + offBh + p * a.NH * 128, &mBh, &full[s], ks * BK, a.frow0 + p * a.NH);
+        if (a.npass >= 2)
+          tc::tma_load_2d(st + offBl + p * a.NH * 128, &mBl, &full[s], ks * BK, a.frow0 + p * a.NH);
+      }
+      ++issued;
+    }
+    for (int i = std::max(0, issued - STAGES); i < issued; ++i)
+      tc::mbar_wait(&full[i % STAGES], (i / STAGES) & 1, WAIT_LIMIT);
+  } else if (warp == 1 && lane == 0) {
+    const uint32_t idesc = tc::idesc_bf16_f32(BM, a.NH);
+    for (int ks = ks0; ks < ks1; ++ks) {
+      const int i = ks - ks0, s = i % STAGES;
+      const uint32_t ph = (i / STAGES) & 1;
+      if (abort_flag || !tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
+        abort_flag = 1;
+        atomicExch(a.err, TC_ERR_TIMEOUT_MMA);
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t st = tc::smem_u32(smem + s * stage_bytes);
+#pragma unroll
+      for (int k = 0; k < BK / 16; ++k) {
+        const uint32_t acc = (i > 0 || k > 0) ? 1u : 0u;
+        const uint64_t dah = tc::desc_kmajor_sw128(st + 32 * k);
+        for (int p = 0; p < a.nparts; ++p) {
+          const uint32_t dcol = tY + p * a.NH;
+          const uint64_t dbh = tc::desc_kmajor_sw128(st + offBh + p * a.NH * 128 + 32 * k);
+          tc::mma_bf16(dcol, dah, dbh, idesc, acc);
+          if (a.npass >= 2) {
+            const uint64_t dbl = tc::desc_kmajor_sw128(st + offBl + p * a.NH * 128 + 32 * k);
+            tc::mma_bf16(dcol, dah, dbl, idesc, 1u);
+          }
+          if (a.npass >= 3) {
+            const uint64_t dal = tc::desc_kmajor_sw128(st + offAl + 32 * k);
+            tc::mma_bf16(dcol, dal, dbh, idesc, 1u);
+          }
+        }
+      }
+      tc::mma_commit(&empty[s]);
+    }
+    tc::mma_commit(&accb);
+  }
+  __syncwarp();
+  const bool ok = tc::mbar_wait(&accb, 0, WAIT_LIMIT);
+  tc::tc_fence_after();
+  if (!ok && lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
+  const int row = warp * 32 + lane;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  float* out = a.ypart + ((int64_t)split * a.MP + m0 + row) * a.NB;
+  const bool empty_split = ks1 <= ks0;
+  if (ok) {
+    for (int c = 0; c < (a.nparts * a.NH) / 16; ++c) {
+      float v[16];
+      tc::tmem_ld16(tY + lane_off + c * 16, v);
+      if (abort_flag) continue;
+      if (empty_split) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0.f;
+      }
+      float4* o = reinterpret_cast<float4*>(out + c * 16);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 2) tc::tmem_dealloc(tmem_base, tcols);
+}
+
+// ------------------------------------------------------------------ small kernels
+// Extended back-projection taps, BF16 hi/lo:  Wb'[view][ch][t'] for the (T+2)^2 window,
+// t' = dj'*(T+2) + di', holding wb[view][ch][(dj'-sb-1)*T + (di'-sa-1)] (0 elsewhere).
+__global__ void k_tc_build_wbx(const float* __restrict__ wb, int N, int Z, int T, int64_t nch, int CHP, int KB,
+                               bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  const int T2 = T + 2, h = (N - 1) / 2;
+  const int64_t total = (int64_t)N * N * CHP * KB;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e % KB);
+    const int64_t r = e / KB;
+    const int64_t ch = r % CHP;
+    const int view = (int)(r / CHP);
+    float val = 0.f;
+    if (ch < nch && k < T2 * T2) {
+      const int u = view % N, v = view / N;
+      const int alpha = (int)((ch / Z) % N), beta = (int)(ch / ((int64_t)Z * N));
+      const int sa = (alpha - u + h + N) / N - 1, sb = (beta - v + h + N) / N - 1;  // floor division
+      const int dj = k / T2 - sb - 1, di = k % T2 - sa - 1;
+      if (dj >= 0 && dj < T && di >= 0 && di < T)
+        val = wb[((int64_t)view * nch + ch) * T * T + dj * T + di];
+    }
+    bf16 h16, l16;
+    split_bf16(val, h16, l16);
+    hi[e] = h16;
+    lo[e] = l16;
+  }
+}
+
+// Forward taps transposed, BF16 hi/lo: Wf'[view][t][ch] = wf[view][ch][t] (t < T^2).
+__global__ void k_tc_build_wft(const float* __restrict__ wf, int N, int T, int64_t nch, int CHP, int NB,
+                               bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  const int64_t total = (int64_t)N * N * NB * CHP;
+  const int TT = T * T;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ch = e % CHP;
+    const int64_t r = e / CHP;
+    const int t = (int)(r % NB);
+    const int view = (int)(r / NB);
+    float val = 0.f;
+    if (ch < nch && t < TT) val = wf[((int64_t)view * nch + ch) * TT + t];
+    bf16 h16, l16;
+    split_bf16(val, h16, l16);
+    hi[e] = h16;
+    lo[e] = l16;
+  }
+}
+
+// im2col of the ratio image (or of ones when R == nullptr) over the (T+2)^2 window.
+__global__ void k_tc_im2col(const float* __restrict__ R, int Li, int Lj, int LL, int MP, int T, int KB,
+                            bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  const int T2 = T + 2, q = (T - 1) / 2;
+  const int64_t total = (int64_t)MP * KB;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e % KB);
+    const int pos = (int)(e / KB);
+    float val = 0.f;
+    if (pos < LL && k < T2 * T2) {
+      const int b = pos / Li, a = pos - (pos / Li) * Li;
+      const int j = b + k / T2 - q - 1, i = a + k % T2 - q - 1;
+      if (j >= 0 && j < Lj && i >= 0 && i < Li) val = R ? R[j * Li + i] : 1.f;
+    }
+    bf16 h16, l16;
+    split_bf16(val, h16, l16);
+    hi[e] = h16;
+    if (lo) lo[e] = l16;
+  }
+}
+
+// Phase-major FP32 volume -> Xb[p][ch] BF16 hi/lo (32x32 tiles through shared memory).
+__global__ void k_tc_pack_x(const float* __restrict__ X, int Li, int Pa, int LL, int64_t plane, int64_t nch,
+                            int CHP, int MP, bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  __shared__ float t[32][33];
+  const int p0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const int ch = c0 + r, p = p0 + tx;
+    float v = 0.f;
+    if (ch < nch && p < LL) v = X[(int64_t)ch * plane + (int64_t)(p / Li) * Pa + p % Li];
+    t[r][tx] = v;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int p = p0 + r, ch = c0 + tx;
+    if (p < MP && ch < CHP) {
+      bf16 h16, l16;
+      split_bf16(t[tx][r], h16, l16);
+      hi[(int64_t)p * CHP + ch] = h16;
+      if (lo) lo[(int64_t)p * CHP + ch] = l16;
+    }
+  }
+}
+
+// HX[j][i] = sum_split sum_{db,da} Y[split][(j+db-q)*Li + (i+da-q)][db*T+da]; ratio -> R.
+__global__ void k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, int Li, int Lj,
+                                  int T, const float* __restrict__ lfsub, float* __restrict__ hx_out,
+                                  float* __restrict__ rimg) {
+  const int LL = Li * Lj;
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i0 >= LL) return;
+  const int q = (T - 1) / 2;
+  const int j = i0 / Li, i = i0 - (i0 / Li) * Li;
+  float s = 0.f;
+  for (int db = 0; db < T; ++db) {
+    const int b = j + db - q;
+    if (b < 0 || b >= Lj) continue;
+    for (int da = 0; da < T; ++da) {
+      const int a = i + da - q;
+      if (a < 0 || a >= Li) continue;
+      const int64_t p = (int64_t)b * Li + a;
+      for (int sp = 0; sp < splits; ++sp) s += ypart[((int64_t)sp * MP + p) * NB + db * T + da];
+    }
+  }
+  if (hx_out) hx_out[i0] = s;
+  if (rimg) {
+    float r = lfsub[i0] / s;
+    if (!isfinite(r)) r = 0.f;
+    rimg[i0] = r;
+  }
+}
+
+// ------------------------------------------------------------------ host side
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int get_encoder() {
+  if (g_encode) return MLF_OK;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  MLF_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+  if (q != cudaDriverEntryPointSuccess || !fn)
+    return fail(MLF_ERR_CUDA, "cuTensorMapEncodeTiled not available from the driver");
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return MLF_OK;
+}
+
+// 2-D BF16 matrix [rows][cols] (cols contiguous, multiple of 64), box 64 x box_rows, SW128.
+int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+  MLF_TRY(get_encoder());
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * 2};
+  cuuint32_t box[2] = {64, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(MLF_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return MLF_OK;
+}
+
+inline int rup(int a, int b) { return (a + b - 1) / b * b; }
+
+}  // namespace
+
+struct TcPsfState {
+  int KB = 0, NB = 0, NH = 0, nparts = 1, CHP = 0;
+  DevBuf wbx_hi, wbx_lo, wft_hi, wft_lo;
+  CUtensorMap mBh, mBl, mFh, mFl;
+};
+
+struct TcSolverState {
+  int MP = 0, splits = 1, ks_per_split = 0, KSF = 0;
+  DevBuf ar_hi, ar_lo, a1, xb_hi, xb_lo, ypart, rimg, err;
+  CUtensorMap mARh, mARl, mA1, mXh, mXl;
+};
+
+void tc_psf_free(TcPsfState* t) { delete t; }
+void tc_solver_free(TcSolverState* t) { delete t; }
+
+int tc_psf_prepare(Psf* p, cudaStream_t st) {
+  if (p->tc) return MLF_OK;
+  if (p->T > 17) return fail(MLF_ERR_UNSUPPORTED, "tensor-core path: tap count above 17");
+  std::unique_ptr<TcPsfState> t(new TcPsfState());
+  t->KB = rup((p->T + 2) * (p->T + 2), BK);
+  const int TT = p->T * p->T;
+  t->NB = rup(TT, 16);
+  if (t->NB > 256) {
+    t->NB = rup(TT, 32);
+    t->NH = t->NB / 2;
+    t->nparts = 2;
+  } else {
+    t->NH = t->NB;
+    t->nparts = 1;
+  }
+  t->CHP = rup((int)p->nch, 128);
+  const int V = p->N * p->N;
+  const size_t nb = (size_t)V * t->CHP * t->KB, nf = (size_t)V * t->NB * t->CHP;
+  MLF_TRY(t->wbx_hi.alloc(nb * 2, "tc back-projection taps"));
+  MLF_TRY(t->wbx_lo.alloc(nb * 2, "tc back-projection taps"));
+  MLF_TRY(t->wft_hi.alloc(nf * 2, "tc forward taps"));
+  MLF_TRY(t->wft_lo.alloc(nf * 2, "tc forward taps"));
+  k_tc_build_wbx<<<4096, 256, 0, st>>>(p->wb.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP, t->KB,
+                                       t->wbx_hi.as<bf16>(), t->wbx_lo.as<bf16>());
+  k_tc_build_wft<<<4096, 256, 0, st>>>(p->wf.as<float>(), p->N, p->T, p->nch, t->CHP, t->NB,
+                                       t->wft_hi.as<bf16>(), t->wft_lo.as<bf16>());
+  MLF_CUDA(cudaGetLastError());
+  MLF_TRY(make_map(&t->mBh, t->wbx_hi.p, (uint64_t)V * t->CHP, t->KB, BWD_BN));
+  MLF_TRY(make_map(&t->mBl, t->wbx_lo.p, (uint64_t)V * t->CHP, t->KB, BWD_BN));
+  MLF_TRY(make_map(&t->mFh, t->wft_hi.p, (uint64_t)V * t->NB, t->CHP, t->NH));
+  MLF_TRY(make_map(&t->mFl, t->wft_lo.p, (uint64_t)V * t->NB, t->CHP, t->NH));
+  MLF_CUDA(cudaFuncSetAttribute(k_tc_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BWD_SMEM));
+  const size_t fsmem = (size_t)STAGES * (2 * TILE_A + 2 * t->NB * 128) + 1024;
+  MLF_CUDA(cudaFuncSetAttribute(k_tc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+  p->tc = t.release();
+  return MLF_OK;
+}
+
+size_t tc_psf_bytes(const Psf* p) {
+  if (!p->tc) return 0;
+  return p->tc->wbx_hi.bytes + p->tc->wbx_lo.bytes + p->tc->wft_hi.bytes + p->tc->wft_lo.bytes;
+}
+
+int tc_solver_prepare(Solver* s, cudaStream_t st) {
+  MLF_TRY(tc_psf_prepare(s->psf, st));
+  if (s->tc) return MLF_OK;
+  const TcPsfState* tp = s->psf->tc;
+  std::unique_ptr<TcSolverState> t(new TcSolverState());
+  const int LL = s->Li * s->Lj;
+  t->MP = rup(LL, BM);
+  t->KSF = tp->CHP / BK;
+  int nsm = 0;
+  MLF_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device));
+  const int mt = t->MP / BM;
+  t->splits = std::max(1, std::min(t->KSF, nsm / std::max(1, mt)));
+  t->ks_per_split = (t->KSF + t->splits - 1) / t->splits;
+  t->splits = (t->KSF + t->ks_per_split - 1) / t->ks_per_split;
+  MLF_TRY(t->ar_hi.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
+  MLF_TRY(t->ar_lo.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
+  MLF_TRY(t->a1.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
+  MLF_TRY(t->xb_hi.alloc((size_t)t->MP * tp->CHP * 2, "tc volume"));
+  MLF_TRY(t->xb_lo.alloc((size_t)t->MP * tp->CHP * 2, "tc volume"));
+  MLF_TRY(t->ypart.alloc((size_t)t->splits * t->MP * tp->NB * 4, "tc forward partials"));
+  MLF_TRY(t->rimg.alloc((size_t)LL * 4, "tc ratio image"));
+  MLF_TRY(t->err.alloc(sizeof(int), "tc error flag"));
+  MLF_CUDA(cudaMemsetAsync(t->xb_hi.p, 0, t->xb_hi.bytes, st));
+  MLF_CUDA(cudaMemsetAsync(t->xb_lo.p, 0, t->xb_lo.bytes, st));
+  MLF_CUDA(cudaMemsetAsync(t->err.p, 0, sizeof(int), st));
+  k_tc_im2col<<<1024, 256, 0, st>>>(nullptr, s->Li, s->Lj, LL, t->MP, s->T, tp->KB, t->a1.as<bf16>(), nullptr);
+  MLF_CUDA(cudaGetLastError());
+  MLF_TRY(make_map(&t->mARh, t->ar_hi.p, t->MP, tp->KB, BM));
+  MLF_TRY(make_map(&t->mARl, t->ar_lo.p, t->MP, tp->KB, BM));
+  MLF_TRY(make_map(&t->mA1, t->a1.p, t->MP, tp->KB, BM));
+  MLF_TRY(make_map(&t->mXh, t->xb_hi.p, t->MP, tp->CHP, BM));
+  MLF_TRY(make_map(&t->mXl, t->xb_lo.p, t->MP, tp->CHP, BM));
+  s->tc = t.release();
+  return MLF_OK;
+}
+
+size_t tc_solver_bytes(const Solver* s) {
+  if (!s->tc) return 0;
+  const TcSolverState* t = s->tc;
+  return t->ar_hi.bytes + t->ar_lo.bytes + t->a1.bytes + t->xb_hi.bytes + t->xb_lo.bytes + t->ypart.bytes +
+         t->rimg.bytes + t->err.bytes;
+}
+
+namespace {
+
+void passes_of(int precision, int* pc, int* pd, int* pf) {
+  if (precision == MLF_PREC_BF16) {
+    *pc = 1; *pd = 1; *pf = 1;
+  } else if (precision == MLF_PREC_BF16X2) {
+    *pc = 2; *pd = 2; *pf = 2;
+  } else {
+    *pc = 3; *pd = 2; *pf = 3;
+  }
+}
+
+int tc_fwd_launch(Solver* s, int precision, int view, cudaStream_t st) {
+  const TcPsfState* tp = s->psf->tc;
+  TcSolverState* t = s->tc;
+  int pc, pd, pf;
+  passes_of(precision, &pc, &pd, &pf);
+  TcFwdArgs a{};
+  a.ypart = t->ypart.as<float>();
+  a.err = t->err.as<int>();
+  a.MP = t->MP;
+  a.NB = tp->NB;
+  a.NH = tp->NH;
+  a.nparts = tp->nparts;
+  a.ks_per_split = t->ks_per_split;
+  a.KS = t->KSF;
+  a.frow0 = view * tp->NB;
+  a.npass = pf;
+  const size_t fsmem = (size_t)STAGES * (2 * TILE_A + 2 * tp->NB * 128) + 1024;
+  k_tc_fwd<<<dim3(t->MP / BM, t->splits), 128, fsmem, st>>>(t->mXh, t->mXl, tp->mFh, tp->mFl, a);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+int tc_col2im(Solver* s, int view, bool ratio, float* hx_out, cudaStream_t st) {
+  const TcPsfState* tp = s->psf->tc;
+  TcSolverState* t = s->tc;
+  const int LL = s->Li * s->Lj;
+  const float* lfsub = s->lfs.as<float>() + (int64_t)view * LL;
+  k_tc_col2im_ratio<<<(LL + 127) / 128, 128, 0, st>>>(t->ypart.as<float>(), t->splits, t->MP, tp->NB, s->Li,
+                                                      s->Lj, s->T, lfsub, hx_out,
+                                                      ratio ? t->rimg.as<float>() : nullptr);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+int tc_im2col_ratio(Solver* s, int precision, cudaStream_t st) {
+  const TcPsfState* tp = s->psf->tc;
+  TcSolverState* t = s->tc;
+  const int LL = s->Li * s->Lj;
+  k_tc_im2col<<<1024, 256, 0, st>>>(t->rimg.as<float>(), s->Li, s->Lj, LL, t->MP, s->T, tp->KB,
+                                    t->ar_hi.as<bf16>(),
+                                    precision == MLF_PREC_BF16X3 ? t->ar_lo.as<bf16>() : nullptr);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+int tc_bwd_launch(Solver* s, int precision, int view, float w, cudaStream_t st) {
+  const TcPsfState* tp = s->psf->tc;
+  TcSolverState* t = s->tc;
+  int pc, pd, pf;
+  passes_of(precision, &pc, &pd, &pf);
+  TcBwdArgs a{};
+  a.X = s->X.as<float>();
+  a.xb_hi = t->xb_hi.as<bf16>();
+  a.xb_lo = t->xb_lo.as<bf16>();
+  a.err = t->err.as<int>();
+  a.plane = s->plane;
+  a.w = w;
+  a.Li = s->Li; a.Lj = s->Lj; a.Pa = s->Pa; a.LL = s->Li * s->Lj;
+  a.CHP = tp->CHP; a.nch = (int)s->nch; a.KB = tp->KB; a.brow0 = view * tp->CHP;
+  a.npass_c = pc;
+  a.npass_d = pd;
+  a.write_lo = pf >= 3 ? 1 : 0;
+  k_tc_bwd<<<dim3(t->MP / BM, tp->CHP / BWD_BN), 128, BWD_SMEM, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh,
+                                                                     tp->mBl, a);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+}  // namespace
+
+int tc_pack_volume(Solver* s, int precision, cudaStream_t st) {
+  TcSolverState* t = s->tc;
+  const TcPsfState* tp = s->psf->tc;
+  const int LL = s->Li * s->Lj;
+  dim3 grid((t->MP + 31) / 32, (tp->CHP + 31) / 32);
+  k_tc_pack_x<<<grid, dim3(32, 8), 0, st>>>(s->X.as<float>(), s->Li, s->Pa, LL, s->plane, s->nch, tp->CHP, t->MP,
+                                            t->xb_hi.as<bf16>(),
+                                            precision == MLF_PREC_BF16X3 ? t->xb_lo.as<bf16>() : nullptr);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+// One RL iteration on the tensor cores (the view loop); the caller adds the sample filter.
+int tc_enqueue_views(Solver* s, int precision, int64_t* launches, cudaStream_t st) {
+  const std::vector<int>& views = s->psf->view_order;
+  const int V = (int)views.size();
+  if (V == 0) return MLF_OK;
+  int64_t n = 0;
+  MLF_TRY(tc_pack_volume(s, precision, st));
+  MLF_TRY(timing_mark(s, st));
+  MLF_TRY(tc_fwd_launch(s, precision, views[0], st));
+  MLF_TRY(timing_mark(s, st));
+  MLF_TRY(tc_col2im(s, views[0], true, nullptr, st));
+  MLF_TRY(tc_im2col_ratio(s, precision, st));
+  n += 4;
+  for (int k = 0; k < V; ++k) {
+    const int cur = views[k];
+    MLF_TRY(timing_mark(s, st));
+    MLF_TRY(tc_bwd_launch(s, precision, cur, (float)s->psf->weights[cur], st));
+    ++n;
+    if (k + 1 < V) {
+      MLF_TRY(tc_fwd_launch(s, precision, views[k + 1], st));
+      MLF_TRY(timing_mark(s, st));
+      MLF_TRY(tc_col2im(s, views[k + 1], true, nullptr, st));
+      MLF_TRY(tc_im2col_ratio(s, precision, st));
+      n += 3;
+    } else {
+      MLF_TRY(timing_mark(s, st));
+    }
+  }
+  if (launches) *launches += n;
+  return MLF_OK;
+}
+
+// Forward projection of one view with the tensor cores (parity tests): vol phase-major
+// already in s->X; result HX -> hx_out.
+int tc_forward_view(Solver* s, int precision, int view, float* hx_out, cudaStream_t st) {
+  MLF_TRY(tc_solver_prepare(s, st));
+  MLF_TRY(tc_pack_volume(s, precision, st));
+  MLF_TRY(tc_fwd_launch(s, precision, view, st));
+  return tc_col2im(s, view, false, hx_out, st);
+}
+
+// One RL view step on the tensor cores (parity tests): X phase-major in s->X, the
+// sub-aperture images in s->lfs; updates s->X.
+int tc_view_step(Solver* s, int precision, int view, float w, cudaStream_t st) {
+  MLF_TRY(tc_solver_prepare(s, st));
+  MLF_TRY(tc_pack_volume(s, precision, st));
+  MLF_TRY(tc_fwd_launch(s, precision, view, st));
+  MLF_TRY(tc_col2im(s, view, true, nullptr, st));
+  MLF_TRY(tc_im2col_ratio(s, precision, st));
+  return tc_bwd_launch(s, precision, view, w, st);
+}
+
+int tc_check_error(Solver* s) {
+  if (!s->tc) return MLF_OK;
+  int e = 0;
+  MLF_CUDA(cudaMemcpy(&e, s->tc->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e != 0) {
+    cudaMemset(s->tc->err.p, 0, sizeof(int));
+    return fail(MLF_ERR_TIMEOUT, "tensor-core kernel wait timed out (code " + std::to_string(e) + ")");
+  }
+  return MLF_OK;
+}
+
+}  // namespace mlf
