@@ -164,6 +164,7 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="one solve of --iters iterations and exit (for ncu captures)")
     ap.add_argument("--iters", type=int, default=None)
+    ap.add_argument("--mixed", default="bf16x2", help="tensor-core precision timed beside plain FP32 ('' to skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -230,6 +231,42 @@ def main():
     n_views = st["n_views"]
     value = ws * w.voxels / (ms * 1e-3)
 
+    # mixed precision (tensor cores) on the same workload, error vs the plain FP32 volume
+    mixed = None
+    if args.mixed:
+        ref_vol = out_dev.clone()
+        mix_out = torch.empty_like(out_dev)
+        for _ in range(max(1, args.warmup)):
+            solver.run(lf_dev, w.iters, precision=args.mixed, out=mix_out, want_stats=False)
+        barrier()
+        m0 = torch.cuda.Event(enable_timing=True)
+        m1 = torch.cuda.Event(enable_timing=True)
+        mk_ms = 0.0
+        mk_n = 0
+        mlaunch = 0
+        m0.record(stream)
+        for _ in range(args.steps):
+            solver.run(lf_dev, w.iters, precision=args.mixed, out=mix_out, want_stats=True)
+            st2 = solver.last_stats
+            mk_ms += st2["view_kernel_ms"]
+            mk_n += st2["view_kernel_launches"]
+            mlaunch += st2["kernel_launches"]
+        m1.record(stream)
+        barrier()
+        mms = m0.elapsed_time(m1) / args.steps
+        d = (mix_out.double() - ref_vol.double()).norm() / ref_vol.double().norm()
+        mflop = algorithmic_flop_per_view(Xr, Xc, Z, psf.S, psf.N) * n_views * w.iters * args.steps
+        mixed = {"precision": args.mixed, "value": ws * w.voxels / (mms * 1e-3), "unit": "voxels/s",
+                 "ms_per_step": mms, "speedup_vs_plain_fp32": ms / mms,
+                 "rel_l2_vs_plain_fp32": float(d),
+                 "gpu_launches": int(mlaunch),
+                 "view_kernels_ms_per_view": mk_ms / max(1, mk_n),
+                 "roofline": {"bound": "tensor", "achieved": mflop / (mk_ms * 1e-3) / 1e12,
+                              "peak": _measured_bf16(), "unit": "TFLOP/s",
+                              "frac": (mflop / (mk_ms * 1e-3) / 1e12) / _measured_bf16() if _measured_bf16() else None,
+                              "note": "algorithmic flop of the projections / time of the two GEMM kernels "
+                                      "(back projection + update, next-view forward); peak = measured bf16 burst"}}
+
     # e2e: pinned host image in, pinned host volume out, through mlf_solver_run
     lf_host = torch.empty((Xc, Xr), dtype=torch.float32, pin_memory=True).t()
     lf_host.copy_(torch.as_tensor(np.ascontiguousarray(lf)))
@@ -281,7 +318,7 @@ def main():
                        "views_per_iteration": n_views, "parallelism": f"replicas x{ws}",
                        "l2": "inputs larger than L2 (projector taps 4.6 GB, volume 206 MB)"},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks,
-            "impl": "ours"}
+            "impl": "ours", "mixed": mixed}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         rng = np.random.default_rng(0)
         planes = 4
@@ -296,6 +333,13 @@ def main():
     psf.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _measured_bf16():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
+    except Exception:
+        return None
 
 
 def _measured_hbm():

@@ -40,9 +40,10 @@ enum mlf_status_code {
 
 enum mlf_precision {
   MLF_PREC_FP32 = 0,       /* plain FP32 FMA projector (the drop-in path) */
-  MLF_PREC_BF16X3 = 1,     /* tensor-core BF16 split hi+lo operands, FP32 accumulate */
-  MLF_PREC_BF16 = 2,       /* tensor-core single BF16 operands, FP32 accumulate */
-  MLF_PREC_BF16X2 = 3      /* tensor-core BF16, taps split hi+lo (2 passes), FP32 accumulate */
+  MLF_PREC_BF16X3 = 1,     /* tensor cores: taps and activations split hi+lo BF16 (3 passes) */
+  MLF_PREC_BF16 = 2,       /* tensor cores: single BF16 operands (1 pass) */
+  MLF_PREC_BF16X2 = 3      /* tensor cores: activations split hi+lo, taps single BF16 (2 passes) */
+  /* all tensor-core modes accumulate in FP32; ratio, update, filter and sums stay FP32 */
 };
 
 typedef struct mlf_psf mlf_psf;       /* phase-space PSF resident in HBM */

@@ -14,11 +14,12 @@
 // absorbing the per-channel phase shift s_alpha, s_beta into zero-padded taps), A1 = the
 // same im2col of the all-ones image (0/1, exact in BF16).  Operands are BF16, optionally
 // split hi + lo (x = hi + lo, both BF16) with the products accumulated in FP32 in TMEM:
-//   MLF_PREC_BF16    C = ARh Wbh                 Y = Xh Wfh
-//   MLF_PREC_BF16X2  C = ARh (Wbh + Wbl)         Y = Xh (Wfh + Wfl)
-//   MLF_PREC_BF16X3  C = ARh Wbh + ARh Wbl + ARl Wbh, Y likewise
-// (D always uses Wbh + Wbl when the taps are split, so C/D is a weighted mean with the same
-// weights).  The ratio, the update, the depth sums (inside C, D, Y) and the sample filter
+//   MLF_PREC_BF16    C = ARh Wbh                   Y = Xh Wfh
+//   MLF_PREC_BF16X2  C = (ARh + ARl) Wbh           Y = (Xh + Xl) Wfh      (activations split)
+//   MLF_PREC_BF16X3  C = ARh Wbh + ARh Wbl + ARl Wbh, Y likewise          (both split)
+// D uses exactly the tap values C uses (Wbh, or Wbh + Wbl when the taps are split), so C/D
+// is a weighted mean of R with consistent weights.  Splitting the activations (X, R) rather
+// than the taps is the more accurate two-pass form: the tap rounding cancels in C/D.  The ratio, the update, the depth sums (inside C, D, Y) and the sample filter
 // stay in FP32.
 //
 // Both GEMM kernels are warp-specialised: warp 0 issues TMA tile loads (128-byte swizzle)
@@ -69,7 +70,8 @@ struct TcBwdArgs {
   int64_t plane;
   float w;
   int Li, Lj, Pa, LL, CHP, nch, KB, brow0;  // brow0 = view * CHP (row of this view in Wb')
-  int npass_c, npass_d;                     // MMA passes for C (1..3) and D (1..2)
+  int use_alo;                              // add ARl * Wbh to C (activation split)
+  int use_blo;                              // add ARh * Wbl to C and A1 * Wbl to D (tap split)
   int write_lo;                             // also emit the lo half of Xb
 };
 
@@ -91,7 +93,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BWD_BN;
   const int KS = a.KB / BK;
-  const bool need_blo = a.npass_c >= 2 || a.npass_d >= 2;
+  const bool need_blo = a.use_blo != 0, need_alo = a.use_alo != 0;
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       tc::mbar_init(&full[s], 1);
@@ -112,8 +114,8 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
 
   if (warp == 0 && lane == 0) {
     // ---------------- TMA producer
-    // Ah + A1 + Bh always; Al for three passes; Bl when the taps are split
-    const uint32_t bytes = 3 * TILE_A + (a.npass_c >= 3 ? TILE_A : 0) + (need_blo ? TILE_A : 0);
+    // Ah + A1 + Bh always; Al when the activations are split; Bl when the taps are split
+    const uint32_t bytes = 3 * TILE_A + (need_alo ? TILE_A : 0) + (need_blo ? TILE_A : 0);
     int issued = 0;
     for (int ks = 0; ks < KS; ++ks) {
       const int s = ks % STAGES;
@@ -126,7 +128,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       uint8_t* st = smem + s * BWD_STAGE;
       tc::mbar_arrive_expect_tx(&full[s], bytes);
       tc::tma_load_2d(st + BWD_OFF_AHI, &mAh, &full[s], ks * BK, m0);
-      if (a.npass_c >= 3) tc::tma_load_2d(st + BWD_OFF_ALO, &mAl, &full[s], ks * BK, m0);
+      if (need_alo) tc::tma_load_2d(st + BWD_OFF_ALO, &mAl, &full[s], ks * BK, m0);
       tc::tma_load_2d(st + BWD_OFF_A1, &mA1, &full[s], ks * BK, m0);
       tc::tma_load_2d(st + BWD_OFF_BHI, &mBh, &full[s], ks * BK, a.brow0 + n0);
       if (need_blo) tc::tma_load_2d(st + BWD_OFF_BLO, &mBl, &full[s], ks * BK, a.brow0 + n0);
@@ -158,10 +160,10 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
         tc::mma_bf16(tD, da1, dbh, idesc, acc);
         if (need_blo) {
           const uint64_t dbl = tc::desc_kmajor_sw128(st + BWD_OFF_BLO + 32 * k);
-          if (a.npass_c >= 2) tc::mma_bf16(tC, dah, dbl, idesc, 1u);
-          if (a.npass_d >= 2) tc::mma_bf16(tD, da1, dbl, idesc, 1u);
+          tc::mma_bf16(tC, dah, dbl, idesc, 1u);
+          tc::mma_bf16(tD, da1, dbl, idesc, 1u);
         }
-        if (a.npass_c >= 3) {
+        if (need_alo) {
           const uint64_t dal = tc::desc_kmajor_sw128(st + BWD_OFF_ALO + 32 * k);
           tc::mma_bf16(tC, dal, dbh, idesc, 1u);
         }
@@ -223,7 +225,8 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
 struct TcFwdArgs {
   float* ypart;  // [split][MP][NB]
   int* err;
-  int MP, NB, NH, nparts, ks_per_split, KS, frow0, npass;  // frow0 = view * NB
+  int MP, NB, NH, nparts, ks_per_split, KS, frow0;  // frow0 = view * NB
+  int use_alo, use_blo;                             // activation / tap hi+lo splits
 };
 
 __global__ void __launch_bounds__(128, 1)
@@ -261,7 +264,7 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
   const uint32_t tY = tmem_base;
 
   if (warp == 0 && lane == 0) {
-    const uint32_t bytes = TILE_A * (a.npass >= 3 ? 2 : 1) + tileB * (a.npass >= 2 ? 2 : 1);
+    const uint32_t bytes = TILE_A * (a.use_alo ? 2 : 1) + tileB * (a.use_blo ? 2 : 1);
     int issued = 0;
     for (int ks = ks0; ks < ks1; ++ks) {
       const int i = ks - ks0, s = i % STAGES;
@@ -274,10 +277,10 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       uint8_t* st = smem + s * stage_bytes;
       tc::mbar_arrive_expect_tx(&full[s], bytes);
       tc::tma_load_2d(st, &mAh, &full[s], ks * BK, m0);
-      if (a.npass >= 3) tc::tma_load_2d(st + offAl, &mAl, &full[s], ks * BK, m0);
+      if (a.use_alo) tc::tma_load_2d(st + offAl, &mAl, &full[s], ks * BK, m0);
       for (int p = 0; p < a.nparts; ++p) {
         tc::tma_load_2d(st + offBh + p * a.NH * 128, &mBh, &full[s], ks * BK, a.frow0 + p * a.NH);
-        if (a.npass >= 2)
+        if (a.use_blo)
           tc::tma_load_2d(st + offBl + p * a.NH * 128, &mBl, &full[s], ks * BK, a.frow0 + p * a.NH);
       }
       ++issued;
@@ -304,11 +307,11 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
           const uint32_t dcol = tY + p * a.NH;
           const uint64_t dbh = tc::desc_kmajor_sw128(st + offBh + p * a.NH * 128 + 32 * k);
           tc::mma_bf16(dcol, dah, dbh, idesc, acc);
-          if (a.npass >= 2) {
+          if (a.use_blo) {
             const uint64_t dbl = tc::desc_kmajor_sw128(st + offBl + p * a.NH * 128 + 32 * k);
             tc::mma_bf16(dcol, dah, dbl, idesc, 1u);
           }
-          if (a.npass >= 3) {
+          if (a.use_alo) {
             const uint64_t dal = tc::desc_kmajor_sw128(st + offAl + 32 * k);
             tc::mma_bf16(dcol, dal, dbh, idesc, 1u);
           }
@@ -603,21 +606,18 @@ size_t tc_solver_bytes(const Solver* s) {
 
 namespace {
 
-void passes_of(int precision, int* pc, int* pd, int* pf) {
-  if (precision == MLF_PREC_BF16) {
-    *pc = 1; *pd = 1; *pf = 1;
-  } else if (precision == MLF_PREC_BF16X2) {
-    *pc = 2; *pd = 2; *pf = 2;
-  } else {
-    *pc = 3; *pd = 2; *pf = 3;
-  }
+// (activation split, tap split) per precision mode
+void splits_of(int precision, int* alo, int* blo) {
+  *alo = (precision == MLF_PREC_BF16X2 || precision == MLF_PREC_BF16X3) ? 1 : 0;
+  *blo = (precision == MLF_PREC_BF16X3) ? 1 : 0;
 }
+bool act_split(int precision) { return precision == MLF_PREC_BF16X2 || precision == MLF_PREC_BF16X3; }
 
 int tc_fwd_launch(Solver* s, int precision, int view, cudaStream_t st) {
   const TcPsfState* tp = s->psf->tc;
   TcSolverState* t = s->tc;
-  int pc, pd, pf;
-  passes_of(precision, &pc, &pd, &pf);
+  int alo, blo;
+  splits_of(precision, &alo, &blo);
   TcFwdArgs a{};
   a.ypart = t->ypart.as<float>();
   a.err = t->err.as<int>();
@@ -628,7 +628,8 @@ int tc_fwd_launch(Solver* s, int precision, int view, cudaStream_t st) {
   a.ks_per_split = t->ks_per_split;
   a.KS = t->KSF;
   a.frow0 = view * tp->NB;
-  a.npass = pf;
+  a.use_alo = alo;
+  a.use_blo = blo;
   const size_t fsmem = (size_t)STAGES * (2 * TILE_A + 2 * tp->NB * 128) + 1024;
   k_tc_fwd<<<dim3(t->MP / BM, t->splits), 128, fsmem, st>>>(t->mXh, t->mXl, tp->mFh, tp->mFl, a);
   MLF_CUDA(cudaGetLastError());
@@ -652,8 +653,7 @@ int tc_im2col_ratio(Solver* s, int precision, cudaStream_t st) {
   TcSolverState* t = s->tc;
   const int LL = s->Li * s->Lj;
   k_tc_im2col<<<1024, 256, 0, st>>>(t->rimg.as<float>(), s->Li, s->Lj, LL, t->MP, s->T, tp->KB,
-                                    t->ar_hi.as<bf16>(),
-                                    precision == MLF_PREC_BF16X3 ? t->ar_lo.as<bf16>() : nullptr);
+                                    t->ar_hi.as<bf16>(), act_split(precision) ? t->ar_lo.as<bf16>() : nullptr);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
 }
@@ -661,8 +661,8 @@ int tc_im2col_ratio(Solver* s, int precision, cudaStream_t st) {
 int tc_bwd_launch(Solver* s, int precision, int view, float w, cudaStream_t st) {
   const TcPsfState* tp = s->psf->tc;
   TcSolverState* t = s->tc;
-  int pc, pd, pf;
-  passes_of(precision, &pc, &pd, &pf);
+  int alo, blo;
+  splits_of(precision, &alo, &blo);
   TcBwdArgs a{};
   a.X = s->X.as<float>();
   a.xb_hi = t->xb_hi.as<bf16>();
@@ -672,9 +672,9 @@ int tc_bwd_launch(Solver* s, int precision, int view, float w, cudaStream_t st) 
   a.w = w;
   a.Li = s->Li; a.Lj = s->Lj; a.Pa = s->Pa; a.LL = s->Li * s->Lj;
   a.CHP = tp->CHP; a.nch = (int)s->nch; a.KB = tp->KB; a.brow0 = view * tp->CHP;
-  a.npass_c = pc;
-  a.npass_d = pd;
-  a.write_lo = pf >= 3 ? 1 : 0;
+  a.use_alo = alo;
+  a.use_blo = blo;
+  a.write_lo = alo;
   k_tc_bwd<<<dim3(t->MP / BM, tp->CHP / BWD_BN), 128, BWD_SMEM, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh,
                                                                      tp->mBl, a);
   MLF_CUDA(cudaGetLastError());
@@ -689,8 +689,7 @@ int tc_pack_volume(Solver* s, int precision, cudaStream_t st) {
   const int LL = s->Li * s->Lj;
   dim3 grid((t->MP + 31) / 32, (tp->CHP + 31) / 32);
   k_tc_pack_x<<<grid, dim3(32, 8), 0, st>>>(s->X.as<float>(), s->Li, s->Pa, LL, s->plane, s->nch, tp->CHP, t->MP,
-                                            t->xb_hi.as<bf16>(),
-                                            precision == MLF_PREC_BF16X3 ? t->xb_lo.as<bf16>() : nullptr);
+                                            t->xb_hi.as<bf16>(), act_split(precision) ? t->xb_lo.as<bf16>() : nullptr);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
 }

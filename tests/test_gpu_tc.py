@@ -3,7 +3,7 @@
 Tolerances (relative L2), from the operand rounding of each mode:
   bf16x3  (hi+lo split of taps and activations, 3 MMA passes)  1e-5 per projection,
           1e-4 for a whole solve (the FP32 bar);
-  bf16x2  (taps split, activations single BF16)                 5e-3 per view step,
+  bf16x2  (activations split, taps single BF16)                 5e-3 per view step,
           1e-3 for a whole solve (the mixed-precision bar);
   bf16    (single BF16)                                         5e-3 per view step,
           2e-3 for a whole solve.
@@ -19,7 +19,7 @@ from mesolf_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-STEP_TOL = {"bf16x3": 1e-5, "bf16x2": 5e-3, "bf16": 5e-3}
+STEP_TOL = {"bf16x3": 1e-5, "bf16x2": 2e-3, "bf16": 5e-3}
 SOLVE_TOL = {"bf16x3": 1e-4, "bf16x2": 1e-3, "bf16": 2e-3}
 
 
