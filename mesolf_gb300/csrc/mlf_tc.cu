@@ -52,6 +52,10 @@ constexpr uint32_t WAIT_LIMIT = 1u << 22;  // polls; ~0.3-1 s with the back-off 
 
 enum TcErr { TC_ERR_TIMEOUT_PRODUCER = 1, TC_ERR_TIMEOUT_MMA = 2, TC_ERR_TIMEOUT_EPILOGUE = 3 };
 
+// shared abort flag written by one role and polled by the others
+__device__ __forceinline__ bool aborted(const int* f) { return *reinterpret_cast<const volatile int*>(f) != 0; }
+__device__ __forceinline__ void set_abort(int* f) { *reinterpret_cast<volatile int*>(f) = 1; }
+
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
@@ -80,145 +84,192 @@ constexpr int BWD_OFF_AHI = 0, BWD_OFF_ALO = TILE_A, BWD_OFF_A1 = 2 * TILE_A;
 constexpr int BWD_OFF_BHI = 3 * TILE_A, BWD_OFF_BLO = 4 * TILE_A;
 constexpr int BWD_STAGE = 5 * TILE_A;  // 80 KB
 constexpr size_t BWD_SMEM = (size_t)STAGES * BWD_STAGE + 1024;
+constexpr int BWD_EPI_WARPS = 8;                       // 2 per TMEM lane quadrant
+constexpr int BWD_THREADS = 32 * (2 + BWD_EPI_WARPS);  // producer, MMA, epilogue
 
-__global__ void __launch_bounds__(128, 1)
+// Persistent over (position tile, channel tile) pairs.  Warp 0: TMA producer; warp 1: TMEM
+// owner and MMA issuer; warps 2..9: epilogue.  The C and D accumulators are double
+// buffered in TMEM (2 x 256 columns) so the epilogue of one tile overlaps the MMAs of the
+// next.  Epilogue warp e covers TMEM lanes 32*(e%4).. and channel half (e-2)/4.
+__global__ void __launch_bounds__(BWD_THREADS, 1)
 k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
          const __grid_constant__ CUtensorMap mA1, const __grid_constant__ CUtensorMap mBh,
-         const __grid_constant__ CUtensorMap mBl, TcBwdArgs a) {
+         const __grid_constant__ CUtensorMap mBl, TcBwdArgs a, int mtiles, int ntiles) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
-  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], accb;
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], mdone;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BWD_BN;
   const int KS = a.KB / BK;
+  const int total = mtiles * ntiles;
   const bool need_blo = a.use_blo != 0, need_alo = a.use_alo != 0;
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    tc::mbar_init(&accb, 1);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&tfull[b], 1);
+      tc::mbar_init(&tempty[b], BWD_EPI_WARPS);
+    }
+    tc::mbar_init(&mdone, 1);
     tc::fence_mbar_init();
     abort_flag = 0;
     tc::tma_prefetch_desc(&mAh);
     tc::tma_prefetch_desc(&mA1);
     tc::tma_prefetch_desc(&mBh);
   }
-  if (warp == 2) tc::tmem_alloc(&tmem_base, 256);
+  if (warp == 1) tc::tmem_alloc(&tmem_base, 512);
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
-  const uint32_t tC = tmem_base, tD = tmem_base + 128;
 
-  if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer
-    // Ah + A1 + Bh always; Al when the activations are split; Bl when the taps are split
-    const uint32_t bytes = 3 * TILE_A + (need_alo ? TILE_A : 0) + (need_blo ? TILE_A : 0);
-    int issued = 0;
-    for (int ks = 0; ks < KS; ++ks) {
-      const int s = ks % STAGES;
-      const uint32_t ph = (ks / STAGES) & 1;
-      if (!tc::mbar_wait(&empty[s], ph ^ 1, WAIT_LIMIT)) {
-        abort_flag = 1;
-        atomicExch(a.err, TC_ERR_TIMEOUT_PRODUCER);
-        break;
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer (continuous ring over all tiles of this CTA)
+      const uint32_t bytes = 3 * TILE_A + (need_alo ? TILE_A : 0) + (need_blo ? TILE_A : 0);
+      int it = 0;
+      for (int t = blockIdx.x; t < total && !aborted(&abort_flag); t += gridDim.x) {
+        const int m0 = (t % mtiles) * BM, n0 = (t / mtiles) * BWD_BN;
+        for (int ks = 0; ks < KS; ++ks, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!tc::mbar_wait(&empty[s], ph ^ 1, WAIT_LIMIT)) {
+            set_abort(&abort_flag);
+            atomicExch(a.err, TC_ERR_TIMEOUT_PRODUCER);
+            break;
+          }
+          uint8_t* st = smem + s * BWD_STAGE;
+          tc::mbar_arrive_expect_tx(&full[s], bytes);
+          tc::tma_load_2d(st + BWD_OFF_AHI, &mAh, &full[s], ks * BK, m0);
+          if (need_alo) tc::tma_load_2d(st + BWD_OFF_ALO, &mAl, &full[s], ks * BK, m0);
+          tc::tma_load_2d(st + BWD_OFF_A1, &mA1, &full[s], ks * BK, m0);
+          tc::tma_load_2d(st + BWD_OFF_BHI, &mBh, &full[s], ks * BK, a.brow0 + n0);
+          if (need_blo) tc::tma_load_2d(st + BWD_OFF_BLO, &mBl, &full[s], ks * BK, a.brow0 + n0);
+        }
       }
-      uint8_t* st = smem + s * BWD_STAGE;
-      tc::mbar_arrive_expect_tx(&full[s], bytes);
-      tc::tma_load_2d(st + BWD_OFF_AHI, &mAh, &full[s], ks * BK, m0);
-      if (need_alo) tc::tma_load_2d(st + BWD_OFF_ALO, &mAl, &full[s], ks * BK, m0);
-      tc::tma_load_2d(st + BWD_OFF_A1, &mA1, &full[s], ks * BK, m0);
-      tc::tma_load_2d(st + BWD_OFF_BHI, &mBh, &full[s], ks * BK, a.brow0 + n0);
-      if (need_blo) tc::tma_load_2d(st + BWD_OFF_BLO, &mBl, &full[s], ks * BK, a.brow0 + n0);
-      ++issued;
+      // drain: every issued copy must have landed before the CTA can exit
+      for (int i = std::max(0, it - STAGES); i < it; ++i)
+        tc::mbar_wait(&full[i % STAGES], (i / STAGES) & 1, WAIT_LIMIT);
     }
-    // drain: every issued copy must have landed before the CTA can exit
-    for (int ks = std::max(0, issued - STAGES); ks < issued; ++ks)
-      tc::mbar_wait(&full[ks % STAGES], (ks / STAGES) & 1, WAIT_LIMIT);
-  } else if (warp == 1 && lane == 0) {
-    // ---------------- MMA issuer
-    const uint32_t idesc = tc::idesc_bf16_f32(BM, BWD_BN);
-    for (int ks = 0; ks < KS; ++ks) {
-      const int s = ks % STAGES;
-      const uint32_t ph = (ks / STAGES) & 1;
-      if (abort_flag || !tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
-        abort_flag = 1;
-        atomicExch(a.err, TC_ERR_TIMEOUT_MMA);
-        break;
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      const uint32_t idesc = tc::idesc_bf16_f32(BM, BWD_BN);
+      int it = 0, ti = 0;
+      for (int t = blockIdx.x; t < total && !aborted(&abort_flag); t += gridDim.x, ++ti) {
+        const int buf = ti & 1;
+        const uint32_t tph = (ti >> 1) & 1;
+        if (!tc::mbar_wait(&tempty[buf], tph ^ 1, WAIT_LIMIT)) {
+          set_abort(&abort_flag);
+          atomicExch(a.err, TC_ERR_TIMEOUT_MMA);
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t tC = tmem_base + buf * 256, tD = tC + 128;
+        bool ok = true;
+        for (int ks = 0; ks < KS; ++ks, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
+            set_abort(&abort_flag);
+            atomicExch(a.err, TC_ERR_TIMEOUT_MMA);
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t st = tc::smem_u32(smem + s * BWD_STAGE);
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k) {
+            const uint32_t acc = (ks > 0 || k > 0) ? 1u : 0u;
+            const uint64_t dah = tc::desc_kmajor_sw128(st + BWD_OFF_AHI + 32 * k);
+            const uint64_t da1 = tc::desc_kmajor_sw128(st + BWD_OFF_A1 + 32 * k);
+            const uint64_t dbh = tc::desc_kmajor_sw128(st + BWD_OFF_BHI + 32 * k);
+            tc::mma_bf16(tC, dah, dbh, idesc, acc);
+            tc::mma_bf16(tD, da1, dbh, idesc, acc);
+            if (need_blo) {
+              const uint64_t dbl = tc::desc_kmajor_sw128(st + BWD_OFF_BLO + 32 * k);
+              tc::mma_bf16(tC, dah, dbl, idesc, 1u);
+              tc::mma_bf16(tD, da1, dbl, idesc, 1u);
+            }
+            if (need_alo) {
+              const uint64_t dal = tc::desc_kmajor_sw128(st + BWD_OFF_ALO + 32 * k);
+              tc::mma_bf16(tC, dal, dbh, idesc, 1u);
+            }
+          }
+          tc::mma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        tc::mma_commit(&tfull[buf]);
       }
+      // every issued MMA must have completed before TMEM is released
+      tc::mma_commit(&mdone);
+      tc::mbar_wait(&mdone, 0, WAIT_LIMIT);
+    }
+  } else {
+    // ---------------- epilogue: update X, emit Xb
+    const int e = warp - 2;
+    const int quad = warp & 3;                 // TMEM lanes 32*quad .. 32*quad+31
+    const int chalf = e / 4;                   // channel half of the tile
+    const int row = quad * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    int ti = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++ti) {
+      const int buf = ti & 1;
+      const uint32_t tph = (ti >> 1) & 1;
+      const int m0 = (t % mtiles) * BM, n0 = (t / mtiles) * BWD_BN;
+      const bool ok = !aborted(&abort_flag) && tc::mbar_wait(&tfull[buf], tph, WAIT_LIMIT);
       tc::tc_fence_after();
-      const uint32_t st = tc::smem_u32(smem + s * BWD_STAGE);
+      if (!ok) {
+        if (lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
+        set_abort(&abort_flag);
+        break;
+      }
+      const int pos = m0 + row;
+      const bool pos_ok = pos < a.LL;
+      const int b = pos_ok ? pos / a.Li : 0, aa = pos_ok ? pos - b * a.Li : 0;
+      const int64_t xoff = (int64_t)b * a.Pa + aa;
+      const uint32_t tC = tmem_base + buf * 256 + lane_off, tD = tC + 128;
+      for (int c = chalf * 4; c < chalf * 4 + 4; ++c) {
+        float cv[16], dv[16], xo[16];
+        tc::tmem_ld16(tC + c * 16, cv);
+        tc::tmem_ld16(tD + c * 16, dv);
+        const int chb = n0 + c * 16;
+        float* xbase = a.X + (int64_t)chb * a.plane + xoff;
 #pragma unroll
-      for (int k = 0; k < BK / 16; ++k) {
-        const uint32_t acc = (ks > 0 || k > 0) ? 1u : 0u;
-        const uint64_t dah = tc::desc_kmajor_sw128(st + BWD_OFF_AHI + 32 * k);
-        const uint64_t da1 = tc::desc_kmajor_sw128(st + BWD_OFF_A1 + 32 * k);
-        const uint64_t dbh = tc::desc_kmajor_sw128(st + BWD_OFF_BHI + 32 * k);
-        tc::mma_bf16(tC, dah, dbh, idesc, acc);
-        tc::mma_bf16(tD, da1, dbh, idesc, acc);
-        if (need_blo) {
-          const uint64_t dbl = tc::desc_kmajor_sw128(st + BWD_OFF_BLO + 32 * k);
-          tc::mma_bf16(tC, dah, dbl, idesc, 1u);
-          tc::mma_bf16(tD, da1, dbl, idesc, 1u);
-        }
-        if (need_alo) {
-          const uint64_t dal = tc::desc_kmajor_sw128(st + BWD_OFF_ALO + 32 * k);
-          tc::mma_bf16(tC, dal, dbh, idesc, 1u);
-        }
-      }
-      tc::mma_commit(&empty[s]);
-    }
-    tc::mma_commit(&accb);  // always: completes once every issued MMA has finished
-  }
-  __syncwarp();
-
-  // ---------------- epilogue: update X, emit Xb (all 4 warps, 32 TMEM lanes each)
-  const bool ok = tc::mbar_wait(&accb, 0, WAIT_LIMIT);
-  tc::tc_fence_after();
-  if (!ok && lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
-  const int row = warp * 32 + lane;
-  const int pos = m0 + row;
-  const bool pos_ok = pos < a.LL;
-  const int b = pos_ok ? pos / a.Li : 0, aa = pos_ok ? pos - b * a.Li : 0;
-  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
-  if (ok) {
-    for (int c = 0; c < BWD_BN / 16; ++c) {
-      float cv[16], dv[16];
-      tc::tmem_ld16(tC + lane_off + c * 16, cv);
-      tc::tmem_ld16(tD + lane_off + c * 16, dv);
-      if (abort_flag) continue;
-      __align__(16) bf16 hi[16];
-      __align__(16) bf16 lo[16];
+        for (int j = 0; j < 16; ++j) xo[j] = (pos_ok && chb + j < a.nch) ? xbase[(int64_t)j * a.plane] : 0.f;
+        __align__(16) bf16 hi[16];
+        __align__(16) bf16 lo[16];
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int ch = n0 + c * 16 + j;
-        float xn = 0.f;
-        if (pos_ok && ch < a.nch) {
-          float* xp = a.X + (int64_t)ch * a.plane + (int64_t)b * a.Pa + aa;
-          const float xo = *xp;
-          float xc = xo * cv[j] / dv[j];                 // :130  X .* C ./ D
-          if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;        // :132-134
-          xn = xc * a.w + (1.f - a.w) * xo;               // :136
-          if (xn < 0.f) xn = 0.f;                         // :137
-          *xp = xn;
+        for (int j = 0; j < 16; ++j) {
+          float xn = 0.f;
+          if (pos_ok && chb + j < a.nch) {
+            float xc = xo[j] * cv[j] / dv[j];             // :130  X .* C ./ D
+            if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;       // :132-134
+            xn = xc * a.w + (1.f - a.w) * xo[j];           // :136
+            if (xn < 0.f) xn = 0.f;                        // :137
+            xbase[(int64_t)j * a.plane] = xn;
+          }
+          split_bf16(xn, hi[j], lo[j]);
         }
-        split_bf16(xn, hi[j], lo[j]);
+        uint4* dh = reinterpret_cast<uint4*>(a.xb_hi + (int64_t)pos * a.CHP + chb);
+        dh[0] = reinterpret_cast<uint4*>(hi)[0];
+        dh[1] = reinterpret_cast<uint4*>(hi)[1];
+        if (a.write_lo) {
+          uint4* dl = reinterpret_cast<uint4*>(a.xb_lo + (int64_t)pos * a.CHP + chb);
+          dl[0] = reinterpret_cast<uint4*>(lo)[0];
+          dl[1] = reinterpret_cast<uint4*>(lo)[1];
+        }
       }
-      uint4* dh = reinterpret_cast<uint4*>(a.xb_hi + (int64_t)pos * a.CHP + n0 + c * 16);
-      dh[0] = reinterpret_cast<uint4*>(hi)[0];
-      dh[1] = reinterpret_cast<uint4*>(hi)[1];
-      if (a.write_lo) {
-        uint4* dl = reinterpret_cast<uint4*>(a.xb_lo + (int64_t)pos * a.CHP + n0 + c * 16);
-        dl[0] = reinterpret_cast<uint4*>(lo)[0];
-        dl[1] = reinterpret_cast<uint4*>(lo)[1];
-      }
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&tempty[buf]);
     }
   }
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 2) tc::tmem_dealloc(tmem_base, 256);
+  if (warp == 1) tc::tmem_dealloc(tmem_base, 512);
 }
 
 // ------------------------------------------------------------------ forward projection
@@ -270,7 +321,7 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       const int i = ks - ks0, s = i % STAGES;
       const uint32_t ph = (i / STAGES) & 1;
       if (!tc::mbar_wait(&empty[s], ph ^ 1, WAIT_LIMIT)) {
-        abort_flag = 1;
+        set_abort(&abort_flag);
         atomicExch(a.err, TC_ERR_TIMEOUT_PRODUCER);
         break;
       }
@@ -292,8 +343,8 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
     for (int ks = ks0; ks < ks1; ++ks) {
       const int i = ks - ks0, s = i % STAGES;
       const uint32_t ph = (i / STAGES) & 1;
-      if (abort_flag || !tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
-        abort_flag = 1;
+      if (aborted(&abort_flag) || !tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
+        set_abort(&abort_flag);
         atomicExch(a.err, TC_ERR_TIMEOUT_MMA);
         break;
       }
@@ -333,7 +384,7 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
     for (int c = 0; c < (a.nparts * a.NH) / 16; ++c) {
       float v[16];
       tc::tmem_ld16(tY + lane_off + c * 16, v);
-      if (abort_flag) continue;
+      if (aborted(&abort_flag)) continue;
       if (empty_split) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) v[j] = 0.f;
@@ -510,7 +561,7 @@ struct TcPsfState {
 };
 
 struct TcSolverState {
-  int MP = 0, splits = 1, ks_per_split = 0, KSF = 0;
+  int MP = 0, splits = 1, ks_per_split = 0, KSF = 0, nsm = 0;
   DevBuf ar_hi, ar_lo, a1, xb_hi, xb_lo, ypart, rimg, err;
   CUtensorMap mARh, mARl, mA1, mXh, mXl;
 };
@@ -572,6 +623,7 @@ int tc_solver_prepare(Solver* s, cudaStream_t st) {
   int nsm = 0;
   MLF_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device));
   const int mt = t->MP / BM;
+  t->nsm = nsm;
   t->splits = std::max(1, std::min(t->KSF, nsm / std::max(1, mt)));
   t->ks_per_split = (t->KSF + t->splits - 1) / t->splits;
   t->splits = (t->KSF + t->ks_per_split - 1) / t->ks_per_split;
@@ -675,8 +727,9 @@ int tc_bwd_launch(Solver* s, int precision, int view, float w, cudaStream_t st) 
   a.use_alo = alo;
   a.use_blo = blo;
   a.write_lo = alo;
-  k_tc_bwd<<<dim3(t->MP / BM, tp->CHP / BWD_BN), 128, BWD_SMEM, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh,
-                                                                     tp->mBl, a);
+  const int mt = t->MP / BM, nt = tp->CHP / BWD_BN;
+  const int grid = std::min(mt * nt, t->nsm);
+  k_tc_bwd<<<grid, BWD_THREADS, BWD_SMEM, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, a, mt, nt);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
 }
