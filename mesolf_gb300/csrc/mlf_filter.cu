@@ -348,7 +348,7 @@ int filter_run(Solver* s, cudaStream_t st) {
   const int64_t n = s->Xr * s->Xc * Z;
   const int eg = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
   float* V = s->Xtmp.as<float>();
-  k_unphase<<<eg, 256, 0, st>>>(s->X.as<float>(), s->N, Z, s->Li, s->Pa, s->plane, s->Xr, s->Xc, V);
+  k_unphase<<<eg, 256, 0, st>>>(s->X.as<float>(), s->N, Z, s->Li, s->lay_Pa, s->lay_plane, s->Xr, s->Xc, V);
   const int gr = (int)((s->Xc + kLines - 1) / kLines), gc = (int)((s->Xr + kLines - 1) / kLines);
   double* sin = f.sums.as<double>();
   double* sout = sin + (size_t)nzf * f.max_blocks;
@@ -358,7 +358,7 @@ int filter_run(Solver* s, cudaStream_t st) {
   k_filter_c<<<dim3(gc, nzf), kFiltThreads, sizeof(float) * s->Xc * kPad, st>>>(
       V, g, zl, pe, f.cy.as<float>(), wlo_y, nt_y, (int)s->Xc, sout);
   k_filter_scale<<<(Z + 255) / 256, 256, 0, st>>>(sin, gr, sout, gc, zl, nzf, Z, scale);
-  k_rephase<<<eg, 256, 0, st>>>(V, scale, s->N, Z, s->Pa, s->plane, s->Xr, s->Xc, s->X.as<float>());
+  k_rephase<<<eg, 256, 0, st>>>(V, scale, s->N, Z, s->lay_Pa, s->lay_plane, s->Xr, s->Xc, s->X.as<float>());
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
 }

@@ -88,8 +88,11 @@ struct Solver {
   int device = 0;
   int64_t Xr = 0, Xc = 0;
   int N = 0, Z = 0, Li = 0, Lj = 0, q = 0, T = 0;
-  int Pa = 0;          // row pitch (floats) of a phase-major plane
+  int Pa = 0;          // row pitch (floats) of a phase-major plane (FP32 kernels)
   int64_t plane = 0;   // floats per plane (Lj * Pa)
+  int64_t plane_tc = 0;  // floats per plane in the tensor-core layout (pitch Li, linear positions)
+  int lay_Pa = 0;        // layout of X in the current solve: FP32 (Pa, plane) or
+  int64_t lay_plane = 0; // tensor-core (Li, plane_tc)
   int64_t nch = 0;
   // view-kernel geometry
   int tilesA = 0, tilesB = 0, tps = 0, slots = 0, threads = 0, grid = 0;

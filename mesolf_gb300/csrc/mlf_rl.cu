@@ -153,7 +153,17 @@ int grid_for(int64_t n, int threads = 256) {
 }
 
 Geo geo_of(const Solver* s) {
-  return Geo{s->N, s->Z, s->Li, s->Lj, s->Pa, s->plane, s->Xr, s->Xc};
+  return Geo{s->N, s->Z, s->Li, s->Lj, s->lay_Pa, s->lay_plane, s->Xr, s->Xc};
+}
+
+void use_layout(Solver* s, int precision) {
+  if (precision == MLF_PREC_FP32) {
+    s->lay_Pa = s->Pa;
+    s->lay_plane = s->plane;
+  } else {
+    s->lay_Pa = s->Li;
+    s->lay_plane = s->plane_tc;
+  }
 }
 
 ViewArgs view_args(Solver* s) {
@@ -365,7 +375,10 @@ int solver_init(Solver* s) {
   const int64_t max_blocks = (s->nch + s->slots - 1) / s->slots;
   s->grid = (int)std::min<int64_t>(max_blocks, (int64_t)nsm * per_sm);
 
-  const int64_t vol = s->nch * s->plane;
+  s->plane_tc = (int64_t)round_up(s->Li * s->Lj, 32);
+  s->lay_Pa = s->Pa;
+  s->lay_plane = s->plane;
+  const int64_t vol = s->nch * std::max(s->plane, s->plane_tc);
   const int64_t LL = (int64_t)s->Li * s->Lj;
   MLF_TRY(s->X.alloc(vol * sizeof(float), "volume"));
   MLF_TRY(s->Xtmp.alloc(vol * sizeof(float), "scratch volume"));
@@ -383,6 +396,7 @@ int solver_init(Solver* s) {
 
 int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const float* d_warm,
                float* d_out, mlf_stats* stats, cudaStream_t st) {
+  use_layout(s, precision);
   if (precision != MLF_PREC_FP32) MLF_TRY(tc_solver_prepare(s, st));
   const Geo g = geo_of(s);
   const int64_t n_img = s->Xr * s->Xc;
@@ -404,8 +418,8 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
   } else {
     const int nb = 256;
     k_sum_partial<<<nb, 256, 0, st>>>(d_lf, n_img, s->red.as<double>());
-    k_init_flat<<<grid_for(s->nch * s->plane), 256, 0, st>>>(
-        s->X.as<float>(), s->Li, s->Lj, s->Pa, s->plane, s->nch, s->red.as<double>(), nb,
+    k_init_flat<<<grid_for(s->nch * s->Li * s->Lj), 256, 0, st>>>(
+        s->X.as<float>(), s->Li, s->Lj, s->lay_Pa, s->lay_plane, s->nch, s->red.as<double>(), nb,
         1.0 / (double)n_vol);
     launches += 2;
   }
@@ -442,6 +456,7 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
 }
 
 int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaStream_t st) {
+  use_layout(s, MLF_PREC_FP32);
   const Geo g = geo_of(s);
   const int64_t n_vol = s->Xr * s->Xc * s->Z;
   k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->Xtmp.as<float>());
@@ -457,6 +472,8 @@ int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaS
 
 int forward_view_prec(Solver* s, const float* d_vol, int u, int v, int precision, float* d_hx, cudaStream_t st) {
   if (precision == MLF_PREC_FP32) return forward_view(s, d_vol, u, v, d_hx, st);
+  use_layout(s, precision);
+  MLF_TRY(tc_solver_prepare(s, st));
   const Geo g = geo_of(s);
   const int64_t n_vol = s->Xr * s->Xc * s->Z;
   k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->X.as<float>());
@@ -465,6 +482,7 @@ int forward_view_prec(Solver* s, const float* d_vol, int u, int v, int precision
 }
 
 int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cudaStream_t st) {
+  use_layout(s, MLF_PREC_FP32);
   const Geo g = geo_of(s);
   const int LL = s->Li * s->Lj;
   MLF_CUDA(cudaMemsetAsync(s->rpad.p, 0, s->rpad.bytes, st));
@@ -484,6 +502,8 @@ int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cu
 
 int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, double w, int precision,
                  cudaStream_t st) {
+  use_layout(s, precision);
+  if (precision != MLF_PREC_FP32) MLF_TRY(tc_solver_prepare(s, st));
   const Geo g = geo_of(s);
   const int64_t n_img = s->Xr * s->Xc, n_vol = n_img * s->Z;
   const int view = u + s->N * v;
@@ -503,6 +523,7 @@ int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, doubl
 }
 
 int sample_filter(Solver* s, float* d_vol, cudaStream_t st) {
+  use_layout(s, MLF_PREC_FP32);
   const Geo g = geo_of(s);
   const int64_t n_vol = s->Xr * s->Xc * s->Z;
   k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->X.as<float>());

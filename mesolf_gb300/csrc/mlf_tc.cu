@@ -67,43 +67,66 @@ __device__ __forceinline__ void split_bf16(float x, bf16& hi, bf16& lo) {
 
 // ------------------------------------------------------------------ back projection + update
 struct TcBwdArgs {
-  float* X;
   bf16* xb_hi;
   bf16* xb_lo;
   int* err;
-  int64_t plane;
   float w;
-  int Li, Lj, Pa, LL, CHP, nch, KB, brow0;  // brow0 = view * CHP (row of this view in Wb')
-  int use_alo;                              // add ARl * Wbh to C (activation split)
-  int use_blo;                              // add ARh * Wbl to C and A1 * Wbl to D (tap split)
-  int write_lo;                             // also emit the lo half of Xb
+  int Li, LL, CHP, nch, KB, brow0;  // brow0 = view * CHP (row of this view in Wb')
+  int use_alo;                      // add ARl * Wbh to C (activation split)
+  int use_blo;                      // add ARh * Wbl to C and A1 * Wbl to D (tap split)
+  int write_lo;                     // also emit the lo half of Xb
 };
 
-constexpr int BWD_BN = 128;  // channels per tile
-constexpr int BWD_OFF_AHI = 0, BWD_OFF_ALO = TILE_A, BWD_OFF_A1 = 2 * TILE_A;
-constexpr int BWD_OFF_BHI = 3 * TILE_A, BWD_OFF_BLO = 4 * TILE_A;
-constexpr int BWD_STAGE = 5 * TILE_A;  // 80 KB
-constexpr size_t BWD_SMEM = (size_t)STAGES * BWD_STAGE + 1024;
+constexpr int BWD_BN = 128;                            // channels per tile
 constexpr int BWD_EPI_WARPS = 8;                       // 2 per TMEM lane quadrant
 constexpr int BWD_THREADS = 32 * (2 + BWD_EPI_WARPS);  // producer, MMA, epilogue
+constexpr int XTILE = BM * BWD_BN * 4;                 // FP32 X tile, 64 KB
 
-// Persistent over (position tile, channel tile) pairs.  Warp 0: TMA producer; warp 1: TMEM
-// owner and MMA issuer; warps 2..9: epilogue.  The C and D accumulators are double
-// buffered in TMEM (2 x 256 columns) so the epilogue of one tile overlaps the MMAs of the
-// next.  Epilogue warp e covers TMEM lanes 32*(e%4).. and channel half (e-2)/4.
+// Stage layout for a precision mode: Ah | [Al] | A1 | Bh | [Bl]
+struct BwdLayout {
+  int offAl, offA1, offBh, offBl, stage;
+};
+__host__ __device__ inline BwdLayout bwd_layout(int use_alo, int use_blo) {
+  BwdLayout L;
+  int o = TILE_A;
+  L.offAl = use_alo ? o : 0;
+  if (use_alo) o += TILE_A;
+  L.offA1 = o;
+  o += TILE_A;
+  L.offBh = o;
+  o += TILE_A;
+  L.offBl = use_blo ? o : 0;
+  if (use_blo) o += TILE_A;
+  L.stage = o;
+  return L;
+}
+inline size_t bwd_smem_bytes(int use_alo, int use_blo) {
+  return (size_t)STAGES * bwd_layout(use_alo, use_blo).stage + XTILE + 1024;
+}
+
+// Persistent over (position tile, channel tile) pairs.  Warp 0: TMA producer of the
+// operand ring; warp 1: TMEM owner and MMA issuer; warps 2..9: epilogue.  The C and D
+// accumulators are double buffered in TMEM (2 x 256 columns) so the epilogue of one tile
+// overlaps the MMAs of the next.  The X tile (128 positions x 128 channels, FP32) moves
+// HBM -> shared memory -> HBM by TMA: it is loaded while the tile's MMAs run, updated in
+// place by the epilogue, and stored back in bulk.  Epilogue warp e covers TMEM lanes
+// 32*(e%4).. and channel half (e-2)/4.
 __global__ void __launch_bounds__(BWD_THREADS, 1)
 k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
          const __grid_constant__ CUtensorMap mA1, const __grid_constant__ CUtensorMap mBh,
-         const __grid_constant__ CUtensorMap mBl, TcBwdArgs a, int mtiles, int ntiles) {
+         const __grid_constant__ CUtensorMap mBl, const __grid_constant__ CUtensorMap mX, TcBwdArgs a,
+         int mtiles, int ntiles) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
-  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], mdone;
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull, mdone;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int KS = a.KB / BK;
   const int total = mtiles * ntiles;
   const bool need_blo = a.use_blo != 0, need_alo = a.use_alo != 0;
+  const BwdLayout L = bwd_layout(a.use_alo, a.use_blo);
+  float* xs = reinterpret_cast<float*>(smem + STAGES * L.stage);  // [128 ch][128 pos]
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       tc::mbar_init(&full[s], 1);
@@ -113,12 +136,14 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       tc::mbar_init(&tfull[b], 1);
       tc::mbar_init(&tempty[b], BWD_EPI_WARPS);
     }
+    tc::mbar_init(&xfull, 1);
     tc::mbar_init(&mdone, 1);
     tc::fence_mbar_init();
     abort_flag = 0;
     tc::tma_prefetch_desc(&mAh);
     tc::tma_prefetch_desc(&mA1);
     tc::tma_prefetch_desc(&mBh);
+    tc::tma_prefetch_desc(&mX);
   }
   if (warp == 1) tc::tmem_alloc(&tmem_base, 512);
   tc::tc_fence_before();
@@ -140,13 +165,13 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
             atomicExch(a.err, TC_ERR_TIMEOUT_PRODUCER);
             break;
           }
-          uint8_t* st = smem + s * BWD_STAGE;
+          uint8_t* st = smem + s * L.stage;
           tc::mbar_arrive_expect_tx(&full[s], bytes);
-          tc::tma_load_2d(st + BWD_OFF_AHI, &mAh, &full[s], ks * BK, m0);
-          if (need_alo) tc::tma_load_2d(st + BWD_OFF_ALO, &mAl, &full[s], ks * BK, m0);
-          tc::tma_load_2d(st + BWD_OFF_A1, &mA1, &full[s], ks * BK, m0);
-          tc::tma_load_2d(st + BWD_OFF_BHI, &mBh, &full[s], ks * BK, a.brow0 + n0);
-          if (need_blo) tc::tma_load_2d(st + BWD_OFF_BLO, &mBl, &full[s], ks * BK, a.brow0 + n0);
+          tc::tma_load_2d(st, &mAh, &full[s], ks * BK, m0);
+          if (need_alo) tc::tma_load_2d(st + L.offAl, &mAl, &full[s], ks * BK, m0);
+          tc::tma_load_2d(st + L.offA1, &mA1, &full[s], ks * BK, m0);
+          tc::tma_load_2d(st + L.offBh, &mBh, &full[s], ks * BK, a.brow0 + n0);
+          if (need_blo) tc::tma_load_2d(st + L.offBl, &mBl, &full[s], ks * BK, a.brow0 + n0);
         }
       }
       // drain: every issued copy must have landed before the CTA can exit
@@ -179,22 +204,22 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
             break;
           }
           tc::tc_fence_after();
-          const uint32_t st = tc::smem_u32(smem + s * BWD_STAGE);
+          const uint32_t st = tc::smem_u32(smem + s * L.stage);
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k) {
             const uint32_t acc = (ks > 0 || k > 0) ? 1u : 0u;
-            const uint64_t dah = tc::desc_kmajor_sw128(st + BWD_OFF_AHI + 32 * k);
-            const uint64_t da1 = tc::desc_kmajor_sw128(st + BWD_OFF_A1 + 32 * k);
-            const uint64_t dbh = tc::desc_kmajor_sw128(st + BWD_OFF_BHI + 32 * k);
+            const uint64_t dah = tc::desc_kmajor_sw128(st + 32 * k);
+            const uint64_t da1 = tc::desc_kmajor_sw128(st + L.offA1 + 32 * k);
+            const uint64_t dbh = tc::desc_kmajor_sw128(st + L.offBh + 32 * k);
             tc::mma_bf16(tC, dah, dbh, idesc, acc);
             tc::mma_bf16(tD, da1, dbh, idesc, acc);
             if (need_blo) {
-              const uint64_t dbl = tc::desc_kmajor_sw128(st + BWD_OFF_BLO + 32 * k);
+              const uint64_t dbl = tc::desc_kmajor_sw128(st + L.offBl + 32 * k);
               tc::mma_bf16(tC, dah, dbl, idesc, 1u);
               tc::mma_bf16(tD, da1, dbl, idesc, 1u);
             }
             if (need_alo) {
-              const uint64_t dal = tc::desc_kmajor_sw128(st + BWD_OFF_ALO + 32 * k);
+              const uint64_t dal = tc::desc_kmajor_sw128(st + L.offAl + 32 * k);
               tc::mma_bf16(tC, dal, dbh, idesc, 1u);
             }
           }
@@ -208,19 +233,25 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       tc::mbar_wait(&mdone, 0, WAIT_LIMIT);
     }
   } else {
-    // ---------------- epilogue: update X, emit Xb
+    // ---------------- epilogue: update X in shared memory, emit Xb, bulk-store X
     const int e = warp - 2;
+    const bool leader = (e == 0 && lane == 0);
     const int quad = warp & 3;                 // TMEM lanes 32*quad .. 32*quad+31
     const int chalf = e / 4;                   // channel half of the tile
     const int row = quad * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    if (leader && blockIdx.x < total) {
+      tc::mbar_arrive_expect_tx(&xfull, XTILE);
+      tc::tma_load_2d(xs, &mX, &xfull, (blockIdx.x % mtiles) * BM, (blockIdx.x / mtiles) * BWD_BN);
+    }
     int ti = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x, ++ti) {
       const int buf = ti & 1;
       const uint32_t tph = (ti >> 1) & 1;
       const int m0 = (t % mtiles) * BM, n0 = (t / mtiles) * BWD_BN;
-      const bool ok = !aborted(&abort_flag) && tc::mbar_wait(&tfull[buf], tph, WAIT_LIMIT);
+      bool ok = !aborted(&abort_flag) && tc::mbar_wait(&tfull[buf], tph, WAIT_LIMIT);
       tc::tc_fence_after();
+      ok = ok && tc::mbar_wait(&xfull, ti & 1, WAIT_LIMIT);
       if (!ok) {
         if (lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
         set_abort(&abort_flag);
@@ -228,28 +259,25 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       }
       const int pos = m0 + row;
       const bool pos_ok = pos < a.LL;
-      const int b = pos_ok ? pos / a.Li : 0, aa = pos_ok ? pos - b * a.Li : 0;
-      const int64_t xoff = (int64_t)b * a.Pa + aa;
       const uint32_t tC = tmem_base + buf * 256 + lane_off, tD = tC + 128;
       for (int c = chalf * 4; c < chalf * 4 + 4; ++c) {
-        float cv[16], dv[16], xo[16];
+        float cv[16], dv[16];
         tc::tmem_ld16(tC + c * 16, cv);
         tc::tmem_ld16(tD + c * 16, dv);
         const int chb = n0 + c * 16;
-        float* xbase = a.X + (int64_t)chb * a.plane + xoff;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) xo[j] = (pos_ok && chb + j < a.nch) ? xbase[(int64_t)j * a.plane] : 0.f;
         __align__(16) bf16 hi[16];
         __align__(16) bf16 lo[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
+          float* xp = xs + (c * 16 + j) * BM + row;
           float xn = 0.f;
           if (pos_ok && chb + j < a.nch) {
-            float xc = xo[j] * cv[j] / dv[j];             // :130  X .* C ./ D
+            const float xo = *xp;
+            float xc = xo * cv[j] / dv[j];                 // :130  X .* C ./ D
             if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;       // :132-134
-            xn = xc * a.w + (1.f - a.w) * xo[j];           // :136
+            xn = xc * a.w + (1.f - a.w) * xo;              // :136
             if (xn < 0.f) xn = 0.f;                        // :137
-            xbase[(int64_t)j * a.plane] = xn;
+            *xp = xn;
           }
           split_bf16(xn, hi[j], lo[j]);
         }
@@ -262,9 +290,28 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
           dl[1] = reinterpret_cast<uint4*>(lo)[1];
         }
       }
+      // TMEM buffer free for the MMA warp
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&tempty[buf]);
+      // X tile back to HBM, then the next tile's X into the same buffer
+      tc::fence_proxy_async_smem();
+      tc::named_bar_sync(1, 32 * BWD_EPI_WARPS);
+      if (leader) {
+        tc::tma_store_2d(&mX, xs, m0, n0);
+        tc::bulk_commit();
+        tc::bulk_wait_read0();
+        const int tn = t + gridDim.x;
+        if (tn < total) {
+          tc::mbar_arrive_expect_tx(&xfull, XTILE);
+          tc::tma_load_2d(xs, &mX, &xfull, (tn % mtiles) * BM, (tn / mtiles) * BWD_BN);
+        }
+      }
+    }
+    if (leader) {
+      tc::bulk_wait0();
+      // a load still in flight after an abort must land before the CTA exits
+      if (aborted(&abort_flag)) tc::mbar_wait(&xfull, ti & 1, WAIT_LIMIT);
     }
   }
   tc::tc_fence_before();
@@ -273,9 +320,11 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
 }
 
 // ------------------------------------------------------------------ forward projection
+constexpr int FWD_MAX_STAGES = 4;
 struct TcFwdArgs {
   float* ypart;  // [split][MP][NB]
   int* err;
+  int stages;    // shared-memory ring depth (2..FWD_MAX_STAGES)
   int MP, NB, NH, nparts, ks_per_split, KS, frow0;  // frow0 = view * NB
   int use_alo, use_blo;                             // activation / tap hi+lo splits
 };
@@ -285,7 +334,7 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
          const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, TcFwdArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
-  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], accb;
+  __shared__ __align__(8) uint64_t full[FWD_MAX_STAGES], empty[FWD_MAX_STAGES], accb;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -294,11 +343,12 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
   const int ks0 = split * a.ks_per_split;
   const int ks1 = min(a.KS, ks0 + a.ks_per_split);
   const int tileB = a.NB * 128;  // NB rows x 128 bytes
-  const int offAl = TILE_A, offBh = 2 * TILE_A, offBl = 2 * TILE_A + tileB;
-  const int stage_bytes = 2 * TILE_A + 2 * tileB;
+  const int S = a.stages;
+  const int offAl = TILE_A, offBh = TILE_A * (a.use_alo ? 2 : 1), offBl = offBh + tileB;
+  const int stage_bytes = offBh + tileB * (a.use_blo ? 2 : 1);
   const uint32_t tcols = a.NB > 256 ? 512u : 256u;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
+    for (int s = 0; s < S; ++s) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
@@ -318,8 +368,8 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
     const uint32_t bytes = TILE_A * (a.use_alo ? 2 : 1) + tileB * (a.use_blo ? 2 : 1);
     int issued = 0;
     for (int ks = ks0; ks < ks1; ++ks) {
-      const int i = ks - ks0, s = i % STAGES;
-      const uint32_t ph = (i / STAGES) & 1;
+      const int i = ks - ks0, s = i % S;
+      const uint32_t ph = (i / S) & 1;
       if (!tc::mbar_wait(&empty[s], ph ^ 1, WAIT_LIMIT)) {
         set_abort(&abort_flag);
         atomicExch(a.err, TC_ERR_TIMEOUT_PRODUCER);
@@ -336,13 +386,13 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       }
       ++issued;
     }
-    for (int i = std::max(0, issued - STAGES); i < issued; ++i)
-      tc::mbar_wait(&full[i % STAGES], (i / STAGES) & 1, WAIT_LIMIT);
+    for (int i = std::max(0, issued - S); i < issued; ++i)
+      tc::mbar_wait(&full[i % S], (i / S) & 1, WAIT_LIMIT);
   } else if (warp == 1 && lane == 0) {
     const uint32_t idesc = tc::idesc_bf16_f32(BM, a.NH);
     for (int ks = ks0; ks < ks1; ++ks) {
-      const int i = ks - ks0, s = i % STAGES;
-      const uint32_t ph = (i / STAGES) & 1;
+      const int i = ks - ks0, s = i % S;
+      const uint32_t ph = (i / S) & 1;
       if (aborted(&abort_flag) || !tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
         set_abort(&abort_flag);
         atomicExch(a.err, TC_ERR_TIMEOUT_MMA);
@@ -495,30 +545,33 @@ __global__ void k_tc_pack_x(const float* __restrict__ X, int Li, int Pa, int LL,
 }
 
 // HX[j][i] = sum_split sum_{db,da} Y[split][(j+db-q)*Li + (i+da-q)][db*T+da]; ratio -> R.
+// One warp per output: lanes stride over the taps, then a fixed shuffle tree (deterministic).
 __global__ void k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, int Li, int Lj,
                                   int T, const float* __restrict__ lfsub, float* __restrict__ hx_out,
                                   float* __restrict__ rimg) {
   const int LL = Li * Lj;
-  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i0 = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
   if (i0 >= LL) return;
   const int q = (T - 1) / 2;
   const int j = i0 / Li, i = i0 - (i0 / Li) * Li;
   float s = 0.f;
-  for (int db = 0; db < T; ++db) {
-    const int b = j + db - q;
-    if (b < 0 || b >= Lj) continue;
-    for (int da = 0; da < T; ++da) {
-      const int a = i + da - q;
-      if (a < 0 || a >= Li) continue;
-      const int64_t p = (int64_t)b * Li + a;
-      for (int sp = 0; sp < splits; ++sp) s += ypart[((int64_t)sp * MP + p) * NB + db * T + da];
-    }
+  for (int t = lane; t < T * T; t += 32) {
+    const int db = t / T, da = t - (t / T) * T;
+    const int b = j + db - q, a = i + da - q;
+    if (b < 0 || b >= Lj || a < 0 || a >= Li) continue;
+    const int64_t p = (int64_t)b * Li + a;
+    for (int sp = 0; sp < splits; ++sp) s += __ldg(ypart + ((int64_t)sp * MP + p) * NB + t);
   }
-  if (hx_out) hx_out[i0] = s;
-  if (rimg) {
-    float r = lfsub[i0] / s;
-    if (!isfinite(r)) r = 0.f;
-    rimg[i0] = r;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    if (hx_out) hx_out[i0] = s;
+    if (rimg) {
+      float r = lfsub[i0] / s;
+      if (!isfinite(r)) r = 0.f;
+      rimg[i0] = r;
+    }
   }
 }
 
@@ -564,6 +617,7 @@ struct TcSolverState {
   int MP = 0, splits = 1, ks_per_split = 0, KSF = 0, nsm = 0;
   DevBuf ar_hi, ar_lo, a1, xb_hi, xb_lo, ypart, rimg, err;
   CUtensorMap mARh, mARl, mA1, mXh, mXl;
+  CUtensorMap mXv;  // the FP32 volume in the tensor-core layout [nch][plane], box 128 x 128
 };
 
 void tc_psf_free(TcPsfState* t) { delete t; }
@@ -600,9 +654,8 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
   MLF_TRY(make_map(&t->mBl, t->wbx_lo.p, (uint64_t)V * t->CHP, t->KB, BWD_BN));
   MLF_TRY(make_map(&t->mFh, t->wft_hi.p, (uint64_t)V * t->NB, t->CHP, t->NH));
   MLF_TRY(make_map(&t->mFl, t->wft_lo.p, (uint64_t)V * t->NB, t->CHP, t->NH));
-  MLF_CUDA(cudaFuncSetAttribute(k_tc_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BWD_SMEM));
-  const size_t fsmem = (size_t)STAGES * (2 * TILE_A + 2 * t->NB * 128) + 1024;
-  MLF_CUDA(cudaFuncSetAttribute(k_tc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+  MLF_CUDA(cudaFuncSetAttribute(k_tc_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem_bytes(1, 1)));
+  MLF_CUDA(cudaFuncSetAttribute(k_tc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
   p->tc = t.release();
   return MLF_OK;
 }
@@ -645,6 +698,17 @@ int tc_solver_prepare(Solver* s, cudaStream_t st) {
   MLF_TRY(make_map(&t->mA1, t->a1.p, t->MP, tp->KB, BM));
   MLF_TRY(make_map(&t->mXh, t->xb_hi.p, t->MP, tp->CHP, BM));
   MLF_TRY(make_map(&t->mXl, t->xb_lo.p, t->MP, tp->CHP, BM));
+  {
+    MLF_TRY(get_encoder());
+    cuuint64_t dims[2] = {(cuuint64_t)s->plane_tc, (cuuint64_t)s->nch};
+    cuuint64_t strides[1] = {(cuuint64_t)s->plane_tc * 4};
+    cuuint32_t box[2] = {BM, BWD_BN};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = g_encode(&t->mXv, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->X.p, dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(MLF_ERR_CUDA, "cuTensorMapEncodeTiled (volume) failed: " + std::to_string((int)r));
+  }
   s->tc = t.release();
   return MLF_OK;
 }
@@ -682,7 +746,9 @@ int tc_fwd_launch(Solver* s, int precision, int view, cudaStream_t st) {
   a.frow0 = view * tp->NB;
   a.use_alo = alo;
   a.use_blo = blo;
-  const size_t fsmem = (size_t)STAGES * (2 * TILE_A + 2 * tp->NB * 128) + 1024;
+  const size_t stage = (size_t)TILE_A * (alo ? 2 : 1) + (size_t)tp->NB * 128 * (blo ? 2 : 1);
+  a.stages = (int)std::max<size_t>(2, std::min<size_t>(FWD_MAX_STAGES, (226 * 1024) / stage));
+  const size_t fsmem = (size_t)a.stages * stage + 1024;
   k_tc_fwd<<<dim3(t->MP / BM, t->splits), 128, fsmem, st>>>(t->mXh, t->mXl, tp->mFh, tp->mFl, a);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
@@ -693,7 +759,7 @@ int tc_col2im(Solver* s, int view, bool ratio, float* hx_out, cudaStream_t st) {
   TcSolverState* t = s->tc;
   const int LL = s->Li * s->Lj;
   const float* lfsub = s->lfs.as<float>() + (int64_t)view * LL;
-  k_tc_col2im_ratio<<<(LL + 127) / 128, 128, 0, st>>>(t->ypart.as<float>(), t->splits, t->MP, tp->NB, s->Li,
+  k_tc_col2im_ratio<<<(LL + 7) / 8, 256, 0, st>>>(t->ypart.as<float>(), t->splits, t->MP, tp->NB, s->Li,
                                                       s->Lj, s->T, lfsub, hx_out,
                                                       ratio ? t->rimg.as<float>() : nullptr);
   MLF_CUDA(cudaGetLastError());
@@ -716,20 +782,19 @@ int tc_bwd_launch(Solver* s, int precision, int view, float w, cudaStream_t st) 
   int alo, blo;
   splits_of(precision, &alo, &blo);
   TcBwdArgs a{};
-  a.X = s->X.as<float>();
   a.xb_hi = t->xb_hi.as<bf16>();
   a.xb_lo = t->xb_lo.as<bf16>();
   a.err = t->err.as<int>();
-  a.plane = s->plane;
   a.w = w;
-  a.Li = s->Li; a.Lj = s->Lj; a.Pa = s->Pa; a.LL = s->Li * s->Lj;
+  a.Li = s->Li; a.LL = s->Li * s->Lj;
   a.CHP = tp->CHP; a.nch = (int)s->nch; a.KB = tp->KB; a.brow0 = view * tp->CHP;
   a.use_alo = alo;
   a.use_blo = blo;
   a.write_lo = alo;
   const int mt = t->MP / BM, nt = tp->CHP / BWD_BN;
   const int grid = std::min(mt * nt, t->nsm);
-  k_tc_bwd<<<grid, BWD_THREADS, BWD_SMEM, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, a, mt, nt);
+  k_tc_bwd<<<grid, BWD_THREADS, bwd_smem_bytes(alo, blo), st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl,
+                                                                 t->mXv, a, mt, nt);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
 }
@@ -741,7 +806,7 @@ int tc_pack_volume(Solver* s, int precision, cudaStream_t st) {
   const TcPsfState* tp = s->psf->tc;
   const int LL = s->Li * s->Lj;
   dim3 grid((t->MP + 31) / 32, (tp->CHP + 31) / 32);
-  k_tc_pack_x<<<grid, dim3(32, 8), 0, st>>>(s->X.as<float>(), s->Li, s->Pa, LL, s->plane, s->nch, tp->CHP, t->MP,
+  k_tc_pack_x<<<grid, dim3(32, 8), 0, st>>>(s->X.as<float>(), s->Li, s->Li, LL, s->plane_tc, s->nch, tp->CHP, t->MP,
                                             t->xb_hi.as<bf16>(), act_split(precision) ? t->xb_lo.as<bf16>() : nullptr);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
