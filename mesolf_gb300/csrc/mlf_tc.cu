@@ -609,6 +609,7 @@ inline int rup(int a, int b) { return (a + b - 1) / b * b; }
 
 struct TcPsfState {
   int KB = 0, NB = 0, NH = 0, nparts = 1, CHP = 0;
+  int fwd_dyn_max = 0;  // dynamic shared memory available to the forward GEMM
   DevBuf wbx_hi, wbx_lo, wft_hi, wft_lo;
   CUtensorMap mBh, mBl, mFh, mFl;
 };
@@ -654,8 +655,20 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
   MLF_TRY(make_map(&t->mBl, t->wbx_lo.p, (uint64_t)V * t->CHP, t->KB, BWD_BN));
   MLF_TRY(make_map(&t->mFh, t->wft_hi.p, (uint64_t)V * t->NB, t->CHP, t->NH));
   MLF_TRY(make_map(&t->mFl, t->wft_lo.p, (uint64_t)V * t->NB, t->CHP, t->NH));
-  MLF_CUDA(cudaFuncSetAttribute(k_tc_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem_bytes(1, 1)));
-  MLF_CUDA(cudaFuncSetAttribute(k_tc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  {
+    int optin = 0, dev = 0;
+    MLF_CUDA(cudaGetDevice(&dev));
+    MLF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fb, ff;
+    MLF_CUDA(cudaFuncGetAttributes(&fb, k_tc_bwd));
+    MLF_CUDA(cudaFuncGetAttributes(&ff, k_tc_fwd));
+    const size_t need_b = bwd_smem_bytes(1, 1);
+    if (need_b + fb.sharedSizeBytes > (size_t)optin)
+      return fail(MLF_ERR_UNSUPPORTED, "tensor-core back projection needs more shared memory than the device offers");
+    MLF_CUDA(cudaFuncSetAttribute(k_tc_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_b));
+    t->fwd_dyn_max = optin - (int)ff.sharedSizeBytes;
+    MLF_CUDA(cudaFuncSetAttribute(k_tc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, t->fwd_dyn_max));
+  }
   p->tc = t.release();
   return MLF_OK;
 }
@@ -747,7 +760,7 @@ int tc_fwd_launch(Solver* s, int precision, int view, cudaStream_t st) {
   a.use_alo = alo;
   a.use_blo = blo;
   const size_t stage = (size_t)TILE_A * (alo ? 2 : 1) + (size_t)tp->NB * 128 * (blo ? 2 : 1);
-  a.stages = (int)std::max<size_t>(2, std::min<size_t>(FWD_MAX_STAGES, (226 * 1024) / stage));
+  a.stages = (int)std::max<size_t>(2, std::min<size_t>(FWD_MAX_STAGES, (size_t)(tp->fwd_dyn_max - 1024) / stage));
   const size_t fsmem = (size_t)a.stages * stage + 1024;
   k_tc_fwd<<<dim3(t->MP / BM, t->splits), 128, fsmem, st>>>(t->mXh, t->mXl, tp->mFh, tp->mFl, a);
   MLF_CUDA(cudaGetLastError());
