@@ -78,9 +78,10 @@ struct TcBwdArgs {
 };
 
 constexpr int BWD_BN = 128;                            // channels per tile
-constexpr int BWD_EPI_WARPS = 8;                       // 2 per TMEM lane quadrant
+constexpr int BWD_EPI_WARPS = 16;                      // 4 per TMEM lane quadrant
 constexpr int BWD_THREADS = 32 * (2 + BWD_EPI_WARPS);  // producer, MMA, epilogue
-constexpr int XTILE = BM * BWD_BN * 4;                 // FP32 X tile, 64 KB
+constexpr int XTILE = BM * BWD_BN * 4;                 // FP32 X tile, 64 KB (two 32 KB halves)
+constexpr int XHALF = XTILE / 2;
 
 // Stage layout for a precision mode: Ah | [Al] | A1 | Bh | [Bl]
 struct BwdLayout {
@@ -109,8 +110,10 @@ inline size_t bwd_smem_bytes(int use_alo, int use_blo) {
 // accumulators are double buffered in TMEM (2 x 256 columns) so the epilogue of one tile
 // overlaps the MMAs of the next.  The X tile (128 positions x 128 channels, FP32) moves
 // HBM -> shared memory -> HBM by TMA: it is loaded while the tile's MMAs run, updated in
-// place by the epilogue, and stored back in bulk.  Epilogue warp e covers TMEM lanes
-// 32*(e%4).. and channel half (e-2)/4.
+// place by the epilogue, and stored back in bulk.  The tile is handled as two 64-channel
+// halves, each with its own shared-memory buffer, barrier and leader thread, so one half's
+// store and reload overlap the other half's arithmetic.  Epilogue warp e (warp e+2) covers
+// TMEM lanes 32*((e+2)%4).., channel half e/8 and the 32-channel quarter ((e%8)/4).
 __global__ void __launch_bounds__(BWD_THREADS, 1)
 k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
          const __grid_constant__ CUtensorMap mA1, const __grid_constant__ CUtensorMap mBh,
@@ -118,7 +121,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
          int mtiles, int ntiles) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
-  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull, mdone;
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull[2], mdone;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -136,7 +139,8 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       tc::mbar_init(&tfull[b], 1);
       tc::mbar_init(&tempty[b], BWD_EPI_WARPS);
     }
-    tc::mbar_init(&xfull, 1);
+    tc::mbar_init(&xfull[0], 1);
+    tc::mbar_init(&xfull[1], 1);
     tc::mbar_init(&mdone, 1);
     tc::fence_mbar_init();
     abort_flag = 0;
@@ -235,14 +239,17 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
   } else {
     // ---------------- epilogue: update X in shared memory, emit Xb, bulk-store X
     const int e = warp - 2;
-    const bool leader = (e == 0 && lane == 0);
+    const int half = e >> 3;                   // channels 64*half .. 64*half+63
+    const int sub = (e & 7) >> 2;              // 32-channel quarter inside the half
+    const bool leader = ((e & 7) == 0 && lane == 0);
     const int quad = warp & 3;                 // TMEM lanes 32*quad .. 32*quad+31
-    const int chalf = e / 4;                   // channel half of the tile
     const int row = quad * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    float* xh = xs + half * (XHALF / 4);       // [64 ch][128 pos]
+    uint64_t* xf = &xfull[half];
     if (leader && blockIdx.x < total) {
-      tc::mbar_arrive_expect_tx(&xfull, XTILE);
-      tc::tma_load_2d(xs, &mX, &xfull, (blockIdx.x % mtiles) * BM, (blockIdx.x / mtiles) * BWD_BN);
+      tc::mbar_arrive_expect_tx(xf, XHALF);
+      tc::tma_load_2d(xh, &mX, xf, (blockIdx.x % mtiles) * BM, (blockIdx.x / mtiles) * BWD_BN + 64 * half);
     }
     int ti = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x, ++ti) {
@@ -251,7 +258,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       const int m0 = (t % mtiles) * BM, n0 = (t / mtiles) * BWD_BN;
       bool ok = !aborted(&abort_flag) && tc::mbar_wait(&tfull[buf], tph, WAIT_LIMIT);
       tc::tc_fence_after();
-      ok = ok && tc::mbar_wait(&xfull, ti & 1, WAIT_LIMIT);
+      ok = ok && tc::mbar_wait(xf, ti & 1, WAIT_LIMIT);
       if (!ok) {
         if (lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
         set_abort(&abort_flag);
@@ -260,20 +267,21 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       const int pos = m0 + row;
       const bool pos_ok = pos < a.LL;
       const uint32_t tC = tmem_base + buf * 256 + lane_off, tD = tC + 128;
-      for (int c = chalf * 4; c < chalf * 4 + 4; ++c) {
+#pragma unroll
+      for (int cc = 0; cc < 2; ++cc) {
+        const int c = half * 4 + sub * 2 + cc;  // 16-channel chunk of the tile
         float cv[16], dv[16];
-        tc::tmem_ld16(tC + c * 16, cv);
-        tc::tmem_ld16(tD + c * 16, dv);
+        tc::tmem_ld16x2(tC + c * 16, tD + c * 16, cv, dv);
         const int chb = n0 + c * 16;
         __align__(16) bf16 hi[16];
         __align__(16) bf16 lo[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          float* xp = xs + (c * 16 + j) * BM + row;
+          float* xp = xh + ((sub * 2 + cc) * 16 + j) * BM + row;
           float xn = 0.f;
           if (pos_ok && chb + j < a.nch) {
             const float xo = *xp;
-            float xc = xo * cv[j] / dv[j];                 // :130  X .* C ./ D
+            float xc = __fdividef(xo * cv[j], dv[j]);      // :130  X .* C ./ D
             if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;       // :132-134
             xn = xc * a.w + (1.f - a.w) * xo;              // :136
             if (xn < 0.f) xn = 0.f;                        // :137
@@ -294,24 +302,24 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&tempty[buf]);
-      // X tile back to HBM, then the next tile's X into the same buffer
+      // this half of the X tile back to HBM, then the next tile's half into the same buffer
       tc::fence_proxy_async_smem();
-      tc::named_bar_sync(1, 32 * BWD_EPI_WARPS);
+      tc::named_bar_sync(1 + half, 32 * (BWD_EPI_WARPS / 2));
       if (leader) {
-        tc::tma_store_2d(&mX, xs, m0, n0);
+        tc::tma_store_2d(&mX, xh, m0, n0 + 64 * half);
         tc::bulk_commit();
         tc::bulk_wait_read0();
         const int tn = t + gridDim.x;
         if (tn < total) {
-          tc::mbar_arrive_expect_tx(&xfull, XTILE);
-          tc::tma_load_2d(xs, &mX, &xfull, (tn % mtiles) * BM, (tn / mtiles) * BWD_BN);
+          tc::mbar_arrive_expect_tx(xf, XHALF);
+          tc::tma_load_2d(xh, &mX, xf, (tn % mtiles) * BM, (tn / mtiles) * BWD_BN + 64 * half);
         }
       }
     }
     if (leader) {
       tc::bulk_wait0();
       // a load still in flight after an abort must land before the CTA exits
-      if (aborted(&abort_flag)) tc::mbar_wait(&xfull, ti & 1, WAIT_LIMIT);
+      if (aborted(&abort_flag)) tc::mbar_wait(xf, ti & 1, WAIT_LIMIT);
     }
   }
   tc::tc_fence_before();
@@ -715,7 +723,7 @@ int tc_solver_prepare(Solver* s, cudaStream_t st) {
     MLF_TRY(get_encoder());
     cuuint64_t dims[2] = {(cuuint64_t)s->plane_tc, (cuuint64_t)s->nch};
     cuuint64_t strides[1] = {(cuuint64_t)s->plane_tc * 4};
-    cuuint32_t box[2] = {BM, BWD_BN};
+    cuuint32_t box[2] = {BM, BWD_BN / 2};
     cuuint32_t es[2] = {1, 1};
     CUresult r = g_encode(&t->mXv, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->X.p, dims, strides, box, es,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
