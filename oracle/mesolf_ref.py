@@ -155,6 +155,26 @@ def gen_phasespace_psf(H, Ht):
     return Hps, Htc
 
 
+def phasespace_view(H, Ht, u, v):
+    """``Hps(:,:,u,v,:)`` and ``Htc(:,:,u,v,:)`` of the normalised PSF pair for one view
+    (0-based), without materialising the full 5-D arrays (same closed form as
+    :func:`gen_phasespace_psf`, per-depth sums as :func:`normalize_psf`)."""
+    K0, N, Z = H.shape[0], H.shape[2], H.shape[4]
+    S, i1 = phase_space_size(K0, N)
+    h = (N - 1) // 2
+    sH = np.array([np.asarray(H[:, :, :, :, z], np.float64).sum() for z in range(Z)])
+    sHt = np.array([np.asarray(Ht[:, :, :, :, z], np.float64).sum() for z in range(Z)])
+    p = np.arange(S)
+    src_ab = N - 1 - (p % N)
+    rp, rq = p + u - h, p + v - h
+    vr, vq = (rp >= 0) & (rp < S), (rq >= 0) & (rq < S)
+    rr, cc = np.clip(rp, 0, S - 1) + i1, np.clip(rq, 0, S - 1) + i1
+    hv = np.asarray(H[rr[:, None], cc[None, :], src_ab[:, None], src_ab[None, :], :], np.float64)
+    hv = hv * (vr[:, None] & vq[None, :])[:, :, None] / sH
+    tv = np.asarray(Ht[i1:i1 + S, i1:i1 + S, u, v, :], np.float64) / sHt
+    return hv, tv
+
+
 # ----------------------------------------------------------------------------- a4
 def view_weights(Hps):
     """View weights, ``recon_theory_phase_space_LFM_with_filter.m:20,30-38``."""

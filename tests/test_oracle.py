@@ -183,3 +183,21 @@ def test_rl_view_step_flux_and_positivity():
     X = R.recon_phase_space(LF, H, Ht, 1)
     assert X.shape == (60, 45, 3)
     assert np.isfinite(X).all() and (X >= 0).all()
+
+
+def test_c_port_matches_numpy_oracle():
+    """The C/OpenMP port used for the CPU baseline agrees with the numpy oracle."""
+    from oracle import cbuild
+    rng = np.random.default_rng(9)
+    N, S, Z = 15, 45, 3
+    h = rng.random((S, S, Z))
+    t = rng.random((S, S, Z))
+    X = rng.random((60, 75, Z))
+    LF = rng.random((60, 75)) * 100
+    np.testing.assert_allclose(cbuild.forward(h, X, N), R.forward_ps(h, X, N), rtol=1e-12)
+    Rimg = rng.random((4, 5))
+    np.testing.assert_allclose(cbuild.backward(t, Rimg, 3, 11, N), R.backward_ps(t, Rimg, 3, 11, N),
+                               rtol=1e-12, atol=1e-14)
+    ref = R.rl_view_step(X, LF, h[:, :, None, None, :].repeat(15, 2).repeat(15, 3),
+                         t[:, :, None, None, :].repeat(15, 2).repeat(15, 3), 3, 11, 0.3, N)
+    np.testing.assert_allclose(cbuild.view_step(h, t, LF, X, 3, 11, 0.3, N), ref, rtol=1e-11)
