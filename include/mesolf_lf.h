@@ -48,6 +48,7 @@ enum mlf_precision {
 
 typedef struct mlf_psf mlf_psf;       /* phase-space PSF resident in HBM */
 typedef struct mlf_solver mlf_solver; /* per-image-size solve context (scratch in HBM) */
+typedef struct mlf_batch mlf_batch;   /* many patches solved together on the tensor cores */
 
 typedef struct mlf_stats {
   int32_t n_views;              /* active views per iteration (weight != 0) */
@@ -120,6 +121,23 @@ int mlf_solver_destroy(mlf_solver* s);
 int64_t mlf_solver_device_bytes(const mlf_solver* s);
 int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t precision,
                    const float* warm_start, float* vol_out, mlf_stats* stats, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Batched solve of independent patches (the reference solves patches one MATLAB process
+ * at a time: mesolf.m:55-98 with SI.worker_ix).  All patches share one PSF; patch k has
+ * Xr[k] x Xc[k] pixels (multiples of N, uneven sizes allowed) and uses the PSF planes
+ * [z0[k], z0[k] + nz[k]) -- its result equals a solve with the PSF cut to those planes
+ * (per-depth normalisation makes a plane range a PSF of its own; the view weights are
+ * recomputed for the range).  Each view step of all patches is one launch of the
+ * tensor-core GEMMs over the concatenated lenslet positions; precision must be one of the
+ * MLF_PREC_BF16* modes.  lfimg[k], warm[k] (warm may be NULL or hold NULLs) and vol_out[k]
+ * (Xr[k] x Xc[k] x nz[k]) are device pointers.  Synchronous when stats != NULL. */
+int mlf_batch_create(mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int64_t* Xc, const int32_t* z0,
+                     const int32_t* nz, mlf_batch** out);
+int mlf_batch_destroy(mlf_batch* b);
+int64_t mlf_batch_device_bytes(const mlf_batch* b);
+int mlf_batch_run(mlf_batch* b, const float* const* lfimg, int32_t max_iter, int32_t precision,
+                  const float* const* warm, float* const* vol_out, mlf_stats* stats, void* stream);
 
 /* One-shot form with the reference's argument order (H, Ht raw PSFs).  Builds the PSF
  * and a solver, runs, frees.  Synchronous. */

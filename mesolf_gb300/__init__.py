@@ -5,8 +5,8 @@ holds its build recipe, ctypes bindings, the reference-shaped Python entry point
 the seeded synthetic workload generators.
 """
 from ._lib import MesoLFError, load as load_library  # noqa: F401
-from .api import (PhaseSpacePSF, RLSolver, mex_lfm_convolution_vec,  # noqa: F401
+from .api import (BatchSolver, PhaseSpacePSF, RLSolver, mex_lfm_convolution_vec,  # noqa: F401
                   recon_theory_phase_space_LFM_with_filter)
 
-__all__ = ["MesoLFError", "load_library", "PhaseSpacePSF", "RLSolver", "mex_lfm_convolution_vec",
+__all__ = ["MesoLFError", "load_library", "BatchSolver", "PhaseSpacePSF", "RLSolver", "mex_lfm_convolution_vec",
            "recon_theory_phase_space_LFM_with_filter"]

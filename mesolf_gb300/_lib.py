@@ -46,6 +46,10 @@ SIGNATURES = {
     "mlf_rl_view_step_prec": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, ctypes.c_double, _i32, _vp]),
     "mlf_forward_view_prec": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i32, _vp, _vp]),
     "mlf_forward_view_static": (ctypes.c_int, [_vp, _vp, _i64, _i64, _i32, _i32, _vp, _vp]),
+    "mlf_batch_create": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "mlf_batch_destroy": (ctypes.c_int, [_vp]),
+    "mlf_batch_device_bytes": (_i64, [_vp]),
+    "mlf_batch_run": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp]),
 }
 
 

@@ -218,6 +218,74 @@ class RLSolver:
             pass
 
 
+class BatchSolver:
+    """Independent patches solved together on the tensor cores (one launch per view step
+    for all of them).  ``shapes`` = [(Xr, Xc), ...]; ``planes`` = [(z0, nz), ...] plane
+    ranges of the shared PSF (default: all planes)."""
+
+    def __init__(self, psf: PhaseSpacePSF, shapes, planes=None):
+        lib = _lib.load()
+        self.psf = psf
+        self.shapes = [(int(a), int(b)) for a, b in shapes]
+        P = len(self.shapes)
+        if planes is None:
+            planes = [(0, psf.Z)] * P
+        self.planes = [(int(a), int(b)) for a, b in planes]
+        xr = (ctypes.c_int64 * P)(*[a for a, _ in self.shapes])
+        xc = (ctypes.c_int64 * P)(*[b for _, b in self.shapes])
+        z0 = (ctypes.c_int32 * P)(*[a for a, _ in self.planes])
+        nz = (ctypes.c_int32 * P)(*[b for _, b in self.planes])
+        h = ctypes.c_void_p()
+        check(lib.mlf_batch_create(psf.handle, P, xr, xc, z0, nz, ctypes.byref(h)))
+        self._h = h
+        self.last_stats = None
+
+    @property
+    def device_bytes(self):
+        return int(_lib.load().mlf_batch_device_bytes(self._h))
+
+    def run(self, lfimgs, max_iter, precision="bf16x2", warm=None, outs=None, stream=None, want_stats=True):
+        """Device (torch CUDA) images in, list of (Xr, Xc, nz) device volumes out."""
+        import torch
+        lib = _lib.load()
+        P = len(self.shapes)
+        keep = []
+        lp = (ctypes.c_void_p * P)()
+        for k, im in enumerate(lfimgs):
+            t, ptr = _fortran(im)
+            keep.append(t)
+            lp[k] = ptr
+        wp = None
+        if warm is not None:
+            wp = (ctypes.c_void_p * P)()
+            for k, x in enumerate(warm):
+                if x is not None:
+                    t, ptr = _fortran(x)
+                    keep.append(t)
+                    wp[k] = ptr
+        if outs is None:
+            outs = [_empty_like_kind(lfimgs[k], (self.shapes[k][0], self.shapes[k][1], self.planes[k][1]))[0]
+                    for k in range(P)]
+        op = (ctypes.c_void_p * P)(*[o.data_ptr() for o in outs])
+        st = MLFStats()
+        check(lib.mlf_batch_run(self._h, lp, int(max_iter), PRECISIONS[precision], wp, op,
+                                ctypes.byref(st) if want_stats else None, _stream_of(lfimgs[0], stream)))
+        self.last_stats = st.as_dict() if want_stats else None
+        del keep
+        return outs
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().mlf_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def recon_theory_phase_space_LFM_with_filter(LFIMG, H, Ht, maxIter, gpuFlag=True, gpu_id=1,
                                              precision="fp32"):
     """Same arguments as the reference solver; returns the volume as a host float64

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <vector>
 
 #include "mlf_internal.h"
 
@@ -66,6 +67,12 @@ using namespace mlf;
 
 struct mlf_psf : public mlf::Psf {};
 struct mlf_solver : public mlf::Solver {};
+struct mlf_batch {
+  mlf::Psf* psf = nullptr;
+  std::vector<std::unique_ptr<mlf::Solver>> members;  // per-patch geometry, filter plan, scratch
+  mlf::TcSolverState* work = nullptr;
+  ~mlf_batch() { mlf::tc_solver_free(work); }
+};
 
 namespace {
 
@@ -251,6 +258,79 @@ int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t 
   MLF_TRY(finish_out(o, st));
   if (o.host || warm_tmp.p || dlf != lfimg) MLF_CUDA(cudaStreamSynchronize(st));
   return MLF_OK;
+}
+
+int mlf_batch_create(mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int64_t* Xc, const int32_t* z0,
+                     const int32_t* nz, mlf_batch** out) {
+  clear_error();
+  if (!psf || !Xr || !Xc || !z0 || !nz || !out) return fail(MLF_ERR_INVALID, "mlf_batch_create: null pointer");
+  *out = nullptr;
+  if (npatch < 1) return fail(MLF_ERR_INVALID, "mlf_batch_create: need at least one patch");
+  std::unique_ptr<mlf_batch> b(new mlf_batch());
+  b->psf = psf;
+  int dev = 0;
+  MLF_CUDA(cudaGetDevice(&dev));
+  if (dev != psf->device) return fail(MLF_ERR_INVALID, "mlf_batch_create: PSF lives on another device");
+  for (int k = 0; k < npatch; ++k) {
+    if (Xr[k] < psf->N || Xc[k] < psf->N || Xr[k] % psf->N || Xc[k] % psf->N)
+      return fail(MLF_ERR_INVALID, "mlf_batch_create: patch " + std::to_string(k) +
+                                       ": image sides must be positive multiples of Nnum");
+    if (z0[k] < 0 || nz[k] < 1 || z0[k] + nz[k] > psf->Z)
+      return fail(MLF_ERR_INVALID, "mlf_batch_create: patch " + std::to_string(k) + ": plane range outside the PSF");
+    std::unique_ptr<mlf::Solver> m(new mlf::Solver());
+    m->psf = psf;
+    m->device = dev;
+    m->lite = true;
+    m->Xr = Xr[k];
+    m->Xc = Xc[k];
+    m->Z = nz[k];
+    m->z0 = z0[k];
+    MLF_TRY(solver_init(m.get()));
+    b->members.push_back(std::move(m));
+  }
+  std::vector<mlf::Solver*> ms;
+  for (auto& m : b->members) ms.push_back(m.get());
+  MLF_TRY(tc_work_create(psf, ms, &b->work, nullptr));
+  MLF_CUDA(cudaDeviceSynchronize());
+  *out = b.release();
+  return MLF_OK;
+}
+
+int mlf_batch_destroy(mlf_batch* b) {
+  clear_error();
+  delete b;
+  return MLF_OK;
+}
+
+int64_t mlf_batch_device_bytes(const mlf_batch* b) {
+  if (!b) return 0;
+  size_t n = tc_work_bytes(b->work);
+  for (auto& m : b->members) n += m->bytes();
+  return (int64_t)n;
+}
+
+int mlf_batch_run(mlf_batch* b, const float* const* lfimg, int32_t max_iter, int32_t precision,
+                  const float* const* warm, float* const* vol_out, mlf_stats* stats, void* stream) {
+  clear_error();
+  if (!b || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_batch_run: null pointer");
+  if (max_iter < 0) return fail(MLF_ERR_INVALID, "mlf_batch_run: maxIter must be >= 0");
+  if (precision != MLF_PREC_BF16 && precision != MLF_PREC_BF16X2 && precision != MLF_PREC_BF16X3)
+    return fail(MLF_ERR_UNSUPPORTED, "mlf_batch_run: batches run on the tensor cores (MLF_PREC_BF16*); "
+                                     "use mlf_solver_run per patch for MLF_PREC_FP32");
+  const size_t P = b->members.size();
+  std::vector<const float*> lf(P), wm(P);
+  std::vector<float*> out(P);
+  std::vector<mlf::Solver*> ms;
+  for (size_t k = 0; k < P; ++k) {
+    lf[k] = lfimg[k];
+    wm[k] = warm ? warm[k] : nullptr;
+    out[k] = vol_out[k];
+    if (!lf[k] || !out[k]) return fail(MLF_ERR_INVALID, "mlf_batch_run: null image or output pointer");
+    if (!is_device_ptr(lf[k]) || !is_device_ptr(out[k]) || (wm[k] && !is_device_ptr(wm[k])))
+      return fail(MLF_ERR_INVALID, "mlf_batch_run: device pointers required");
+    ms.push_back(b->members[k].get());
+  }
+  return tc_run(b->work, ms, lf, wm, out, max_iter, precision, stats, ms[0], static_cast<cudaStream_t>(stream));
 }
 
 int mlf_rl_solve(const float* lfimg, int64_t Xr, int64_t Xc, const float* H, const float* Ht,

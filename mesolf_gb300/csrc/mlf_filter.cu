@@ -31,31 +31,30 @@ struct FGeo {
   int Z;
 };
 
-// Phase-major -> MATLAB layout for all planes (into the scratch volume).
-__global__ void k_unphase(const float* __restrict__ X, int N, int Z, int Li, int Pa, int64_t plane,
-                          int64_t Xr, int64_t Xc, float* __restrict__ V) {
-  const int64_t n = Xr * Xc * Z;
+__device__ __forceinline__ int64_t unphase_index(const PatchGeo& g, int64_t e) {
+  const int64_t r = e % g.Xr;
+  const int64_t c = (e / g.Xr) % g.Xc;
+  const int z = (int)(e / (g.Xr * g.Xc));
+  const int64_t ch = ((c % g.N) * g.N + (r % g.N)) * g.Zch + g.z0 + z;
+  return ch * g.plane + (c / g.N) * g.Pa + (r / g.N);
+}
+
+// Phase-major -> MATLAB layout for the patch's planes (into the scratch volume).
+__global__ void k_unphase(const float* __restrict__ X, PatchGeo g, float* __restrict__ V) {
+  const int64_t n = g.Xr * g.Xc * g.Z;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = e % Xr;
-    const int64_t c = (e / Xr) % Xc;
-    const int z = (int)(e / (Xr * Xc));
-    const int64_t ch = ((c % N) * N + (r % N)) * Z + z;
-    V[e] = X[ch * plane + (c / N) * Pa + (r / N)];
-  }
+       e += (int64_t)gridDim.x * blockDim.x)
+    V[e] = X[unphase_index(g, e)];
 }
 
 // MATLAB layout -> phase-major, scaling each plane by scale[z].
-__global__ void k_rephase(const float* __restrict__ V, const double* __restrict__ scale, int N, int Z,
-                          int Pa, int64_t plane, int64_t Xr, int64_t Xc, float* __restrict__ X) {
-  const int64_t n = Xr * Xc * Z;
+__global__ void k_rephase(const float* __restrict__ V, const double* __restrict__ scale, PatchGeo g,
+                          float* __restrict__ X) {
+  const int64_t n = g.Xr * g.Xc * g.Z;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = e % Xr;
-    const int64_t c = (e / Xr) % Xc;
-    const int z = (int)(e / (Xr * Xc));
-    const int64_t ch = ((c % N) * N + (r % N)) * Z + z;
-    X[ch * plane + (c / N) * Pa + (r / N)] = (float)((double)V[e] * scale[z]);
+    const int z = (int)(e / (g.Xr * g.Xc));
+    X[unphase_index(g, e)] = (float)((double)V[e] * scale[z]);
   }
 }
 
@@ -330,7 +329,8 @@ int filter_init(Solver* s) {
   return MLF_OK;
 }
 
-int filter_run(Solver* s, cudaStream_t st) {
+// The filter of one patch whose volume lives in X with layout g (g.Z planes, the plan's).
+int filter_run_geo(Solver* s, const PatchGeo& g, float* X, cudaStream_t st) {
   FilterPlan& f = s->filt;
   const int Z = s->Z;
   int nzf = 0;
@@ -344,21 +344,21 @@ int filter_run(Solver* s, cudaStream_t st) {
   const int* nt_x = wlo_x + ne;
   const int* wlo_y = nt_x + ne;
   const int* nt_y = wlo_y + ne;
-  const FGeo g{s->Xr, s->Xc, Z};
+  const FGeo fg{s->Xr, s->Xc, Z};
   const int64_t n = s->Xr * s->Xc * Z;
   const int eg = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
   float* V = s->Xtmp.as<float>();
-  k_unphase<<<eg, 256, 0, st>>>(s->X.as<float>(), s->N, Z, s->Li, s->lay_Pa, s->lay_plane, s->Xr, s->Xc, V);
+  k_unphase<<<eg, 256, 0, st>>>(X, g, V);
   const int gr = (int)((s->Xc + kLines - 1) / kLines), gc = (int)((s->Xr + kLines - 1) / kLines);
   double* sin = f.sums.as<double>();
   double* sout = sin + (size_t)nzf * f.max_blocks;
   double* scale = sout + (size_t)nzf * f.max_blocks;
   k_filter_r<<<dim3(gr, nzf), kFiltThreads, sizeof(float) * s->Xr * kPad, st>>>(
-      V, g, zl, pe, f.cx.as<float>(), wlo_x, nt_x, (int)s->Xr, sin);
+      V, fg, zl, pe, f.cx.as<float>(), wlo_x, nt_x, (int)s->Xr, sin);
   k_filter_c<<<dim3(gc, nzf), kFiltThreads, sizeof(float) * s->Xc * kPad, st>>>(
-      V, g, zl, pe, f.cy.as<float>(), wlo_y, nt_y, (int)s->Xc, sout);
+      V, fg, zl, pe, f.cy.as<float>(), wlo_y, nt_y, (int)s->Xc, sout);
   k_filter_scale<<<(Z + 255) / 256, 256, 0, st>>>(sin, gr, sout, gc, zl, nzf, Z, scale);
-  k_rephase<<<eg, 256, 0, st>>>(V, scale, s->N, Z, s->lay_Pa, s->lay_plane, s->Xr, s->Xc, s->X.as<float>());
+  k_rephase<<<eg, 256, 0, st>>>(V, scale, g, X);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
 }

@@ -45,9 +45,18 @@ struct DevBuf {
 bool is_device_ptr(const void* ptr);
 
 struct TcPsfState;     // tensor-core operands of a PSF (mlf_tc.cu)
-struct TcSolverState;  // tensor-core scratch of a solver (mlf_tc.cu)
+struct TcSolverState;  // tensor-core work set of one or more patches (mlf_tc.cu)
 void tc_psf_free(TcPsfState* t);
 void tc_solver_free(TcSolverState* t);
+
+// Where a patch's volume lives in a phase-major buffer: channel
+// ch = (beta*N + alpha)*Zch + z0 + z (z < Z planes of the patch), position b*Pa + a inside
+// a plane of `plane` floats.  The plain FP32 solver uses Zch = Z, z0 = 0, Pa padded to 4;
+// the tensor-core work set uses Pa = Li and one plane spanning all its patches.
+struct PatchGeo {
+  int N, Z, Zch, z0, Li, Lj, Pa;
+  int64_t plane, Xr, Xc;
+};
 
 // ------------------------------------------------------------------ PSF
 // Per-view projector taps in phase-major ("polyphase") form.  For view (u, v) (0-based,
@@ -63,7 +72,9 @@ struct Psf {
   int64_t taps_per_view = 0; // nch * T * T
   DevBuf wf, wb;             // float [N*N][nch][T*T]
   std::vector<double> weights;  // N*N, index u + N*v (MATLAB weight(u+1, v+1))
+  std::vector<double> wsum_vz;  // [N*N][Z] FP64 sums of Hps(:,:,u,v,z) (weights of plane ranges)
   std::vector<int> view_order;  // active views in spiral order (view = u + N*v)
+  std::vector<int> spiral;      // all N*N views in spiral order
   TcPsfState* tc = nullptr;     // built on the first tensor-core solve
   ~Psf() { tc_psf_free(tc); }
   size_t bytes() const;
@@ -90,9 +101,6 @@ struct Solver {
   int N = 0, Z = 0, Li = 0, Lj = 0, q = 0, T = 0;
   int Pa = 0;          // row pitch (floats) of a phase-major plane (FP32 kernels)
   int64_t plane = 0;   // floats per plane (Lj * Pa)
-  int64_t plane_tc = 0;  // floats per plane in the tensor-core layout (pitch Li, linear positions)
-  int lay_Pa = 0;        // layout of X in the current solve: FP32 (Pa, plane) or
-  int64_t lay_plane = 0; // tensor-core (Li, plane_tc)
   int64_t nch = 0;
   // view-kernel geometry
   int tilesA = 0, tilesB = 0, tps = 0, slots = 0, threads = 0, grid = 0;
@@ -113,6 +121,8 @@ struct Solver {
   std::vector<cudaEvent_t> tev;
   int tev_used = 0;
   bool timing = false;
+  bool lite = false;            // batch member: geometry, filter plan and filter scratch only
+  int z0 = 0;                   // first PSF plane of this patch (batch members)
   TcSolverState* tc = nullptr;  // built on the first tensor-core solve
   ~Solver();
   size_t bytes() const;
@@ -127,20 +137,36 @@ int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaS
 int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cudaStream_t st);
 int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, double w, int precision,
                  cudaStream_t st);
+// layout kernels on an arbitrary PatchGeo (mlf_rl.cu)
+int launch_extract_views(const float* d_lf, const PatchGeo& g, float* lfs, int64_t view_stride, int64_t off,
+                         cudaStream_t st);
+int launch_to_phase(const float* d_vol, const PatchGeo& g, float* X, cudaStream_t st);
+int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st);
+// flat initial guess sum(lf)/(Xr*Xc*Z) on the patch's planes, 0 on the other channels
+int launch_init_flat(const float* d_lf, const PatchGeo& g, float* X, double* scratch, cudaStream_t st);
+int filter_run_geo(Solver* s, const PatchGeo& g, float* X, cudaStream_t st);
+PatchGeo solver_geo(const Solver* s);
+std::vector<double> psf_range_weights(const Psf* p, int z0, int nz);
+int rl_iteration_count_views(const std::vector<std::vector<double>>& w);
 int forward_view_prec(Solver* s, const float* d_vol, int u, int v, int precision, float* d_hx, cudaStream_t st);
 int sample_filter(Solver* s, float* d_vol, cudaStream_t st);
 int filter_init(Solver* s);
 int timing_mark(Solver* s, cudaStream_t st);
-// tensor-core path (mlf_tc.cu)
+// tensor-core path (mlf_tc.cu).  A work set covers P patches (P = 1 for a single solver);
+// `members[p]` supplies each patch's geometry, filter plan and filter scratch.
 int tc_psf_prepare(Psf* p, cudaStream_t st);
+int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState** out, cudaStream_t st);
 int tc_solver_prepare(Solver* s, cudaStream_t st);
-int tc_enqueue_views(Solver* s, int precision, int64_t* launches, cudaStream_t st);
-int tc_pack_volume(Solver* s, int precision, cudaStream_t st);
-int tc_forward_view(Solver* s, int precision, int view, float* hx_out, cudaStream_t st);
-int tc_view_step(Solver* s, int precision, int view, float w, cudaStream_t st);
-int tc_check_error(Solver* s);
+// full solve: lf[p], warm[p] (nullable), out[p] device pointers in MATLAB layout
+int tc_run(TcSolverState* w, const std::vector<Solver*>& members, const std::vector<const float*>& lf,
+           const std::vector<const float*>& warm, const std::vector<float*>& out, int max_iter, int precision,
+           mlf_stats* stats, Solver* timing_owner, cudaStream_t st);
+int tc_forward_view(Solver* s, int precision, const float* d_vol, int view, float* hx_out, cudaStream_t st);
+int tc_view_step(Solver* s, int precision, const float* d_lf, float* d_vol, int view, float w, cudaStream_t st);
+int tc_check_error(TcSolverState* w);
 size_t tc_psf_bytes(const Psf* p);
 size_t tc_solver_bytes(const Solver* s);
+size_t tc_work_bytes(const TcSolverState* w);
 int filter_run(Solver* s, cudaStream_t st);
 int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,
                  int64_t kw, int nnum, float* d_out, cudaStream_t st);

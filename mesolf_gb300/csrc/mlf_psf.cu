@@ -114,23 +114,22 @@ __global__ void k_build_taps(const float* __restrict__ H, const float* __restric
   }
 }
 
-// wsum[view] = sum over x, y, z of Hps(:, :, u, v, :) in FP64 (one block per view,
+// wsum[view][z] = sum over x, y of Hps(:, :, u, v, z) in FP64 (one block per (view, z),
 // fixed order).
 __global__ void k_view_sums(const float* __restrict__ H, const double* __restrict__ invH, TapGeom g,
                             double* wsum) {
   __shared__ double sh[32];
-  const int view = blockIdx.x;
+  const int view = blockIdx.x, z = blockIdx.y;
   const int u = view % g.N, v = view / g.N;
-  const int64_t n = (int64_t)g.S * g.S * g.Z;
+  const int64_t n = (int64_t)g.S * g.S;
   double s = 0.0;
   for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
     const int p = (int)(e % g.S);
-    const int pq = (int)((e / g.S) % g.S);
-    const int z = (int)(e / ((int64_t)g.S * g.S));
+    const int pq = (int)(e / g.S);
     s += hps_value(H, invH, g, u, v, p, pq, z);
   }
   s = block_sum_d(s, sh);
-  if (threadIdx.x == 0) wsum[view] = s;
+  if (threadIdx.x == 0) wsum[(int64_t)view * g.Z + z] = s;
 }
 
 // gen_spiral, recon_theory_phase_space_LFM_with_filter.m:156-188 (1-based outputs).
@@ -178,7 +177,7 @@ int psf_build(Psf* psf, const float* dH, const float* dHt, cudaStream_t st) {
   DevBuf part, inv, wsum;
   MLF_TRY(part.alloc(sizeof(double) * Z * kSumBlocks * 2, "psf sums"));
   MLF_TRY(inv.alloc(sizeof(double) * Z * 2, "psf sums"));
-  MLF_TRY(wsum.alloc(sizeof(double) * N * N, "psf weights"));
+  MLF_TRY(wsum.alloc(sizeof(double) * N * N * Z, "psf weights"));
   double* partH = part.as<double>();
   double* partHt = partH + (int64_t)Z * kSumBlocks;
   double* invH = inv.as<double>();
@@ -194,12 +193,15 @@ int psf_build(Psf* psf, const float* dH, const float* dHt, cudaStream_t st) {
   MLF_TRY(psf->wb.alloc(nt * sizeof(float), "psf backward taps"));
   k_build_taps<<<2048, 256, 0, st>>>(dH, dHt, invH, invHt, g, psf->wf.as<float>(),
                                      psf->wb.as<float>());
-  k_view_sums<<<N * N, 512, 0, st>>>(dH, invH, g, wsum.as<double>());
+  k_view_sums<<<dim3(N * N, Z), 256, 0, st>>>(dH, invH, g, wsum.as<double>());
   MLF_CUDA(cudaGetLastError());
 
-  std::vector<double> w(N * N);
-  MLF_CUDA(cudaMemcpyAsync(w.data(), wsum.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost, st));
+  psf->wsum_vz.assign((size_t)N * N * Z, 0.0);
+  MLF_CUDA(cudaMemcpyAsync(psf->wsum_vz.data(), wsum.p, sizeof(double) * N * N * Z, cudaMemcpyDeviceToHost, st));
   MLF_CUDA(cudaStreamSynchronize(st));
+  std::vector<double> w(N * N, 0.0);
+  for (int v = 0; v < N * N; ++v)
+    for (int z = 0; z < Z; ++z) w[v] += psf->wsum_vz[(size_t)v * Z + z];
 
   // weights (recon_…_with_filter.m:30-38), FP64 on the host, IEEE NaN semantics kept
   for (double& x : w)
@@ -222,8 +224,10 @@ int psf_build(Psf* psf, const float* dH, const float* dHt, cudaStream_t st) {
   std::vector<int> ii, jj;
   gen_spiral(N, ii, jj);
   psf->view_order.clear();
+  psf->spiral.clear();
   for (int k = 0; k < N * N; ++k) {
     const int u = ii[k] - 1, v = jj[k] - 1;
+    psf->spiral.push_back(u + N * v);
     if (w[u + N * v] == 0.0) continue;
     psf->view_order.push_back(u + N * v);
   }

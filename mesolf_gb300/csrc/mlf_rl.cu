@@ -4,8 +4,9 @@
 // the spiral view loop (forward projection, ratio, back projection, update, blend) and
 // the per-iteration sample_filter.  Each view step is one launch of the fused view
 // kernel (back projection + D + update of view k, forward projection of view k+1) plus
-// one launch of the partial-sum reduction that forms the next ratio image.  One
-// iteration is captured once as a CUDA graph and replayed.
+// one launch of the partial-sum reduction that forms the next ratio image.  The
+// mixed-precision (tensor-core) forms are in mlf_tc.cu; this file keeps the layout
+// kernels, which take a PatchGeo so they also serve the patches of a batch.
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -40,10 +41,10 @@ __global__ void k_sum_partial(const float* __restrict__ a, int64_t n, double* pa
   }
 }
 
-// Flat initial guess, recon_…_with_filter.m:72-73: ones/sum(ones)*sum(LFIMG).  Only the
-// valid positions of each plane are written (row padding stays zero).
-__global__ void k_init_flat(float* X, int Li, int Lj, int Pa, int64_t plane, int64_t nch,
-                            const double* part, int nparts, double inv_count) {
+// Flat initial guess, recon_…_with_filter.m:72-73: ones/sum(ones)*sum(LFIMG) on the
+// patch's planes (channels whose z is outside [z0, z0+Z) get 0).  Only the valid
+// positions of each plane are written (row padding stays as it is).
+__global__ void k_init_flat(float* X, PatchGeo g, const double* part, int nparts, double inv_count) {
   __shared__ float val;
   if (threadIdx.x == 0) {
     double s = 0.0;
@@ -51,59 +52,53 @@ __global__ void k_init_flat(float* X, int Li, int Lj, int Pa, int64_t plane, int
     val = (float)(inv_count * s);
   }
   __syncthreads();
-  const int64_t n = nch * Li * Lj;
+  const int64_t LL = (int64_t)g.Li * g.Lj;
+  const int64_t n = (int64_t)g.N * g.N * g.Zch * LL;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t ch = i / ((int64_t)Li * Lj);
-    const int rem = (int)(i - ch * Li * Lj);
-    X[ch * plane + (int64_t)(rem / Li) * Pa + rem % Li] = val;
+    const int64_t ch = i / LL;
+    const int rem = (int)(i - ch * LL);
+    const int z = (int)(ch % g.Zch) - g.z0;
+    X[ch * g.plane + (int64_t)(rem / g.Li) * g.Pa + rem % g.Li] = (z >= 0 && z < g.Z) ? val : 0.f;
   }
 }
 
-struct Geo {
-  int N, Z, Li, Lj, Pa;
-  int64_t plane, Xr, Xc;
-};
+__device__ __forceinline__ int64_t phase_index(const PatchGeo& g, int64_t e) {
+  const int64_t r = e % g.Xr;
+  const int64_t c = (e / g.Xr) % g.Xc;
+  const int z = (int)(e / (g.Xr * g.Xc));
+  const int alpha = (int)(r % g.N), a = (int)(r / g.N);
+  const int beta = (int)(c % g.N), b = (int)(c / g.N);
+  const int64_t ch = ((int64_t)beta * g.N + alpha) * g.Zch + g.z0 + z;
+  return ch * g.plane + (int64_t)b * g.Pa + a;
+}
 
 // MATLAB (Xr, Xc, Z) volume -> phase-major planes; one thread per voxel of the input.
-__global__ void k_to_phase(const float* __restrict__ vol, Geo g, float* __restrict__ X) {
+__global__ void k_to_phase(const float* __restrict__ vol, PatchGeo g, float* __restrict__ X) {
   const int64_t n = g.Xr * g.Xc * g.Z;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = e % g.Xr;
-    const int64_t c = (e / g.Xr) % g.Xc;
-    const int z = (int)(e / (g.Xr * g.Xc));
-    const int alpha = (int)(r % g.N), a = (int)(r / g.N);
-    const int beta = (int)(c % g.N), b = (int)(c / g.N);
-    const int64_t ch = ((int64_t)beta * g.N + alpha) * g.Z + z;
-    X[ch * g.plane + (int64_t)b * g.Pa + a] = vol[e];
-  }
+       e += (int64_t)gridDim.x * blockDim.x)
+    X[phase_index(g, e)] = vol[e];
 }
 
-__global__ void k_from_phase(const float* __restrict__ X, Geo g, float* __restrict__ vol) {
+__global__ void k_from_phase(const float* __restrict__ X, PatchGeo g, float* __restrict__ vol) {
   const int64_t n = g.Xr * g.Xc * g.Z;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = e % g.Xr;
-    const int64_t c = (e / g.Xr) % g.Xc;
-    const int z = (int)(e / (g.Xr * g.Xc));
-    const int alpha = (int)(r % g.N), a = (int)(r / g.N);
-    const int beta = (int)(c % g.N), b = (int)(c / g.N);
-    const int64_t ch = ((int64_t)beta * g.N + alpha) * g.Z + z;
-    vol[e] = X[ch * g.plane + (int64_t)b * g.Pa + a];
-  }
+       e += (int64_t)gridDim.x * blockDim.x)
+    vol[e] = X[phase_index(g, e)];
 }
 
-// Sub-aperture images, LFIMG(u:N:end, v:N:end) for every view u + N*v: lfs[view][b*Li + a].
-__global__ void k_extract_views(const float* __restrict__ lf, Geo g, float* __restrict__ lfs) {
+// Sub-aperture images, LFIMG(u:N:end, v:N:end) for every view u + N*v:
+// lfs[view * view_stride + off + b*Li + a].
+__global__ void k_extract_views(const float* __restrict__ lf, PatchGeo g, float* __restrict__ lfs,
+                                int64_t view_stride, int64_t off) {
   const int64_t n = g.Xr * g.Xc;
-  const int64_t LL = (int64_t)g.Li * g.Lj;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = e % g.Xr, c = e / g.Xr;
     const int u = (int)(r % g.N), a = (int)(r / g.N);
     const int v = (int)(c % g.N), b = (int)(c / g.N);
-    lfs[(int64_t)(u + g.N * v) * LL + (int64_t)b * g.Li + a] = lf[e];
+    lfs[(int64_t)(u + g.N * v) * view_stride + off + (int64_t)b * g.Li + a] = lf[e];
   }
 }
 
@@ -152,19 +147,6 @@ int grid_for(int64_t n, int threads = 256) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
 }
 
-Geo geo_of(const Solver* s) {
-  return Geo{s->N, s->Z, s->Li, s->Lj, s->lay_Pa, s->lay_plane, s->Xr, s->Xc};
-}
-
-void use_layout(Solver* s, int precision) {
-  if (precision == MLF_PREC_FP32) {
-    s->lay_Pa = s->Pa;
-    s->lay_plane = s->plane;
-  } else {
-    s->lay_Pa = s->Li;
-    s->lay_plane = s->plane_tc;
-  }
-}
 
 ViewArgs view_args(Solver* s) {
   ViewArgs a{};
@@ -264,14 +246,12 @@ int run_reduce(Solver* s, int view, float* hx_out, bool ratio, cudaStream_t st) 
   return MLF_OK;
 }
 
-// One RL iteration (recon_…_with_filter.m:100-142), stream-ordered.
-int enqueue_iteration(Solver* s, int precision, int64_t* launches, cudaStream_t st) {
+// One RL iteration of the plain FP32 path (recon_…_with_filter.m:100-142), stream-ordered.
+int enqueue_iteration(Solver* s, int64_t* launches, cudaStream_t st) {
   const std::vector<int>& views = s->psf->view_order;
   const int V = (int)views.size();
   int64_t n = 0;
-  if (precision != MLF_PREC_FP32) {
-    MLF_TRY(tc_enqueue_views(s, precision, &n, st));
-  } else if (V > 0) {
+  if (V > 0) {
     MLF_TRY(run_view(s, MODE_FWD, views[0], views[0], 0.f, true, st));
     MLF_TRY(run_reduce(s, views[0], nullptr, true, st));
     n += 2;
@@ -287,8 +267,8 @@ int enqueue_iteration(Solver* s, int precision, int64_t* launches, cudaStream_t 
       }
     }
   }
-  MLF_TRY(filter_run(s, st));
-  n += 3;
+  MLF_TRY(filter_run_geo(s, solver_geo(s), s->X.as<float>(), st));
+  n += 5;
   if (launches) *launches += n;
   return MLF_OK;
 }
@@ -310,10 +290,64 @@ size_t Psf::bytes() const { return wf.bytes + wb.bytes + tc_psf_bytes(this); }
 
 bool view_taps_supported(int T) { return T >= 3 && T <= 17 && (T % 2) == 1; }
 
+PatchGeo solver_geo(const Solver* s) {
+  return PatchGeo{s->N, s->Z, s->Z, 0, s->Li, s->Lj, s->Pa, s->plane, s->Xr, s->Xc};
+}
+
+int launch_extract_views(const float* d_lf, const PatchGeo& g, float* lfs, int64_t view_stride, int64_t off,
+                         cudaStream_t st) {
+  k_extract_views<<<grid_for(g.Xr * g.Xc), 256, 0, st>>>(d_lf, g, lfs, view_stride, off);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+int launch_to_phase(const float* d_vol, const PatchGeo& g, float* X, cudaStream_t st) {
+  k_to_phase<<<grid_for(g.Xr * g.Xc * g.Z), 256, 0, st>>>(d_vol, g, X);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st) {
+  k_from_phase<<<grid_for(g.Xr * g.Xc * g.Z), 256, 0, st>>>(X, g, d_vol);
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+int launch_init_flat(const float* d_lf, const PatchGeo& g, float* X, double* scratch, cudaStream_t st) {
+  const int nb = 256;
+  k_sum_partial<<<nb, 256, 0, st>>>(d_lf, g.Xr * g.Xc, scratch);
+  k_init_flat<<<grid_for((int64_t)g.N * g.N * g.Zch * g.Li * g.Lj), 256, 0, st>>>(
+      X, g, scratch, nb, 1.0 / ((double)g.Xr * g.Xc * g.Z));
+  MLF_CUDA(cudaGetLastError());
+  return MLF_OK;
+}
+
+// Weights of a plane range [z0, z0+nz) of the PSF: recon_…_with_filter.m:30-38 applied to
+// sum over those planes of Hps(:,:,u,v,z) (per-plane normalisation makes a plane subset
+// of the PSF a PSF of its own).
+std::vector<double> psf_range_weights(const Psf* p, int z0, int nz) {
+  const int V = p->N * p->N;
+  std::vector<double> w(V, 0.0);
+  for (int v = 0; v < V; ++v)
+    for (int z = z0; z < z0 + nz; ++z) w[v] += p->wsum_vz[(size_t)v * p->Z + z];
+  for (double& x : w)
+    if (std::isnan(x)) x = 0.0;
+  double tot = 0.0;
+  for (double x : w) tot += x;
+  for (double& x : w) x = x / tot;
+  double mn = w[0];
+  for (double x : w) mn = (x < mn || std::isnan(mn)) ? x : mn;
+  for (double& x : w) x = x - mn;
+  double mx = w[0];
+  for (double x : w) mx = (x > mx || std::isnan(mx)) ? x : mx;
+  for (double& x : w) x = x / mx;
+  for (double& x : w)
+    if (x < 0.2) x = 0.0;
+  for (double& x : w) x = x * 0.3;
+  return w;
+}
+
 int solver_init(Solver* s) {
   Psf* p = s->psf;
   s->N = p->N;
-  s->Z = p->Z;
+  if (!s->lite) s->Z = p->Z;
   s->q = p->q;
   s->T = p->T;
   s->nch = p->nch;
@@ -324,6 +358,12 @@ int solver_init(Solver* s) {
                                          " not in {3,5,...,17} (K0 up to 255 at N = 15)");
   s->Pa = round_up(s->Li, 4);
   s->plane = (int64_t)s->Lj * s->Pa;
+  if (s->lite) {
+    // batch member: geometry, filter plan and filter scratch only
+    MLF_TRY(s->Xtmp.alloc((size_t)s->Xr * s->Xc * s->Z * sizeof(float), "filter scratch"));
+    MLF_TRY(s->red.alloc(4096 * sizeof(double), "reduction scratch"));
+    return filter_init(s);
+  }
   s->tilesA = ceil_div(s->Li, 4);
   s->tilesB = ceil_div(s->Lj, 8);
   s->tps = s->tilesA * s->tilesB;
@@ -375,10 +415,7 @@ int solver_init(Solver* s) {
   const int64_t max_blocks = (s->nch + s->slots - 1) / s->slots;
   s->grid = (int)std::min<int64_t>(max_blocks, (int64_t)nsm * per_sm);
 
-  s->plane_tc = (int64_t)round_up(s->Li * s->Lj, 32);
-  s->lay_Pa = s->Pa;
-  s->lay_plane = s->plane;
-  const int64_t vol = s->nch * std::max(s->plane, s->plane_tc);
+  const int64_t vol = s->nch * s->plane;
   const int64_t LL = (int64_t)s->Li * s->Lj;
   MLF_TRY(s->X.alloc(vol * sizeof(float), "volume"));
   MLF_TRY(s->Xtmp.alloc(vol * sizeof(float), "scratch volume"));
@@ -396,11 +433,11 @@ int solver_init(Solver* s) {
 
 int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const float* d_warm,
                float* d_out, mlf_stats* stats, cudaStream_t st) {
-  use_layout(s, precision);
-  if (precision != MLF_PREC_FP32) MLF_TRY(tc_solver_prepare(s, st));
-  const Geo g = geo_of(s);
-  const int64_t n_img = s->Xr * s->Xc;
-  const int64_t n_vol = n_img * s->Z;
+  if (precision != MLF_PREC_FP32) {
+    MLF_TRY(tc_solver_prepare(s, st));
+    return tc_run(s->tc, {s}, {d_lf}, {d_warm}, {d_out}, max_iter, precision, stats, s, st);
+  }
+  const PatchGeo g = solver_geo(s);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (stats) {
     MLF_CUDA(cudaEventCreate(&e0));
@@ -410,24 +447,18 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
   int64_t launches = 0;
   s->timing = stats != nullptr;
   s->tev_used = 0;
-  k_extract_views<<<grid_for(n_img), 256, 0, st>>>(d_lf, g, s->lfs.as<float>());
+  MLF_TRY(launch_extract_views(d_lf, g, s->lfs.as<float>(), (int64_t)s->Li * s->Lj, 0, st));
   ++launches;
   if (d_warm) {
-    k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_warm, g, s->X.as<float>());
+    MLF_TRY(launch_to_phase(d_warm, g, s->X.as<float>(), st));
     ++launches;
   } else {
-    const int nb = 256;
-    k_sum_partial<<<nb, 256, 0, st>>>(d_lf, n_img, s->red.as<double>());
-    k_init_flat<<<grid_for(s->nch * s->Li * s->Lj), 256, 0, st>>>(
-        s->X.as<float>(), s->Li, s->Lj, s->lay_Pa, s->lay_plane, s->nch, s->red.as<double>(), nb,
-        1.0 / (double)n_vol);
+    MLF_TRY(launch_init_flat(d_lf, g, s->X.as<float>(), s->red.as<double>(), st));
     launches += 2;
   }
-  MLF_CUDA(cudaGetLastError());
-  for (int it = 0; it < max_iter; ++it) MLF_TRY(enqueue_iteration(s, precision, &launches, st));
-  k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->X.as<float>(), g, d_out);
+  for (int it = 0; it < max_iter; ++it) MLF_TRY(enqueue_iteration(s, &launches, st));
+  MLF_TRY(launch_from_phase(s->X.as<float>(), g, d_out, st));
   ++launches;
-  MLF_CUDA(cudaGetLastError());
   if (stats) {
     MLF_CUDA(cudaEventRecord(e1, st));
     MLF_CUDA(cudaEventSynchronize(e1));
@@ -448,7 +479,6 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     stats->view_kernel_ms = vk;
     stats->view_kernel_launches = s->tev_used / 2;
     stats->kernel_launches = launches;
-    if (precision != MLF_PREC_FP32) MLF_TRY(tc_check_error(s));
   }
   s->timing = false;
   s->tev_used = 0;
@@ -456,11 +486,7 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
 }
 
 int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaStream_t st) {
-  use_layout(s, MLF_PREC_FP32);
-  const Geo g = geo_of(s);
-  const int64_t n_vol = s->Xr * s->Xc * s->Z;
-  k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->Xtmp.as<float>());
-  MLF_CUDA(cudaGetLastError());
+  MLF_TRY(launch_to_phase(d_vol, solver_geo(s), s->Xtmp.as<float>(), st));
   ViewArgs a = view_args(s);
   a.X = s->Xtmp.as<float>();
   a.u = u; a.v = v; a.w = 0.f; a.do_fwd = 1;
@@ -472,18 +498,11 @@ int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaS
 
 int forward_view_prec(Solver* s, const float* d_vol, int u, int v, int precision, float* d_hx, cudaStream_t st) {
   if (precision == MLF_PREC_FP32) return forward_view(s, d_vol, u, v, d_hx, st);
-  use_layout(s, precision);
   MLF_TRY(tc_solver_prepare(s, st));
-  const Geo g = geo_of(s);
-  const int64_t n_vol = s->Xr * s->Xc * s->Z;
-  k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->X.as<float>());
-  MLF_CUDA(cudaGetLastError());
-  return tc_forward_view(s, precision, u + s->N * v, d_hx, st);
+  return tc_forward_view(s, precision, d_vol, u + s->N * v, d_hx, st);
 }
 
 int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cudaStream_t st) {
-  use_layout(s, MLF_PREC_FP32);
-  const Geo g = geo_of(s);
   const int LL = s->Li * s->Lj;
   MLF_CUDA(cudaMemsetAsync(s->rpad.p, 0, s->rpad.bytes, st));
   k_fill_rpad<<<ceil_div(LL, 256), 256, 0, st>>>(d_proj, s->Li, s->Lj, s->rpad.as<float>(), s->RP, s->q + 1);
@@ -494,44 +513,30 @@ int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cu
   a.wb = wb_of(s, u + s->N * v);
   a.wf = wf_of(s, u + s->N * v);
   MLF_TRY(launch_view_kernel(s->T, MODE_BWDC, a, s->grid, s->threads, s->smem, st));
-  const int64_t n_vol = s->Xr * s->Xc * s->Z;
-  k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->Xtmp.as<float>(), g, d_out);
-  MLF_CUDA(cudaGetLastError());
-  return MLF_OK;
+  return launch_from_phase(s->Xtmp.as<float>(), solver_geo(s), d_out, st);
 }
 
 int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, double w, int precision,
                  cudaStream_t st) {
-  use_layout(s, precision);
-  if (precision != MLF_PREC_FP32) MLF_TRY(tc_solver_prepare(s, st));
-  const Geo g = geo_of(s);
-  const int64_t n_img = s->Xr * s->Xc, n_vol = n_img * s->Z;
   const int view = u + s->N * v;
-  k_extract_views<<<grid_for(n_img), 256, 0, st>>>(d_lf, g, s->lfs.as<float>());
-  k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->X.as<float>());
-  MLF_CUDA(cudaGetLastError());
   if (precision != MLF_PREC_FP32) {
-    MLF_TRY(tc_view_step(s, precision, view, (float)w, st));
-  } else {
-    MLF_TRY(run_view(s, MODE_FWD, view, view, 0.f, true, st));
-    MLF_TRY(run_reduce(s, view, nullptr, true, st));
-    MLF_TRY(run_view(s, MODE_STEP, view, -1, (float)w, false, st));
+    MLF_TRY(tc_solver_prepare(s, st));
+    return tc_view_step(s, precision, d_lf, d_vol, view, (float)w, st);
   }
-  k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->X.as<float>(), g, d_vol);
-  MLF_CUDA(cudaGetLastError());
-  return MLF_OK;
+  const PatchGeo g = solver_geo(s);
+  MLF_TRY(launch_extract_views(d_lf, g, s->lfs.as<float>(), (int64_t)s->Li * s->Lj, 0, st));
+  MLF_TRY(launch_to_phase(d_vol, g, s->X.as<float>(), st));
+  MLF_TRY(run_view(s, MODE_FWD, view, view, 0.f, true, st));
+  MLF_TRY(run_reduce(s, view, nullptr, true, st));
+  MLF_TRY(run_view(s, MODE_STEP, view, -1, (float)w, false, st));
+  return launch_from_phase(s->X.as<float>(), g, d_vol, st);
 }
 
 int sample_filter(Solver* s, float* d_vol, cudaStream_t st) {
-  use_layout(s, MLF_PREC_FP32);
-  const Geo g = geo_of(s);
-  const int64_t n_vol = s->Xr * s->Xc * s->Z;
-  k_to_phase<<<grid_for(n_vol), 256, 0, st>>>(d_vol, g, s->X.as<float>());
-  MLF_CUDA(cudaGetLastError());
-  MLF_TRY(filter_run(s, st));
-  k_from_phase<<<grid_for(n_vol), 256, 0, st>>>(s->X.as<float>(), g, d_vol);
-  MLF_CUDA(cudaGetLastError());
-  return MLF_OK;
+  const PatchGeo g = solver_geo(s);
+  MLF_TRY(launch_to_phase(d_vol, g, s->X.as<float>(), st));
+  MLF_TRY(filter_run_geo(s, g, s->X.as<float>(), st));
+  return launch_from_phase(s->X.as<float>(), g, d_vol, st);
 }
 
 // ---------------------------------------------------------------- dispatch per T

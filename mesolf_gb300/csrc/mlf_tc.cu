@@ -70,8 +70,10 @@ struct TcBwdArgs {
   bf16* xb_hi;
   bf16* xb_lo;
   int* err;
-  float w;
-  int Li, LL, CHP, nch, KB, brow0;  // brow0 = view * CHP (row of this view in Wb')
+  const int* tile_patch;  // patch of each position tile
+  const int* pinfo;       // per patch: Li, Lj, LL, pos0, z0, nz, -, -
+  const float* wrow;      // per patch: weight of the current view (0: view inactive for it)
+  int CHP, nch, KB, brow0, Zch;  // brow0 = view * CHP (row of this view in Wb'); Zch = PSF planes
   int use_alo;                      // add ARl * Wbh to C (activation split)
   int use_blo;                      // add ARh * Wbl to C and A1 * Wbl to D (tap split)
   int write_lo;                     // also emit the lo half of Xb
@@ -265,7 +267,11 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
         break;
       }
       const int pos = m0 + row;
-      const bool pos_ok = pos < a.LL;
+      const int pp = __ldg(a.tile_patch + (t % mtiles));
+      const int* pi = a.pinfo + 8 * pp;
+      const bool pos_ok = pos - __ldg(pi + 3) < __ldg(pi + 2);
+      const int pz0 = __ldg(pi + 4), pnz = __ldg(pi + 5);
+      const float wv = __ldg(a.wrow + pp);
       const uint32_t tC = tmem_base + buf * 256 + lane_off, tD = tC + 128;
 #pragma unroll
       for (int cc = 0; cc < 2; ++cc) {
@@ -279,11 +285,12 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
         for (int j = 0; j < 16; ++j) {
           float* xp = xh + ((sub * 2 + cc) * 16 + j) * BM + row;
           float xn = 0.f;
-          if (pos_ok && chb + j < a.nch) {
+          const int zr = (chb + j) % a.Zch - pz0;
+          if (pos_ok && chb + j < a.nch && zr >= 0 && zr < pnz) {
             const float xo = *xp;
             float xc = __fdividef(xo * cv[j], dv[j]);      // :130  X .* C ./ D
             if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;       // :132-134
-            xn = xc * a.w + (1.f - a.w) * xo;              // :136
+            xn = xc * wv + (1.f - wv) * xo;                // :136
             if (xn < 0.f) xn = 0.f;                        // :137
             *xp = xn;
           }
@@ -506,20 +513,25 @@ __global__ void k_tc_build_wft(const float* __restrict__ wf, int N, int T, int64
   }
 }
 
-// im2col of the ratio image (or of ones when R == nullptr) over the (T+2)^2 window.
-__global__ void k_tc_im2col(const float* __restrict__ R, int Li, int Lj, int LL, int MP, int T, int KB,
-                            bf16* __restrict__ hi, bf16* __restrict__ lo) {
+// im2col of the ratio images (or of ones when R == nullptr) over the (T+2)^2 window, for
+// all patches: row = global position, R indexed by global position.
+__global__ void k_tc_im2col(const float* __restrict__ R, const int* __restrict__ tile_patch,
+                            const int* __restrict__ pinfo, int MP, int T, int KB, bf16* __restrict__ hi,
+                            bf16* __restrict__ lo) {
   const int T2 = T + 2, q = (T - 1) / 2;
   const int64_t total = (int64_t)MP * KB;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(e % KB);
     const int pos = (int)(e / KB);
+    const int* pi = pinfo + 8 * tile_patch[pos / BM];
+    const int Li = pi[0], Lj = pi[1], LL = pi[2], pos0 = pi[3];
+    const int local = pos - pos0;
     float val = 0.f;
-    if (pos < LL && k < T2 * T2) {
-      const int b = pos / Li, a = pos - (pos / Li) * Li;
+    if (local < LL && k < T2 * T2) {
+      const int b = local / Li, a = local - (local / Li) * Li;
       const int j = b + k / T2 - q - 1, i = a + k % T2 - q - 1;
-      if (j >= 0 && j < Lj && i >= 0 && i < Li) val = R ? R[j * Li + i] : 1.f;
+      if (j >= 0 && j < Lj && i >= 0 && i < Li) val = R ? R[pos0 + j * Li + i] : 1.f;
     }
     bf16 h16, l16;
     split_bf16(val, h16, l16);
@@ -528,17 +540,15 @@ __global__ void k_tc_im2col(const float* __restrict__ R, int Li, int Lj, int LL,
   }
 }
 
-// Phase-major FP32 volume -> Xb[p][ch] BF16 hi/lo (32x32 tiles through shared memory).
-__global__ void k_tc_pack_x(const float* __restrict__ X, int Li, int Pa, int LL, int64_t plane, int64_t nch,
-                            int CHP, int MP, bf16* __restrict__ hi, bf16* __restrict__ lo) {
+// X[ch][p] (FP32, [nch][MP]) -> Xb[p][ch] BF16 hi/lo (32x32 tiles through shared memory).
+__global__ void k_tc_pack_x(const float* __restrict__ X, int64_t nch, int CHP, int MP, bf16* __restrict__ hi,
+                            bf16* __restrict__ lo) {
   __shared__ float t[32][33];
   const int p0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
   for (int r = ty; r < 32; r += 8) {
     const int ch = c0 + r, p = p0 + tx;
-    float v = 0.f;
-    if (ch < nch && p < LL) v = X[(int64_t)ch * plane + (int64_t)(p / Li) * Pa + p % Li];
-    t[r][tx] = v;
+    t[r][tx] = (ch < nch && p < MP) ? X[(int64_t)ch * MP + p] : 0.f;
   }
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
@@ -552,33 +562,38 @@ __global__ void k_tc_pack_x(const float* __restrict__ X, int Li, int Pa, int LL,
   }
 }
 
-// HX[j][i] = sum_split sum_{db,da} Y[split][(j+db-q)*Li + (i+da-q)][db*T+da]; ratio -> R.
-// One warp per output: lanes stride over the taps, then a fixed shuffle tree (deterministic).
-__global__ void k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, int Li, int Lj,
-                                  int T, const float* __restrict__ lfsub, float* __restrict__ hx_out,
+// HX[j][i] = sum_split sum_{db,da} Y[split][(j+db-q)*Li + (i+da-q)][db*T+da] for every valid
+// position of every patch; ratio R = LF_sub ./ HX (non-finite -> 0).  One warp per output:
+// lanes stride over the taps, then a fixed shuffle tree (deterministic).
+__global__ void k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, int T,
+                                  const int* __restrict__ tile_patch, const int* __restrict__ pinfo,
+                                  const float* __restrict__ lfsub, float* __restrict__ hx_out,
                                   float* __restrict__ rimg) {
-  const int LL = Li * Lj;
-  const int i0 = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int pos = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (i0 >= LL) return;
+  if (pos >= MP) return;
+  const int* pi = pinfo + 8 * tile_patch[pos / BM];
+  const int Li = pi[0], Lj = pi[1], LL = pi[2], pos0 = pi[3];
+  const int local = pos - pos0;
+  if (local >= LL) return;
   const int q = (T - 1) / 2;
-  const int j = i0 / Li, i = i0 - (i0 / Li) * Li;
+  const int j = local / Li, i = local - (local / Li) * Li;
   float s = 0.f;
   for (int t = lane; t < T * T; t += 32) {
     const int db = t / T, da = t - (t / T) * T;
     const int b = j + db - q, a = i + da - q;
     if (b < 0 || b >= Lj || a < 0 || a >= Li) continue;
-    const int64_t p = (int64_t)b * Li + a;
+    const int64_t p = (int64_t)pos0 + (int64_t)b * Li + a;
     for (int sp = 0; sp < splits; ++sp) s += __ldg(ypart + ((int64_t)sp * MP + p) * NB + t);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) {
-    if (hx_out) hx_out[i0] = s;
+    if (hx_out) hx_out[pos] = s;
     if (rimg) {
-      float r = lfsub[i0] / s;
+      float r = lfsub[pos] / s;
       if (!isfinite(r)) r = 0.f;
-      rimg[i0] = r;
+      rimg[pos] = r;
     }
   }
 }
@@ -622,11 +637,16 @@ struct TcPsfState {
   CUtensorMap mBh, mBl, mFh, mFl;
 };
 
+// Work set of P patches sharing one PSF: positions of all patches concatenated (each
+// patch padded to whole 128-position tiles), the FP32 volume X[ch][position] of every
+// patch, the BF16 operand buffers, the union view order and per-patch view weights.
 struct TcSolverState {
-  int MP = 0, splits = 1, ks_per_split = 0, KSF = 0, nsm = 0;
-  DevBuf ar_hi, ar_lo, a1, xb_hi, xb_lo, ypart, rimg, err;
-  CUtensorMap mARh, mARl, mA1, mXh, mXl;
-  CUtensorMap mXv;  // the FP32 volume in the tensor-core layout [nch][plane], box 128 x 128
+  int P = 0, MP = 0, Zch = 0, splits = 1, ks_per_split = 0, KSF = 0, nsm = 0;
+  std::vector<int> pos0, Li, Lj, LL, z0, nz;
+  std::vector<int> views;   // union of the patches' active views, spiral order
+  std::vector<float> wtab;  // [views][P]
+  DevBuf X, lfs, rimg, tile_patch, pinfo, wtab_dev, wscratch, ar_hi, ar_lo, a1, xb_hi, xb_lo, ypart, err;
+  CUtensorMap mARh, mARl, mA1, mXh, mXl, mXv;
 };
 
 void tc_psf_free(TcPsfState* t) { delete t; }
@@ -686,33 +706,86 @@ size_t tc_psf_bytes(const Psf* p) {
   return p->tc->wbx_hi.bytes + p->tc->wbx_lo.bytes + p->tc->wft_hi.bytes + p->tc->wft_lo.bytes;
 }
 
-int tc_solver_prepare(Solver* s, cudaStream_t st) {
-  MLF_TRY(tc_psf_prepare(s->psf, st));
-  if (s->tc) return MLF_OK;
-  const TcPsfState* tp = s->psf->tc;
+size_t tc_work_bytes(const TcSolverState* t) {
+  if (!t) return 0;
+  return t->X.bytes + t->lfs.bytes + t->rimg.bytes + t->tile_patch.bytes + t->pinfo.bytes + t->wtab_dev.bytes +
+         t->wscratch.bytes + t->ar_hi.bytes + t->ar_lo.bytes + t->a1.bytes + t->xb_hi.bytes + t->xb_lo.bytes +
+         t->ypart.bytes + t->err.bytes;
+}
+
+size_t tc_solver_bytes(const Solver* s) { return tc_work_bytes(s->tc); }
+
+int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState** out, cudaStream_t st) {
+  MLF_TRY(tc_psf_prepare(psf, st));
+  const TcPsfState* tp = psf->tc;
   std::unique_ptr<TcSolverState> t(new TcSolverState());
-  const int LL = s->Li * s->Lj;
-  t->MP = rup(LL, BM);
+  t->P = (int)members.size();
+  t->Zch = psf->Z;
+  int off = 0;
+  std::vector<int> info(8 * t->P, 0), tiles;
+  for (int p = 0; p < t->P; ++p) {
+    const Solver* m = members[p];
+    t->pos0.push_back(off);
+    t->Li.push_back(m->Li);
+    t->Lj.push_back(m->Lj);
+    t->LL.push_back(m->Li * m->Lj);
+    t->z0.push_back(m->z0);
+    t->nz.push_back(m->Z);
+    const int* v = &info[8 * p];
+    (void)v;
+    info[8 * p + 0] = m->Li;
+    info[8 * p + 1] = m->Lj;
+    info[8 * p + 2] = m->Li * m->Lj;
+    info[8 * p + 3] = off;
+    info[8 * p + 4] = m->z0;
+    info[8 * p + 5] = m->Z;
+    const int padded = rup(m->Li * m->Lj, BM);
+    for (int k = 0; k < padded / BM; ++k) tiles.push_back(p);
+    off += padded;
+  }
+  t->MP = off;
+  // union view order and per-patch weights (plane ranges give per-patch weights)
+  std::vector<std::vector<double>> w(t->P);
+  for (int p = 0; p < t->P; ++p) w[p] = psf_range_weights(psf, t->z0[p], t->nz[p]);
+  for (int view : psf->spiral) {
+    bool any = false;
+    for (int p = 0; p < t->P; ++p) any = any || w[p][view] != 0.0;
+    if (!any) continue;
+    t->views.push_back(view);
+    for (int p = 0; p < t->P; ++p) t->wtab.push_back((float)w[p][view]);
+  }
   t->KSF = tp->CHP / BK;
-  int nsm = 0;
-  MLF_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device));
+  MLF_CUDA(cudaDeviceGetAttribute(&t->nsm, cudaDevAttrMultiProcessorCount, members[0]->device));
   const int mt = t->MP / BM;
-  t->nsm = nsm;
-  t->splits = std::max(1, std::min(t->KSF, nsm / std::max(1, mt)));
+  t->splits = std::max(1, std::min(t->KSF, t->nsm / std::max(1, mt)));
   t->ks_per_split = (t->KSF + t->splits - 1) / t->splits;
   t->splits = (t->KSF + t->ks_per_split - 1) / t->ks_per_split;
+  const int64_t nch = psf->nch;
+  MLF_TRY(t->X.alloc((size_t)nch * t->MP * 4, "tc volume (FP32)"));
+  MLF_TRY(t->lfs.alloc((size_t)psf->N * psf->N * t->MP * 4, "tc sub-aperture images"));
+  MLF_TRY(t->rimg.alloc((size_t)t->MP * 4, "tc ratio image"));
+  MLF_TRY(t->tile_patch.alloc(tiles.size() * sizeof(int), "tc tables"));
+  MLF_TRY(t->pinfo.alloc(info.size() * sizeof(int), "tc tables"));
+  MLF_TRY(t->wtab_dev.alloc(std::max<size_t>(1, t->wtab.size()) * sizeof(float), "tc weights"));
+  MLF_TRY(t->wscratch.alloc(std::max(1, t->P) * sizeof(float), "tc weights"));
   MLF_TRY(t->ar_hi.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->ar_lo.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->a1.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
-  MLF_TRY(t->xb_hi.alloc((size_t)t->MP * tp->CHP * 2, "tc volume"));
-  MLF_TRY(t->xb_lo.alloc((size_t)t->MP * tp->CHP * 2, "tc volume"));
+  MLF_TRY(t->xb_hi.alloc((size_t)t->MP * tp->CHP * 2, "tc volume (BF16)"));
+  MLF_TRY(t->xb_lo.alloc((size_t)t->MP * tp->CHP * 2, "tc volume (BF16)"));
   MLF_TRY(t->ypart.alloc((size_t)t->splits * t->MP * tp->NB * 4, "tc forward partials"));
-  MLF_TRY(t->rimg.alloc((size_t)LL * 4, "tc ratio image"));
   MLF_TRY(t->err.alloc(sizeof(int), "tc error flag"));
+  MLF_CUDA(cudaMemcpy(t->tile_patch.p, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice));
+  MLF_CUDA(cudaMemcpy(t->pinfo.p, info.data(), info.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (!t->wtab.empty())
+    MLF_CUDA(cudaMemcpy(t->wtab_dev.p, t->wtab.data(), t->wtab.size() * sizeof(float), cudaMemcpyHostToDevice));
+  MLF_CUDA(cudaMemsetAsync(t->X.p, 0, t->X.bytes, st));
+  MLF_CUDA(cudaMemsetAsync(t->lfs.p, 0, t->lfs.bytes, st));
   MLF_CUDA(cudaMemsetAsync(t->xb_hi.p, 0, t->xb_hi.bytes, st));
   MLF_CUDA(cudaMemsetAsync(t->xb_lo.p, 0, t->xb_lo.bytes, st));
   MLF_CUDA(cudaMemsetAsync(t->err.p, 0, sizeof(int), st));
-  k_tc_im2col<<<1024, 256, 0, st>>>(nullptr, s->Li, s->Lj, LL, t->MP, s->T, tp->KB, t->a1.as<bf16>(), nullptr);
+  k_tc_im2col<<<2048, 256, 0, st>>>(nullptr, t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP, psf->T, tp->KB,
+                                    t->a1.as<bf16>(), nullptr);
   MLF_CUDA(cudaGetLastError());
   MLF_TRY(make_map(&t->mARh, t->ar_hi.p, t->MP, tp->KB, BM));
   MLF_TRY(make_map(&t->mARl, t->ar_lo.p, t->MP, tp->KB, BM));
@@ -721,24 +794,22 @@ int tc_solver_prepare(Solver* s, cudaStream_t st) {
   MLF_TRY(make_map(&t->mXl, t->xb_lo.p, t->MP, tp->CHP, BM));
   {
     MLF_TRY(get_encoder());
-    cuuint64_t dims[2] = {(cuuint64_t)s->plane_tc, (cuuint64_t)s->nch};
-    cuuint64_t strides[1] = {(cuuint64_t)s->plane_tc * 4};
+    cuuint64_t dims[2] = {(cuuint64_t)t->MP, (cuuint64_t)nch};
+    cuuint64_t strides[1] = {(cuuint64_t)t->MP * 4};
     cuuint32_t box[2] = {BM, BWD_BN / 2};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = g_encode(&t->mXv, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->X.p, dims, strides, box, es,
+    CUresult r = g_encode(&t->mXv, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, t->X.p, dims, strides, box, es,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(MLF_ERR_CUDA, "cuTensorMapEncodeTiled (volume) failed: " + std::to_string((int)r));
   }
-  s->tc = t.release();
+  *out = t.release();
   return MLF_OK;
 }
 
-size_t tc_solver_bytes(const Solver* s) {
-  if (!s->tc) return 0;
-  const TcSolverState* t = s->tc;
-  return t->ar_hi.bytes + t->ar_lo.bytes + t->a1.bytes + t->xb_hi.bytes + t->xb_lo.bytes + t->ypart.bytes +
-         t->rimg.bytes + t->err.bytes;
+int tc_solver_prepare(Solver* s, cudaStream_t st) {
+  if (s->tc) return MLF_OK;
+  return tc_work_create(s->psf, {s}, &s->tc, st);
 }
 
 namespace {
@@ -750,9 +821,12 @@ void splits_of(int precision, int* alo, int* blo) {
 }
 bool act_split(int precision) { return precision == MLF_PREC_BF16X2 || precision == MLF_PREC_BF16X3; }
 
-int tc_fwd_launch(Solver* s, int precision, int view, cudaStream_t st) {
-  const TcPsfState* tp = s->psf->tc;
-  TcSolverState* t = s->tc;
+PatchGeo work_geo(const TcSolverState* t, const Solver* m, int p) {
+  return PatchGeo{m->N, t->nz[p], t->Zch, t->z0[p], t->Li[p], t->Lj[p], t->Li[p], (int64_t)t->MP, m->Xr, m->Xc};
+}
+
+int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cudaStream_t st) {
+  const TcPsfState* tp = psf->tc;
   int alo, blo;
   splits_of(precision, &alo, &blo);
   TcFwdArgs a{};
@@ -775,40 +849,34 @@ int tc_fwd_launch(Solver* s, int precision, int view, cudaStream_t st) {
   return MLF_OK;
 }
 
-int tc_col2im(Solver* s, int view, bool ratio, float* hx_out, cudaStream_t st) {
-  const TcPsfState* tp = s->psf->tc;
-  TcSolverState* t = s->tc;
-  const int LL = s->Li * s->Lj;
-  const float* lfsub = s->lfs.as<float>() + (int64_t)view * LL;
-  k_tc_col2im_ratio<<<(LL + 7) / 8, 256, 0, st>>>(t->ypart.as<float>(), t->splits, t->MP, tp->NB, s->Li,
-                                                      s->Lj, s->T, lfsub, hx_out,
-                                                      ratio ? t->rimg.as<float>() : nullptr);
+int tc_col2im(const Psf* psf, TcSolverState* t, int view, bool ratio, float* hx_out, cudaStream_t st) {
+  k_tc_col2im_ratio<<<(t->MP + 7) / 8, 256, 0, st>>>(
+      t->ypart.as<float>(), t->splits, t->MP, psf->tc->NB, psf->T, t->tile_patch.as<int>(), t->pinfo.as<int>(),
+      t->lfs.as<float>() + (int64_t)view * t->MP, hx_out, ratio ? t->rimg.as<float>() : nullptr);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
 }
 
-int tc_im2col_ratio(Solver* s, int precision, cudaStream_t st) {
-  const TcPsfState* tp = s->psf->tc;
-  TcSolverState* t = s->tc;
-  const int LL = s->Li * s->Lj;
-  k_tc_im2col<<<1024, 256, 0, st>>>(t->rimg.as<float>(), s->Li, s->Lj, LL, t->MP, s->T, tp->KB,
-                                    t->ar_hi.as<bf16>(), act_split(precision) ? t->ar_lo.as<bf16>() : nullptr);
+int tc_im2col_ratio(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st) {
+  k_tc_im2col<<<2048, 256, 0, st>>>(t->rimg.as<float>(), t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP,
+                                    psf->T, psf->tc->KB, t->ar_hi.as<bf16>(),
+                                    act_split(precision) ? t->ar_lo.as<bf16>() : nullptr);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
 }
 
-int tc_bwd_launch(Solver* s, int precision, int view, float w, cudaStream_t st) {
-  const TcPsfState* tp = s->psf->tc;
-  TcSolverState* t = s->tc;
+int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, const float* wrow, cudaStream_t st) {
+  const TcPsfState* tp = psf->tc;
   int alo, blo;
   splits_of(precision, &alo, &blo);
   TcBwdArgs a{};
   a.xb_hi = t->xb_hi.as<bf16>();
   a.xb_lo = t->xb_lo.as<bf16>();
   a.err = t->err.as<int>();
-  a.w = w;
-  a.Li = s->Li; a.LL = s->Li * s->Lj;
-  a.CHP = tp->CHP; a.nch = (int)s->nch; a.KB = tp->KB; a.brow0 = view * tp->CHP;
+  a.tile_patch = t->tile_patch.as<int>();
+  a.pinfo = t->pinfo.as<int>();
+  a.wrow = wrow;
+  a.CHP = tp->CHP; a.nch = (int)psf->nch; a.KB = tp->KB; a.brow0 = view * tp->CHP; a.Zch = t->Zch;
   a.use_alo = alo;
   a.use_blo = blo;
   a.write_lo = alo;
@@ -820,77 +888,142 @@ int tc_bwd_launch(Solver* s, int precision, int view, float w, cudaStream_t st) 
   return MLF_OK;
 }
 
-}  // namespace
-
-int tc_pack_volume(Solver* s, int precision, cudaStream_t st) {
-  TcSolverState* t = s->tc;
-  const TcPsfState* tp = s->psf->tc;
-  const int LL = s->Li * s->Lj;
-  dim3 grid((t->MP + 31) / 32, (tp->CHP + 31) / 32);
-  k_tc_pack_x<<<grid, dim3(32, 8), 0, st>>>(s->X.as<float>(), s->Li, s->Li, LL, s->plane_tc, s->nch, tp->CHP, t->MP,
-                                            t->xb_hi.as<bf16>(), act_split(precision) ? t->xb_lo.as<bf16>() : nullptr);
+int tc_pack(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st) {
+  dim3 grid((t->MP + 31) / 32, (psf->tc->CHP + 31) / 32);
+  k_tc_pack_x<<<grid, dim3(32, 8), 0, st>>>(t->X.as<float>(), psf->nch, psf->tc->CHP, t->MP, t->xb_hi.as<bf16>(),
+                                            act_split(precision) ? t->xb_lo.as<bf16>() : nullptr);
   MLF_CUDA(cudaGetLastError());
   return MLF_OK;
 }
 
-// One RL iteration on the tensor cores (the view loop); the caller adds the sample filter.
-int tc_enqueue_views(Solver* s, int precision, int64_t* launches, cudaStream_t st) {
-  const std::vector<int>& views = s->psf->view_order;
-  const int V = (int)views.size();
+// The view loop of one iteration over all patches of the work set.
+int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* timer, int64_t* launches,
+                     cudaStream_t st) {
+  const int V = (int)t->views.size();
   if (V == 0) return MLF_OK;
   int64_t n = 0;
-  MLF_TRY(tc_pack_volume(s, precision, st));
-  MLF_TRY(timing_mark(s, st));
-  MLF_TRY(tc_fwd_launch(s, precision, views[0], st));
-  MLF_TRY(timing_mark(s, st));
-  MLF_TRY(tc_col2im(s, views[0], true, nullptr, st));
-  MLF_TRY(tc_im2col_ratio(s, precision, st));
+  MLF_TRY(tc_pack(psf, t, precision, st));
+  MLF_TRY(timing_mark(timer, st));
+  MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[0], st));
+  MLF_TRY(timing_mark(timer, st));
+  MLF_TRY(tc_col2im(psf, t, t->views[0], true, nullptr, st));
+  MLF_TRY(tc_im2col_ratio(psf, t, precision, st));
   n += 4;
   for (int k = 0; k < V; ++k) {
-    const int cur = views[k];
-    MLF_TRY(timing_mark(s, st));
-    MLF_TRY(tc_bwd_launch(s, precision, cur, (float)s->psf->weights[cur], st));
+    MLF_TRY(timing_mark(timer, st));
+    MLF_TRY(tc_bwd_launch(psf, t, precision, t->views[k], t->wtab_dev.as<float>() + (size_t)k * t->P, st));
     ++n;
     if (k + 1 < V) {
-      MLF_TRY(tc_fwd_launch(s, precision, views[k + 1], st));
-      MLF_TRY(timing_mark(s, st));
-      MLF_TRY(tc_col2im(s, views[k + 1], true, nullptr, st));
-      MLF_TRY(tc_im2col_ratio(s, precision, st));
+      MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[k + 1], st));
+      MLF_TRY(timing_mark(timer, st));
+      MLF_TRY(tc_col2im(psf, t, t->views[k + 1], true, nullptr, st));
+      MLF_TRY(tc_im2col_ratio(psf, t, precision, st));
       n += 3;
     } else {
-      MLF_TRY(timing_mark(s, st));
+      MLF_TRY(timing_mark(timer, st));
     }
   }
   if (launches) *launches += n;
   return MLF_OK;
 }
 
-// Forward projection of one view with the tensor cores (parity tests): vol phase-major
-// already in s->X; result HX -> hx_out.
-int tc_forward_view(Solver* s, int precision, int view, float* hx_out, cudaStream_t st) {
-  MLF_TRY(tc_solver_prepare(s, st));
-  MLF_TRY(tc_pack_volume(s, precision, st));
-  MLF_TRY(tc_fwd_launch(s, precision, view, st));
-  return tc_col2im(s, view, false, hx_out, st);
+}  // namespace
+
+int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vector<const float*>& lf,
+           const std::vector<const float*>& warm, const std::vector<float*>& out, int max_iter, int precision,
+           mlf_stats* stats, Solver* timer, cudaStream_t st) {
+  const Psf* psf = members[0]->psf;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (stats) {
+    MLF_CUDA(cudaEventCreate(&e0));
+    MLF_CUDA(cudaEventCreate(&e1));
+    MLF_CUDA(cudaEventRecord(e0, st));
+  }
+  timer->timing = stats != nullptr;
+  timer->tev_used = 0;
+  int64_t launches = 0;
+  for (int p = 0; p < t->P; ++p) {
+    const PatchGeo g = work_geo(t, members[p], p);
+    float* Xp = t->X.as<float>() + t->pos0[p];
+    MLF_TRY(launch_extract_views(lf[p], g, t->lfs.as<float>(), t->MP, t->pos0[p], st));
+    if (warm[p]) {
+      MLF_TRY(launch_to_phase(warm[p], g, Xp, st));
+      launches += 2;
+    } else {
+      MLF_TRY(launch_init_flat(lf[p], g, Xp, members[p]->red.as<double>(), st));
+      launches += 3;
+    }
+  }
+  for (int it = 0; it < max_iter; ++it) {
+    MLF_TRY(tc_enqueue_views(psf, t, precision, timer, &launches, st));
+    for (int p = 0; p < t->P; ++p) {
+      MLF_TRY(filter_run_geo(members[p], work_geo(t, members[p], p), t->X.as<float>() + t->pos0[p], st));
+      launches += 5;
+    }
+  }
+  for (int p = 0; p < t->P; ++p) {
+    MLF_TRY(launch_from_phase(t->X.as<float>() + t->pos0[p], work_geo(t, members[p], p), out[p], st));
+    ++launches;
+  }
+  if (stats) {
+    MLF_CUDA(cudaEventRecord(e1, st));
+    MLF_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    MLF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    stats->n_views = (int)t->views.size();
+    stats->iterations = max_iter;
+    stats->gpu_ms = ms;
+    stats->view_ms = (max_iter > 0 && stats->n_views > 0) ? ms / (max_iter * stats->n_views) : 0.0;
+    double vk = 0.0;
+    for (int k = 0; k + 1 < timer->tev_used; k += 2) {
+      float tt = 0.f;
+      MLF_CUDA(cudaEventElapsedTime(&tt, timer->tev[k], timer->tev[k + 1]));
+      vk += tt;
+    }
+    stats->view_kernel_ms = vk;
+    stats->view_kernel_launches = timer->tev_used / 2;
+    stats->kernel_launches = launches;
+    MLF_TRY(tc_check_error(t));
+  }
+  timer->timing = false;
+  timer->tev_used = 0;
+  return MLF_OK;
 }
 
-// One RL view step on the tensor cores (parity tests): X phase-major in s->X, the
-// sub-aperture images in s->lfs; updates s->X.
-int tc_view_step(Solver* s, int precision, int view, float w, cudaStream_t st) {
-  MLF_TRY(tc_solver_prepare(s, st));
-  MLF_TRY(tc_pack_volume(s, precision, st));
-  MLF_TRY(tc_fwd_launch(s, precision, view, st));
-  MLF_TRY(tc_col2im(s, view, true, nullptr, st));
-  MLF_TRY(tc_im2col_ratio(s, precision, st));
-  return tc_bwd_launch(s, precision, view, w, st);
+// Forward projection of one view with the tensor cores (parity tests), single solver.
+int tc_forward_view(Solver* s, int precision, const float* d_vol, int view, float* hx_out, cudaStream_t st) {
+  TcSolverState* t = s->tc;
+  MLF_TRY(launch_to_phase(d_vol, work_geo(t, s, 0), t->X.as<float>(), st));
+  MLF_TRY(tc_pack(s->psf, t, precision, st));
+  MLF_TRY(tc_fwd_launch(s->psf, t, precision, view, st));
+  return tc_col2im(s->psf, t, view, false, hx_out, st);
 }
 
-int tc_check_error(Solver* s) {
-  if (!s->tc) return MLF_OK;
+// One RL view step on the tensor cores (parity tests), single solver.
+int tc_view_step(Solver* s, int precision, const float* d_lf, float* d_vol, int view, float w, cudaStream_t st) {
+  TcSolverState* t = s->tc;
+  const PatchGeo g = work_geo(t, s, 0);
+  MLF_TRY(launch_extract_views(d_lf, g, t->lfs.as<float>(), t->MP, 0, st));
+  MLF_TRY(launch_to_phase(d_vol, g, t->X.as<float>(), st));
+  MLF_CUDA(cudaMemcpyAsync(t->wscratch.p, &w, sizeof(float), cudaMemcpyHostToDevice, st));
+  MLF_TRY(tc_pack(s->psf, t, precision, st));
+  MLF_TRY(tc_fwd_launch(s->psf, t, precision, view, st));
+  MLF_TRY(tc_col2im(s->psf, t, view, true, nullptr, st));
+  MLF_TRY(tc_im2col_ratio(s->psf, t, precision, st));
+  MLF_TRY(tc_bwd_launch(s->psf, t, precision, view, t->wscratch.as<float>(), st));
+  MLF_TRY(launch_from_phase(t->X.as<float>(), g, d_vol, st));
+  MLF_CUDA(cudaStreamSynchronize(st));
+  return MLF_OK;
+}
+
+int tc_check_error(TcSolverState* t) {
+  if (!t) return MLF_OK;
   int e = 0;
-  MLF_CUDA(cudaMemcpy(&e, s->tc->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  MLF_CUDA(cudaMemcpy(&e, t->err.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (e != 0) {
-    cudaMemset(s->tc->err.p, 0, sizeof(int));
+    cudaMemset(t->err.p, 0, sizeof(int));
     return fail(MLF_ERR_TIMEOUT, "tensor-core kernel wait timed out (code " + std::to_string(e) + ")");
   }
   return MLF_OK;
