@@ -52,6 +52,16 @@ void DevBuf::release() {
   bytes = 0;
 }
 
+int allow_max_dyn_smem(const void* func) {
+  int dev = 0, optin = 0;
+  MLF_CUDA(cudaGetDevice(&dev));
+  MLF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  MLF_CUDA(cudaFuncGetAttributes(&fa, func));
+  MLF_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  return MLF_OK;
+}
+
 bool is_device_ptr(const void* ptr) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {

@@ -67,11 +67,11 @@ k_conv_vec(const float* __restrict__ in, int W, int H, const float* __restrict__
 int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,
                  int64_t kw, int nnum, float* d_out, cudaStream_t st) {
   const size_t smem = sizeof(float) * (size_t)(CV_STRIP + CV_TY - 1) * (CV_TX + kw - 1);
-  MLF_CUDA(cudaFuncSetAttribute(k_conv_vec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MLF_TRY(allow_max_dyn_smem((const void*)k_conv_vec));
   const dim3 grid((unsigned)((W + CV_TX - 1) / CV_TX), (unsigned)((H + CV_TY - 1) / CV_TY), (unsigned)n);
   k_conv_vec<<<grid, dim3(CV_TX, CV_TY), smem, st>>>(d_bitmap, (int)W, (int)H, d_kernels, (int)kw,
                                                      nnum, d_out);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 

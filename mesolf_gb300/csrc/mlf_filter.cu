@@ -324,8 +324,8 @@ int filter_init(Solver* s) {
   MLF_CUDA(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
   if ((int)std::max(smem_r, smem_c) > dev_smem)
     return fail(MLF_ERR_UNSUPPORTED, "image side too large for the sample filter's line buffers");
-  MLF_CUDA(cudaFuncSetAttribute(k_filter_r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-  MLF_CUDA(cudaFuncSetAttribute(k_filter_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+  MLF_TRY(allow_max_dyn_smem((const void*)k_filter_r));
+  MLF_TRY(allow_max_dyn_smem((const void*)k_filter_c));
   return MLF_OK;
 }
 
@@ -359,7 +359,7 @@ int filter_run_geo(Solver* s, const PatchGeo& g, float* X, cudaStream_t st) {
       V, fg, zl, pe, f.cy.as<float>(), wlo_y, nt_y, (int)s->Xc, sout);
   k_filter_scale<<<(Z + 255) / 256, 256, 0, st>>>(sin, gr, sout, gc, zl, nzf, Z, scale);
   k_rephase<<<eg, 256, 0, st>>>(V, scale, g, X);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 

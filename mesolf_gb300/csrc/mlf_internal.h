@@ -22,6 +22,16 @@ void clear_error();
       return ::mlf::fail(MLF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// after a kernel launch: report the launch site with the error
+#define MLF_LAUNCHED()                                                                           \
+  do {                                                                                           \
+    cudaError_t e_ = cudaGetLastError();                                                         \
+    if (e_ != cudaSuccess)                                                                       \
+      return ::mlf::fail(MLF_ERR_CUDA, std::string(__FILE__).substr(std::string(__FILE__).rfind('/') + 1) + \
+                                           ":" + std::to_string(__LINE__) + ": kernel launch: " + \
+                                           cudaGetErrorString(e_));                              \
+  } while (0)
+
 #define MLF_TRY(call)             \
   do {                            \
     int st_ = (call);             \
@@ -43,6 +53,10 @@ struct DevBuf {
 
 // true if ptr is device (or managed) memory usable by kernels on the current device
 bool is_device_ptr(const void* ptr);
+
+// Allow `func` the device's whole opt-in dynamic shared memory (minus its static usage).
+// The attribute is global to the function, so it is never lowered for one caller's size.
+int allow_max_dyn_smem(const void* func);
 
 struct TcPsfState;     // tensor-core operands of a PSF (mlf_tc.cu)
 struct TcSolverState;  // tensor-core work set of one or more patches (mlf_tc.cu)

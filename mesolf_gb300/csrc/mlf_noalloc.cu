@@ -145,15 +145,14 @@ __global__ void k_static_reduce(const float* __restrict__ part, int nparts, int 
 template <int T>
 int run_static(const StaticFwdArgs& a, int nsm, size_t smem, int threads, int max_grid, cudaStream_t st,
                int* grid_out) {
-  if (smem > 48 * 1024)
-    MLF_CUDA(cudaFuncSetAttribute(k_fwd_static<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (smem > 48 * 1024) MLF_TRY(allow_max_dyn_smem((const void*)k_fwd_static<T>));
   int per_sm = 1;
   MLF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fwd_static<T>, threads, smem));
   const int64_t want = (a.nch + a.slots - 1) / a.slots;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>({want, (int64_t)nsm * std::max(1, per_sm),
                                                                   (int64_t)max_grid}));
   k_fwd_static<T><<<grid, threads, smem, st>>>(a);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   *grid_out = grid;
   return MLF_OK;
 }
@@ -217,6 +216,6 @@ extern "C" int mlf_forward_view_static(const mlf_psf* psf_handle, const float* v
     default: return fail(MLF_ERR_UNSUPPORTED, "mlf_forward_view_static: unsupported tap count");
   }
   k_static_reduce<<<(int)((LL + 255) / 256), 256, 0, st>>>(a.part, grid, (int)LL, hx);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }

@@ -186,7 +186,7 @@ int psf_build(Psf* psf, const float* dH, const float* dHt, cudaStream_t st) {
   k_slice_sums<<<dim3(kSumBlocks, Z), kSumThreads, 0, st>>>(dHt, slice, partHt);
   k_inv_sums<<<(Z + 127) / 128, 128, 0, st>>>(partH, kSumBlocks, Z, invH);
   k_inv_sums<<<(Z + 127) / 128, 128, 0, st>>>(partHt, kSumBlocks, Z, invHt);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
 
   const size_t nt = (size_t)N * N * psf->taps_per_view;
   MLF_TRY(psf->wf.alloc(nt * sizeof(float), "psf forward taps"));
@@ -194,7 +194,7 @@ int psf_build(Psf* psf, const float* dH, const float* dHt, cudaStream_t st) {
   k_build_taps<<<2048, 256, 0, st>>>(dH, dHt, invH, invHt, g, psf->wf.as<float>(),
                                      psf->wb.as<float>());
   k_view_sums<<<dim3(N * N, Z), 256, 0, st>>>(dH, invH, g, wsum.as<double>());
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
 
   psf->wsum_vz.assign((size_t)N * N * Z, 0.0);
   MLF_CUDA(cudaMemcpyAsync(psf->wsum_vz.data(), wsum.p, sizeof(double) * N * N * Z, cudaMemcpyDeviceToHost, st));

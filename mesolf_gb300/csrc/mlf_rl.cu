@@ -242,7 +242,7 @@ int run_reduce(Solver* s, int view, float* hx_out, bool ratio, cudaStream_t st) 
   k_reduce_ratio<<<ceil_div(LL, 256), 256, 0, st>>>(
       s->part.as<float>(), s->grid, s->Li, s->Lj, lfsub, hx_out,
       ratio ? s->rpad.as<float>() : nullptr, s->RP, s->q + 1);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 
@@ -297,17 +297,17 @@ PatchGeo solver_geo(const Solver* s) {
 int launch_extract_views(const float* d_lf, const PatchGeo& g, float* lfs, int64_t view_stride, int64_t off,
                          cudaStream_t st) {
   k_extract_views<<<grid_for(g.Xr * g.Xc), 256, 0, st>>>(d_lf, g, lfs, view_stride, off);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 int launch_to_phase(const float* d_vol, const PatchGeo& g, float* X, cudaStream_t st) {
   k_to_phase<<<grid_for(g.Xr * g.Xc * g.Z), 256, 0, st>>>(d_vol, g, X);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st) {
   k_from_phase<<<grid_for(g.Xr * g.Xc * g.Z), 256, 0, st>>>(X, g, d_vol);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 int launch_init_flat(const float* d_lf, const PatchGeo& g, float* X, double* scratch, cudaStream_t st) {
@@ -315,7 +315,7 @@ int launch_init_flat(const float* d_lf, const PatchGeo& g, float* X, double* scr
   k_sum_partial<<<nb, 256, 0, st>>>(d_lf, g.Xr * g.Xc, scratch);
   k_init_flat<<<grid_for((int64_t)g.N * g.N * g.Zch * g.Li * g.Lj), 256, 0, st>>>(
       X, g, scratch, nb, 1.0 / ((double)g.Xr * g.Xc * g.Z));
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 
@@ -506,7 +506,7 @@ int backward_view(Solver* s, const float* d_proj, int u, int v, float* d_out, cu
   const int LL = s->Li * s->Lj;
   MLF_CUDA(cudaMemsetAsync(s->rpad.p, 0, s->rpad.bytes, st));
   k_fill_rpad<<<ceil_div(LL, 256), 256, 0, st>>>(d_proj, s->Li, s->Lj, s->rpad.as<float>(), s->RP, s->q + 1);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   ViewArgs a = view_args(s);
   a.Cout = s->Xtmp.as<float>();
   a.u = u; a.v = v; a.w = 0.f; a.do_fwd = 0;

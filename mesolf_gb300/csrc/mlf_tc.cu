@@ -678,7 +678,7 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
                                        t->wbx_hi.as<bf16>(), t->wbx_lo.as<bf16>());
   k_tc_build_wft<<<4096, 256, 0, st>>>(p->wf.as<float>(), p->N, p->T, p->nch, t->CHP, t->NB,
                                        t->wft_hi.as<bf16>(), t->wft_lo.as<bf16>());
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   MLF_TRY(make_map(&t->mBh, t->wbx_hi.p, (uint64_t)V * t->CHP, t->KB, BWD_BN));
   MLF_TRY(make_map(&t->mBl, t->wbx_lo.p, (uint64_t)V * t->CHP, t->KB, BWD_BN));
   MLF_TRY(make_map(&t->mFh, t->wft_hi.p, (uint64_t)V * t->NB, t->CHP, t->NH));
@@ -786,7 +786,7 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_CUDA(cudaMemsetAsync(t->err.p, 0, sizeof(int), st));
   k_tc_im2col<<<2048, 256, 0, st>>>(nullptr, t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP, psf->T, tp->KB,
                                     t->a1.as<bf16>(), nullptr);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   MLF_TRY(make_map(&t->mARh, t->ar_hi.p, t->MP, tp->KB, BM));
   MLF_TRY(make_map(&t->mARl, t->ar_lo.p, t->MP, tp->KB, BM));
   MLF_TRY(make_map(&t->mA1, t->a1.p, t->MP, tp->KB, BM));
@@ -845,7 +845,7 @@ int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cud
   a.stages = (int)std::max<size_t>(2, std::min<size_t>(FWD_MAX_STAGES, (size_t)(tp->fwd_dyn_max - 1024) / stage));
   const size_t fsmem = (size_t)a.stages * stage + 1024;
   k_tc_fwd<<<dim3(t->MP / BM, t->splits), 128, fsmem, st>>>(t->mXh, t->mXl, tp->mFh, tp->mFl, a);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 
@@ -853,7 +853,7 @@ int tc_col2im(const Psf* psf, TcSolverState* t, int view, bool ratio, float* hx_
   k_tc_col2im_ratio<<<(t->MP + 7) / 8, 256, 0, st>>>(
       t->ypart.as<float>(), t->splits, t->MP, psf->tc->NB, psf->T, t->tile_patch.as<int>(), t->pinfo.as<int>(),
       t->lfs.as<float>() + (int64_t)view * t->MP, hx_out, ratio ? t->rimg.as<float>() : nullptr);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 
@@ -861,7 +861,7 @@ int tc_im2col_ratio(const Psf* psf, TcSolverState* t, int precision, cudaStream_
   k_tc_im2col<<<2048, 256, 0, st>>>(t->rimg.as<float>(), t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP,
                                     psf->T, psf->tc->KB, t->ar_hi.as<bf16>(),
                                     act_split(precision) ? t->ar_lo.as<bf16>() : nullptr);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 
@@ -884,7 +884,7 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   const int grid = std::min(mt * nt, t->nsm);
   k_tc_bwd<<<grid, BWD_THREADS, bwd_smem_bytes(alo, blo), st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl,
                                                                  t->mXv, a, mt, nt);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 
@@ -892,7 +892,7 @@ int tc_pack(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st) {
   dim3 grid((t->MP + 31) / 32, (psf->tc->CHP + 31) / 32);
   k_tc_pack_x<<<grid, dim3(32, 8), 0, st>>>(t->X.as<float>(), psf->nch, psf->tc->CHP, t->MP, t->xb_hi.as<bf16>(),
                                             act_split(precision) ? t->xb_lo.as<bf16>() : nullptr);
-  MLF_CUDA(cudaGetLastError());
+  MLF_LAUNCHED();
   return MLF_OK;
 }
 

@@ -274,17 +274,10 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
 
 #define MLF_INSTANTIATE_VIEW(T)                                                                  \
   int prepare_view_T##T(size_t smem) {                                                          \
-    cudaError_t e = cudaFuncSetAttribute(k_view<T, MODE_FWD>,                                   \
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    if (e == cudaSuccess)                                                                       \
-      e = cudaFuncSetAttribute(k_view<T, MODE_STEP>,                                            \
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
-    if (e == cudaSuccess)                                                                       \
-      e = cudaFuncSetAttribute(k_view<T, MODE_BWDC>,                                            \
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
-    if (e != cudaSuccess)                                                                       \
-      return fail(MLF_ERR_CUDA, std::string("view kernel attributes: ") + cudaGetErrorString(e)); \
-    return MLF_OK;                                                                              \
+    (void)smem;                                                                                 \
+    MLF_TRY(allow_max_dyn_smem((const void*)k_view<T, MODE_FWD>));                              \
+    MLF_TRY(allow_max_dyn_smem((const void*)k_view<T, MODE_STEP>));                             \
+    return allow_max_dyn_smem((const void*)k_view<T, MODE_BWDC>);                               \
   }                                                                                             \
   int occupancy_view_T##T(int threads, size_t smem, int* blocks) {                              \
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_view<T, MODE_STEP>, \
