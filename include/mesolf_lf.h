@@ -169,6 +169,21 @@ int mlf_rl_view_step_prec(mlf_solver* s, const float* lfimg, float* vol, int32_t
                           int32_t precision, void* stream);
 int mlf_forward_view_prec(mlf_solver* s, const float* vol, int32_t u, int32_t v, int32_t precision,
                           float* hx, void* stream);
+/* Full light-field forward projection of a volume, the reference's forwardProjectGPU
+ * (src/recon/forwardProjectGPU.m:1-20; CPU twin forwardProjectACC.m:1-18 without the
+ * CAindex crop): LF = sum_{a,b,z} conv2(vol_z .* [phase (a,b)], H(:,:,a,b,z), 'same').
+ * Evaluated through the phase-space operator: pixel (u + N*i, v + N*j) of the LF image is
+ * view (u, v)'s forward projection at lenslet (i, j), for all N*N views.  This equals the
+ * reference's sum wherever each H(:,:,a,b,z) lies inside the phase-space crop of side
+ * S = K0 - mod(K0 - N, 2N) (gen_phasespace_PSF_theory.m:8-9).  raw_psf = 1 projects with H
+ * as given; raw_psf = 0 with the per-plane normalised H (the operator the RL solve uses).
+ * vol (dev, Xr x Xc x Z) and lf_out (dev, Xr x Xc).  Stream-ordered. */
+int mlf_forward_project(mlf_solver* s, const float* vol, float* lf_out, int32_t raw_psf, int32_t precision,
+                        void* stream);
+/* The same for every patch of a batch (vols[k]: Xr[k] x Xc[k] x nz[k], projected with
+ * the PSF planes [z0[k], z0[k] + nz[k])), on the tensor cores (MLF_PREC_BF16*). */
+int mlf_batch_forward_project(mlf_batch* b, const float* const* vols, float* const* lf_out, int32_t raw_psf,
+                              int32_t precision, void* stream);
 /* The per-iteration flux-preserving NIP low-pass, sample_filter (recon_…_with_filter.m:222-240,
  * filter bank :44-61), applied in place to vol (dev, Xr x Xc x Z). */
 int mlf_sample_filter(mlf_solver* s, float* vol, void* stream);

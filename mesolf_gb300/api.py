@@ -201,6 +201,17 @@ class RLSolver:
         del lk
         return vol
 
+    def forward_project(self, vol, raw_psf=True, precision="fp32", stream=None):
+        """Full light-field image (Xr, Xc) of a device (Xr, Xc, Z) volume, the reference's
+        ``forwardProjectGPU(H, vol)`` (``src/recon/forwardProjectGPU.m:1-20``).  ``raw_psf``
+        projects with H as given (True) or with the per-plane normalised H of the solve."""
+        vk, vp = _fortran(vol)
+        lf, lp = _empty_like_kind(vol, (self.Xr, self.Xc))
+        check(_lib.load().mlf_forward_project(self._h, vp, lp, 1 if raw_psf else 0, PRECISIONS[precision],
+                                              _stream_of(vol, stream)))
+        del vk
+        return lf
+
     def sample_filter(self, vol, stream=None):
         """The per-iteration flux-preserving low-pass on a device volume, in place."""
         check(_lib.load().mlf_sample_filter(self._h, vol.data_ptr(), _stream_of(vol, stream)))
@@ -271,6 +282,23 @@ class BatchSolver:
         check(lib.mlf_batch_run(self._h, lp, int(max_iter), PRECISIONS[precision], wp, op,
                                 ctypes.byref(st) if want_stats else None, _stream_of(lfimgs[0], stream)))
         self.last_stats = st.as_dict() if want_stats else None
+        del keep
+        return outs
+
+    def forward_project(self, vols, raw_psf=True, precision="bf16x3", stream=None):
+        """Full light-field images of device volumes (patch k: (Xr, Xc, nz) with the PSF
+        planes of its range) on the tensor cores; returns a list of (Xr, Xc) device arrays."""
+        P = len(self.shapes)
+        keep = []
+        vp = (ctypes.c_void_p * P)()
+        for k, v in enumerate(vols):
+            t, ptr = _fortran(v)
+            keep.append(t)
+            vp[k] = ptr
+        outs = [_empty_like_kind(vols[k], self.shapes[k])[0] for k in range(P)]
+        op = (ctypes.c_void_p * P)(*[o.data_ptr() for o in outs])
+        check(_lib.load().mlf_batch_forward_project(self._h, vp, op, 1 if raw_psf else 0, PRECISIONS[precision],
+                                                    _stream_of(vols[0], stream)))
         del keep
         return outs
 

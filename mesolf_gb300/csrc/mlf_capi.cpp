@@ -398,6 +398,37 @@ int mlf_forward_view_prec(mlf_solver* s, const float* vol, int32_t u, int32_t v,
   return forward_view_prec(s, vol, u, v, precision, hx, static_cast<cudaStream_t>(stream));
 }
 
+int mlf_forward_project(mlf_solver* s, const float* vol, float* lf_out, int32_t raw_psf, int32_t precision,
+                        void* stream) {
+  clear_error();
+  if (!s || !vol || !lf_out) return fail(MLF_ERR_INVALID, "mlf_forward_project: null pointer");
+  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2) return fail(MLF_ERR_INVALID, "mlf_forward_project: unknown precision");
+  if (!is_device_ptr(vol) || !is_device_ptr(lf_out)) return fail(MLF_ERR_INVALID, "mlf_forward_project: device pointers required");
+  return forward_project(s, vol, lf_out, raw_psf ? s->psf->hsum_dev.as<float>() : nullptr, precision,
+                         static_cast<cudaStream_t>(stream));
+}
+
+int mlf_batch_forward_project(mlf_batch* b, const float* const* vols, float* const* lf_out, int32_t raw_psf,
+                              int32_t precision, void* stream) {
+  clear_error();
+  if (!b || !vols || !lf_out) return fail(MLF_ERR_INVALID, "mlf_batch_forward_project: null pointer");
+  if (precision != MLF_PREC_BF16 && precision != MLF_PREC_BF16X2 && precision != MLF_PREC_BF16X3)
+    return fail(MLF_ERR_UNSUPPORTED, "mlf_batch_forward_project: batches run on the tensor cores (MLF_PREC_BF16*)");
+  const size_t P = b->members.size();
+  std::vector<const float*> v(P);
+  std::vector<float*> o(P);
+  std::vector<mlf::Solver*> ms;
+  for (size_t k = 0; k < P; ++k) {
+    v[k] = vols[k];
+    o[k] = lf_out[k];
+    if (!v[k] || !o[k] || !is_device_ptr(v[k]) || !is_device_ptr(o[k]))
+      return fail(MLF_ERR_INVALID, "mlf_batch_forward_project: device pointers required");
+    ms.push_back(b->members[k].get());
+  }
+  return tc_forward_project(b->work, ms, v, o, precision, raw_psf ? b->psf->hsum_dev.as<float>() : nullptr,
+                            static_cast<cudaStream_t>(stream));
+}
+
 int mlf_sample_filter(mlf_solver* s, float* vol, void* stream) {
   clear_error();
   if (!s || !vol) return fail(MLF_ERR_INVALID, "mlf_sample_filter: null pointer");

@@ -87,6 +87,8 @@ struct Psf {
   DevBuf wf, wb;             // float [N*N][nch][T*T]
   std::vector<double> weights;  // N*N, index u + N*v (MATLAB weight(u+1, v+1))
   std::vector<double> wsum_vz;  // [N*N][Z] FP64 sums of Hps(:,:,u,v,z) (weights of plane ranges)
+  std::vector<double> hsum_z;   // [Z] FP64 sums of the raw H(:,:,:,:,z)
+  DevBuf hsum_dev;              // float [Z], the same on the device
   std::vector<int> view_order;  // active views in spiral order (view = u + N*v)
   std::vector<int> spiral;      // all N*N views in spiral order
   TcPsfState* tc = nullptr;     // built on the first tensor-core solve
@@ -154,7 +156,12 @@ int rl_view_step(Solver* s, const float* d_lf, float* d_vol, int u, int v, doubl
 // layout kernels on an arbitrary PatchGeo (mlf_rl.cu)
 int launch_extract_views(const float* d_lf, const PatchGeo& g, float* lfs, int64_t view_stride, int64_t off,
                          cudaStream_t st);
-int launch_to_phase(const float* d_vol, const PatchGeo& g, float* X, cudaStream_t st);
+int launch_to_phase(const float* d_vol, const PatchGeo& g, float* X, cudaStream_t st,
+                    const float* zscale = nullptr);
+int launch_scatter_views(const float* lfs, const PatchGeo& g, float* d_lf, int64_t view_stride, int64_t off,
+                         cudaStream_t st);
+int forward_project(Solver* s, const float* d_vol, float* d_lf, const float* d_zscale, int precision,
+                    cudaStream_t st);
 int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st);
 // flat initial guess sum(lf)/(Xr*Xc*Z) on the patch's planes, 0 on the other channels
 int launch_init_flat(const float* d_lf, const PatchGeo& g, float* X, double* scratch, cudaStream_t st);
@@ -176,6 +183,9 @@ int tc_run(TcSolverState* w, const std::vector<Solver*>& members, const std::vec
            const std::vector<const float*>& warm, const std::vector<float*>& out, int max_iter, int precision,
            mlf_stats* stats, Solver* timing_owner, cudaStream_t st);
 int tc_forward_view(Solver* s, int precision, const float* d_vol, int view, float* hx_out, cudaStream_t st);
+// full LF images of vols[p] (all N*N views), zscale as in forward_project
+int tc_forward_project(TcSolverState* w, const std::vector<Solver*>& members, const std::vector<const float*>& vols,
+                       const std::vector<float*>& lf_out, int precision, const float* zscale, cudaStream_t st);
 int tc_view_step(Solver* s, int precision, const float* d_lf, float* d_vol, int view, float w, cudaStream_t st);
 int tc_check_error(TcSolverState* w);
 size_t tc_psf_bytes(const Psf* p);

@@ -198,7 +198,17 @@ int psf_build(Psf* psf, const float* dH, const float* dHt, cudaStream_t st) {
 
   psf->wsum_vz.assign((size_t)N * N * Z, 0.0);
   MLF_CUDA(cudaMemcpyAsync(psf->wsum_vz.data(), wsum.p, sizeof(double) * N * N * Z, cudaMemcpyDeviceToHost, st));
+  std::vector<double> inv_h(Z);
+  MLF_CUDA(cudaMemcpyAsync(inv_h.data(), invH, sizeof(double) * Z, cudaMemcpyDeviceToHost, st));
   MLF_CUDA(cudaStreamSynchronize(st));
+  psf->hsum_z.resize(Z);
+  std::vector<float> hs(Z);
+  for (int z = 0; z < Z; ++z) {
+    psf->hsum_z[z] = 1.0 / inv_h[z];
+    hs[z] = (float)psf->hsum_z[z];
+  }
+  MLF_TRY(psf->hsum_dev.alloc(sizeof(float) * Z, "psf plane sums"));
+  MLF_CUDA(cudaMemcpy(psf->hsum_dev.p, hs.data(), sizeof(float) * Z, cudaMemcpyHostToDevice));
   std::vector<double> w(N * N, 0.0);
   for (int v = 0; v < N * N; ++v)
     for (int z = 0; z < Z; ++z) w[v] += psf->wsum_vz[(size_t)v * Z + z];

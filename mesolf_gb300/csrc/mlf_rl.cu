@@ -74,11 +74,13 @@ __device__ __forceinline__ int64_t phase_index(const PatchGeo& g, int64_t e) {
 }
 
 // MATLAB (Xr, Xc, Z) volume -> phase-major planes; one thread per voxel of the input.
-__global__ void k_to_phase(const float* __restrict__ vol, PatchGeo g, float* __restrict__ X) {
+// zscale (nullable): per-plane factor applied on the way in.
+__global__ void k_to_phase(const float* __restrict__ vol, PatchGeo g, float* __restrict__ X,
+                           const float* __restrict__ zscale) {
   const int64_t n = g.Xr * g.Xc * g.Z;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x)
-    X[phase_index(g, e)] = vol[e];
+    X[phase_index(g, e)] = zscale ? vol[e] * zscale[e / (g.Xr * g.Xc)] : vol[e];
 }
 
 __global__ void k_from_phase(const float* __restrict__ X, PatchGeo g, float* __restrict__ vol) {
@@ -99,6 +101,19 @@ __global__ void k_extract_views(const float* __restrict__ lf, PatchGeo g, float*
     const int u = (int)(r % g.N), a = (int)(r / g.N);
     const int v = (int)(c % g.N), b = (int)(c / g.N);
     lfs[(int64_t)(u + g.N * v) * view_stride + off + (int64_t)b * g.Li + a] = lf[e];
+  }
+}
+
+// Inverse of k_extract_views: LF(u + N*a, v + N*b) = lfs[(u + N*v) * view_stride + off + b*Li + a].
+__global__ void k_scatter_views(const float* __restrict__ lfs, PatchGeo g, float* __restrict__ lf,
+                                int64_t view_stride, int64_t off) {
+  const int64_t n = g.Xr * g.Xc;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e % g.Xr, c = e / g.Xr;
+    const int u = (int)(r % g.N), a = (int)(r / g.N);
+    const int v = (int)(c % g.N), b = (int)(c / g.N);
+    lf[e] = lfs[(int64_t)(u + g.N * v) * view_stride + off + (int64_t)b * g.Li + a];
   }
 }
 
@@ -215,7 +230,12 @@ int timing_mark(Solver* s, cudaStream_t st) {
       s->tev.push_back(e);
     }
   }
-  MLF_CUDA(cudaEventRecord(s->tev[s->tev_used++], st));
+  // Inside a stream capture the record must become a graph node of its own.
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  MLF_CUDA(cudaStreamIsCapturing(st, &cs));
+  MLF_CUDA(cudaEventRecordWithFlags(s->tev[s->tev_used++], st,
+                                    cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
+                                                                        : cudaEventRecordDefault));
   return MLF_OK;
 }
 
@@ -300,8 +320,14 @@ int launch_extract_views(const float* d_lf, const PatchGeo& g, float* lfs, int64
   MLF_LAUNCHED();
   return MLF_OK;
 }
-int launch_to_phase(const float* d_vol, const PatchGeo& g, float* X, cudaStream_t st) {
-  k_to_phase<<<grid_for(g.Xr * g.Xc * g.Z), 256, 0, st>>>(d_vol, g, X);
+int launch_to_phase(const float* d_vol, const PatchGeo& g, float* X, cudaStream_t st, const float* zscale) {
+  k_to_phase<<<grid_for(g.Xr * g.Xc * g.Z), 256, 0, st>>>(d_vol, g, X, zscale);
+  MLF_LAUNCHED();
+  return MLF_OK;
+}
+int launch_scatter_views(const float* lfs, const PatchGeo& g, float* d_lf, int64_t view_stride, int64_t off,
+                         cudaStream_t st) {
+  k_scatter_views<<<grid_for(g.Xr * g.Xc), 256, 0, st>>>(lfs, g, d_lf, view_stride, off);
   MLF_LAUNCHED();
   return MLF_OK;
 }
@@ -494,6 +520,33 @@ int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaS
   a.wf = wf_of(s, u + s->N * v);
   MLF_TRY(launch_view_kernel(s->T, MODE_FWD, a, s->grid, s->threads, s->smem, st));
   return run_reduce(s, u + s->N * v, d_hx, false, st);
+}
+
+// Full light-field image of a volume: the forward projections of all N*N views
+// interleaved, LF(u + N*a, v + N*b) = HX_{u,v}(a, b).  `zscale` (nullable, device, Z
+// floats) multiplies each plane first; with the plane sums of the raw H it turns the
+// solver's per-plane normalised PSF back into H.
+int forward_project(Solver* s, const float* d_vol, float* d_lf, const float* d_zscale, int precision,
+                    cudaStream_t st) {
+  if (precision != MLF_PREC_FP32) {
+    MLF_TRY(tc_solver_prepare(s, st));
+    return tc_forward_project(s->tc, {s}, {d_vol}, {d_lf}, precision, d_zscale, st);
+  }
+  if (s->lite) return fail(MLF_ERR_INVALID, "forward projection needs a full solver context");
+  const PatchGeo g = solver_geo(s);
+  const int N = s->N;
+  const int64_t LL = (int64_t)s->Li * s->Lj;
+  MLF_TRY(launch_to_phase(d_vol, g, s->Xtmp.as<float>(), st, d_zscale));
+  for (int view = 0; view < N * N; ++view) {
+    ViewArgs a = view_args(s);
+    a.X = s->Xtmp.as<float>();
+    a.u = view % N; a.v = view / N; a.w = 0.f; a.do_fwd = 1;
+    a.wb = wb_of(s, view);
+    a.wf = wf_of(s, view);
+    MLF_TRY(launch_view_kernel(s->T, MODE_FWD, a, s->grid, s->threads, s->smem, st));
+    MLF_TRY(run_reduce(s, view, s->lfs.as<float>() + view * LL, false, st));
+  }
+  return launch_scatter_views(s->lfs.as<float>(), g, d_lf, LL, 0, st);
 }
 
 int forward_view_prec(Solver* s, const float* d_vol, int u, int v, int precision, float* d_hx, cudaStream_t st) {

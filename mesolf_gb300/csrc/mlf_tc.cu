@@ -647,6 +647,24 @@ struct TcSolverState {
   std::vector<float> wtab;  // [views][P]
   DevBuf X, lfs, rimg, tile_patch, pinfo, wtab_dev, wscratch, ar_hi, ar_lo, a1, xb_hi, xb_lo, ypart, err;
   CUtensorMap mARh, mARl, mA1, mXh, mXl, mXv;
+  // One RL iteration (view loop + filters of every patch) as an instantiated CUDA graph,
+  // per precision and with / without per-view timing nodes.  All buffers above are fixed
+  // for the life of the work set, so a captured iteration stays valid.
+  struct Iteration {
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;  // kernel nodes
+    int tev_used = 0;      // timing events recorded by one replay
+  };
+  Iteration iter[4][2];
+  // Captures run on this private stream (the legacy default stream cannot be captured);
+  // the instantiated graph is then launched on the caller's stream.
+  cudaStream_t capture_stream = nullptr;
+  ~TcSolverState() {
+    for (auto& row : iter)
+      for (auto& g : row)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+  }
 };
 
 void tc_psf_free(TcPsfState* t) { delete t; }
@@ -927,6 +945,39 @@ int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* ti
   return MLF_OK;
 }
 
+// Capture one RL iteration over the work set into an executable graph.
+int capture_iteration(const Psf* psf, TcSolverState* t, const std::vector<Solver*>& members, int precision,
+                      Solver* timer, TcSolverState::Iteration* out) {
+  if (!t->capture_stream) MLF_CUDA(cudaStreamCreateWithFlags(&t->capture_stream, cudaStreamNonBlocking));
+  cudaStream_t st = t->capture_stream;
+  MLF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  int64_t launches = 0;
+  int rc = tc_enqueue_views(psf, t, precision, timer, &launches, st);
+  for (int p = 0; rc == MLF_OK && p < t->P; ++p) {
+    rc = filter_run_geo(members[p], work_geo(t, members[p], p), t->X.as<float>() + t->pos0[p], st);
+    launches += 5;
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &g);
+  if (rc != MLF_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(MLF_ERR_CUDA, std::string("capture of the RL iteration: ") + cudaGetErrorString(ce));
+  }
+  const cudaError_t ie = cudaGraphInstantiateWithFlags(&out->exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) {
+    out->exec = nullptr;
+    return fail(MLF_ERR_CUDA, std::string("instantiate the RL iteration graph: ") + cudaGetErrorString(ie));
+  }
+  out->launches = launches;
+  out->tev_used = timer->tev_used;
+  return MLF_OK;
+}
+
 }  // namespace
 
 int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vector<const float*>& lf,
@@ -954,12 +1005,17 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
       launches += 3;
     }
   }
-  for (int it = 0; it < max_iter; ++it) {
-    MLF_TRY(tc_enqueue_views(psf, t, precision, timer, &launches, st));
-    for (int p = 0; p < t->P; ++p) {
-      MLF_TRY(filter_run_geo(members[p], work_geo(t, members[p], p), t->X.as<float>() + t->pos0[p], st));
-      launches += 5;
+  if (max_iter > 0) {
+    TcSolverState::Iteration& g = t->iter[precision & 3][timer->timing ? 1 : 0];
+    if (!g.exec) {
+      timer->tev_used = 0;
+      MLF_TRY(capture_iteration(psf, t, members, precision, timer, &g));
     }
+    // The timing events of the graph are re-recorded by every replay; the per-view kernel
+    // time reported is that of the last iteration, times the iteration count.
+    timer->tev_used = g.tev_used;
+    for (int it = 0; it < max_iter; ++it) MLF_CUDA(cudaGraphLaunch(g.exec, st));
+    launches += g.launches * max_iter;
   }
   for (int p = 0; p < t->P; ++p) {
     MLF_TRY(launch_from_phase(t->X.as<float>() + t->pos0[p], work_geo(t, members[p], p), out[p], st));
@@ -982,8 +1038,8 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
       MLF_CUDA(cudaEventElapsedTime(&tt, timer->tev[k], timer->tev[k + 1]));
       vk += tt;
     }
-    stats->view_kernel_ms = vk;
-    stats->view_kernel_launches = timer->tev_used / 2;
+    stats->view_kernel_ms = vk * max_iter;
+    stats->view_kernel_launches = (int64_t)(timer->tev_used / 2) * max_iter;
     stats->kernel_launches = launches;
     MLF_TRY(tc_check_error(t));
   }
@@ -999,6 +1055,23 @@ int tc_forward_view(Solver* s, int precision, const float* d_vol, int view, floa
   MLF_TRY(tc_pack(s->psf, t, precision, st));
   MLF_TRY(tc_fwd_launch(s->psf, t, precision, view, st));
   return tc_col2im(s->psf, t, view, false, hx_out, st);
+}
+
+int tc_forward_project(TcSolverState* t, const std::vector<Solver*>& members, const std::vector<const float*>& vols,
+                       const std::vector<float*>& lf_out, int precision, const float* zscale, cudaStream_t st) {
+  const Psf* psf = members[0]->psf;
+  const int N = psf->N;
+  for (int p = 0; p < t->P; ++p)
+    MLF_TRY(launch_to_phase(vols[p], work_geo(t, members[p], p), t->X.as<float>() + t->pos0[p], st,
+                            zscale ? zscale + t->z0[p] : nullptr));
+  MLF_TRY(tc_pack(psf, t, precision, st));
+  for (int view = 0; view < N * N; ++view) {
+    MLF_TRY(tc_fwd_launch(psf, t, precision, view, st));
+    MLF_TRY(tc_col2im(psf, t, view, false, t->lfs.as<float>() + (int64_t)view * t->MP, st));
+  }
+  for (int p = 0; p < t->P; ++p)
+    MLF_TRY(launch_scatter_views(t->lfs.as<float>(), work_geo(t, members[p], p), lf_out[p], t->MP, t->pos0[p], st));
+  return MLF_OK;
 }
 
 // One RL view step on the tensor cores (parity tests), single solver.

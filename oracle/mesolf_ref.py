@@ -431,11 +431,14 @@ def rl_view_step(X, LFIMG, Hps, Htc, u, v, w, N):
     return rl_update(X, C, D, w)
 
 
-def recon_phase_space(LFIMG, H, Ht, maxIter, X0=None, callback=None):
+def recon_phase_space(LFIMG, H, Ht, maxIter, X0=None, callback=None, view_step=None):
     """``recon_theory_phase_space_LFM_with_filter`` (``…_with_filter.m:10-151``), FP64.
 
     ``X0`` (optional) replaces the flat initial guess of ``:72-73`` (warm start).
     ``callback(it, X)`` is called after each iteration's ``sample_filter``.
+    ``view_step(h_uv, t_uv, LFIMG, X, u, v, w, N)`` (optional) replaces ``rl_view_step``
+    with an equivalent implementation (the C/OpenMP port in ``oracle/mlf_oracle.c``), so
+    that large fixtures can be generated in reasonable time.
     """
     LFIMG = np.asarray(LFIMG, dtype=np.float64)
     Hn, Htn = normalize_psf(H, Ht)                                   # :13-16
@@ -457,7 +460,10 @@ def recon_phase_space(LFIMG, H, Ht, maxIter, X0=None, callback=None):
                 v = j_idx[(u2 - 1) * N + v2 - 1] - 1
                 if w[u, v] == 0:
                     continue
-                X = rl_view_step(X, LFIMG, Hps, Htc, u, v, w[u, v], N)
+                if view_step is None:
+                    X = rl_view_step(X, LFIMG, Hps, Htc, u, v, w[u, v], N)
+                else:
+                    X = view_step(Hps[:, :, u, v, :], Htc[:, :, u, v, :], LFIMG, X, u, v, w[u, v], N)
         X = sample_filter(X, F)                                      # :142
         if callback is not None:
             callback(it, X)

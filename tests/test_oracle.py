@@ -201,3 +201,22 @@ def test_c_port_matches_numpy_oracle():
     ref = R.rl_view_step(X, LF, h[:, :, None, None, :].repeat(15, 2).repeat(15, 3),
                          t[:, :, None, None, :].repeat(15, 2).repeat(15, 3), 3, 11, 0.3, N)
     np.testing.assert_allclose(cbuild.view_step(h, t, LF, X, 3, 11, 0.3, N), ref, rtol=1e-11)
+
+
+def test_full_forward_equals_interleaved_phase_space_views():
+    """a17 through the phase-space operator: forwardProjectGPU.m's sum over (a, b, z) of
+    conv2(vol_z .* phase(a, b), H(:,:,a,b,z), 'same') equals, pixel (u + N i, v + N j),
+    view (u, v)'s phase-space forward projection at lenslet (i, j) with the per-plane
+    normalised PSF times the plane sums of H (PSF inside the crop)."""
+    w = synth.small_config(lenslets=(3, 2), K0=61, Z=3)
+    H, Ht = w.psf()
+    vol = np.random.default_rng(1).random((45, 30, 3))
+    full = R.forward_project_full(H, vol)
+    Hn, Htn = R.normalize_psf(H, Ht)
+    Hps, _ = R.gen_phasespace_psf(Hn, Htn)
+    sums = H.astype(np.float64).sum(axis=(0, 1, 2, 3))
+    lf = np.zeros_like(full)
+    for u in range(15):
+        for v in range(15):
+            lf[u::15, v::15] = R.forward_ps(Hps[:, :, u, v, :], vol * sums, 15)
+    assert np.abs(lf - full).max() <= 1e-12 * np.abs(full).max()
