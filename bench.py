@@ -169,6 +169,8 @@ def main():
                     help="one solve of --iters iterations and exit (for ncu captures)")
     ap.add_argument("--iters", type=int, default=None)
     ap.add_argument("--mixed", default="bf16x2", help="tensor-core precision timed beside plain FP32 ('' to skip)")
+    ap.add_argument("--serve-frames", type=int, default=4,
+                    help="frames of the 36-patch 18 Hz serving stream (0 to skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -330,12 +332,110 @@ def main():
                                 "sample": f"one full RL view step ({Xr}x{Xc}x{planes}) of the FP64 C/OpenMP oracle "
                                           f"port on {thr} host threads ({t:.2f} s), extrapolated to "
                                           f"{n_views} views x {w.iters} iterations"}
+    if args.serve_frames > 0 and args.mixed:
+        solver.close()
+        del out_dev, lf_dev
+        torch.cuda.empty_cache()
+        line["serving"] = serve_block(psf, args.serve_frames, args.mixed, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
     solver.close()
     psf.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+SERVE_DESC = ("6x6 patch carpet (36 patches, 45-71 lenslets per side, 51 planes, the same PSF), frames at "
+              "18 Hz +-10% jitter, AR(1) (rho 0.95) soma intensities, 2000-photon Poisson images, warm start "
+              "from the previous frame, 3 RL iterations")
+
+
+def serve_block(psf, n_frames, precision, dev, fp32_patches=2):
+    """The serving stream: frames of the 36-patch carpet arriving at 18 Hz +-10% through
+    SolveServer (continuous batching over two lanes, admission by free HBM, warm start).
+    Returns p50 / p99 latency (arrival -> volume in host memory), deconvolved voxels/s over
+    the stream, and the plain FP32 per-patch solve rate on the same frames for comparison."""
+    import torch
+    from mesolf_gb300 import BatchSolver, RLSolver, synth
+    from mesolf_gb300.api import _fortran
+    from mesolf_gb300.serve import SolveServer
+    N, Z = psf.N, psf.Z
+    shapes = synth.carpet_geometry()
+    geo = [(sh, (0, Z)) for sh in shapes]
+    density = 2000.0 / (1005 * 1005 * 51)
+    streams = [synth.SomaStream(sh, Z, int(round(density * sh[0] * sh[1] * Z)), seed=100 + k, device=dev)
+               for k, sh in enumerate(shapes)]
+    # frames: volumes rendered on the GPU, projected by the batched forward projector
+    gen = BatchSolver(psf, shapes)
+    rng = torch.Generator(device=dev)
+    rng.manual_seed(11)
+    frames, scale = [], None
+    t_gen = time.perf_counter()
+    for f in range(n_frames + 1):
+        vols = [st.step() for st in streams]
+        lfs = gen.forward_project(vols, raw_psf=True, precision="bf16x3")
+        if scale is None:
+            scale = [2000.0 / float(lf.max()) for lf in lfs]
+        frames.append([torch.poisson((lf.clamp(min=0) * sc).contiguous(), generator=rng).cpu().numpy()
+                       for lf, sc in zip(lfs, scale)])
+        del vols, lfs
+    gen.close()
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t_gen
+    torch.cuda.empty_cache()
+    srv = SolveServer(psf, geo, iters=3, precision=precision, lanes=2)
+    # frame 0 warms the server up (work sets, graphs, first cold-started volumes); not timed
+    for p in range(len(geo)):
+        srv.submit(p, 0, frames[0][p])
+    srv.drain()
+    srv._lat.clear(); srv._voxels = 0; srv._batches.clear(); srv._t_first = None; srv._t_last = 0.0
+    period = 1.0 / 18.0
+    jit = np.random.default_rng(3).uniform(-0.1, 0.1, n_frames)
+    futs = {}
+    t_next = time.perf_counter() + 0.01
+    for f in range(1, n_frames + 1):
+        while time.perf_counter() < t_next:
+            time.sleep(max(0.0, min(0.002, t_next - time.perf_counter())))
+        for p in range(len(geo)):
+            futs[p, f] = srv.submit(p, f, frames[f][p], t_arrival=t_next)
+        t_next += period * (1.0 + jit[f - 1])
+    res = {k: v.result() for k, v in futs.items()}
+    srv.drain()
+    rep = srv.report()
+    # the same frames' last two results through the plain FP32 drop-in path, from the same
+    # warm start; error of the served volumes against them
+    f_last = n_frames
+    fp32_t, fp32_vox, errs = 0.0, 0, []
+    prev = {p: np.array(res[p, f_last - 1]) if n_frames > 1 else None for p in range(fp32_patches)}
+    for p in range(fp32_patches):
+        s = RLSolver(psf, shapes[p])
+        lf = _fortran(torch.as_tensor(np.ascontiguousarray(frames[f_last][p])).to(dev))[0]
+        warm = None if prev[p] is None else _fortran(torch.as_tensor(np.ascontiguousarray(prev[p])).to(dev))[0]
+        out = s.run(lf, 3, precision="fp32", warm_start=warm, want_stats=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = s.run(lf, 3, precision="fp32", warm_start=warm, want_stats=False)
+        torch.cuda.synchronize()
+        fp32_t += time.perf_counter() - t0
+        fp32_vox += shapes[p][0] * shapes[p][1] * Z
+        o = out.cpu().numpy().astype(np.float64)
+        errs.append(float(np.linalg.norm(np.asarray(res[p, f_last], np.float64) - o) / np.linalg.norm(o)))
+        s.close()
+    srv.close()
+    fp32_rate = fp32_vox / fp32_t
+    frame_vox = sum(a * b * Z for a, b in shapes)
+    return {"workload": "carpet6x6_lenslets45-71_z51_k231_it3_18hz", "desc": SERVE_DESC,
+            "precision": precision, "frames": n_frames, "requests": rep["requests"],
+            "p50_ms": rep["p50_ms"], "p99_ms": rep["p99_ms"], "max_ms": rep["max_ms"],
+            "frame_period_ms": 1000.0 / 18.0, "voxels_per_s": rep["voxels_per_s"],
+            "voxels_per_frame": frame_vox, "frames_per_s_sustained": rep["voxels_per_s"] / frame_vox,
+            "mean_batch_patches": rep["mean_batch"], "batches": rep["batches"],
+            "plain_fp32_voxels_per_s": fp32_rate, "speedup_vs_plain_fp32": rep["voxels_per_s"] / fp32_rate,
+            "plain_fp32_ms_per_frame": 1e3 * frame_vox / fp32_rate,
+            "rel_l2_vs_plain_fp32_same_warm_start": errs,
+            "frame_generation_s": t_gen,
+            "note": "latency = scheduled arrival -> volume in pinned host memory; arrivals faster than the "
+                    "service rate queue up, so p50/p99 grow with the stream length"}
 
 
 def _measured_bf16():

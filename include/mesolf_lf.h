@@ -135,6 +135,10 @@ int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t 
 int mlf_batch_create(mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int64_t* Xc, const int32_t* z0,
                      const int32_t* nz, mlf_batch** out);
 int mlf_batch_destroy(mlf_batch* b);
+/* Device bytes mlf_batch_create would allocate for these patches (an upper bound, for
+ * admission by free HBM before creating the work set).  No allocation. */
+int mlf_batch_plan_bytes(const mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int64_t* Xc,
+                         const int32_t* z0, const int32_t* nz, int64_t* bytes);
 int64_t mlf_batch_device_bytes(const mlf_batch* b);
 int mlf_batch_run(mlf_batch* b, const float* const* lfimg, int32_t max_iter, int32_t precision,
                   const float* const* warm, float* const* vol_out, mlf_stats* stats, void* stream);

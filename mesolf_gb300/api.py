@@ -255,6 +255,21 @@ class BatchSolver:
     def device_bytes(self):
         return int(_lib.load().mlf_batch_device_bytes(self._h))
 
+    @staticmethod
+    def plan_bytes(psf: PhaseSpacePSF, shapes, planes=None):
+        """Device bytes a BatchSolver for these patches would allocate (upper bound; no
+        allocation), for admission by free HBM."""
+        P = len(shapes)
+        if planes is None:
+            planes = [(0, psf.Z)] * P
+        xr = (ctypes.c_int64 * P)(*[int(a) for a, _ in shapes])
+        xc = (ctypes.c_int64 * P)(*[int(b) for _, b in shapes])
+        z0 = (ctypes.c_int32 * P)(*[int(a) for a, _ in planes])
+        nz = (ctypes.c_int32 * P)(*[int(b) for _, b in planes])
+        out = ctypes.c_int64()
+        check(_lib.load().mlf_batch_plan_bytes(psf.handle, P, xr, xc, z0, nz, ctypes.byref(out)))
+        return int(out.value)
+
     def run(self, lfimgs, max_iter, precision="bf16x2", warm=None, outs=None, stream=None, want_stats=True):
         """Device (torch CUDA) images in, list of (Xr, Xc, nz) device volumes out."""
         import torch

@@ -35,6 +35,7 @@ void clear_error() {
 int DevBuf::alloc(size_t n, const char* what) {
   release();
   if (n == 0) n = 16;
+  std::lock_guard<std::recursive_mutex> lk(device_mutex());
   cudaError_t e = cudaMalloc(&p, n);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -46,8 +47,16 @@ int DevBuf::alloc(size_t n, const char* what) {
   return MLF_OK;
 }
 
+std::recursive_mutex& device_mutex() {
+  static std::recursive_mutex m;
+  return m;
+}
+
 void DevBuf::release() {
-  if (p) cudaFree(p);
+  if (p) {
+    std::lock_guard<std::recursive_mutex> lk(device_mutex());
+    cudaFree(p);
+  }
   p = nullptr;
   bytes = 0;
 }
@@ -301,8 +310,31 @@ int mlf_batch_create(mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int6
   std::vector<mlf::Solver*> ms;
   for (auto& m : b->members) ms.push_back(m.get());
   MLF_TRY(tc_work_create(psf, ms, &b->work, nullptr));
-  MLF_CUDA(cudaDeviceSynchronize());
+  MLF_CUDA(cudaStreamSynchronize(nullptr));
   *out = b.release();
+  return MLF_OK;
+}
+
+int mlf_batch_plan_bytes(const mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int64_t* Xc,
+                         const int32_t* z0, const int32_t* nz, int64_t* bytes) {
+  clear_error();
+  if (!psf || npatch < 1 || !Xr || !Xc || !z0 || !nz || !bytes) return fail(MLF_ERR_INVALID, "mlf_batch_plan_bytes: bad argument");
+  int nsm = 0;
+  MLF_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, psf->device));
+  std::vector<int> li, lj;
+  size_t members = 0;
+  for (int k = 0; k < npatch; ++k) {
+    if (Xr[k] < psf->N || Xc[k] < psf->N || Xr[k] % psf->N || Xc[k] % psf->N || z0[k] < 0 || nz[k] < 1 ||
+        z0[k] + nz[k] > psf->Z)
+      return fail(MLF_ERR_INVALID, "mlf_batch_plan_bytes: patch " + std::to_string(k) + ": bad geometry");
+    li.push_back((int)(Xr[k] / psf->N));
+    lj.push_back((int)(Xc[k] / psf->N));
+    // filter scratch volume, reduction scratch, filter kernels and sums (upper bounds)
+    const int64_t gmax = (std::max(Xr[k], Xc[k]) + 31) / 32;
+    members += (size_t)(Xr[k] * Xc[k] * nz[k] * 4 + 4096 * 8 + (int64_t)nz[k] * (Xr[k] + Xc[k]) * 4 +
+                        6 * (int64_t)nz[k] * 4 + (2 * (int64_t)nz[k] * gmax + nz[k]) * 8);
+  }
+  *bytes = (int64_t)(members + tc_work_plan_bytes(psf, li, lj, nsm));
   return MLF_OK;
 }
 

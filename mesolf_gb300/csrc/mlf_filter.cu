@@ -183,7 +183,11 @@ __global__ void k_filter_scale(const double* sin, int nin, const double* sout, i
   double a = 0.0, b = 0.0;
   for (int i = 0; i < nin; ++i) a += sin[(int64_t)k * nin + i];
   for (int i = 0; i < nout; ++i) b += sout[(int64_t)k * nout + i];
-  scale[z] = a / b;
+  // An all-zero plane (flux underflowed to 0) stays zero.  The reference's
+  // sum_before * buf / sum(buf) would give 0/0 = NaN there (…_with_filter.m:233), which the
+  // next update's blend (1-w)*X would carry forward; FP32 planes reach exact zero long
+  // before FP64 ones do.
+  scale[z] = (b != 0.0) ? a / b : 0.0;
 }
 
 // |fft(g)|, g[n] = exp(-((n + 1 - L/2) / w)^2), by direct DFT in FP64.

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -50,6 +51,11 @@ struct DevBuf {
   void release();
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
+
+// Serialises CUDA graph captures against device memory allocation and release in this
+// library (cudaFree synchronises the device, which would invalidate a capture running
+// on another thread).  Recursive: releases can nest inside locked regions.
+std::recursive_mutex& device_mutex();
 
 // true if ptr is device (or managed) memory usable by kernels on the current device
 bool is_device_ptr(const void* ptr);
@@ -191,6 +197,8 @@ int tc_check_error(TcSolverState* w);
 size_t tc_psf_bytes(const Psf* p);
 size_t tc_solver_bytes(const Solver* s);
 size_t tc_work_bytes(const TcSolverState* w);
+// device bytes tc_work_create would allocate for patches of Li[p] x Lj[p] lenslets (upper bound)
+size_t tc_work_plan_bytes(const Psf* psf, const std::vector<int>& Li, const std::vector<int>& Lj, int nsm);
 int filter_run(Solver* s, cudaStream_t st);
 int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,
                  int64_t kw, int nnum, float* d_out, cudaStream_t st);

@@ -733,6 +733,27 @@ size_t tc_work_bytes(const TcSolverState* t) {
 
 size_t tc_solver_bytes(const Solver* s) { return tc_work_bytes(s->tc); }
 
+size_t tc_work_plan_bytes(const Psf* psf, const std::vector<int>& Li, const std::vector<int>& Lj, int nsm) {
+  const int KB = rup((psf->T + 2) * (psf->T + 2), BK);
+  const int TT = psf->T * psf->T;
+  const int NB = rup(TT, 16) > 256 ? rup(TT, 32) : rup(TT, 16);
+  const int64_t CHP = rup((int)psf->nch, 128);
+  int64_t MP = 0, tiles = 0;
+  for (size_t p = 0; p < Li.size(); ++p) {
+    MP += rup(Li[p] * Lj[p], BM);
+    tiles += rup(Li[p] * Lj[p], BM) / BM;
+  }
+  const int KSF = (int)(CHP / BK);
+  const int mt = (int)(MP / BM);
+  int splits = std::max(1, std::min(KSF, nsm / std::max(1, mt)));
+  const int ksp = (KSF + splits - 1) / splits;
+  splits = (KSF + ksp - 1) / ksp;
+  const int64_t P = (int64_t)Li.size();
+  return (size_t)(psf->nch * MP * 4 + (int64_t)psf->N * psf->N * MP * 4 + MP * 4 + tiles * 4 + 8 * P * 4 +
+                  (int64_t)psf->N * psf->N * P * 4 + P * 4 + 3 * MP * KB * 2 + 2 * MP * CHP * 2 +
+                  (int64_t)splits * MP * NB * 4 + 4);
+}
+
 int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState** out, cudaStream_t st) {
   MLF_TRY(tc_psf_prepare(psf, st));
   const TcPsfState* tp = psf->tc;
@@ -950,6 +971,7 @@ int capture_iteration(const Psf* psf, TcSolverState* t, const std::vector<Solver
                       Solver* timer, TcSolverState::Iteration* out) {
   if (!t->capture_stream) MLF_CUDA(cudaStreamCreateWithFlags(&t->capture_stream, cudaStreamNonBlocking));
   cudaStream_t st = t->capture_stream;
+  std::lock_guard<std::recursive_mutex> lk(device_mutex());
   MLF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   int64_t launches = 0;
   int rc = tc_enqueue_views(psf, t, precision, timer, &launches, st);

@@ -23,7 +23,8 @@ import dataclasses
 import numpy as np
 
 __all__ = ["make_psf", "make_volume", "forward_project_full", "poisson_image",
-           "Workload", "config1", "config2", "small_config", "fortran32"]
+           "Workload", "config1", "config2", "small_config", "fortran32",
+           "carpet_geometry", "SomaStream", "uneven_batch_geometry"]
 
 
 def fortran32(a):
@@ -187,3 +188,76 @@ def small_config(lenslets=(9, 8), K0=61, Z=7, iters=2, seed=0, n_obj=12, name=No
     z = np.arange(Z) - Z // 2
     return Workload(name or f"small{lenslets[0]}x{lenslets[1]}x{Z}_k{K0}", 15, tuple(lenslets),
                     K0, z, None, n_obj, 3.0, "uniform", 0.01, 1000.0, iters, seed)
+
+
+# ----------------------------------------------------------------------------- streams
+def carpet_geometry(n_side=6, lenslets=(45, 71), N=15, seed=5):
+    """Image shapes of an n_side x n_side patch carpet, lenslets per side uniform in the
+    closed range ``lenslets`` (seeded)."""
+    rng = np.random.default_rng(seed)
+    L = rng.integers(lenslets[0], lenslets[1] + 1, size=(n_side * n_side, 2))
+    return [(int(a) * N, int(b) * N) for a, b in L]
+
+
+def uneven_batch_geometry(n=64, lenslets=(31, 71), planes=(26, 101), Z=101, N=15, seed=4):
+    """Shapes and plane ranges of n independent patches: lenslets per side uniform in
+    ``lenslets``, plane count uniform in ``planes``, each range placed at a uniform offset
+    inside the PSF's Z planes (seeded)."""
+    rng = np.random.default_rng(seed)
+    L = rng.integers(lenslets[0], lenslets[1] + 1, size=(n, 2))
+    nz = rng.integers(planes[0], planes[1] + 1, size=n)
+    z0 = [int(rng.integers(0, Z - k + 1)) for k in nz]
+    return [(int(a) * N, int(b) * N) for a, b in L], [(z, int(k)) for z, k in zip(z0, nz)]
+
+
+class SomaStream:
+    """Soma field of one patch whose intensities follow a slow AR(1) random walk across
+    frames (x_f = rho x_{f-1} + sqrt(1 - rho^2) e_f, intensity = base * exp(0.25 x_f)),
+    rendered on the GPU: impulses at integer soma centres blurred by separable Gaussians
+    (lateral sigma in px, axial sigma in planes), plus a constant background.  Volumes are
+    (Xr, Xc, Z) float32 torch tensors in column-major layout."""
+
+    def __init__(self, shape, Z, n_obj, sigma=4.0, sigma_z=1.0, background=0.02, rho=0.95,
+                 seed=0, device="cuda"):
+        import torch
+        self.torch = torch
+        self.shape = (int(shape[0]), int(shape[1]), int(Z))
+        rng = np.random.default_rng(seed)
+        Xr, Xc, Z = self.shape
+        self.idx = torch.as_tensor(rng.integers(0, Xr, n_obj) + Xr * (rng.integers(0, Xc, n_obj) +
+                                   Xc * rng.integers(0, Z, n_obj)), device=device)
+        self.base = torch.as_tensor(rng.lognormal(0.0, 0.5, n_obj), dtype=torch.float32, device=device)
+        self.x = torch.zeros(n_obj, dtype=torch.float32, device=device)
+        self.rho = rho
+        self.gen = torch.Generator(device=device)
+        self.gen.manual_seed(int(seed) + 17)
+        self.background = background
+        self.device = device
+
+        def g(s):
+            r = int(np.ceil(4 * s))
+            k = np.exp(-np.arange(-r, r + 1) ** 2 / (2 * s * s))
+            return torch.as_tensor(k, dtype=torch.float32, device=device).view(1, 1, -1), r
+
+        self.gl, self.rl = g(sigma)
+        self.gz, self.rz = g(sigma_z)
+
+    def _blur_last(self, v, k, r):
+        F = self.torch.nn.functional
+        sh = v.shape
+        return F.conv1d(v.reshape(-1, 1, sh[-1]), k, padding=r).reshape(sh)
+
+    def step(self):
+        torch = self.torch
+        e = torch.randn(self.x.shape, generator=self.gen, device=self.device)
+        self.x = self.rho * self.x + float(np.sqrt(1 - self.rho ** 2)) * e
+        amp = self.base * torch.exp(0.25 * self.x)
+        Xr, Xc, Z = self.shape
+        v = torch.zeros(Xr * Xc * Z, dtype=torch.float32, device=self.device)
+        v.index_add_(0, self.idx, amp)
+        v = v.view(Z, Xc, Xr)                                   # column-major (Xr, Xc, Z)
+        v = self._blur_last(v, self.gl, self.rl)                # along Xr
+        v = self._blur_last(v.transpose(1, 2).contiguous(), self.gl, self.rl).transpose(1, 2)   # Xc
+        v = self._blur_last(v.permute(1, 2, 0).contiguous(), self.gz, self.rz).permute(2, 0, 1)  # Z
+        v = v.contiguous() + self.background
+        return v.permute(2, 1, 0)

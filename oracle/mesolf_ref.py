@@ -410,7 +410,11 @@ def sample_filter(X, F):
             img = X[:, :, z]
             s0 = img.sum()
             buf = freq_filter(img, F[:, :, idx[z]])
-            out[:, :, z] = s0 * buf / buf.sum()
+            sb = buf.sum()
+            # :233 divides by sum(buf); for an all-zero plane that is 0/0 = NaN in MATLAB.
+            # Kept as zero here (and in the CUDA filter): planes underflow to exact zero in
+            # FP32 long before FP64, and a NaN plane would poison every later iteration.
+            out[:, :, z] = s0 * buf / sb if sb != 0 else 0.0
     return out
 
 

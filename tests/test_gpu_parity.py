@@ -152,6 +152,19 @@ def test_sample_filter_matches_oracle(cuda, shape, Z):
     assert rel_l2(got, ref) <= 1e-6
 
 
+def test_sample_filter_zero_plane_stays_zero(cuda):
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver
+    w = synth.small_config(lenslets=(4, 3), K0=61, Z=5)
+    H, Ht = w.psf()
+    X = np.random.default_rng(4).uniform(0.5, 1.5, (60, 45, 5)).astype(np.float32)
+    X[:, :, 2] = 0.0
+    s = RLSolver(PhaseSpacePSF(H, Ht), (60, 45))
+    got = to_host(s.sample_filter(to_dev(X)))
+    assert np.isfinite(got).all() and not got[:, :, 2].any()
+    ref = R.sample_filter(X.astype(np.float64), R.nip_filter_bank(60, 45, 5, 15))
+    assert rel_l2(got, ref) <= 1e-6
+
+
 # ------------------------------------------------------------------------------ RL solve
 RL_CASES = [((5, 4), 61, 3, 2), ((4, 6), 91, 5, 2), ((3, 3), 231, 3, 1), ((8, 7), 61, 7, 3)]
 

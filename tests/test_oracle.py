@@ -220,3 +220,13 @@ def test_full_forward_equals_interleaved_phase_space_views():
         for v in range(15):
             lf[u::15, v::15] = R.forward_ps(Hps[:, :, u, v, :], vol * sums, 15)
     assert np.abs(lf - full).max() <= 1e-12 * np.abs(full).max()
+
+
+def test_sample_filter_zero_plane_stays_zero():
+    """An all-zero plane is passed as zeros (the reference's 0/0 would be NaN)."""
+    F = R.nip_filter_bank(30, 45, 5, 15)
+    X = np.random.default_rng(0).random((30, 45, 5))
+    X[:, :, 2] = 0.0
+    Y = R.sample_filter(X, F)
+    assert np.isfinite(Y).all() and not Y[:, :, 2].any()
+    assert np.allclose(Y[:, :, 1].sum(), X[:, :, 1].sum())
