@@ -118,6 +118,23 @@ int64_t mlf_psf_device_bytes(const mlf_psf* psf);
  * Synchronous when any pointer is host memory or stats != NULL. */
 int mlf_solver_create(mlf_psf* psf, int64_t Xr, int64_t Xc, mlf_solver** out);
 int mlf_solver_destroy(mlf_solver* s);
+/* Solver variants.  MLF_VARIANT_PEELING is the solve inside
+ * recon_theory_phase_space_LFM_with_filter_simple_peeling.m: filter bank of floor(Z/3)
+ * rounded down to even (:55-58) and the update X .* C ./ (D + 1e-10) (:149). */
+enum mlf_variant { MLF_VARIANT_BASE = 0, MLF_VARIANT_PEELING = 1 };
+int mlf_solver_create_variant(mlf_psf* psf, int64_t Xr, int64_t Xc, int32_t variant, mlf_solver** out);
+/* [Xguess, LFIMG, proj_sensor] = recon_theory_phase_space_LFM_with_filter_simple_peeling(
+ *     LFIMG, H, Ht, maxIter, gpuFlag, gpu_id)  (…_simple_peeling.m:13-266), on a solver made
+ * with MLF_VARIANT_PEELING: RL solve; forward-project the top plane and its >10 %-of-max
+ * mask with the normalised H (all N*N views); scale the projection to the image over the
+ * mask, subtract 0.9 of it from the image (clamped at 0); solve again from the flat guess;
+ * put the first solve's top plane back.  lfimg, vol_out (Xr x Xc x Z) and the optional
+ * lf_peeled_out / proj_sensor_out (Xr x Xc) are device pointers.  The top-plane
+ * projections run in FP32 for MLF_PREC_FP32 and on the tensor cores with both operands
+ * split (MLF_PREC_BF16X3) otherwise.  Stream-ordered; synchronous when stats != NULL. */
+int mlf_solver_run_peeling(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t precision,
+                           float* vol_out, float* lf_peeled_out, float* proj_sensor_out, mlf_stats* stats,
+                           void* stream);
 int64_t mlf_solver_device_bytes(const mlf_solver* s);
 int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t precision,
                    const float* warm_start, float* vol_out, mlf_stats* stats, void* stream);

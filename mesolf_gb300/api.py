@@ -139,12 +139,15 @@ class PhaseSpacePSF:
 class RLSolver:
     """Solve context for one image size (scratch volume, sub-aperture images, graphs)."""
 
-    def __init__(self, psf: PhaseSpacePSF, image_shape):
+    VARIANTS = {"base": 0, "peeling": 1}
+
+    def __init__(self, psf: PhaseSpacePSF, image_shape, variant="base"):
         lib = _lib.load()
         self.psf = psf
         self.Xr, self.Xc = int(image_shape[0]), int(image_shape[1])
+        self.variant = variant
         h = ctypes.c_void_p()
-        check(lib.mlf_solver_create(psf.handle, self.Xr, self.Xc, ctypes.byref(h)))
+        check(lib.mlf_solver_create_variant(psf.handle, self.Xr, self.Xc, self.VARIANTS[variant], ctypes.byref(h)))
         self._h = h
         self.last_stats = None
 
@@ -169,6 +172,21 @@ class RLSolver:
         self.last_stats = st.as_dict() if want_stats else None
         del lk, wk
         return out
+
+    def run_peeling(self, lfimg, max_iter, precision="fp32", stream=None, want_stats=True):
+        """The peeling solve (``…_with_filter_simple_peeling.m:13-266``) on a device image;
+        needs ``variant="peeling"``.  Returns (volume, peeled image, proj_sensor) on the device."""
+        lk, lp = _fortran(lfimg)
+        vol, vp = _empty_like_kind(lfimg, (self.Xr, self.Xc, self.psf.Z))
+        lf2, l2p = _empty_like_kind(lfimg, (self.Xr, self.Xc))
+        proj, pp = _empty_like_kind(lfimg, (self.Xr, self.Xc))
+        st = MLFStats()
+        check(_lib.load().mlf_solver_run_peeling(self._h, lp, int(max_iter), PRECISIONS[precision], vp, l2p, pp,
+                                                 ctypes.byref(st) if want_stats else None,
+                                                 _stream_of(lfimg, stream)))
+        self.last_stats = st.as_dict() if want_stats else None
+        del lk
+        return vol, lf2, proj
 
     def forward_view(self, vol, u, v, stream=None, precision="fp32"):
         """HX of view (u, v) (0-based) for a device volume -> (Xr/N, Xc/N) device array."""
@@ -353,3 +371,27 @@ def recon_theory_phase_space_LFM_with_filter(LFIMG, H, Ht, maxIter, gpuFlag=True
     finally:
         psf.close()
     return np.asarray(vol, dtype=np.float64)
+
+
+def recon_theory_phase_space_LFM_with_filter_simple_peeling(LFIMG, H_origin, Ht_origin, maxIter, gpuFlag=True,
+                                                            gpu_id=1, precision="fp32"):
+    """``[Xguess, LFIMG, proj_sensor] = recon_theory_phase_space_LFM_with_filter_simple_peeling(
+    LFIMG, H_origin, Ht_origin, maxIter, gpuFlag, gpu_id)`` (``…_simple_peeling.m:13``): host
+    float64 arrays out, as the reference gathers them.  ``gpuFlag`` must be true."""
+    if not gpuFlag:
+        raise _lib.MesoLFError(_lib.MLF_ERR_UNSUPPORTED,
+                               "gpuFlag=false: libmesolf_lf.so implements only the GPU path")
+    import torch
+    torch.cuda.set_device(int(gpu_id) - 1)
+    psf = PhaseSpacePSF(H_origin, Ht_origin)
+    try:
+        solver = RLSolver(psf, np.shape(LFIMG), variant="peeling")
+        try:
+            lf = _fortran(torch.as_tensor(np.ascontiguousarray(np.asarray(LFIMG, np.float32))).cuda())[0]
+            vol, lf2, proj = solver.run_peeling(lf, maxIter, precision=precision)
+            out = tuple(x.double().cpu().numpy() for x in (vol, lf2, proj))
+        finally:
+            solver.close()
+    finally:
+        psf.close()
+    return out

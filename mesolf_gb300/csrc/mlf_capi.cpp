@@ -250,6 +250,39 @@ int mlf_solver_create(mlf_psf* psf, int64_t Xr, int64_t Xc, mlf_solver** out) {
   return MLF_OK;
 }
 
+int mlf_solver_create_variant(mlf_psf* psf, int64_t Xr, int64_t Xc, int32_t variant, mlf_solver** out) {
+  clear_error();
+  if (variant != MLF_VARIANT_BASE && variant != MLF_VARIANT_PEELING)
+    return fail(MLF_ERR_INVALID, "mlf_solver_create_variant: unknown variant");
+  if (!psf || !out) return fail(MLF_ERR_INVALID, "mlf_solver_create_variant: null pointer");
+  *out = nullptr;
+  if (Xr < psf->N || Xc < psf->N || Xr % psf->N || Xc % psf->N)
+    return fail(MLF_ERR_INVALID, "mlf_solver_create_variant: image sides must be positive multiples of Nnum");
+  std::unique_ptr<mlf_solver> s(new mlf_solver());
+  s->psf = psf;
+  s->Xr = Xr;
+  s->Xc = Xc;
+  s->variant = variant;
+  MLF_TRY(current_device(&s->device));
+  if (s->device != psf->device) return fail(MLF_ERR_INVALID, "mlf_solver_create_variant: PSF lives on another device");
+  MLF_TRY(solver_init(s.get()));
+  *out = s.release();
+  return MLF_OK;
+}
+
+int mlf_solver_run_peeling(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t precision, float* vol_out,
+                           float* lf_peeled_out, float* proj_sensor_out, mlf_stats* stats, void* stream) {
+  clear_error();
+  if (!s || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: null pointer");
+  if (max_iter < 0) return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: maxIter must be >= 0");
+  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2)
+    return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: unknown precision");
+  for (const void* p : {(const void*)lfimg, (const void*)vol_out, (const void*)lf_peeled_out, (const void*)proj_sensor_out})
+    if (p && !is_device_ptr(p)) return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: device pointers required");
+  return peel_solve(s, lfimg, max_iter, precision, vol_out, lf_peeled_out, proj_sensor_out, stats,
+                    static_cast<cudaStream_t>(stream));
+}
+
 int mlf_solver_destroy(mlf_solver* s) {
   clear_error();
   delete s;

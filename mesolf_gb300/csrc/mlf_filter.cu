@@ -262,8 +262,14 @@ int filter_init(Solver* s) {
   FilterPlan& f = s->filt;
   const int Z = s->Z, N = s->N;
   // omega_NIP_array and the plane -> bank-entry map, recon_…_with_filter.m:21-26,54-56,224-231
+  // base: ceil(Z/3) rounded up to even; peeling variant (…_simple_peeling.m:55-58): floor(Z/3)
+  // rounded down to even
   int R = (int)std::ceil(Z / 3.0);
   if (R % 2 == 1) R += 1;
+  if (s->variant == MLF_VARIANT_PEELING) {
+    R = Z / 3;
+    if (R % 2 == 1) R -= 1;
+  }
   const int nb = 3 * R;
   std::vector<double> om(nb);
   for (int i = 0; i < nb; ++i) {

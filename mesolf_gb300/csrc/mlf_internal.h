@@ -119,6 +119,7 @@ struct FilterPlan {
 struct Solver {
   Psf* psf = nullptr;
   int device = 0;
+  int variant = MLF_VARIANT_BASE;  // MLF_VARIANT_PEELING: floor-rounded filter bank, D + 1e-10
   int64_t Xr = 0, Xc = 0;
   int N = 0, Z = 0, Li = 0, Lj = 0, q = 0, T = 0;
   int Pa = 0;          // row pitch (floats) of a phase-major plane (FP32 kernels)
@@ -168,6 +169,10 @@ int launch_scatter_views(const float* lfs, const PatchGeo& g, float* d_lf, int64
                          cudaStream_t st);
 int forward_project(Solver* s, const float* d_vol, float* d_lf, const float* d_zscale, int precision,
                     cudaStream_t st);
+// the peeling variant's two solves and top-plane peel (…_simple_peeling.m:13-266)
+int peel_solve(Solver* s, const float* d_lf, int max_iter, int precision, float* d_out, float* d_lf_peeled,
+               float* d_proj, mlf_stats* stats, cudaStream_t st);
+inline float solver_d_eps(const Solver* s) { return s->variant == MLF_VARIANT_PEELING ? 1e-10f : 0.f; }
 int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st);
 // flat initial guess sum(lf)/(Xr*Xc*Z) on the patch's planes, 0 on the other channels
 int launch_init_flat(const float* d_lf, const PatchGeo& g, float* X, double* scratch, cudaStream_t st);
@@ -216,6 +221,7 @@ struct ViewArgs {
   const int* rngA;     // [3][maxc][2]
   const int* rngB;     // [3][maxc][2]
   float w;             // view weight
+  float d_eps;         // added to D in the update (1e-10 in the peeling variant, else 0)
   int u, v;            // current view (backward / update)
   int do_fwd;          // MODE_STEP: also project with wf
   int N, Z, Li, Lj, Pa, q;

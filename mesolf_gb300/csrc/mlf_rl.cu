@@ -104,6 +104,88 @@ __global__ void k_extract_views(const float* __restrict__ lf, PatchGeo g, float*
   }
 }
 
+// ---- top-plane peeling (…_simple_peeling.m:183-205)
+constexpr int kPeelBlocks = 256;
+
+__global__ void k_max_partial(const float* __restrict__ a, int64_t n, float* part) {
+  __shared__ float sh[32];
+  float m = -INFINITY;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, a[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) m = fmaxf(m, sh[i]);
+    part[blockIdx.x] = fmaxf(m, sh[0]);
+  }
+}
+
+// sum(m .* a) and sum(m .* b) per block (FP64), into part[blockIdx] and part[gridDim + blockIdx]
+__global__ void k_dot2_partial(const float* __restrict__ m, const float* __restrict__ a,
+                               const float* __restrict__ b, int64_t n, double* part) {
+  __shared__ double sh[2][32];
+  double sa = 0.0, sb = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    sa += (double)m[i] * a[i];
+    sb += (double)m[i] * b[i];
+  }
+  sa = warp_sum_d(sa);
+  sb = warp_sum_d(sb);
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = sa;
+    sh[1][threadIdx.x >> 5] = sb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ra = 0.0, rb = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+      ra += sh[0][i];
+      rb += sh[1][i];
+    }
+    part[blockIdx.x] = ra;
+    part[gridDim.x + blockIdx.x] = rb;
+  }
+}
+
+// plane 0 of the mask volume: top > 0.1 * max(top)   (:190)
+__global__ void k_peel_mask(const float* __restrict__ top, int64_t n, const float* maxpart, int nb,
+                            float* __restrict__ vol) {
+  __shared__ float thr;
+  if (threadIdx.x == 0) {
+    float m = -INFINITY;
+    for (int i = 0; i < nb; ++i) m = fmaxf(m, maxpart[i]);
+    thr = (float)((double)m * 0.1);
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    vol[i] = top[i] > thr ? 1.f : 0.f;
+}
+
+// proj *= sum(pm .* LF) / sum(pm .* proj) with pm = projm / sum(projm)  (:195-199);
+// LF2 = max(LF - 0.9 * proj, 0)  (:202-203)
+__global__ void k_peel_apply(const float* __restrict__ lf, const float* __restrict__ proj, int64_t n,
+                             const double* sum_m, const double* dots, int nb, float* __restrict__ lf2,
+                             float* __restrict__ proj_out) {
+  __shared__ float scale;
+  if (threadIdx.x == 0) {
+    double sm = 0.0, a = 0.0, b = 0.0;
+    for (int i = 0; i < nb; ++i) {
+      sm += sum_m[i];
+      a += dots[i];
+      b += dots[nb + i];
+    }
+    scale = (float)((a / sm) / (b / sm));
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float p = proj[i] * scale;
+    proj_out[i] = p;
+    const float r = lf[i] - p * 0.9f;
+    lf2[i] = r < 0.f ? 0.f : r;
+  }
+}
+
 // Inverse of k_extract_views: LF(u + N*a, v + N*b) = lfs[(u + N*v) * view_stride + off + b*Li + a].
 __global__ void k_scatter_views(const float* __restrict__ lfs, PatchGeo g, float* __restrict__ lf,
                                 int64_t view_stride, int64_t off) {
@@ -174,6 +256,7 @@ ViewArgs view_args(Solver* s) {
   a.clsB = cls + 3 * s->Li;
   a.rngA = cls + 3 * s->Li + 3 * s->Lj;
   a.rngB = a.rngA + 3 * s->maxc * 2;
+  a.d_eps = solver_d_eps(s);
   a.N = s->N; a.Z = s->Z; a.Li = s->Li; a.Lj = s->Lj; a.Pa = s->Pa; a.q = s->q;
   a.plane = s->plane; a.nch = s->nch;
   a.tilesA = s->tilesA; a.tilesB = s->tilesB; a.tps = s->tps; a.slots = s->slots;
@@ -512,6 +595,7 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
 }
 
 int forward_view(Solver* s, const float* d_vol, int u, int v, float* d_hx, cudaStream_t st) {
+  MLF_CUDA(cudaMemsetAsync(s->Xtmp.p, 0, s->Xtmp.bytes, st));  // zero row padding (see forward_project)
   MLF_TRY(launch_to_phase(d_vol, solver_geo(s), s->Xtmp.as<float>(), st));
   ViewArgs a = view_args(s);
   a.X = s->Xtmp.as<float>();
@@ -536,6 +620,8 @@ int forward_project(Solver* s, const float* d_vol, float* d_lf, const float* d_z
   const PatchGeo g = solver_geo(s);
   const int N = s->N;
   const int64_t LL = (int64_t)s->Li * s->Lj;
+  // the scratch's row padding must be zero (the filter also uses it, in another layout)
+  MLF_CUDA(cudaMemsetAsync(s->Xtmp.p, 0, s->Xtmp.bytes, st));
   MLF_TRY(launch_to_phase(d_vol, g, s->Xtmp.as<float>(), st, d_zscale));
   for (int view = 0; view < N * N; ++view) {
     ViewArgs a = view_args(s);
@@ -547,6 +633,55 @@ int forward_project(Solver* s, const float* d_vol, float* d_lf, const float* d_z
     MLF_TRY(run_reduce(s, view, s->lfs.as<float>() + view * LL, false, st));
   }
   return launch_scatter_views(s->lfs.as<float>(), g, d_lf, LL, 0, st);
+}
+
+int peel_solve(Solver* s, const float* d_lf, int max_iter, int precision, float* d_out, float* d_lf_peeled,
+               float* d_proj, mlf_stats* stats, cudaStream_t st) {
+  if (s->variant != MLF_VARIANT_PEELING)
+    return fail(MLF_ERR_INVALID, "peeling solve needs a solver created with MLF_VARIANT_PEELING");
+  const int64_t n_img = s->Xr * s->Xc, n_vol = n_img * s->Z;
+  DevBuf top, vol, proj, projm, lf2, proj_out, part;
+  MLF_TRY(top.alloc(n_img * 4, "peeling top plane"));
+  MLF_TRY(vol.alloc(n_vol * 4, "peeling volume"));
+  MLF_TRY(proj.alloc(n_img * 4, "peeling projection"));
+  MLF_TRY(projm.alloc(n_img * 4, "peeling projection"));
+  MLF_TRY(lf2.alloc(n_img * 4, "peeled image"));
+  MLF_TRY(proj_out.alloc(n_img * 4, "peeling projection"));
+  MLF_TRY(part.alloc(sizeof(double) * 3 * kPeelBlocks + sizeof(float) * kPeelBlocks, "peeling sums"));
+  double* sum_m = part.as<double>();
+  double* dots = sum_m + kPeelBlocks;
+  float* maxp = reinterpret_cast<float*>(dots + 2 * kPeelBlocks);
+  const int fprec = precision == MLF_PREC_FP32 ? MLF_PREC_FP32 : MLF_PREC_BF16X3;
+
+  mlf_stats s1{};
+  MLF_TRY(solver_run(s, d_lf, max_iter, precision, nullptr, d_out, stats ? &s1 : nullptr, st));  // :118-172
+  MLF_CUDA(cudaMemcpyAsync(top.p, d_out, n_img * 4, cudaMemcpyDeviceToDevice, st));              // :183
+  MLF_CUDA(cudaMemsetAsync(vol.p, 0, n_vol * 4, st));
+  MLF_CUDA(cudaMemcpyAsync(vol.p, top.p, n_img * 4, cudaMemcpyDeviceToDevice, st));              // :184-185
+  MLF_TRY(forward_project(s, vol.as<float>(), proj.as<float>(), nullptr, fprec, st));            // :191
+  k_max_partial<<<kPeelBlocks, 256, 0, st>>>(top.as<float>(), n_img, maxp);
+  k_peel_mask<<<grid_for(n_img), 256, 0, st>>>(top.as<float>(), n_img, maxp, kPeelBlocks, vol.as<float>());
+  MLF_LAUNCHED();
+  MLF_TRY(forward_project(s, vol.as<float>(), projm.as<float>(), nullptr, fprec, st));           // :193
+  k_sum_partial<<<kPeelBlocks, 256, 0, st>>>(projm.as<float>(), n_img, sum_m);
+  k_dot2_partial<<<kPeelBlocks, 256, 0, st>>>(projm.as<float>(), d_lf, proj.as<float>(), n_img, dots);
+  k_peel_apply<<<grid_for(n_img), 256, 0, st>>>(d_lf, proj.as<float>(), n_img, sum_m, dots, kPeelBlocks,
+                                               lf2.as<float>(), proj_out.as<float>());
+  MLF_LAUNCHED();
+  MLF_TRY(solver_run(s, lf2.as<float>(), max_iter, precision, nullptr, d_out, stats, st));       // :208-257
+  MLF_CUDA(cudaMemcpyAsync(d_out, top.p, n_img * 4, cudaMemcpyDeviceToDevice, st));              // :262
+  if (d_lf_peeled) MLF_CUDA(cudaMemcpyAsync(d_lf_peeled, lf2.p, n_img * 4, cudaMemcpyDeviceToDevice, st));
+  if (d_proj) MLF_CUDA(cudaMemcpyAsync(d_proj, proj_out.p, n_img * 4, cudaMemcpyDeviceToDevice, st));
+  if (stats) {
+    stats->gpu_ms += s1.gpu_ms;
+    stats->iterations += s1.iterations;
+    stats->view_kernel_ms += s1.view_kernel_ms;
+    stats->view_kernel_launches += s1.view_kernel_launches;
+    stats->kernel_launches += s1.kernel_launches + 9 + 2 * (int64_t)s->N * s->N * 2;
+  }
+  // the scratch buffers are released on return: wait for the work that reads them
+  MLF_CUDA(cudaStreamSynchronize(st));
+  return MLF_OK;
 }
 
 int forward_view_prec(Solver* s, const float* d_vol, int u, int v, int precision, float* d_hx, cudaStream_t st) {

@@ -77,6 +77,7 @@ struct TcBwdArgs {
   int use_alo;                      // add ARl * Wbh to C (activation split)
   int use_blo;                      // add ARh * Wbl to C and A1 * Wbl to D (tap split)
   int write_lo;                     // also emit the lo half of Xb
+  float d_eps;                      // added to D (peeling variant)
 };
 
 constexpr int BWD_BN = 128;                            // channels per tile
@@ -288,7 +289,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
           const int zr = (chb + j) % a.Zch - pz0;
           if (pos_ok && chb + j < a.nch && zr >= 0 && zr < pnz) {
             const float xo = *xp;
-            float xc = __fdividef(xo * cv[j], dv[j]);      // :130  X .* C ./ D
+            float xc = __fdividef(xo * cv[j], dv[j] + a.d_eps);   // :130  X .* C ./ D
             if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;       // :132-134
             xn = xc * wv + (1.f - wv) * xo;                // :136
             if (xn < 0.f) xn = 0.f;                        // :137
@@ -642,6 +643,7 @@ struct TcPsfState {
 // patch, the BF16 operand buffers, the union view order and per-patch view weights.
 struct TcSolverState {
   int P = 0, MP = 0, Zch = 0, splits = 1, ks_per_split = 0, KSF = 0, nsm = 0;
+  float d_eps = 0.f;  // the members' variant (all the same)
   std::vector<int> pos0, Li, Lj, LL, z0, nz;
   std::vector<int> views;   // union of the patches' active views, spiral order
   std::vector<float> wtab;  // [views][P]
@@ -760,6 +762,7 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   std::unique_ptr<TcSolverState> t(new TcSolverState());
   t->P = (int)members.size();
   t->Zch = psf->Z;
+  t->d_eps = solver_d_eps(members[0]);
   int off = 0;
   std::vector<int> info(8 * t->P, 0), tiles;
   for (int p = 0; p < t->P; ++p) {
@@ -919,6 +922,7 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   a.use_alo = alo;
   a.use_blo = blo;
   a.write_lo = alo;
+  a.d_eps = t->d_eps;
   const int mt = t->MP / BM, nt = tp->CHP / BWD_BN;
   const int grid = std::min(mt * nt, t->nsm);
   k_tc_bwd<<<grid, BWD_THREADS, bwd_smem_bytes(alo, blo), st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl,

@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
               const float c = acc[y][x];
               const float d = dtab[cb * A.maxc + __ldg(cA + a)];
               const float xo = xrow[x];
-              float xc = xo * c / d;                       // :130  X .* C ./ D
+              float xc = xo * c / (d + A.d_eps);           // :130  X .* C ./ D
               if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;     // :132-134 NaN, Inf, < 0
               float xn = xc * A.w + (1.f - A.w) * xo;       // :136
               if (xn < 0.f) xn = 0.f;                      // :137

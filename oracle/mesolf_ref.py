@@ -191,12 +191,20 @@ def view_weights(Hps):
 
 
 # ----------------------------------------------------------------------------- a5
-def nip_omegas(Z, N):
-    """``omega_NIP_array`` of ``recon_theory_phase_space_LFM_with_filter.m:21-26,54-56``."""
+def nip_omegas(Z, N, variant="base"):
+    """``omega_NIP_array`` of ``recon_theory_phase_space_LFM_with_filter.m:21-26,54-56``.
+
+    ``variant="peeling"``: ``…_with_filter_simple_peeling.m:55-58`` takes ``floor(Z/3)``
+    rounded DOWN to even instead of ``ceil(Z/3)`` rounded up."""
     omega_NIP = N - 7
-    R = int(math.ceil(Z / 3))
-    if R % 2 == 1:
-        R += 1
+    if variant == "peeling":
+        R = Z // 3
+        if R % 2 == 1:
+            R -= 1
+    else:
+        R = int(math.ceil(Z / 3))
+        if R % 2 == 1:
+            R += 1
     nb = 3 * R
     axis = np.arange(1, nb + 1, dtype=np.float64) - nb / 2
     om = omega_NIP * np.exp(-(axis / 100.0 * 2 * np.sqrt(np.log(2))) ** 2)
@@ -204,13 +212,13 @@ def nip_omegas(Z, N):
     return om
 
 
-def nip_filter_bank(size_h, size_w, Z, N):
+def nip_filter_bank(size_h, size_w, Z, N, variant="base"):
     """Literal filter bank, ``recon_theory_phase_space_LFM_with_filter.m:44-61``.
 
     ``F_i = |fftshift(fft2(exp(-((xx/w_i)^2+(yy/w_i)^2))))| / max`` on the grid
     ``x=(1:size_h)-size_h/2``, ``y=(1:size_w)-size_w/2``.  Returns (size_h, size_w, 3R).
     """
-    om = nip_omegas(Z, N)
+    om = nip_omegas(Z, N, variant)
     x = np.arange(1, size_h + 1, dtype=np.float64) - size_h / 2
     y = np.arange(1, size_w + 1, dtype=np.float64) - size_w / 2
     yy, xx = np.meshgrid(y, x)
@@ -379,10 +387,11 @@ def backward_ps(t_uv, R, u, v, N):
 
 
 # ----------------------------------------------------------------------------- a14
-def rl_update(X, C, D, w):
-    """Multiplicative update, ``…_with_filter.m:130-137``."""
+def rl_update(X, C, D, w, d_eps=0.0):
+    """Multiplicative update, ``…_with_filter.m:130-137``.  ``d_eps=1e-10`` is the peeling
+    variant's ``Xguess .* XguessCor ./ (buf + 1e-10)`` (``…_simple_peeling.m:149``)."""
     with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
-        Xc = X * C / D
+        Xc = X * C / (D + d_eps)
     Xc[np.isnan(Xc)] = 0
     Xc[np.isinf(Xc)] = 0
     Xc[Xc < 0] = 0
@@ -426,16 +435,16 @@ def _ratio(LF_sub, HX):
     return R
 
 
-def rl_view_step(X, LFIMG, Hps, Htc, u, v, w, N):
+def rl_view_step(X, LFIMG, Hps, Htc, u, v, w, N, d_eps=0.0):
     """One view of the inner loop (``…_with_filter.m:109-137``), 0-based (u, v)."""
     HX = forward_ps(Hps[:, :, u, v, :], X, N)
     R = _ratio(LFIMG[u::N, v::N], HX)
     C = backward_ps(Htc[:, :, u, v, :], R, u, v, N)
     D = backward_ps(Htc[:, :, u, v, :], np.ones_like(R), u, v, N)
-    return rl_update(X, C, D, w)
+    return rl_update(X, C, D, w, d_eps)
 
 
-def recon_phase_space(LFIMG, H, Ht, maxIter, X0=None, callback=None, view_step=None):
+def recon_phase_space(LFIMG, H, Ht, maxIter, X0=None, callback=None, view_step=None, variant="base"):
     """``recon_theory_phase_space_LFM_with_filter`` (``…_with_filter.m:10-151``), FP64.
 
     ``X0`` (optional) replaces the flat initial guess of ``:72-73`` (warm start).
@@ -449,7 +458,8 @@ def recon_phase_space(LFIMG, H, Ht, maxIter, X0=None, callback=None, view_step=N
     Hps, Htc = gen_phasespace_psf(Hn, Htn)                           # :17
     N = Hps.shape[2]
     w = view_weights(Hps)                                            # :20-40
-    F = nip_filter_bank(LFIMG.shape[0], LFIMG.shape[1], Hps.shape[4], N)   # :44-61
+    F = nip_filter_bank(LFIMG.shape[0], LFIMG.shape[1], Hps.shape[4], N, variant)   # :44-61
+    d_eps = 1e-10 if variant == "peeling" else 0.0
     Z = Hps.shape[4]
     if X0 is None:
         X = np.ones((LFIMG.shape[0], LFIMG.shape[1], Z))
@@ -465,13 +475,52 @@ def recon_phase_space(LFIMG, H, Ht, maxIter, X0=None, callback=None, view_step=N
                 if w[u, v] == 0:
                     continue
                 if view_step is None:
-                    X = rl_view_step(X, LFIMG, Hps, Htc, u, v, w[u, v], N)
+                    X = rl_view_step(X, LFIMG, Hps, Htc, u, v, w[u, v], N, d_eps)
                 else:
                     X = view_step(Hps[:, :, u, v, :], Htc[:, :, u, v, :], LFIMG, X, u, v, w[u, v], N)
         X = sample_filter(X, F)                                      # :142
         if callback is not None:
             callback(it, X)
     return X
+
+
+# ----------------------------------------------------------------------------- a16
+PEEL_MASK_RATIO = 0.1     # …_simple_peeling.m:32
+PEEL_REDUCE_RATIO = 0.9   # …_simple_peeling.m:33
+
+
+def recon_phase_space_peeling(LFIMG, H, Ht, maxIter):
+    """``recon_theory_phase_space_LFM_with_filter_simple_peeling`` (``…_simple_peeling.m:13-266``),
+    FP64.  Returns ``(Xguess, LFIMG_peeled, proj_sensor)``.
+
+    As written the reference normalises ``size(H, 5)`` planes before ``H`` exists (:22) and
+    cuts weights at an undefined ``weight_cut`` (:44); this restatement normalises every
+    plane of ``H_origin`` / ``Ht_origin`` and uses the base solver's cut, 0.2
+    (``…_with_filter.m:20``).  The two RL runs differ from the base solver by the
+    ``floor``-rounded filter bank (:55-58) and ``D + 1e-10`` (:149).  Peeling (:183-205): the
+    top plane of the first run and its >10 %-of-max mask are forward-projected with the
+    normalised H (``forwardProjectGPU``, :330-348); the projection is scaled so that its
+    mask-weighted sum matches the image's, 0.9 of it is subtracted from the image (clamped
+    at 0), the second run starts again from the flat guess, and its top plane is replaced by
+    the first run's (:262).
+    """
+    LFIMG = np.asarray(LFIMG, dtype=np.float64)
+    Hn, _ = normalize_psf(H, Ht)
+    X1 = recon_phase_space(LFIMG, H, Ht, maxIter, variant="peeling")
+    top = X1[:, :, 0].copy()
+    dummy = np.zeros_like(X1)
+    dummy[:, :, 0] = top
+    mask = np.zeros_like(X1)
+    mask[:, :, 0] = top > top.max() * PEEL_MASK_RATIO
+    proj = forward_project_full(Hn, dummy)
+    projm = forward_project_full(Hn, mask)
+    projm = projm / projm.sum()
+    proj = proj * (projm * LFIMG).sum() / (projm * proj).sum()
+    LF2 = LFIMG - proj * PEEL_REDUCE_RATIO
+    LF2[LF2 < 0] = 0
+    X2 = recon_phase_space(LF2, H, Ht, maxIter, variant="peeling")
+    X2[:, :, 0] = top
+    return X2, LF2, proj
 
 
 # ----------------------------------------------------------------------------- a18

@@ -55,3 +55,21 @@ def test_batch_forward_project_matches_single(cuda):
     for k, ((z0, nz), v) in enumerate(zip(planes, vols)):
         ref = R.forward_project_full(H[:, :, :, :, z0:z0 + nz], v)
         assert rel_l2(outs[k], ref) <= 1e-5, (k, rel_l2(outs[k], ref))
+
+
+def test_forward_project_after_solve_on_same_solver(cuda):
+    """The FP32 projector's staging buffer is also the filter's scratch; projecting after
+    a solve on the same context must give the same image as on a fresh one."""
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver
+    w = synth.small_config(lenslets=(5, 4), K0=61, Z=5, seed=6)
+    H, Ht = w.psf()
+    vol = w.volume()
+    psf = PhaseSpacePSF(H, Ht)
+    s = RLSolver(psf, vol.shape[:2])
+    fresh = s.forward_project(to_dev(vol)).cpu().numpy()
+    s.run(to_dev(w.measured(H, vol)), 1)
+    again = s.forward_project(to_dev(vol)).cpu().numpy()
+    hx = s.forward_view(to_dev(vol), 3, 11).cpu().numpy()
+    norm = s.forward_project(to_dev(vol), raw_psf=False).cpu().numpy()
+    assert np.array_equal(fresh, again)
+    assert np.array_equal(hx, norm[3::15, 11::15])

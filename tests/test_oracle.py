@@ -230,3 +230,10 @@ def test_sample_filter_zero_plane_stays_zero():
     Y = R.sample_filter(X, F)
     assert np.isfinite(Y).all() and not Y[:, :, 2].any()
     assert np.allclose(Y[:, :, 1].sum(), X[:, :, 1].sum())
+
+
+def test_peeling_filter_bank_rounds_down():
+    """…_simple_peeling.m:55-58: floor(Z/3) rounded down to even (base: ceil, up)."""
+    assert R.nip_omegas(51, 15).size == 54 and R.nip_omegas(51, 15, "peeling").size == 48
+    assert R.nip_omegas(21, 15).size == 24 and R.nip_omegas(21, 15, "peeling").size == 18
+    assert R.nip_omegas(7, 15, "peeling").size == 6
