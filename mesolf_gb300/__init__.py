@@ -7,7 +7,9 @@ the seeded synthetic workload generators.
 from ._lib import MesoLFError, load as load_library  # noqa: F401
 from .api import (BatchSolver, PhaseSpacePSF, RLSolver, mex_lfm_convolution_vec,  # noqa: F401
                   recon_theory_phase_space_LFM_with_filter,
-                  recon_theory_phase_space_LFM_with_filter_simple_peeling)
+                  recon_theory_phase_space_LFM_with_filter_simple_peeling, forwardProjectGPU,
+                  forwardProjectACC, forwardProjectGPU_discrete, forwardProjectGPU_skip_2D)
 
 __all__ = ["MesoLFError", "load_library", "BatchSolver", "PhaseSpacePSF", "RLSolver", "mex_lfm_convolution_vec",
-           "recon_theory_phase_space_LFM_with_filter", "recon_theory_phase_space_LFM_with_filter_simple_peeling"]
+           "recon_theory_phase_space_LFM_with_filter", "recon_theory_phase_space_LFM_with_filter_simple_peeling",
+           "forwardProjectGPU", "forwardProjectACC", "forwardProjectGPU_discrete", "forwardProjectGPU_skip_2D"]

@@ -395,3 +395,103 @@ def recon_theory_phase_space_LFM_with_filter_simple_peeling(LFIMG, H_origin, Ht_
     finally:
         psf.close()
     return out
+
+
+# ----------------------------------------------------------------------------- full forward projectors
+def phase_space_kept_mask(K0, N):
+    """(K0, K0, N, N) bool: the PSF pixels that the phase-space realignment keeps
+    (``gen_phasespace_PSF_theory.m:8-27``: crop to S = K0 - mod(K0 - N, 2N) starting at
+    i1 = round(K0/2) - fix(S/2), then shift slice (a, b) by (a - h, b - h), h = (N-1)/2, with
+    zero fill).  Projections through the phase-space operator equal the reference's
+    full-resolution sums exactly when every PSF pixel outside this mask is zero."""
+    S = K0 - (K0 - N) % (2 * N)
+    i1 = int(np.floor(K0 / 2 + 0.5)) - S // 2 - 1
+    h = (N - 1) // 2
+    idx = np.arange(K0)
+    rows = np.zeros((K0, N), bool)
+    for a in range(N):
+        lo = i1 + max(0, h - a)
+        hi = i1 + S - 1 - max(0, a - h)
+        rows[:, a] = (idx >= lo) & (idx <= hi)
+    return rows[:, None, :, None] & rows[None, :, None, :]
+
+
+def _project_full(H, vol, precision):
+    import warnings
+
+    import torch
+    H = np.asfortranarray(np.asarray(H, np.float32))
+    K0, N = H.shape[0], H.shape[2]
+    keep = phase_space_kept_mask(K0, N)
+    if np.any(H[~keep[..., None].repeat(H.shape[4], axis=4)] != 0):
+        warnings.warn("PSF has support outside the phase-space crop; those pixels are not projected",
+                      RuntimeWarning, stacklevel=3)
+    psf = PhaseSpacePSF(H, np.asfortranarray(H[::-1, ::-1]))
+    try:
+        s = RLSolver(psf, vol.shape[:2])
+        try:
+            v = _fortran(torch.as_tensor(np.ascontiguousarray(np.asarray(vol, np.float32))).cuda())[0]
+            lf = s.forward_project(v, raw_psf=True, precision=precision)
+            return lf.double().cpu().numpy()
+        finally:
+            s.close()
+    finally:
+        psf.close()
+
+
+def forwardProjectGPU(H, realspace, precision="fp32"):
+    """``TOTALprojection = forwardProjectGPU(H, realspace, ...)`` (``src/recon/forwardProjectGPU.m:1-20``):
+    ``sum_{a,b,z} conv2(realspace_z .* [phase (a, b)], H(:,:,a,b,z), 'same')``, host float64 out."""
+    return _project_full(H, realspace, precision)
+
+
+def forwardProjectACC(H, realspace, CAindex, precision="fp32"):
+    """``forwardProjectACC(H, realspace, CAindex)`` (``src/recon/forwardProjectACC.m:1-18``): the
+    PSF of plane z cropped to rows / columns ``CAindex(z,1):CAindex(z,2)`` (1-based) before the
+    'same' convolution.  The crop must be centred on the PSF (the 'same' centre of the
+    cropped kernel is then the PSF centre), which is how MesoLF builds CAindex."""
+    H = np.asarray(H, np.float32)
+    K0 = H.shape[0]
+    Hc = np.zeros_like(H, order="F")
+    for z in range(H.shape[4]):
+        lo, hi = int(CAindex[z][0]) - 1, int(CAindex[z][1])
+        if (lo + (hi - lo) // 2) != K0 // 2:
+            raise ValueError(f"CAindex row {z}: crop [{lo + 1}, {hi}] is not centred on the {K0}-px PSF")
+        Hc[lo:hi, lo:hi, :, :, z] = H[lo:hi, lo:hi, :, :, z]
+    return _project_full(Hc, realspace, precision)
+
+
+def forwardProjectGPU_discrete(H, realspace, unique_array, max_PSF_size, precision="fp32"):
+    """``forwardProjectGPU_discrete(H, realspace, ..., unique_array, max_PSF_size)``
+    (``src/recon/forwardProjectGPU_discrete.m:1-20``): volume plane cc is projected with PSF
+    plane ``unique_array(cc)`` (1-based) cropped to the central ``2*floor(max_PSF_size/2)+1``
+    pixels.  Planes sharing a PSF plane are summed first (the projection is linear)."""
+    H = np.asarray(H, np.float32)
+    K0 = H.shape[0]
+    half = int(max_PSF_size) // 2
+    c = int(np.ceil(K0 / 2)) - 1
+    zs = sorted(set(int(u) - 1 for u in np.ravel(unique_array)))
+    Hc = np.zeros(H.shape[:4] + (len(zs),), np.float32, order="F")
+    lo, hi = max(0, c - half), min(K0, c + half + 1)
+    vol = np.asarray(realspace, np.float64)
+    v2 = np.zeros(vol.shape[:2] + (len(zs),))
+    for k, z in enumerate(zs):
+        Hc[lo:hi, lo:hi, :, :, k] = H[lo:hi, lo:hi, :, :, z]
+    for cc, u in enumerate(np.ravel(unique_array)):
+        v2[:, :, zs.index(int(u) - 1)] += vol[:, :, cc]
+    return _project_full(Hc, v2, precision)
+
+
+def forwardProjectGPU_skip_2D(H, realspace, step, cc, precision="fp32"):
+    """``forwardProjectGPU_skip_2D(H, realspace, ..., step, cc)``
+    (``src/recon/forwardProjectGPU_skip_2D.m:1-16``): a 2-D image projected with PSF plane
+    ``cc`` (1-based), only the pixels whose lenslet phase (a, b) has ``a, b = 1, 1+step, ...``."""
+    H = np.asarray(H, np.float32)
+    N = H.shape[2]
+    img = np.asarray(realspace, np.float64)
+    keep = np.zeros(img.shape, bool)
+    for a in range(0, N, int(step)):
+        for b in range(0, N, int(step)):
+            keep[a::N, b::N] = True
+    Hz = np.asfortranarray(H[:, :, :, :, int(cc) - 1:int(cc)])
+    return _project_full(Hz, np.where(keep, img, 0.0)[:, :, None], precision)

@@ -620,3 +620,37 @@ def forward_project_full(H, vol, CAindex=None):
         full = np.fft.irfft2(acc, E)
         out += full[m:m + Xr, m:m + Xc]
     return out
+
+
+def forward_project_discrete(H, vol, unique_array, max_PSF_size):
+    """``forwardProjectGPU_discrete.m:1-20``: plane cc projected with PSF plane
+    ``unique_array(cc)`` (1-based), cropped to ``ceil(end/2) -/+ floor(max_PSF_size/2)``."""
+    H = np.asarray(H, dtype=np.float64)
+    K0 = H.shape[0]
+    half = int(max_PSF_size) // 2
+    c = int(math.ceil(K0 / 2))                      # 1-based centre
+    lo, hi = c - half - 1, c + half                 # 0-based [lo, hi)
+    out = 0.0
+    for cc, u in enumerate(np.ravel(unique_array)):
+        Hz = H[lo:hi, lo:hi, :, :, int(u) - 1:int(u)]
+        out = out + forward_project_full(Hz, np.asarray(vol, dtype=np.float64)[:, :, cc:cc + 1])
+    return out
+
+
+def forward_project_skip_2d(H, img, step, cc):
+    """``forwardProjectGPU_skip_2D.m:1-16``: 2-D image, PSF plane ``cc`` (1-based), phases
+    ``aa, bb = 1:step:Nnum`` only."""
+    H = np.asarray(H, dtype=np.float64)
+    N = H.shape[2]
+    img = np.asarray(img, dtype=np.float64)
+    Xr, Xc = img.shape
+    S = H.shape[0]
+    m = S // 2
+    E = (Xr + S - 1, Xc + S - 1)
+    acc = np.zeros((E[0], E[1] // 2 + 1), dtype=np.complex128)
+    for a in range(0, N, int(step)):
+        for b in range(0, N, int(step)):
+            ts = np.zeros((Xr, Xc))
+            ts[a::N, b::N] = img[a::N, b::N]
+            acc += np.fft.rfft2(ts, E) * np.fft.rfft2(H[:, :, a, b, int(cc) - 1], E)
+    return np.fft.irfft2(acc, E)[m:m + Xr, m:m + Xc]

@@ -73,3 +73,23 @@ def test_forward_project_after_solve_on_same_solver(cuda):
     norm = s.forward_project(to_dev(vol), raw_psf=False).cpu().numpy()
     assert np.array_equal(fresh, again)
     assert np.array_equal(hx, norm[3::15, 11::15])
+
+
+def test_reference_projector_mirrors(cuda):
+    """forwardProjectGPU / forwardProjectACC / forwardProjectGPU_discrete /
+    forwardProjectGPU_skip_2D against their FP64 restatements (relative L2 1e-5, FP32)."""
+    from mesolf_gb300 import (forwardProjectACC, forwardProjectGPU, forwardProjectGPU_discrete,
+                              forwardProjectGPU_skip_2D)
+    w = synth.small_config(lenslets=(5, 4), K0=61, Z=5, seed=8)
+    H, _ = w.psf()
+    vol = w.volume()
+    assert rel_l2(forwardProjectGPU(H, vol), R.forward_project_full(H, vol)) <= 1e-5
+    CA = [(31 - r, 31 + r) for r in (30, 20, 4, 6, 30)]       # centred crops (1-based), some cut the support
+    got = forwardProjectACC(H, vol, CA)
+    assert rel_l2(got, R.forward_project_full(H, vol, CA)) <= 1e-5
+    ua = [2, 2, 3, 5, 1, 3]
+    v6 = np.concatenate([vol, vol[:, :, :1] * 0.5], axis=2)
+    got = forwardProjectGPU_discrete(H, v6, ua, 41)
+    assert rel_l2(got, R.forward_project_discrete(H, v6, ua, 41)) <= 1e-5
+    got = forwardProjectGPU_skip_2D(H, vol[:, :, 2], 3, 4)
+    assert rel_l2(got, R.forward_project_skip_2d(H, vol[:, :, 2], 3, 4)) <= 1e-5

@@ -237,3 +237,25 @@ def test_peeling_filter_bank_rounds_down():
     assert R.nip_omegas(51, 15).size == 54 and R.nip_omegas(51, 15, "peeling").size == 48
     assert R.nip_omegas(21, 15).size == 24 and R.nip_omegas(21, 15, "peeling").size == 18
     assert R.nip_omegas(7, 15, "peeling").size == 6
+
+
+def test_phase_space_kept_mask_matches_impulses():
+    """The crop-and-shift region of gen_phasespace_PSF_theory.m: a unit PSF pixel inside the
+    mask projects identically through the phase-space operator and the full sum; one outside
+    is lost."""
+    from mesolf_gb300.api import phase_space_kept_mask
+    K0, N = 61, 15
+    keep = phase_space_kept_mask(K0, N)
+    vol = np.random.default_rng(0).random((90, 90, 1))   # every PSF offset lands inside
+    for (i, j, a, b) in [(8, 30, 7, 3), (15, 30, 0, 3), (14, 30, 0, 3), (52, 40, 7, 7), (46, 30, 14, 2),
+                         (45, 30, 14, 2), (30, 7, 5, 7), (30, 53, 5, 7)]:
+        H = np.zeros((K0, K0, N, N, 1))
+        H[i, j, a, b, 0] = 1.0
+        full = R.forward_project_full(H, vol)
+        Hps, _ = R.gen_phasespace_psf(H, H[::-1, ::-1])
+        lf = np.zeros_like(full)
+        for u in range(N):
+            for v in range(N):
+                lf[u::N, v::N] = R.forward_ps(Hps[:, :, u, v, :], vol, N)
+        same = np.abs(lf - full).max() <= 1e-9 * max(1.0, np.abs(full).max())
+        assert same == bool(keep[i, j, a, b]), (i, j, a, b)
