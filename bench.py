@@ -171,6 +171,8 @@ def main():
     ap.add_argument("--mixed", default="bf16x2", help="tensor-core precision timed beside plain FP32 ('' to skip)")
     ap.add_argument("--serve-frames", type=int, default=4,
                     help="frames of the 36-patch 18 Hz serving stream (0 to skip)")
+    ap.add_argument("--batched-steps", type=int, default=1,
+                    help="timed steps of the 64-patch batched workload (0 to skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -337,6 +339,11 @@ def main():
         del out_dev, lf_dev
         torch.cuda.empty_cache()
         line["serving"] = serve_block(psf, args.serve_frames, args.mixed, dev)
+    if args.batched_steps > 0 and args.mixed:
+        solver.close()
+        psf.close()
+        torch.cuda.empty_cache()
+        line["batched"] = batched_block(args.mixed, dev, steps=args.batched_steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
     solver.close()
@@ -436,6 +443,68 @@ def serve_block(psf, n_frames, precision, dev, fp32_patches=2):
             "frame_generation_s": t_gen,
             "note": "latency = scheduled arrival -> volume in pinned host memory; arrivals faster than the "
                     "service rate queue up, so p50/p99 grow with the stream length"}
+
+
+BATCH_DESC = ("64 independent patches, Nnum 15, lenslets per side uniform in [31, 71], planes uniform in "
+              "[26, 101] of one 101-plane PSF (plane k window 31+4k capped at 255, K0 255), soma density 5e-4 "
+              "per voxel, 2000-photon Poisson images, 5 RL iterations, one persistent launch per view step for "
+              "all patches under a captured CUDA graph per iteration")
+
+
+def batched_block(precision, dev, steps=1, warmup=1, n_patches=64):
+    """The batched uneven-patch workload: all patches in one work set, each RL iteration one
+    CUDA graph.  Deconvolved voxels/s with the images resident in HBM."""
+    import torch
+    from mesolf_gb300 import BatchSolver, PhaseSpacePSF, synth
+    t0 = time.perf_counter()
+    z_idx = np.arange(101)
+    sides = np.minimum(31 + 4 * z_idx, 255)
+    H, Ht = synth.make_psf(int(sides.max()), 15, z_idx, seed=4, plane_sides=sides)
+    psf = PhaseSpacePSF(H, Ht)
+    del H, Ht
+    shapes, planes = synth.uneven_batch_geometry(n=n_patches)
+    b = BatchSolver(psf, shapes, planes)
+    vols = []
+    for k, (sh, (z0, nz)) in enumerate(zip(shapes, planes)):
+        st = synth.SomaStream(sh, nz, int(round(5e-4 * sh[0] * sh[1] * nz)), seed=200 + k, device=dev)
+        vols.append(st.step())
+    lf_clean = b.forward_project(vols, raw_psf=True, precision="bf16x3")
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    imgs = []
+    for lf in lf_clean:
+        sc = 2000.0 / float(lf.max())
+        x = torch.poisson((lf.clamp(min=0) * sc).contiguous(), generator=g)
+        imgs.append(x.t().contiguous().t())          # column-major (Xr, Xc)
+    del vols, lf_clean
+    t_setup = time.perf_counter() - t0
+    voxels = sum(a * c * nz for (a, c), (_, nz) in zip(shapes, planes))
+    outs = None
+    for _ in range(warmup):
+        outs = b.run(imgs, 5, precision=precision, outs=outs, want_stats=False)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream()
+    launches, vk_ms, vk_n = 0, 0.0, 0
+    e0.record(stream)
+    for _ in range(steps):
+        outs = b.run(imgs, 5, precision=precision, outs=outs, want_stats=True)
+        launches += b.last_stats["kernel_launches"]
+        vk_ms += b.last_stats["view_kernel_ms"]
+        vk_n += b.last_stats["view_kernel_launches"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    finite = all(bool(torch.isfinite(o).all()) for o in outs)
+    res = {"workload": "batch64_lenslets31-71_z26-101_k255_it5", "desc": BATCH_DESC, "precision": precision,
+           "patches": n_patches, "voxels": int(voxels), "value": voxels / (ms * 1e-3), "unit": "voxels/s",
+           "ms_per_step": ms, "steps": steps, "warmup": warmup, "views_per_iteration": b.last_stats["n_views"],
+           "gpu_launches": int(launches), "view_kernels_ms_per_view": vk_ms / max(1, vk_n),
+           "device_bytes_work_set": b.device_bytes, "all_finite": finite, "setup_s": t_setup}
+    b.close()
+    psf.close()
+    return res
 
 
 def _measured_bf16():
