@@ -108,6 +108,17 @@ inline size_t bwd_smem_bytes(int use_alo, int use_blo) {
   return (size_t)STAGES * bwd_layout(use_alo, use_blo).stage + XTILE + 1024;
 }
 
+// Tiles whose patch has weight 0 for this view are skipped: the update would leave X (and
+// the BF16 copy written when X last changed) bit for bit as it is.  Every role walks the
+// same sequence.
+__device__ __forceinline__ bool bwd_skip(const TcBwdArgs& a, int t, int mtiles) {
+  return __ldg(a.wrow + __ldg(a.tile_patch + (t % mtiles))) == 0.f;
+}
+__device__ __forceinline__ int bwd_next(const TcBwdArgs& a, int t, int total, int mtiles) {
+  while (t < total && bwd_skip(a, t, mtiles)) t += gridDim.x;
+  return t;
+}
+
 // Persistent over (position tile, channel tile) pairs.  Warp 0: TMA producer of the
 // operand ring; warp 1: TMEM owner and MMA issuer; warps 2..9: epilogue.  The C and D
 // accumulators are double buffered in TMEM (2 x 256 columns) so the epilogue of one tile
@@ -162,7 +173,8 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       // ---------------- TMA producer (continuous ring over all tiles of this CTA)
       const uint32_t bytes = 3 * TILE_A + (need_alo ? TILE_A : 0) + (need_blo ? TILE_A : 0);
       int it = 0;
-      for (int t = blockIdx.x; t < total && !aborted(&abort_flag); t += gridDim.x) {
+      for (int t = bwd_next(a, blockIdx.x, total, mtiles); t < total && !aborted(&abort_flag);
+           t = bwd_next(a, t + gridDim.x, total, mtiles)) {
         const int m0 = (t % mtiles) * BM, n0 = (t / mtiles) * BWD_BN;
         for (int ks = 0; ks < KS; ++ks, ++it) {
           const int s = it % STAGES;
@@ -190,7 +202,8 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       // ---------------- MMA issuer
       const uint32_t idesc = tc::idesc_bf16_f32(BM, BWD_BN);
       int it = 0, ti = 0;
-      for (int t = blockIdx.x; t < total && !aborted(&abort_flag); t += gridDim.x, ++ti) {
+      for (int t = bwd_next(a, blockIdx.x, total, mtiles); t < total && !aborted(&abort_flag);
+           t = bwd_next(a, t + gridDim.x, total, mtiles), ++ti) {
         const int buf = ti & 1;
         const uint32_t tph = (ti >> 1) & 1;
         if (!tc::mbar_wait(&tempty[buf], tph ^ 1, WAIT_LIMIT)) {
@@ -250,12 +263,13 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     float* xh = xs + half * (XHALF / 4);       // [64 ch][128 pos]
     uint64_t* xf = &xfull[half];
-    if (leader && blockIdx.x < total) {
+    const int t_first = bwd_next(a, blockIdx.x, total, mtiles);
+    if (leader && t_first < total) {
       tc::mbar_arrive_expect_tx(xf, XHALF);
-      tc::tma_load_2d(xh, &mX, xf, (blockIdx.x % mtiles) * BM, (blockIdx.x / mtiles) * BWD_BN + 64 * half);
+      tc::tma_load_2d(xh, &mX, xf, (t_first % mtiles) * BM, (t_first / mtiles) * BWD_BN + 64 * half);
     }
     int ti = 0;
-    for (int t = blockIdx.x; t < total; t += gridDim.x, ++ti) {
+    for (int t = t_first; t < total; t = bwd_next(a, t + gridDim.x, total, mtiles), ++ti) {
       const int buf = ti & 1;
       const uint32_t tph = (ti >> 1) & 1;
       const int m0 = (t % mtiles) * BM, n0 = (t / mtiles) * BWD_BN;
@@ -317,7 +331,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
         tc::tma_store_2d(&mX, xh, m0, n0 + 64 * half);
         tc::bulk_commit();
         tc::bulk_wait_read0();
-        const int tn = t + gridDim.x;
+        const int tn = bwd_next(a, t + gridDim.x, total, mtiles);
         if (tn < total) {
           tc::mbar_arrive_expect_tx(xf, XHALF);
           tc::tma_load_2d(xh, &mX, xf, (tn % mtiles) * BM, (tn / mtiles) * BWD_BN + 64 * half);
@@ -343,11 +357,16 @@ struct TcFwdArgs {
   int stages;    // shared-memory ring depth (2..FWD_MAX_STAGES)
   int MP, NB, NH, nparts, ks_per_split, KS, frow0;  // frow0 = view * NB
   int use_alo, use_blo;                             // activation / tap hi+lo splits
+  const float* wview;      // per patch weight of the projected view (nullable: project all)
+  const int* tile_patch;   // patch of each position tile
 };
 
 __global__ void __launch_bounds__(128, 1)
 k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
          const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, TcFwdArgs a) {
+  // a patch that does not use this view needs no projection for it (whole CTA, before any
+  // barrier or TMEM allocation)
+  if (a.wview && __ldg(a.wview + __ldg(a.tile_patch + blockIdx.x)) == 0.f) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   __shared__ __align__(8) uint64_t full[FWD_MAX_STAGES], empty[FWD_MAX_STAGES], accb;
@@ -867,7 +886,9 @@ PatchGeo work_geo(const TcSolverState* t, const Solver* m, int p) {
   return PatchGeo{m->N, t->nz[p], t->Zch, t->z0[p], t->Li[p], t->Lj[p], t->Li[p], (int64_t)t->MP, m->Xr, m->Xc};
 }
 
-int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cudaStream_t st) {
+// wview (nullable): per-patch weights of `view`; patches with weight 0 are not projected.
+int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cudaStream_t st,
+                  const float* wview = nullptr) {
   const TcPsfState* tp = psf->tc;
   int alo, blo;
   splits_of(precision, &alo, &blo);
@@ -883,6 +904,8 @@ int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cud
   a.frow0 = view * tp->NB;
   a.use_alo = alo;
   a.use_blo = blo;
+  a.wview = wview;
+  a.tile_patch = t->tile_patch.as<int>();
   const size_t stage = (size_t)TILE_A * (alo ? 2 : 1) + (size_t)tp->NB * 128 * (blo ? 2 : 1);
   a.stages = (int)std::max<size_t>(2, std::min<size_t>(FWD_MAX_STAGES, (size_t)(tp->fwd_dyn_max - 1024) / stage));
   const size_t fsmem = (size_t)a.stages * stage + 1024;
@@ -947,7 +970,7 @@ int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* ti
   int64_t n = 0;
   MLF_TRY(tc_pack(psf, t, precision, st));
   MLF_TRY(timing_mark(timer, st));
-  MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[0], st));
+  MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[0], st, t->wtab_dev.as<float>()));
   MLF_TRY(timing_mark(timer, st));
   MLF_TRY(tc_col2im(psf, t, t->views[0], true, nullptr, st));
   MLF_TRY(tc_im2col_ratio(psf, t, precision, st));
@@ -957,7 +980,7 @@ int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* ti
     MLF_TRY(tc_bwd_launch(psf, t, precision, t->views[k], t->wtab_dev.as<float>() + (size_t)k * t->P, st));
     ++n;
     if (k + 1 < V) {
-      MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[k + 1], st));
+      MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[k + 1], st, t->wtab_dev.as<float>() + (size_t)(k + 1) * t->P));
       MLF_TRY(timing_mark(timer, st));
       MLF_TRY(tc_col2im(psf, t, t->views[k + 1], true, nullptr, st));
       MLF_TRY(tc_im2col_ratio(psf, t, precision, st));
