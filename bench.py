@@ -461,7 +461,6 @@ def batched_block(precision, dev, steps=1, warmup=1, n_patches=64):
     sides = np.minimum(31 + 4 * z_idx, 255)
     H, Ht = synth.make_psf(int(sides.max()), 15, z_idx, seed=4, plane_sides=sides)
     psf = PhaseSpacePSF(H, Ht)
-    del H, Ht
     shapes, planes = synth.uneven_batch_geometry(n=n_patches)
     b = BatchSolver(psf, shapes, planes)
     vols = []
@@ -497,11 +496,34 @@ def batched_block(precision, dev, steps=1, warmup=1, n_patches=64):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
     finite = all(bool(torch.isfinite(o).all()) for o in outs)
+    # the plain FP32 drop-in on two of the patches (PSF cut to each patch's planes), and the
+    # batched results' error against it
+    from mesolf_gb300 import RLSolver
+    fp32_t, fp32_vox, errs = 0.0, 0, []
+    for k in range(2):
+        (xr, xc), (z0, nz) = shapes[k], planes[k]
+        sub = PhaseSpacePSF(np.asfortranarray(H[:, :, :, :, z0:z0 + nz]), np.asfortranarray(Ht[:, :, :, :, z0:z0 + nz]))
+        s1 = RLSolver(sub, (xr, xc))
+        o = s1.run(imgs[k], 5, precision="fp32", want_stats=False)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        o = s1.run(imgs[k], 5, precision="fp32", want_stats=False)
+        torch.cuda.synchronize()
+        fp32_t += time.perf_counter() - t1
+        fp32_vox += xr * xc * nz
+        errs.append(float((outs[k].double() - o.double()).norm() / o.double().norm()))
+        s1.close()
+        sub.close()
+    del H, Ht
+    fp32_rate = fp32_vox / fp32_t
     res = {"workload": "batch64_lenslets31-71_z26-101_k255_it5", "desc": BATCH_DESC, "precision": precision,
            "patches": n_patches, "voxels": int(voxels), "value": voxels / (ms * 1e-3), "unit": "voxels/s",
            "ms_per_step": ms, "steps": steps, "warmup": warmup, "views_per_iteration": b.last_stats["n_views"],
            "gpu_launches": int(launches), "view_kernels_ms_per_view": vk_ms / max(1, vk_n),
-           "device_bytes_work_set": b.device_bytes, "all_finite": finite, "setup_s": t_setup}
+           "device_bytes_work_set": b.device_bytes, "all_finite": finite, "setup_s": t_setup,
+           "plain_fp32_voxels_per_s": fp32_rate, "speedup_vs_plain_fp32": voxels / (ms * 1e-3) / fp32_rate,
+           "rel_l2_vs_plain_fp32": errs,
+           "plain_fp32_sample": "single FP32 solves (5 iterations) of patches 0 and 1 with the PSF cut to their planes"}
     b.close()
     psf.close()
     return res

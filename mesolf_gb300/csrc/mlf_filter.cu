@@ -35,7 +35,7 @@ __device__ __forceinline__ int64_t unphase_index(const PatchGeo& g, int64_t e) {
   const int64_t r = e % g.Xr;
   const int64_t c = (e / g.Xr) % g.Xc;
   const int z = (int)(e / (g.Xr * g.Xc));
-  const int64_t ch = ((c % g.N) * g.N + (r % g.N)) * g.Zch + g.z0 + z;
+  const int64_t ch = geo_channel(g, (int)(r % g.N), (int)(c % g.N), z);
   return ch * g.plane + (c / g.N) * g.Pa + (r / g.N);
 }
 

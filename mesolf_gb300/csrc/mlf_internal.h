@@ -70,13 +70,24 @@ void tc_psf_free(TcPsfState* t);
 void tc_solver_free(TcSolverState* t);
 
 // Where a patch's volume lives in a phase-major buffer: channel
-// ch = (beta*N + alpha)*Zch + z0 + z (z < Z planes of the patch), position b*Pa + a inside
-// a plane of `plane` floats.  The plain FP32 solver uses Zch = Z, z0 = 0, Pa padded to 4;
-// the tensor-core work set uses Pa = Li and one plane spanning all its patches.
+// ch = (beta*N + alpha)*Zch + z0 + z (z < Z planes of the patch), or, plane-major (pm = 1),
+// ch = (z0 + z)*N*N + beta*N + alpha; position b*Pa + a inside a plane of `plane` floats.
+// The plain FP32 solver uses Zch = Z, z0 = 0, Pa padded to 4, channel-major order; the
+// tensor-core work set uses Pa = Li, one plane spanning all its patches, and the plane-major
+// order, so that a patch's plane range is one contiguous channel range.
 struct PatchGeo {
   int N, Z, Zch, z0, Li, Lj, Pa;
   int64_t plane, Xr, Xc;
+  int pm;
 };
+__host__ __device__ inline int64_t geo_channel(const PatchGeo& g, int alpha, int beta, int z) {
+  return g.pm ? (int64_t)(g.z0 + z) * g.N * g.N + beta * g.N + alpha
+              : ((int64_t)beta * g.N + alpha) * g.Zch + g.z0 + z;
+}
+// plane of channel ch relative to z0 (outside [0, Z) for the other planes)
+__host__ __device__ inline int geo_plane(const PatchGeo& g, int64_t ch) {
+  return (g.pm ? (int)(ch / ((int64_t)g.N * g.N)) : (int)(ch % g.Zch)) - g.z0;
+}
 
 // ------------------------------------------------------------------ PSF
 // Per-view projector taps in phase-major ("polyphase") form.  For view (u, v) (0-based,

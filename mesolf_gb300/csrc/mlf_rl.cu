@@ -58,7 +58,7 @@ __global__ void k_init_flat(float* X, PatchGeo g, const double* part, int nparts
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t ch = i / LL;
     const int rem = (int)(i - ch * LL);
-    const int z = (int)(ch % g.Zch) - g.z0;
+    const int z = geo_plane(g, ch);
     X[ch * g.plane + (int64_t)(rem / g.Li) * g.Pa + rem % g.Li] = (z >= 0 && z < g.Z) ? val : 0.f;
   }
 }
@@ -69,7 +69,7 @@ __device__ __forceinline__ int64_t phase_index(const PatchGeo& g, int64_t e) {
   const int z = (int)(e / (g.Xr * g.Xc));
   const int alpha = (int)(r % g.N), a = (int)(r / g.N);
   const int beta = (int)(c % g.N), b = (int)(c / g.N);
-  const int64_t ch = ((int64_t)beta * g.N + alpha) * g.Zch + g.z0 + z;
+  const int64_t ch = geo_channel(g, alpha, beta, z);
   return ch * g.plane + (int64_t)b * g.Pa + a;
 }
 

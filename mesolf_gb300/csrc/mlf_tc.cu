@@ -2,7 +2,8 @@
 //
 // The per-view operators of recon_theory_phase_space_LFM_with_filter.m:109-137 are cast
 // as two GEMMs over the lenslet grid (positions p = b*Li + a), the volume channels
-// (ch = (beta*N + alpha)*Z + z) and the projector taps:
+// (plane-major, ch = z*N*N + beta*N + alpha, so a patch's plane range is one contiguous
+// channel range and tiles outside it are skipped) and the projector taps:
 //
 //   back projection   C[p, ch] = sum_t' AR[p, t'] * Wb'[ch, t']        (t' in a (T+2)^2 window)
 //   D = bwd(ones)     D[p, ch] = sum_t' A1[p, t'] * Wb'[ch, t']
@@ -73,7 +74,7 @@ struct TcBwdArgs {
   const int* tile_patch;  // patch of each position tile
   const int* pinfo;       // per patch: Li, Lj, LL, pos0, z0, nz, -, -
   const float* wrow;      // per patch: weight of the current view (0: view inactive for it)
-  int CHP, nch, KB, brow0, Zch;  // brow0 = view * CHP (row of this view in Wb'); Zch = PSF planes
+  int CHP, nch, KB, brow0, NN;   // brow0 = view * CHP (row of this view in Wb'); NN = N*N channels per plane
   int use_alo;                      // add ARl * Wbh to C (activation split)
   int use_blo;                      // add ARh * Wbl to C and A1 * Wbl to D (tap split)
   int write_lo;                     // also emit the lo half of Xb
@@ -108,11 +109,16 @@ inline size_t bwd_smem_bytes(int use_alo, int use_blo) {
   return (size_t)STAGES * bwd_layout(use_alo, use_blo).stage + XTILE + 1024;
 }
 
-// Tiles whose patch has weight 0 for this view are skipped: the update would leave X (and
-// the BF16 copy written when X last changed) bit for bit as it is.  Every role walks the
-// same sequence.
+// Tiles whose patch has weight 0 for this view, or whose channels lie outside the patch's
+// planes, are skipped: the update would leave X (and the BF16 copy written when X last
+// changed) bit for bit as it is.  Every role walks the same sequence.
 __device__ __forceinline__ bool bwd_skip(const TcBwdArgs& a, int t, int mtiles) {
-  return __ldg(a.wrow + __ldg(a.tile_patch + (t % mtiles))) == 0.f;
+  const int pp = __ldg(a.tile_patch + (t % mtiles));
+  if (__ldg(a.wrow + pp) == 0.f) return true;
+  // channels are plane-major: skip channel tiles outside the patch's planes
+  const int n0 = (t / mtiles) * BWD_BN;
+  const int c0 = __ldg(a.pinfo + 8 * pp + 4) * a.NN, c1 = c0 + __ldg(a.pinfo + 8 * pp + 5) * a.NN;
+  return n0 + BWD_BN <= c0 || n0 >= c1;
 }
 __device__ __forceinline__ int bwd_next(const TcBwdArgs& a, int t, int total, int mtiles) {
   while (t < total && bwd_skip(a, t, mtiles)) t += gridDim.x;
@@ -300,7 +306,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
         for (int j = 0; j < 16; ++j) {
           float* xp = xh + ((sub * 2 + cc) * 16 + j) * BM + row;
           float xn = 0.f;
-          const int zr = (chb + j) % a.Zch - pz0;
+          const int zr = (chb + j) / a.NN - pz0;
           if (pos_ok && chb + j < a.nch && zr >= 0 && zr < pnz) {
             const float xo = *xp;
             float xc = __fdividef(xo * cv[j], dv[j] + a.d_eps);   // :130  X .* C ./ D
@@ -359,6 +365,8 @@ struct TcFwdArgs {
   int use_alo, use_blo;                             // activation / tap hi+lo splits
   const float* wview;      // per patch weight of the projected view (nullable: project all)
   const int* tile_patch;   // patch of each position tile
+  const int* pinfo;        // per patch: Li, Lj, LL, pos0, z0, nz, -, -
+  int NN;                  // N*N channels per plane (plane-major channels)
 };
 
 __global__ void __launch_bounds__(128, 1)
@@ -375,8 +383,12 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM;
   const int split = blockIdx.y;
-  const int ks0 = split * a.ks_per_split;
-  const int ks1 = min(a.KS, ks0 + a.ks_per_split);
+  // this split's channel blocks, clipped to the patch's planes (an empty range writes zeros)
+  const int* pq = a.pinfo + 8 * __ldg(a.tile_patch + blockIdx.x);
+  const int klo = __ldg(pq + 4) * a.NN / BK;
+  const int khi = ((__ldg(pq + 4) + __ldg(pq + 5)) * a.NN + BK - 1) / BK;
+  const int ks0 = max(split * a.ks_per_split, klo);
+  const int ks1 = min(min(a.KS, split * a.ks_per_split + a.ks_per_split), khi);
   const int tileB = a.NB * 128;  // NB rows x 128 bytes
   const int S = a.stages;
   const int offAl = TILE_A, offBh = TILE_A * (a.use_alo ? 2 : 1), offBl = offBh + tileB;
@@ -485,6 +497,15 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
 }
 
 // ------------------------------------------------------------------ small kernels
+// Tensor-core channels are plane-major (ch = z*N*N + beta*N + alpha); the FP32 tap tables
+// are indexed by the channel-major (beta*N + alpha)*Z + z.
+__device__ __forceinline__ int64_t tc_to_fp32_channel(int64_t ch, int N, int Z, int* alpha, int* beta) {
+  *alpha = (int)(ch % N);
+  *beta = (int)((ch / N) % N);
+  const int z = (int)(ch / ((int64_t)N * N));
+  return ((int64_t)*beta * N + *alpha) * Z + z;
+}
+
 // Extended back-projection taps, BF16 hi/lo:  Wb'[view][ch][t'] for the (T+2)^2 window,
 // t' = dj'*(T+2) + di', holding wb[view][ch][(dj'-sb-1)*T + (di'-sa-1)] (0 elsewhere).
 __global__ void k_tc_build_wbx(const float* __restrict__ wb, int N, int Z, int T, int64_t nch, int CHP, int KB,
@@ -500,11 +521,12 @@ __global__ void k_tc_build_wbx(const float* __restrict__ wb, int N, int Z, int T
     float val = 0.f;
     if (ch < nch && k < T2 * T2) {
       const int u = view % N, v = view / N;
-      const int alpha = (int)((ch / Z) % N), beta = (int)(ch / ((int64_t)Z * N));
+      int alpha, beta;
+      const int64_t chf = tc_to_fp32_channel(ch, N, Z, &alpha, &beta);
       const int sa = (alpha - u + h + N) / N - 1, sb = (beta - v + h + N) / N - 1;  // floor division
       const int dj = k / T2 - sb - 1, di = k % T2 - sa - 1;
       if (dj >= 0 && dj < T && di >= 0 && di < T)
-        val = wb[((int64_t)view * nch + ch) * T * T + dj * T + di];
+        val = wb[((int64_t)view * nch + chf) * T * T + dj * T + di];
     }
     bf16 h16, l16;
     split_bf16(val, h16, l16);
@@ -514,7 +536,7 @@ __global__ void k_tc_build_wbx(const float* __restrict__ wb, int N, int Z, int T
 }
 
 // Forward taps transposed, BF16 hi/lo: Wf'[view][t][ch] = wf[view][ch][t] (t < T^2).
-__global__ void k_tc_build_wft(const float* __restrict__ wf, int N, int T, int64_t nch, int CHP, int NB,
+__global__ void k_tc_build_wft(const float* __restrict__ wf, int N, int Z, int T, int64_t nch, int CHP, int NB,
                                bf16* __restrict__ hi, bf16* __restrict__ lo) {
   const int64_t total = (int64_t)N * N * NB * CHP;
   const int TT = T * T;
@@ -525,7 +547,10 @@ __global__ void k_tc_build_wft(const float* __restrict__ wf, int N, int T, int64
     const int t = (int)(r % NB);
     const int view = (int)(r / NB);
     float val = 0.f;
-    if (ch < nch && t < TT) val = wf[((int64_t)view * nch + ch) * TT + t];
+    if (ch < nch && t < TT) {
+      int alpha, beta;
+      val = wf[((int64_t)view * nch + tc_to_fp32_channel(ch, N, Z, &alpha, &beta)) * TT + t];
+    }
     bf16 h16, l16;
     split_bf16(val, h16, l16);
     hi[e] = h16;
@@ -715,7 +740,7 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
   MLF_TRY(t->wft_lo.alloc(nf * 2, "tc forward taps"));
   k_tc_build_wbx<<<4096, 256, 0, st>>>(p->wb.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP, t->KB,
                                        t->wbx_hi.as<bf16>(), t->wbx_lo.as<bf16>());
-  k_tc_build_wft<<<4096, 256, 0, st>>>(p->wf.as<float>(), p->N, p->T, p->nch, t->CHP, t->NB,
+  k_tc_build_wft<<<4096, 256, 0, st>>>(p->wf.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP, t->NB,
                                        t->wft_hi.as<bf16>(), t->wft_lo.as<bf16>());
   MLF_LAUNCHED();
   MLF_TRY(make_map(&t->mBh, t->wbx_hi.p, (uint64_t)V * t->CHP, t->KB, BWD_BN));
@@ -883,7 +908,7 @@ void splits_of(int precision, int* alo, int* blo) {
 bool act_split(int precision) { return precision == MLF_PREC_BF16X2 || precision == MLF_PREC_BF16X3; }
 
 PatchGeo work_geo(const TcSolverState* t, const Solver* m, int p) {
-  return PatchGeo{m->N, t->nz[p], t->Zch, t->z0[p], t->Li[p], t->Lj[p], t->Li[p], (int64_t)t->MP, m->Xr, m->Xc};
+  return PatchGeo{m->N, t->nz[p], t->Zch, t->z0[p], t->Li[p], t->Lj[p], t->Li[p], (int64_t)t->MP, m->Xr, m->Xc, 1};
 }
 
 // wview (nullable): per-patch weights of `view`; patches with weight 0 are not projected.
@@ -906,6 +931,8 @@ int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cud
   a.use_blo = blo;
   a.wview = wview;
   a.tile_patch = t->tile_patch.as<int>();
+  a.pinfo = t->pinfo.as<int>();
+  a.NN = psf->N * psf->N;
   const size_t stage = (size_t)TILE_A * (alo ? 2 : 1) + (size_t)tp->NB * 128 * (blo ? 2 : 1);
   a.stages = (int)std::max<size_t>(2, std::min<size_t>(FWD_MAX_STAGES, (size_t)(tp->fwd_dyn_max - 1024) / stage));
   const size_t fsmem = (size_t)a.stages * stage + 1024;
@@ -941,7 +968,7 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   a.tile_patch = t->tile_patch.as<int>();
   a.pinfo = t->pinfo.as<int>();
   a.wrow = wrow;
-  a.CHP = tp->CHP; a.nch = (int)psf->nch; a.KB = tp->KB; a.brow0 = view * tp->CHP; a.Zch = t->Zch;
+  a.CHP = tp->CHP; a.nch = (int)psf->nch; a.KB = tp->KB; a.brow0 = view * tp->CHP; a.NN = psf->N * psf->N;
   a.use_alo = alo;
   a.use_blo = blo;
   a.write_lo = alo;
