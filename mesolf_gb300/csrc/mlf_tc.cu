@@ -23,11 +23,13 @@
 // than the taps is the more accurate two-pass form: the tap rounding cancels in C/D.  The ratio, the update, the depth sums (inside C, D, Y) and the sample filter
 // stay in FP32.
 //
-// Both GEMM kernels are warp-specialised: warp 0 issues TMA tile loads (128-byte swizzle)
-// into a 2-stage shared-memory ring, warp 1 issues tcgen05.mma from one thread into TMEM
-// accumulators, warp 2 owns the TMEM allocation, and all four warps run the epilogue
-// (tcgen05.ld, 32 TMEM lanes per warp).  Every wait is bounded; a timeout sets a device
-// error flag, drains in-flight copies and MMAs, frees TMEM and returns.
+// Both GEMM kernels are warp-specialised: one thread issues TMA tile loads (128-byte
+// swizzle) into a shared-memory ring, one thread issues tcgen05.mma into TMEM accumulators,
+// one warp owns the TMEM allocation, and the remaining warps run the epilogue (tcgen05.ld,
+// 32 TMEM lanes per warp).  The volume X stays FP32 in HBM: the back projection updates it
+// through TMA tiles, and the forward GEMM splits each FP32 tile into its BF16 operand in
+// shared memory, so no BF16 copy of the volume is ever written.  Every wait is bounded; a
+// timeout sets a device error flag, drains in-flight copies and MMAs, frees TMEM and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -68,8 +70,6 @@ __device__ __forceinline__ void split_bf16(float x, bf16& hi, bf16& lo) {
 
 // ------------------------------------------------------------------ back projection + update
 struct TcBwdArgs {
-  bf16* xb_hi;
-  bf16* xb_lo;
   int* err;
   const int* tile_patch;  // patch of each position tile
   const int* pinfo;       // per patch: Li, Lj, LL, pos0, z0, nz, -, -
@@ -77,7 +77,6 @@ struct TcBwdArgs {
   int CHP, nch, KB, brow0, NN;   // brow0 = view * CHP (row of this view in Wb'); NN = N*N channels per plane
   int use_alo;                      // add ARl * Wbh to C (activation split)
   int use_blo;                      // add ARh * Wbl to C and A1 * Wbl to D (tap split)
-  int write_lo;                     // also emit the lo half of Xb
   float d_eps;                      // added to D (peeling variant)
 };
 
@@ -141,7 +140,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
          int mtiles, int ntiles) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
-  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull[2], mdone;
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull[2], hdone[2], mdone;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -161,6 +160,8 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
     }
     tc::mbar_init(&xfull[0], 1);
     tc::mbar_init(&xfull[1], 1);
+    tc::mbar_init(&hdone[0], BWD_EPI_WARPS / 2);
+    tc::mbar_init(&hdone[1], BWD_EPI_WARPS / 2);
     tc::mbar_init(&mdone, 1);
     tc::fence_mbar_init();
     abort_flag = 0;
@@ -300,8 +301,6 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
         float cv[16], dv[16];
         tc::tmem_ld16x2(tC + c * 16, tD + c * 16, cv, dv);
         const int chb = n0 + c * 16;
-        __align__(16) bf16 hi[16];
-        __align__(16) bf16 lo[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           float* xp = xh + ((sub * 2 + cc) * 16 + j) * BM + row;
@@ -315,15 +314,6 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
             if (xn < 0.f) xn = 0.f;                        // :137
             *xp = xn;
           }
-          split_bf16(xn, hi[j], lo[j]);
-        }
-        uint4* dh = reinterpret_cast<uint4*>(a.xb_hi + (int64_t)pos * a.CHP + chb);
-        dh[0] = reinterpret_cast<uint4*>(hi)[0];
-        dh[1] = reinterpret_cast<uint4*>(hi)[1];
-        if (a.write_lo) {
-          uint4* dl = reinterpret_cast<uint4*>(a.xb_lo + (int64_t)pos * a.CHP + chb);
-          dl[0] = reinterpret_cast<uint4*>(lo)[0];
-          dl[1] = reinterpret_cast<uint4*>(lo)[1];
         }
       }
       // TMEM buffer free for the MMA warp
@@ -331,9 +321,16 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&tempty[buf]);
       // this half of the X tile back to HBM, then the next tile's half into the same buffer
+      // every warp of this half has written its part (bounded wait, leader only)
       tc::fence_proxy_async_smem();
-      tc::named_bar_sync(1 + half, 32 * (BWD_EPI_WARPS / 2));
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&hdone[half]);
       if (leader) {
+        if (!tc::mbar_wait(&hdone[half], ti & 1, WAIT_LIMIT)) {
+          atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
+          set_abort(&abort_flag);
+          break;
+        }
         tc::tma_store_2d(&mX, xh, m0, n0 + 64 * half);
         tc::bulk_commit();
         tc::bulk_wait_read0();
@@ -369,15 +366,26 @@ struct TcFwdArgs {
   int NN;                  // N*N channels per plane (plane-major channels)
 };
 
-__global__ void __launch_bounds__(128, 1)
-k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
-         const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, TcFwdArgs a) {
+// The forward GEMM reads the FP32 volume directly: each stage's 32 KB region receives the
+// X tile [64 channels][128 positions] by TMA; four converter warps (one position row per
+// thread) take their 64 values into registers, meet on an mbarrier (bounded wait), and
+// write the BF16 hi / lo operand back into the same region in the K-major 128-byte-swizzled
+// layout a TMA load would have produced (16-byte chunk c of row p at chunk c ^ (p & 7)).
+// The MMA warp waits for the converters.  Warp 0: TMA producer; warp 1: MMA issuer;
+// warp 2: TMEM owner; warps 4..7: converters, then the epilogue (TMEM quadrant = warp % 4).
+constexpr int FWD_THREADS = 256;
+constexpr int FWD_XTILE = BM * BK * 4;  // 32 KB: FP32 X tile, then A hi | A lo (16 KB each)
+
+__global__ void __launch_bounds__(FWD_THREADS, 1)
+k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtensorMap mBh,
+         const __grid_constant__ CUtensorMap mBl, TcFwdArgs a) {
   // a patch that does not use this view needs no projection for it (whole CTA, before any
   // barrier or TMEM allocation)
   if (a.wview && __ldg(a.wview + __ldg(a.tile_patch + blockIdx.x)) == 0.f) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
-  __shared__ __align__(8) uint64_t full[FWD_MAX_STAGES], empty[FWD_MAX_STAGES], accb;
+  __shared__ __align__(8) uint64_t full[FWD_MAX_STAGES], rdone[FWD_MAX_STAGES], conv[FWD_MAX_STAGES],
+      empty[FWD_MAX_STAGES], accb;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -391,18 +399,20 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
   const int ks1 = min(min(a.KS, split * a.ks_per_split + a.ks_per_split), khi);
   const int tileB = a.NB * 128;  // NB rows x 128 bytes
   const int S = a.stages;
-  const int offAl = TILE_A, offBh = TILE_A * (a.use_alo ? 2 : 1), offBl = offBh + tileB;
+  const int offAl = TILE_A, offBh = FWD_XTILE, offBl = offBh + tileB;
   const int stage_bytes = offBh + tileB * (a.use_blo ? 2 : 1);
   const uint32_t tcols = a.NB > 256 ? 512u : 256u;
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&rdone[s], 4);
+      tc::mbar_init(&conv[s], 4);
       tc::mbar_init(&empty[s], 1);
     }
     tc::mbar_init(&accb, 1);
     tc::fence_mbar_init();
     abort_flag = 0;
-    tc::tma_prefetch_desc(&mAh);
+    tc::tma_prefetch_desc(&mX);
     tc::tma_prefetch_desc(&mBh);
   }
   if (warp == 2) tc::tmem_alloc(&tmem_base, tcols);
@@ -412,7 +422,7 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
   const uint32_t tY = tmem_base;
 
   if (warp == 0 && lane == 0) {
-    const uint32_t bytes = TILE_A * (a.use_alo ? 2 : 1) + tileB * (a.use_blo ? 2 : 1);
+    const uint32_t bytes = FWD_XTILE + tileB * (a.use_blo ? 2 : 1);
     int issued = 0;
     for (int ks = ks0; ks < ks1; ++ks) {
       const int i = ks - ks0, s = i % S;
@@ -424,8 +434,7 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       }
       uint8_t* st = smem + s * stage_bytes;
       tc::mbar_arrive_expect_tx(&full[s], bytes);
-      tc::tma_load_2d(st, &mAh, &full[s], ks * BK, m0);
-      if (a.use_alo) tc::tma_load_2d(st + offAl, &mAl, &full[s], ks * BK, m0);
+      tc::tma_load_2d(st, &mX, &full[s], m0, ks * BK);
       for (int p = 0; p < a.nparts; ++p) {
         tc::tma_load_2d(st + offBh + p * a.NH * 128, &mBh, &full[s], ks * BK, a.frow0 + p * a.NH);
         if (a.use_blo)
@@ -440,7 +449,8 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
     for (int ks = ks0; ks < ks1; ++ks) {
       const int i = ks - ks0, s = i % S;
       const uint32_t ph = (i / S) & 1;
-      if (aborted(&abort_flag) || !tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
+      if (aborted(&abort_flag) || !tc::mbar_wait(&full[s], ph, WAIT_LIMIT) ||
+          !tc::mbar_wait(&conv[s], ph, WAIT_LIMIT)) {
         set_abort(&abort_flag);
         atomicExch(a.err, TC_ERR_TIMEOUT_MMA);
         break;
@@ -468,27 +478,68 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       tc::mma_commit(&empty[s]);
     }
     tc::mma_commit(&accb);
-  }
-  __syncwarp();
-  const bool ok = tc::mbar_wait(&accb, 0, WAIT_LIMIT);
-  tc::tc_fence_after();
-  if (!ok && lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
-  const int row = warp * 32 + lane;
-  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
-  float* out = a.ypart + ((int64_t)split * a.MP + m0 + row) * a.NB;
-  const bool empty_split = ks1 <= ks0;
-  if (ok) {
-    for (int c = 0; c < (a.nparts * a.NH) / 16; ++c) {
-      float v[16];
-      tc::tmem_ld16(tY + lane_off + c * 16, v);
-      if (aborted(&abort_flag)) continue;
-      if (empty_split) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = 0.f;
+  } else if (warp >= 4) {
+    // converters: FP32 X tile -> BF16 hi / lo operand, in place
+    const int p = threadIdx.x - 128;  // position row of the tile
+    for (int ks = ks0; ks < ks1; ++ks) {
+      const int i = ks - ks0, s = i % S;
+      const uint32_t ph = (i / S) & 1;
+      if (aborted(&abort_flag) || !tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
+        set_abort(&abort_flag);
+        if (lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
+        break;
       }
-      float4* o = reinterpret_cast<float4*>(out + c * 16);
+      uint8_t* st = smem + s * stage_bytes;
+      const float* xf = reinterpret_cast<const float*>(st);  // [64 ch][128 pos]
+      float x[BK];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+      for (int c = 0; c < BK; ++c) x[c] = xf[c * BM + p];
+      // every converter has its values before the region is overwritten (bounded wait)
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&rdone[s]);
+      if (!tc::mbar_wait(&rdone[s], ph, WAIT_LIMIT)) {
+        set_abort(&abort_flag);
+        if (lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
+        break;
+      }
+#pragma unroll
+      for (int c8 = 0; c8 < BK / 8; ++c8) {
+        __align__(16) bf16 hi[8];
+        __align__(16) bf16 lo[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) split_bf16(x[c8 * 8 + j], hi[j], lo[j]);
+        const int off = p * 128 + ((c8 ^ (p & 7)) << 4);
+        *reinterpret_cast<uint4*>(st + off) = *reinterpret_cast<const uint4*>(hi);
+        if (a.use_alo) *reinterpret_cast<uint4*>(st + offAl + off) = *reinterpret_cast<const uint4*>(lo);
+      }
+      tc::fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&conv[s]);
+    }
+  }
+  if (warp >= 4) {
+    __syncwarp();
+    const bool ok = tc::mbar_wait(&accb, 0, WAIT_LIMIT);
+    tc::tc_fence_after();
+    if (!ok && lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
+    const int quad = warp & 3;
+    const int row = quad * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    float* out = a.ypart + ((int64_t)split * a.MP + m0 + row) * a.NB;
+    const bool empty_split = ks1 <= ks0;
+    if (ok) {
+      for (int c = 0; c < (a.nparts * a.NH) / 16; ++c) {
+        float v[16];
+        tc::tmem_ld16(tY + lane_off + c * 16, v);
+        if (aborted(&abort_flag)) continue;
+        if (empty_split) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = 0.f;
+        }
+        float4* o = reinterpret_cast<float4*>(out + c * 16);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+      }
     }
   }
   tc::tc_fence_before();
@@ -585,28 +636,6 @@ __global__ void k_tc_im2col(const float* __restrict__ R, const int* __restrict__
   }
 }
 
-// X[ch][p] (FP32, [nch][MP]) -> Xb[p][ch] BF16 hi/lo (32x32 tiles through shared memory).
-__global__ void k_tc_pack_x(const float* __restrict__ X, int64_t nch, int CHP, int MP, bf16* __restrict__ hi,
-                            bf16* __restrict__ lo) {
-  __shared__ float t[32][33];
-  const int p0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-  for (int r = ty; r < 32; r += 8) {
-    const int ch = c0 + r, p = p0 + tx;
-    t[r][tx] = (ch < nch && p < MP) ? X[(int64_t)ch * MP + p] : 0.f;
-  }
-  __syncthreads();
-  for (int r = ty; r < 32; r += 8) {
-    const int p = p0 + r, ch = c0 + tx;
-    if (p < MP && ch < CHP) {
-      bf16 h16, l16;
-      split_bf16(t[tx][r], h16, l16);
-      hi[(int64_t)p * CHP + ch] = h16;
-      if (lo) lo[(int64_t)p * CHP + ch] = l16;
-    }
-  }
-}
-
 // HX[j][i] = sum_split sum_{db,da} Y[split][(j+db-q)*Li + (i+da-q)][db*T+da] for every valid
 // position of every patch; ratio R = LF_sub ./ HX (non-finite -> 0).  One warp per output:
 // lanes stride over the taps, then a fixed shuffle tree (deterministic).
@@ -691,8 +720,8 @@ struct TcSolverState {
   std::vector<int> pos0, Li, Lj, LL, z0, nz;
   std::vector<int> views;   // union of the patches' active views, spiral order
   std::vector<float> wtab;  // [views][P]
-  DevBuf X, lfs, rimg, tile_patch, pinfo, wtab_dev, wscratch, ar_hi, ar_lo, a1, xb_hi, xb_lo, ypart, err;
-  CUtensorMap mARh, mARl, mA1, mXh, mXl, mXv;
+  DevBuf X, lfs, rimg, tile_patch, pinfo, wtab_dev, wscratch, ar_hi, ar_lo, a1, ypart, err;
+  CUtensorMap mARh, mARl, mA1, mXv;
   // One RL iteration (view loop + filters of every patch) as an instantiated CUDA graph,
   // per precision and with / without per-view timing nodes.  All buffers above are fixed
   // for the life of the work set, so a captured iteration stays valid.
@@ -773,7 +802,7 @@ size_t tc_psf_bytes(const Psf* p) {
 size_t tc_work_bytes(const TcSolverState* t) {
   if (!t) return 0;
   return t->X.bytes + t->lfs.bytes + t->rimg.bytes + t->tile_patch.bytes + t->pinfo.bytes + t->wtab_dev.bytes +
-         t->wscratch.bytes + t->ar_hi.bytes + t->ar_lo.bytes + t->a1.bytes + t->xb_hi.bytes + t->xb_lo.bytes +
+         t->wscratch.bytes + t->ar_hi.bytes + t->ar_lo.bytes + t->a1.bytes +
          t->ypart.bytes + t->err.bytes;
 }
 
@@ -796,7 +825,7 @@ size_t tc_work_plan_bytes(const Psf* psf, const std::vector<int>& Li, const std:
   splits = (KSF + ksp - 1) / ksp;
   const int64_t P = (int64_t)Li.size();
   return (size_t)(psf->nch * MP * 4 + (int64_t)psf->N * psf->N * MP * 4 + MP * 4 + tiles * 4 + 8 * P * 4 +
-                  (int64_t)psf->N * psf->N * P * 4 + P * 4 + 3 * MP * KB * 2 + 2 * MP * CHP * 2 +
+                  (int64_t)psf->N * psf->N * P * 4 + P * 4 + 3 * MP * KB * 2 +
                   (int64_t)splits * MP * NB * 4 + 4);
 }
 
@@ -857,8 +886,6 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_TRY(t->ar_hi.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->ar_lo.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->a1.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
-  MLF_TRY(t->xb_hi.alloc((size_t)t->MP * tp->CHP * 2, "tc volume (BF16)"));
-  MLF_TRY(t->xb_lo.alloc((size_t)t->MP * tp->CHP * 2, "tc volume (BF16)"));
   MLF_TRY(t->ypart.alloc((size_t)t->splits * t->MP * tp->NB * 4, "tc forward partials"));
   MLF_TRY(t->err.alloc(sizeof(int), "tc error flag"));
   MLF_CUDA(cudaMemcpy(t->tile_patch.p, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -867,8 +894,6 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
     MLF_CUDA(cudaMemcpy(t->wtab_dev.p, t->wtab.data(), t->wtab.size() * sizeof(float), cudaMemcpyHostToDevice));
   MLF_CUDA(cudaMemsetAsync(t->X.p, 0, t->X.bytes, st));
   MLF_CUDA(cudaMemsetAsync(t->lfs.p, 0, t->lfs.bytes, st));
-  MLF_CUDA(cudaMemsetAsync(t->xb_hi.p, 0, t->xb_hi.bytes, st));
-  MLF_CUDA(cudaMemsetAsync(t->xb_lo.p, 0, t->xb_lo.bytes, st));
   MLF_CUDA(cudaMemsetAsync(t->err.p, 0, sizeof(int), st));
   k_tc_im2col<<<2048, 256, 0, st>>>(nullptr, t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP, psf->T, tp->KB,
                                     t->a1.as<bf16>(), nullptr);
@@ -876,8 +901,6 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_TRY(make_map(&t->mARh, t->ar_hi.p, t->MP, tp->KB, BM));
   MLF_TRY(make_map(&t->mARl, t->ar_lo.p, t->MP, tp->KB, BM));
   MLF_TRY(make_map(&t->mA1, t->a1.p, t->MP, tp->KB, BM));
-  MLF_TRY(make_map(&t->mXh, t->xb_hi.p, t->MP, tp->CHP, BM));
-  MLF_TRY(make_map(&t->mXl, t->xb_lo.p, t->MP, tp->CHP, BM));
   {
     MLF_TRY(get_encoder());
     cuuint64_t dims[2] = {(cuuint64_t)t->MP, (cuuint64_t)nch};
@@ -933,10 +956,12 @@ int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cud
   a.tile_patch = t->tile_patch.as<int>();
   a.pinfo = t->pinfo.as<int>();
   a.NN = psf->N * psf->N;
-  const size_t stage = (size_t)TILE_A * (alo ? 2 : 1) + (size_t)tp->NB * 128 * (blo ? 2 : 1);
+  const size_t stage = (size_t)FWD_XTILE + (size_t)tp->NB * 128 * (blo ? 2 : 1);
   a.stages = (int)std::max<size_t>(2, std::min<size_t>(FWD_MAX_STAGES, (size_t)(tp->fwd_dyn_max - 1024) / stage));
   const size_t fsmem = (size_t)a.stages * stage + 1024;
-  k_tc_fwd<<<dim3(t->MP / BM, t->splits), 128, fsmem, st>>>(t->mXh, t->mXl, tp->mFh, tp->mFl, a);
+  if (fsmem > (size_t)tp->fwd_dyn_max)
+    return fail(MLF_ERR_UNSUPPORTED, "tensor-core forward projection: taps tile exceeds shared memory");
+  k_tc_fwd<<<dim3(t->MP / BM, t->splits), FWD_THREADS, fsmem, st>>>(t->mXv, tp->mFh, tp->mFl, a);
   MLF_LAUNCHED();
   return MLF_OK;
 }
@@ -962,8 +987,6 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   int alo, blo;
   splits_of(precision, &alo, &blo);
   TcBwdArgs a{};
-  a.xb_hi = t->xb_hi.as<bf16>();
-  a.xb_lo = t->xb_lo.as<bf16>();
   a.err = t->err.as<int>();
   a.tile_patch = t->tile_patch.as<int>();
   a.pinfo = t->pinfo.as<int>();
@@ -971,7 +994,6 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   a.CHP = tp->CHP; a.nch = (int)psf->nch; a.KB = tp->KB; a.brow0 = view * tp->CHP; a.NN = psf->N * psf->N;
   a.use_alo = alo;
   a.use_blo = blo;
-  a.write_lo = alo;
   a.d_eps = t->d_eps;
   const int mt = t->MP / BM, nt = tp->CHP / BWD_BN;
   const int grid = std::min(mt * nt, t->nsm);
@@ -981,13 +1003,6 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   return MLF_OK;
 }
 
-int tc_pack(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st) {
-  dim3 grid((t->MP + 31) / 32, (psf->tc->CHP + 31) / 32);
-  k_tc_pack_x<<<grid, dim3(32, 8), 0, st>>>(t->X.as<float>(), psf->nch, psf->tc->CHP, t->MP, t->xb_hi.as<bf16>(),
-                                            act_split(precision) ? t->xb_lo.as<bf16>() : nullptr);
-  MLF_LAUNCHED();
-  return MLF_OK;
-}
 
 // The view loop of one iteration over all patches of the work set.
 int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* timer, int64_t* launches,
@@ -995,13 +1010,12 @@ int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* ti
   const int V = (int)t->views.size();
   if (V == 0) return MLF_OK;
   int64_t n = 0;
-  MLF_TRY(tc_pack(psf, t, precision, st));
   MLF_TRY(timing_mark(timer, st));
   MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[0], st, t->wtab_dev.as<float>()));
   MLF_TRY(timing_mark(timer, st));
   MLF_TRY(tc_col2im(psf, t, t->views[0], true, nullptr, st));
   MLF_TRY(tc_im2col_ratio(psf, t, precision, st));
-  n += 4;
+  n += 3;
   for (int k = 0; k < V; ++k) {
     MLF_TRY(timing_mark(timer, st));
     MLF_TRY(tc_bwd_launch(psf, t, precision, t->views[k], t->wtab_dev.as<float>() + (size_t)k * t->P, st));
@@ -1128,7 +1142,6 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
 int tc_forward_view(Solver* s, int precision, const float* d_vol, int view, float* hx_out, cudaStream_t st) {
   TcSolverState* t = s->tc;
   MLF_TRY(launch_to_phase(d_vol, work_geo(t, s, 0), t->X.as<float>(), st));
-  MLF_TRY(tc_pack(s->psf, t, precision, st));
   MLF_TRY(tc_fwd_launch(s->psf, t, precision, view, st));
   return tc_col2im(s->psf, t, view, false, hx_out, st);
 }
@@ -1140,7 +1153,6 @@ int tc_forward_project(TcSolverState* t, const std::vector<Solver*>& members, co
   for (int p = 0; p < t->P; ++p)
     MLF_TRY(launch_to_phase(vols[p], work_geo(t, members[p], p), t->X.as<float>() + t->pos0[p], st,
                             zscale ? zscale + t->z0[p] : nullptr));
-  MLF_TRY(tc_pack(psf, t, precision, st));
   for (int view = 0; view < N * N; ++view) {
     MLF_TRY(tc_fwd_launch(psf, t, precision, view, st));
     MLF_TRY(tc_col2im(psf, t, view, false, t->lfs.as<float>() + (int64_t)view * t->MP, st));
@@ -1157,7 +1169,6 @@ int tc_view_step(Solver* s, int precision, const float* d_lf, float* d_vol, int 
   MLF_TRY(launch_extract_views(d_lf, g, t->lfs.as<float>(), t->MP, 0, st));
   MLF_TRY(launch_to_phase(d_vol, g, t->X.as<float>(), st));
   MLF_CUDA(cudaMemcpyAsync(t->wscratch.p, &w, sizeof(float), cudaMemcpyHostToDevice, st));
-  MLF_TRY(tc_pack(s->psf, t, precision, st));
   MLF_TRY(tc_fwd_launch(s->psf, t, precision, view, st));
   MLF_TRY(tc_col2im(s->psf, t, view, true, nullptr, st));
   MLF_TRY(tc_im2col_ratio(s->psf, t, precision, st));
