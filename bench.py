@@ -36,6 +36,10 @@ WORKLOAD_DESC = ("Nnum 15, 67x67 lenslets (1005x1005 px), 51 planes (0-200 um at
                  "PSF 231 px (phase-space 225), 2000 somas, 2000-photon Poisson image, 3 RL iterations")
 
 
+KVIEW_DRAM_BYTES = 386.4e6     # k_view MODE_STEP launch, 1005x1005x51, FP32
+KTC_DRAM_BYTES = {"k_tc_bwd": 382.1e6, "k_tc_fwd": 220.9e6}   # per launch, same workload, bf16x2
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -270,6 +274,7 @@ def main():
                  "gpu_launches": int(mlaunch),
                  "view_kernels_ms_per_view": mk_ms / max(1, mk_n),
                  "roofline": {"bound": "tensor", "achieved": mflop / (mk_ms * 1e-3) / 1e12,
+                              "traffic": KTC_DRAM_BYTES if (Xr, Xc, Z) == (1005, 1005, 51) else None,
                               "peak": _measured_bf16(), "unit": "TFLOP/s",
                               "frac": (mflop / (mk_ms * 1e-3) / 1e12) / _measured_bf16() if _measured_bf16() else None,
                               "note": "algorithmic flop of the projections / time of the two GEMM kernels "
@@ -305,13 +310,9 @@ def main():
     mean_launch_ms = vk_ms / max(1, vk_n)
     # the launches of one iteration do n_views views' worth of work in n_views + 1 launches
     achieved = flop_view * n_views * w.iters * args.steps / (vk_ms * 1e-3) / 1e12
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "k_view_traffic.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get("dram_bytes_per_launch")
-        except Exception:
-            traffic = None
+    # dram__bytes_read.sum + dram__bytes_write.sum of one fused view launch at this workload
+    # (ncu capture on GB300); algorithmic bytes per view are 8 B per voxel = 412 MB
+    traffic = KVIEW_DRAM_BYTES if (Xr, Xc, Z) == (1005, 1005, 51) else None
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if peak else None, "traffic": traffic,
                 "kernel": "k_view (fused back projection + update + next forward projection)",
