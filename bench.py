@@ -335,6 +335,10 @@ def main():
                                 "sample": f"one full RL view step ({Xr}x{Xc}x{planes}) of the FP64 C/OpenMP oracle "
                                           f"port on {thr} host threads ({t:.2f} s), extrapolated to "
                                           f"{n_views} views x {w.iters} iterations"}
+    if rank == 0:
+        solver.close()
+        torch.cuda.empty_cache()
+        line["precision_vs_fp64_oracle"] = precision_block(psf, dev)
     if args.serve_frames > 0 and args.mixed:
         solver.close()
         del out_dev, lf_dev
@@ -528,6 +532,36 @@ def batched_block(precision, dev, steps=1, warmup=1, n_patches=64):
     b.close()
     psf.close()
     return res
+
+
+GOLDEN_C2 = os.path.join(ROOT, "tests", "golden", "lf1005x1005x51_k231.npz")
+
+
+def precision_block(psf, dev):
+    """Error of every precision against the FP64 oracle of the 1005 x 1005 x 51 workload
+    (fixture: the oracle's volume on a fixed sample of 131072 voxels after 3 and 10
+    iterations, and the measured image it was computed from)."""
+    if not os.path.exists(GOLDEN_C2):
+        return {"available": False, "why": "oracle fixture not generated"}
+    import torch
+    from mesolf_gb300 import RLSolver
+    from mesolf_gb300.api import _fortran
+    g = dict(np.load(GOLDEN_C2))
+    s = RLSolver(psf, g["lf"].shape)
+    lf = _fortran(torch.as_tensor(g["lf"].astype(np.float32)).to(dev))[0]
+    rows = []
+    for prec in ("fp32", "bf16x3", "bf16x2", "bf16"):
+        for it in (3, 10):
+            if f"x{it}" not in g:
+                continue
+            vol = s.run(lf, it, precision=prec, want_stats=False).cpu().numpy()
+            ref = g[f"x{it}"].astype(np.float64)
+            got = vol.astype(np.float64).reshape(-1, order="F")[g["idx"]]
+            rows.append({"precision": prec, "iterations": it,
+                         "rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+                         "max_abs": float(np.abs(got - ref).max()), "ref_max": float(np.abs(ref).max())})
+    s.close()
+    return {"available": True, "sample_voxels": int(g["idx"].size), "vs": "FP64 oracle", "rows": rows}
 
 
 def _measured_bf16():
