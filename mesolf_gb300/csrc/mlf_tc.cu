@@ -78,25 +78,28 @@ struct TcBwdArgs {
   int use_alo;                      // add ARl * Wbh to C (activation split)
   int use_blo;                      // add ARh * Wbl to C and A1 * Wbl to D (tap split)
   float d_eps;                      // added to D (peeling variant)
+  const float* dtab;                // D from class tables of the current view: [ncls][ncls][CHP]
+  int q, ncls;                      // (T-1)/2 and 2q+3 classes per axis
 };
 
 constexpr int BWD_BN = 128;                            // channels per tile
 constexpr int BWD_EPI_WARPS = 16;                      // 4 per TMEM lane quadrant
-constexpr int BWD_THREADS = 32 * (2 + BWD_EPI_WARPS);  // producer, MMA, epilogue
+constexpr int BWD_IO_WARP = 2 + BWD_EPI_WARPS;          // X-tile stores and loads
+constexpr int BWD_THREADS = 32 * (3 + BWD_EPI_WARPS);  // producer, MMA, epilogue, X I/O
 constexpr int XTILE = BM * BWD_BN * 4;                 // FP32 X tile, 64 KB (two 32 KB halves)
 constexpr int XHALF = XTILE / 2;
 
-// Stage layout for a precision mode: Ah | [Al] | A1 | Bh | [Bl]
+// Stage layout for a precision mode: Ah | [Al] | [A1] | Bh | [Bl]  (A1 only when D is a GEMM)
 struct BwdLayout {
   int offAl, offA1, offBh, offBl, stage;
 };
-__host__ __device__ inline BwdLayout bwd_layout(int use_alo, int use_blo) {
+__host__ __device__ inline BwdLayout bwd_layout(int use_alo, int use_blo, bool d_gemm) {
   BwdLayout L;
   int o = TILE_A;
   L.offAl = use_alo ? o : 0;
   if (use_alo) o += TILE_A;
   L.offA1 = o;
-  o += TILE_A;
+  if (d_gemm) o += TILE_A;
   L.offBh = o;
   o += TILE_A;
   L.offBl = use_blo ? o : 0;
@@ -104,13 +107,92 @@ __host__ __device__ inline BwdLayout bwd_layout(int use_alo, int use_blo) {
   L.stage = o;
   return L;
 }
-inline size_t bwd_smem_bytes(int use_alo, int use_blo) {
-  return (size_t)STAGES * bwd_layout(use_alo, use_blo).stage + XTILE + 1024;
+inline size_t bwd_smem_bytes(int use_alo, int use_blo, bool d_gemm, int xbufs) {
+  return (size_t)STAGES * bwd_layout(use_alo, use_blo, d_gemm).stage + (size_t)xbufs * XTILE + 1024;
+}
+
+// D from class tables.  On each axis a position's back-projection window (T+2 taps around
+// the lenslet, the channel's phase shift absorbed into zero taps) loses its first k
+// columns when the position is k-1 lenslets from the low edge (class k = 1..q+1) or its
+// last k columns near the high edge (class q+1+k), else nothing (class 0); this needs at
+// least 2q+2 lenslets per side.  dtab[cb][ca][ch] = the sum of the channel's window taps over
+// the rows of class cb and the columns of class ca: exactly the tap values C is built from
+// (hi, or hi + lo when the taps are split), so C / D keeps cancelling their rounding.
+// Class-major, so an epilogue thread's 16 channels are contiguous.
+__device__ __forceinline__ void dtab_range(int c, int q, int T2, int* lo, int* hi) {
+  if (c == 0) {
+    *lo = 0;
+    *hi = T2 - 1;
+  } else if (c <= q + 1) {
+    *lo = c;
+    *hi = T2 - 1;
+  } else {
+    *lo = 0;
+    *hi = T2 - 1 - (c - q - 1);
+  }
+}
+__device__ __forceinline__ void load_dtab16(const float* p, float (&v)[16]) {
+  const float4* p4 = reinterpret_cast<const float4*>(p);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float4 t = __ldg(p4 + k);
+    v[4 * k + 0] = t.x;
+    v[4 * k + 1] = t.y;
+    v[4 * k + 2] = t.z;
+    v[4 * k + 3] = t.w;
+  }
+}
+__device__ __forceinline__ int dtab_class(int i, int L, int q) {
+  if (i <= q) return q + 1 - i;
+  if (i >= L - q - 1) return (q + 1) + (q + 2 - L + i);
+  return 0;
+}
+
+// Tables of all views, built once per PSF and tap split: block = (32 channels, view), 128
+// threads.  The 32 channels' windows go to shared memory, then row sums per (channel, row,
+// class), then the table entries per (channel, class pair), written channel-contiguous.
+constexpr int DTAB_THREADS = 128;
+__host__ __device__ inline int dtab_ch_words(int T) { return ((T + 2) * (T + 2)) | 1; }
+__global__ void __launch_bounds__(DTAB_THREADS) k_tc_dtab(const bf16* __restrict__ hi, const bf16* __restrict__ lo,
+                                                          int CHP, int KB, int T, float* __restrict__ dtab) {
+  extern __shared__ float dsh[];
+  const int T2 = T + 2, q = (T - 1) / 2, nc = 2 * q + 3;
+  const int c0 = blockIdx.x * 32, view = blockIdx.y;
+  const int stride = dtab_ch_words(T);
+  float* W = dsh;                 // [32][stride]
+  float* rs = dsh + 32 * stride;  // [32][stride]: row sums at wy * nc + class
+  const int64_t row0 = (int64_t)view * CHP + c0;
+  for (int e = threadIdx.x; e < 32 * T2 * T2; e += DTAB_THREADS) {
+    const int c = e / (T2 * T2), k = e - c * (T2 * T2);
+    const int64_t r = (row0 + c) * (int64_t)KB + k;
+    W[c * stride + k] = __bfloat162float(hi[r]) + (lo ? __bfloat162float(lo[r]) : 0.f);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < 32 * T2 * nc; e += DTAB_THREADS) {
+    const int c = e & 31, rest = e >> 5;
+    const int wy = rest / nc, cl = rest - wy * nc;
+    int l, h;
+    dtab_range(cl, q, T2, &l, &h);
+    float sum = 0.f;
+    for (int wx = l; wx <= h; ++wx) sum += W[c * stride + wy * T2 + wx];
+    rs[c * stride + rest] = sum;
+  }
+  __syncthreads();
+  float* out = dtab + (int64_t)view * nc * nc * CHP + c0;
+  for (int e = threadIdx.x; e < 32 * nc * nc; e += DTAB_THREADS) {
+    const int c = e & 31, cls = e >> 5;
+    const int cb = cls / nc, ca = cls - cb * nc;
+    int l, h;
+    dtab_range(cb, q, T2, &l, &h);
+    float sum = 0.f;
+    for (int wy = l; wy <= h; ++wy) sum += rs[c * stride + wy * nc + ca];
+    out[(int64_t)cls * CHP + c] = sum;
+  }
 }
 
 // Tiles whose patch has weight 0 for this view, or whose channels lie outside the patch's
-// planes, are skipped: the update would leave X (and the BF16 copy written when X last
-// changed) bit for bit as it is.  Every role walks the same sequence.
+// planes, are skipped: the update would leave X bit for bit as it is.  Every role walks the
+// same sequence.
 __device__ __forceinline__ bool bwd_skip(const TcBwdArgs& a, int t, int mtiles) {
   const int pp = __ldg(a.tile_patch + (t % mtiles));
   if (__ldg(a.wrow + pp) == 0.f) return true;
@@ -125,14 +207,17 @@ __device__ __forceinline__ int bwd_next(const TcBwdArgs& a, int t, int total, in
 }
 
 // Persistent over (position tile, channel tile) pairs.  Warp 0: TMA producer of the
-// operand ring; warp 1: TMEM owner and MMA issuer; warps 2..9: epilogue.  The C and D
-// accumulators are double buffered in TMEM (2 x 256 columns) so the epilogue of one tile
-// overlaps the MMAs of the next.  The X tile (128 positions x 128 channels, FP32) moves
-// HBM -> shared memory -> HBM by TMA: it is loaded while the tile's MMAs run, updated in
-// place by the epilogue, and stored back in bulk.  The tile is handled as two 64-channel
-// halves, each with its own shared-memory buffer, barrier and leader thread, so one half's
-// store and reload overlap the other half's arithmetic.  Epilogue warp e (warp e+2) covers
-// TMEM lanes 32*((e+2)%4).., channel half e/8 and the 32-channel quarter ((e%8)/4).
+// operand ring; warp 1: TMEM owner and MMA issuer; warps 2..17: epilogue; warp 18: X-tile
+// stores and loads (so no epilogue warp ever waits on a copy).  The accumulators
+// are double buffered in TMEM (2 x 256 columns) so the epilogue of one tile overlaps the
+// MMAs of the next.  D is a second GEMM on the im2col of ones (DGEMM) or comes from the
+// per-view class tables.  The X tile (128 positions x 128 channels, FP32) moves HBM -> shared
+// memory -> HBM by TMA in two 64-channel halves, each with its own barriers; with XB = 2
+// buffers per half the I/O warp requests tile i+2 as soon as tile i is stored, so the load
+// of the next tile is in flight while the current one is computed.
+// Epilogue warp e (warp e+2) covers TMEM lanes 32*((e+2)%4).., channel half e/8 and the
+// 32-channel quarter ((e%8)/4).
+template <bool DGEMM, int XB>
 __global__ void __launch_bounds__(BWD_THREADS, 1)
 k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
          const __grid_constant__ CUtensorMap mA1, const __grid_constant__ CUtensorMap mBh,
@@ -140,15 +225,15 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
          int mtiles, int ntiles) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
-  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull[2], hdone[2], mdone;
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull[XB][2], hdone[2][2], mdone;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int KS = a.KB / BK;
   const int total = mtiles * ntiles;
   const bool need_blo = a.use_blo != 0, need_alo = a.use_alo != 0;
-  const BwdLayout L = bwd_layout(a.use_alo, a.use_blo);
-  float* xs = reinterpret_cast<float*>(smem + STAGES * L.stage);  // [128 ch][128 pos]
+  const BwdLayout L = bwd_layout(a.use_alo, a.use_blo, DGEMM);
+  float* xs = reinterpret_cast<float*>(smem + STAGES * L.stage);  // [XB][2 halves][64 ch][128 pos]
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       tc::mbar_init(&full[s], 1);
@@ -157,16 +242,18 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(&tfull[b], 1);
       tc::mbar_init(&tempty[b], BWD_EPI_WARPS);
+      tc::mbar_init(&hdone[b][0], BWD_EPI_WARPS / 2);  // [tile parity][half]
+      tc::mbar_init(&hdone[b][1], BWD_EPI_WARPS / 2);
     }
-    tc::mbar_init(&xfull[0], 1);
-    tc::mbar_init(&xfull[1], 1);
-    tc::mbar_init(&hdone[0], BWD_EPI_WARPS / 2);
-    tc::mbar_init(&hdone[1], BWD_EPI_WARPS / 2);
+    for (int b = 0; b < XB; ++b) {
+      tc::mbar_init(&xfull[b][0], 1);
+      tc::mbar_init(&xfull[b][1], 1);
+    }
     tc::mbar_init(&mdone, 1);
     tc::fence_mbar_init();
     abort_flag = 0;
     tc::tma_prefetch_desc(&mAh);
-    tc::tma_prefetch_desc(&mA1);
+    if (DGEMM) tc::tma_prefetch_desc(&mA1);
     tc::tma_prefetch_desc(&mBh);
     tc::tma_prefetch_desc(&mX);
   }
@@ -178,7 +265,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
   if (warp == 0) {
     if (lane == 0) {
       // ---------------- TMA producer (continuous ring over all tiles of this CTA)
-      const uint32_t bytes = 3 * TILE_A + (need_alo ? TILE_A : 0) + (need_blo ? TILE_A : 0);
+      const uint32_t bytes = (DGEMM ? 3 : 2) * TILE_A + (need_alo ? TILE_A : 0) + (need_blo ? TILE_A : 0);
       int it = 0;
       for (int t = bwd_next(a, blockIdx.x, total, mtiles); t < total && !aborted(&abort_flag);
            t = bwd_next(a, t + gridDim.x, total, mtiles)) {
@@ -195,7 +282,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
           tc::mbar_arrive_expect_tx(&full[s], bytes);
           tc::tma_load_2d(st, &mAh, &full[s], ks * BK, m0);
           if (need_alo) tc::tma_load_2d(st + L.offAl, &mAl, &full[s], ks * BK, m0);
-          tc::tma_load_2d(st + L.offA1, &mA1, &full[s], ks * BK, m0);
+          if (DGEMM) tc::tma_load_2d(st + L.offA1, &mA1, &full[s], ks * BK, m0);
           tc::tma_load_2d(st + L.offBh, &mBh, &full[s], ks * BK, a.brow0 + n0);
           if (need_blo) tc::tma_load_2d(st + L.offBl, &mBl, &full[s], ks * BK, a.brow0 + n0);
         }
@@ -236,14 +323,13 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
           for (int k = 0; k < BK / 16; ++k) {
             const uint32_t acc = (ks > 0 || k > 0) ? 1u : 0u;
             const uint64_t dah = tc::desc_kmajor_sw128(st + 32 * k);
-            const uint64_t da1 = tc::desc_kmajor_sw128(st + L.offA1 + 32 * k);
             const uint64_t dbh = tc::desc_kmajor_sw128(st + L.offBh + 32 * k);
             tc::mma_bf16(tC, dah, dbh, idesc, acc);
-            tc::mma_bf16(tD, da1, dbh, idesc, acc);
+            if (DGEMM) tc::mma_bf16(tD, tc::desc_kmajor_sw128(st + L.offA1 + 32 * k), dbh, idesc, acc);
             if (need_blo) {
               const uint64_t dbl = tc::desc_kmajor_sw128(st + L.offBl + 32 * k);
               tc::mma_bf16(tC, dah, dbl, idesc, 1u);
-              tc::mma_bf16(tD, da1, dbl, idesc, 1u);
+              if (DGEMM) tc::mma_bf16(tD, tc::desc_kmajor_sw128(st + L.offA1 + 32 * k), dbl, idesc, 1u);
             }
             if (need_alo) {
               const uint64_t dal = tc::desc_kmajor_sw128(st + L.offAl + 32 * k);
@@ -259,92 +345,134 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       tc::mma_commit(&mdone);
       tc::mbar_wait(&mdone, 0, WAIT_LIMIT);
     }
-  } else {
-    // ---------------- epilogue: update X in shared memory, emit Xb, bulk-store X
+    // ---------------- epilogue: update X in shared memory
+  } else if (warp < BWD_IO_WARP) {
     const int e = warp - 2;
     const int half = e >> 3;                   // channels 64*half .. 64*half+63
     const int sub = (e & 7) >> 2;              // 32-channel quarter inside the half
-    const bool leader = ((e & 7) == 0 && lane == 0);
     const int quad = warp & 3;                 // TMEM lanes 32*quad .. 32*quad+31
     const int row = quad * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
-    float* xh = xs + half * (XHALF / 4);       // [64 ch][128 pos]
-    uint64_t* xf = &xfull[half];
-    const int t_first = bwd_next(a, blockIdx.x, total, mtiles);
-    if (leader && t_first < total) {
-      tc::mbar_arrive_expect_tx(xf, XHALF);
-      tc::tma_load_2d(xh, &mX, xf, (t_first % mtiles) * BM, (t_first / mtiles) * BWD_BN + 64 * half);
-    }
     int ti = 0;
-    for (int t = t_first; t < total; t = bwd_next(a, t + gridDim.x, total, mtiles), ++ti) {
+    for (int t = bwd_next(a, blockIdx.x, total, mtiles); t < total; t = bwd_next(a, t + gridDim.x, total, mtiles), ++ti) {
       const int buf = ti & 1;
       const uint32_t tph = (ti >> 1) & 1;
+      const int xb = ti % XB;
+      float* xh = xs + (xb * 2 + half) * (XHALF / 4);   // [64 ch][128 pos]
       const int m0 = (t % mtiles) * BM, n0 = (t / mtiles) * BWD_BN;
+      const int pp = __ldg(a.tile_patch + (t % mtiles));
+      const int* pi = a.pinfo + 8 * pp;
+      const int local = m0 + row - __ldg(pi + 3);
+      const bool pos_ok = local < __ldg(pi + 2);
+      // D of this thread's first 16 channels, requested before the waits
+      float dpre[16];
+      int cls = 0;
+      if (!DGEMM) {
+        const int Li = __ldg(pi + 0), Lj = __ldg(pi + 1);
+        const int jj = local / Li, ii = local - jj * Li;
+        if (pos_ok) cls = dtab_class(jj, Lj, a.q) * a.ncls + dtab_class(ii, Li, a.q);
+        load_dtab16(a.dtab + (int64_t)cls * a.CHP + n0 + (half * 4 + sub * 2) * 16, dpre);
+      }
       bool ok = !aborted(&abort_flag) && tc::mbar_wait(&tfull[buf], tph, WAIT_LIMIT);
       tc::tc_fence_after();
-      ok = ok && tc::mbar_wait(xf, ti & 1, WAIT_LIMIT);
+      ok = ok && tc::mbar_wait(&xfull[xb][half], (ti / XB) & 1, WAIT_LIMIT);
       if (!ok) {
         if (lane == 0) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
         set_abort(&abort_flag);
         break;
       }
-      const int pos = m0 + row;
-      const int pp = __ldg(a.tile_patch + (t % mtiles));
-      const int* pi = a.pinfo + 8 * pp;
-      const bool pos_ok = pos - __ldg(pi + 3) < __ldg(pi + 2);
       const int pz0 = __ldg(pi + 4), pnz = __ldg(pi + 5);
       const float wv = __ldg(a.wrow + pp);
       const uint32_t tC = tmem_base + buf * 256 + lane_off, tD = tC + 128;
 #pragma unroll
       for (int cc = 0; cc < 2; ++cc) {
         const int c = half * 4 + sub * 2 + cc;  // 16-channel chunk of the tile
-        float cv[16], dv[16];
-        tc::tmem_ld16x2(tC + c * 16, tD + c * 16, cv, dv);
         const int chb = n0 + c * 16;
+        float cv[16], dv[16];
+        if (DGEMM) {
+          tc::tmem_ld16x2(tC + c * 16, tD + c * 16, cv, dv);
+        } else {
+          if (cc == 0) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) dv[j] = dpre[j];
+          } else {
+            load_dtab16(a.dtab + (int64_t)cls * a.CHP + chb, dv);
+          }
+          tc::tmem_ld16(tC + c * 16, cv);
+        }
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           float* xp = xh + ((sub * 2 + cc) * 16 + j) * BM + row;
-          float xn = 0.f;
           const int zr = (chb + j) / a.NN - pz0;
           if (pos_ok && chb + j < a.nch && zr >= 0 && zr < pnz) {
             const float xo = *xp;
             float xc = __fdividef(xo * cv[j], dv[j] + a.d_eps);   // :130  X .* C ./ D
             if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;       // :132-134
-            xn = xc * wv + (1.f - wv) * xo;                // :136
+            float xn = xc * wv + (1.f - wv) * xo;          // :136
             if (xn < 0.f) xn = 0.f;                        // :137
             *xp = xn;
           }
         }
       }
-      // TMEM buffer free for the MMA warp
+      // TMEM buffer free for the MMA warp; this warp's part of the half written
       tc::tc_fence_before();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&tempty[buf]);
-      // this half of the X tile back to HBM, then the next tile's half into the same buffer
-      // every warp of this half has written its part (bounded wait, leader only)
       tc::fence_proxy_async_smem();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&hdone[half]);
-      if (leader) {
-        if (!tc::mbar_wait(&hdone[half], ti & 1, WAIT_LIMIT)) {
-          atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
+      if (lane == 0) {
+        tc::mbar_arrive(&tempty[buf]);
+        tc::mbar_arrive(&hdone[buf][half]);
+      }
+    }
+  } else if (warp == BWD_IO_WARP) {
+    if (lane == 0) {
+      // ---------------- X I/O: first XB tiles in, then per tile: store both halves once
+      // their epilogue warps are done, and refill the buffer with tile i + XB
+      int issued = 0, ti = 0;
+      int tl = bwd_next(a, blockIdx.x, total, mtiles);
+      for (int b = 0; b < XB && tl < total; ++b, ++issued) {
+        for (int h = 0; h < 2; ++h) {
+          tc::mbar_arrive_expect_tx(&xfull[b][h], XHALF);
+          tc::tma_load_2d(xs + (b * 2 + h) * (XHALF / 4), &mX, &xfull[b][h], (tl % mtiles) * BM,
+                          (tl / mtiles) * BWD_BN + 64 * h);
+        }
+        tl = bwd_next(a, tl + gridDim.x, total, mtiles);
+      }
+      for (int t = bwd_next(a, blockIdx.x, total, mtiles); t < total; t = bwd_next(a, t + gridDim.x, total, mtiles), ++ti) {
+        const int xb = ti % XB;
+        const int m0 = (t % mtiles) * BM, n0 = (t / mtiles) * BWD_BN;
+        bool ok = true;
+        for (int h = 0; h < 2 && ok; ++h) {
+          // one barrier per tile parity: it cannot run two phases ahead, since tile i+2's
+          // X is only loaded after tile i is stored
+          if (aborted(&abort_flag) || !tc::mbar_wait(&hdone[ti & 1][h], (ti >> 1) & 1, WAIT_LIMIT)) {
+            ok = false;
+            break;
+          }
+          tc::tma_store_2d(&mX, xs + (xb * 2 + h) * (XHALF / 4), m0, n0 + 64 * h);
+          tc::bulk_commit();
+        }
+        if (!ok) {
+          if (!aborted(&abort_flag)) atomicExch(a.err, TC_ERR_TIMEOUT_EPILOGUE);
           set_abort(&abort_flag);
           break;
         }
-        tc::tma_store_2d(&mX, xh, m0, n0 + 64 * half);
-        tc::bulk_commit();
         tc::bulk_wait_read0();
-        const int tn = bwd_next(a, t + gridDim.x, total, mtiles);
+        int tn = bwd_next(a, t + gridDim.x, total, mtiles);
+        if (XB == 2 && tn < total) tn = bwd_next(a, tn + gridDim.x, total, mtiles);
         if (tn < total) {
-          tc::mbar_arrive_expect_tx(xf, XHALF);
-          tc::tma_load_2d(xh, &mX, xf, (tn % mtiles) * BM, (tn / mtiles) * BWD_BN + 64 * half);
+          for (int h = 0; h < 2; ++h) {
+            tc::mbar_arrive_expect_tx(&xfull[xb][h], XHALF);
+            tc::tma_load_2d(xs + (xb * 2 + h) * (XHALF / 4), &mX, &xfull[xb][h], (tn % mtiles) * BM,
+                            (tn / mtiles) * BWD_BN + 64 * h);
+          }
+          ++issued;
         }
       }
-    }
-    if (leader) {
       tc::bulk_wait0();
-      // a load still in flight after an abort must land before the CTA exits
-      if (aborted(&abort_flag)) tc::mbar_wait(xf, ti & 1, WAIT_LIMIT);
+      // loads not consumed (after an abort) must land before the CTA exits; a tile whose
+      // stores were issued had its loads consumed
+      for (int k = ti; k < issued; ++k)
+        for (int h = 0; h < 2; ++h) tc::mbar_wait(&xfull[k % XB][h], (k / XB) & 1, WAIT_LIMIT);
     }
   }
   tc::tc_fence_before();
@@ -707,6 +835,8 @@ inline int rup(int a, int b) { return (a + b - 1) / b * b; }
 struct TcPsfState {
   int KB = 0, NB = 0, NH = 0, nparts = 1, CHP = 0;
   int fwd_dyn_max = 0;  // dynamic shared memory available to the forward GEMM
+  int bwd_dyn_max = 0;  // ... and to the back projection (smallest of its instantiations)
+  DevBuf dtab[2];       // D class tables of every view, [view][ncls][ncls][CHP]; taps hi / hi + lo
   DevBuf wbx_hi, wbx_lo, wft_hi, wft_lo;
   CUtensorMap mBh, mBl, mFh, mFl;
 };
@@ -717,6 +847,7 @@ struct TcPsfState {
 struct TcSolverState {
   int P = 0, MP = 0, Zch = 0, splits = 1, ks_per_split = 0, KSF = 0, nsm = 0;
   float d_eps = 0.f;  // the members' variant (all the same)
+  bool dtab_ok = false;  // every patch has >= 2q+2 lenslets per side: D from class tables
   std::vector<int> pos0, Li, Lj, LL, z0, nz;
   std::vector<int> views;   // union of the patches' active views, spiral order
   std::vector<float> wtab;  // [views][P]
@@ -781,12 +912,18 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
     MLF_CUDA(cudaGetDevice(&dev));
     MLF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     cudaFuncAttributes fb, ff;
-    MLF_CUDA(cudaFuncGetAttributes(&fb, k_tc_bwd));
     MLF_CUDA(cudaFuncGetAttributes(&ff, k_tc_fwd));
-    const size_t need_b = bwd_smem_bytes(1, 1);
-    if (need_b + fb.sharedSizeBytes > (size_t)optin)
+    int bmax = optin;
+    for (const void* f : {(const void*)k_tc_bwd<true, 1>, (const void*)k_tc_bwd<false, 1>,
+                          (const void*)k_tc_bwd<false, 2>}) {
+      MLF_CUDA(cudaFuncGetAttributes(&fb, f));
+      MLF_TRY(allow_max_dyn_smem(f));
+      bmax = std::min(bmax, optin - (int)fb.sharedSizeBytes);
+    }
+    MLF_TRY(allow_max_dyn_smem((const void*)k_tc_dtab));
+    t->bwd_dyn_max = bmax;
+    if (bwd_smem_bytes(1, 1, true, 1) > (size_t)bmax)
       return fail(MLF_ERR_UNSUPPORTED, "tensor-core back projection needs more shared memory than the device offers");
-    MLF_CUDA(cudaFuncSetAttribute(k_tc_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_b));
     t->fwd_dyn_max = optin - (int)ff.sharedSizeBytes;
     MLF_CUDA(cudaFuncSetAttribute(k_tc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, t->fwd_dyn_max));
   }
@@ -796,7 +933,8 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
 
 size_t tc_psf_bytes(const Psf* p) {
   if (!p->tc) return 0;
-  return p->tc->wbx_hi.bytes + p->tc->wbx_lo.bytes + p->tc->wft_hi.bytes + p->tc->wft_lo.bytes;
+  return p->tc->wbx_hi.bytes + p->tc->wbx_lo.bytes + p->tc->wft_hi.bytes + p->tc->wft_lo.bytes +
+         p->tc->dtab[0].bytes + p->tc->dtab[1].bytes;
 }
 
 size_t tc_work_bytes(const TcSolverState* t) {
@@ -888,6 +1026,9 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_TRY(t->a1.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->ypart.alloc((size_t)t->splits * t->MP * tp->NB * 4, "tc forward partials"));
   MLF_TRY(t->err.alloc(sizeof(int), "tc error flag"));
+  t->dtab_ok = true;
+  for (int p = 0; p < t->P; ++p)
+    t->dtab_ok = t->dtab_ok && t->Li[p] >= 2 * psf->q + 2 && t->Lj[p] >= 2 * psf->q + 2;
   MLF_CUDA(cudaMemcpy(t->tile_patch.p, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice));
   MLF_CUDA(cudaMemcpy(t->pinfo.p, info.data(), info.size() * sizeof(int), cudaMemcpyHostToDevice));
   if (!t->wtab.empty())
@@ -982,10 +1123,30 @@ int tc_im2col_ratio(const Psf* psf, TcSolverState* t, int precision, cudaStream_
   return MLF_OK;
 }
 
+// D class tables of every view for one tap split, built on first use (outside any graph
+// capture: it allocates) and kept with the PSF.
+int tc_dtab_prepare(const Psf* psf, int precision, cudaStream_t st) {
+  int alo, blo;
+  splits_of(precision, &alo, &blo);
+  TcPsfState* tp = psf->tc;
+  if (tp->dtab[blo].p) return MLF_OK;
+  const int nc = 2 * psf->q + 3, V = psf->N * psf->N;
+  MLF_TRY(tp->dtab[blo].alloc((size_t)V * nc * nc * tp->CHP * sizeof(float), "tc D class tables"));
+  const size_t dsm = sizeof(float) * 64 * (size_t)dtab_ch_words(psf->T);
+  k_tc_dtab<<<dim3(tp->CHP / 32, V), DTAB_THREADS, dsm, st>>>(tp->wbx_hi.as<bf16>(),
+                                                              blo ? tp->wbx_lo.as<bf16>() : nullptr, tp->CHP,
+                                                              tp->KB, psf->T, tp->dtab[blo].as<float>());
+  MLF_LAUNCHED();
+  return MLF_OK;
+}
+
 int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, const float* wrow, cudaStream_t st) {
   const TcPsfState* tp = psf->tc;
   int alo, blo;
   splits_of(precision, &alo, &blo);
+  const bool dgemm = !t->dtab_ok;
+  const int q = psf->q, nc = 2 * q + 3;
+  if (!dgemm && !tp->dtab[blo].p) return fail(MLF_ERR_INVALID, "tensor-core D class tables not prepared");
   TcBwdArgs a{};
   a.err = t->err.as<int>();
   a.tile_patch = t->tile_patch.as<int>();
@@ -995,10 +1156,20 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   a.use_alo = alo;
   a.use_blo = blo;
   a.d_eps = t->d_eps;
+  a.dtab = dgemm ? nullptr : tp->dtab[blo].as<float>() + (int64_t)view * nc * nc * tp->CHP;
+  a.q = q;
+  a.ncls = nc;
   const int mt = t->MP / BM, nt = tp->CHP / BWD_BN;
   const int grid = std::min(mt * nt, t->nsm);
-  k_tc_bwd<<<grid, BWD_THREADS, bwd_smem_bytes(alo, blo), st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl,
-                                                                 t->mXv, a, mt, nt);
+  // two X buffers when they fit (D from tables frees the A1 operand's ring slots)
+  const int xbufs = (!dgemm && bwd_smem_bytes(alo, blo, false, 2) <= (size_t)tp->bwd_dyn_max) ? 2 : 1;
+  const size_t smem = bwd_smem_bytes(alo, blo, dgemm, xbufs);
+  if (dgemm)
+    k_tc_bwd<true, 1><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a, mt, nt);
+  else if (xbufs == 2)
+    k_tc_bwd<false, 2><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a, mt, nt);
+  else
+    k_tc_bwd<false, 1><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a, mt, nt);
   MLF_LAUNCHED();
   return MLF_OK;
 }
@@ -1083,6 +1254,7 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
   timer->timing = stats != nullptr;
   timer->tev_used = 0;
   int64_t launches = 0;
+  if (t->dtab_ok) MLF_TRY(tc_dtab_prepare(psf, precision, st));
   for (int p = 0; p < t->P; ++p) {
     const PatchGeo g = work_geo(t, members[p], p);
     float* Xp = t->X.as<float>() + t->pos0[p];
@@ -1169,6 +1341,7 @@ int tc_view_step(Solver* s, int precision, const float* d_lf, float* d_vol, int 
   MLF_TRY(launch_extract_views(d_lf, g, t->lfs.as<float>(), t->MP, 0, st));
   MLF_TRY(launch_to_phase(d_vol, g, t->X.as<float>(), st));
   MLF_CUDA(cudaMemcpyAsync(t->wscratch.p, &w, sizeof(float), cudaMemcpyHostToDevice, st));
+  if (t->dtab_ok) MLF_TRY(tc_dtab_prepare(s->psf, precision, st));
   MLF_TRY(tc_fwd_launch(s->psf, t, precision, view, st));
   MLF_TRY(tc_col2im(s->psf, t, view, true, nullptr, st));
   MLF_TRY(tc_im2col_ratio(s->psf, t, precision, st));
