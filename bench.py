@@ -40,6 +40,24 @@ KVIEW_DRAM_BYTES = 386.4e6     # k_view MODE_STEP launch, 1005x1005x51, FP32
 KTC_DRAM_BYTES = {"k_tc_bwd": 382.1e6, "k_tc_fwd": 220.9e6}   # per launch, same workload, bf16x2
 
 
+def max_over_ranks(x, ws, dev=None):
+    """The largest value over all ranks (the whole job takes as long as its slowest rank).
+    Works on NCCL (device tensor) and gloo (host tensor) process groups."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    on_dev = dist.get_backend() == "nccl"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev if on_dev else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank, ws, ms_max):
+    """Whole-job throughput of independent replicas: all ranks' units / the slowest time."""
+    return ws * units_per_rank / (ms_max * 1e-3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -125,6 +143,22 @@ def cpu_baseline_sample(H, Ht, lf, u=3, v=5, planes=None):
     t0 = time.perf_counter()
     cbuild.view_step(h, t, lf.astype(np.float64), X, u, v, 0.3, 15)
     return time.perf_counter() - t0, cbuild.threads(), Z
+
+
+def cpu_fft_sample(Xr, Xc, S, calls=3):
+    """Seconds per conv2FFT call of the reference's GPU-branch formulation (conv2FFT.m:1-22 on
+    the exsize grid of recon_…_with_filter.m:78-83), FP64 numpy (pocketfft, one thread).  One
+    view step makes 3 Z such calls (forward per plane, C and D per plane)."""
+    from oracle import mesolf_ref as R
+    rng = np.random.default_rng(0)
+    x = rng.random((Xr, Xc))
+    m = rng.random((S, S))
+    E = R.ex_size((Xr, Xc), S)
+    R.conv2fft(x, m, E)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        R.conv2fft(x, m, E)
+    return (time.perf_counter() - t0) / calls, E
 
 
 def run_reference(args):
@@ -235,13 +269,9 @@ def main():
     e1.record(stream)
     barrier()
     clocks = clk.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, ws, dev)
     n_views = st["n_views"]
-    value = ws * w.voxels / (ms * 1e-3)
+    value = replica_value(w.voxels, ws, ms)
 
     # mixed precision (tensor cores) on the same workload, error vs the plain FP32 volume
     mixed = None
@@ -265,10 +295,10 @@ def main():
             mlaunch += st2["kernel_launches"]
         m1.record(stream)
         barrier()
-        mms = m0.elapsed_time(m1) / args.steps
+        mms = max_over_ranks(m0.elapsed_time(m1) / args.steps, ws, dev)
         d = (mix_out.double() - ref_vol.double()).norm() / ref_vol.double().norm()
         mflop = algorithmic_flop_per_view(Xr, Xc, Z, psf.S, psf.N) * n_views * w.iters * args.steps
-        mixed = {"precision": args.mixed, "value": ws * w.voxels / (mms * 1e-3), "unit": "voxels/s",
+        mixed = {"precision": args.mixed, "value": replica_value(w.voxels, ws, mms), "unit": "voxels/s",
                  "ms_per_step": mms, "speedup_vs_plain_fp32": ms / mms,
                  "rel_l2_vs_plain_fp32": float(d),
                  "gpu_launches": int(mlaunch),
@@ -290,12 +320,8 @@ def main():
     for _ in range(args.steps):
         solver.run(lf_host, w.iters, precision=args.precision, out=out_host, want_stats=False)
     barrier()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    if ws > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = {"value": ws * w.voxels / (e2e_ms * 1e-3), "unit": "voxels/s",
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, ws, dev)
+    e2e = {"value": replica_value(w.voxels, ws, e2e_ms), "unit": "voxels/s",
            "h2d_bytes_per_step": int(Xr * Xc * 4), "d2h_bytes_per_step": int(Xr * Xc * Z * 4),
            "ms_per_step": e2e_ms, "path": "mlf_solver_run, pinned host buffers"}
 
@@ -335,16 +361,24 @@ def main():
                                 "sample": f"one full RL view step ({Xr}x{Xc}x{planes}) of the FP64 C/OpenMP oracle "
                                           f"port on {thr} host threads ({t:.2f} s), extrapolated to "
                                           f"{n_views} views x {w.iters} iterations"}
-    if rank == 0:
+        tc_s, E = cpu_fft_sample(Xr, Xc, psf.S)
+        t_fft = tc_s * 3 * Z * n_views * w.iters
+        line["cpu_baseline"]["fft_variant"] = {
+            "value": w.voxels / t_fft, "unit": "voxels/s", "cores": 1, "kind": "port",
+            "sample": f"3 conv2FFT calls ({Xr}x{Xc} image, {psf.S}x{psf.S} kernel, {E[0]}x{E[1]} grid, FP64 "
+                      f"numpy, {tc_s:.3f} s each), extrapolated to 3 x {Z} calls per view x {n_views} views x "
+                      f"{w.iters} iterations"}
+    # the single-GPU extras (error table, serving stream, batched workload) run at N = 1 only
+    if ws == 1:
         solver.close()
         torch.cuda.empty_cache()
         line["precision_vs_fp64_oracle"] = precision_block(psf, dev)
-    if args.serve_frames > 0 and args.mixed:
+    if ws == 1 and args.serve_frames > 0 and args.mixed:
         solver.close()
         del out_dev, lf_dev
         torch.cuda.empty_cache()
         line["serving"] = serve_block(psf, args.serve_frames, args.mixed, dev)
-    if args.batched_steps > 0 and args.mixed:
+    if ws == 1 and args.batched_steps > 0 and args.mixed:
         solver.close()
         psf.close()
         torch.cuda.empty_cache()
