@@ -483,7 +483,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
 // ------------------------------------------------------------------ forward projection
 constexpr int FWD_MAX_STAGES = 4;
 struct TcFwdArgs {
-  float* ypart;  // [split][MP][NB]
+  float* ypart;  // [split][NB][MP] (tap-major: col2im reads it coalesced)
   int* err;
   int stages;    // shared-memory ring depth (2..FWD_MAX_STAGES)
   int MP, NB, NH, nparts, ks_per_split, KS, frow0;  // frow0 = view * NB
@@ -653,20 +653,15 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtenso
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
-    float* out = a.ypart + ((int64_t)split * a.MP + m0 + row) * a.NB;
+    float* out = a.ypart + (int64_t)split * a.NB * a.MP + m0 + row;  // + t * MP
     const bool empty_split = ks1 <= ks0;
     if (ok) {
       for (int c = 0; c < (a.nparts * a.NH) / 16; ++c) {
         float v[16];
         tc::tmem_ld16(tY + lane_off + c * 16, v);
         if (aborted(&abort_flag)) continue;
-        if (empty_split) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = 0.f;
-        }
-        float4* o = reinterpret_cast<float4*>(out + c * 16);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        for (int j = 0; j < 16; ++j) out[(int64_t)(c * 16 + j) * a.MP] = empty_split ? 0.f : v[j];
       }
     }
   }
@@ -764,36 +759,54 @@ __global__ void k_tc_im2col(const float* __restrict__ R, const int* __restrict__
   }
 }
 
-// HX[j][i] = sum_split sum_{db,da} Y[split][(j+db-q)*Li + (i+da-q)][db*T+da] for every valid
-// position of every patch; ratio R = LF_sub ./ HX (non-finite -> 0).  One warp per output:
-// lanes stride over the taps, then a fixed shuffle tree (deterministic).
-__global__ void k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, int T,
-                                  const int* __restrict__ tile_patch, const int* __restrict__ pinfo,
-                                  const float* __restrict__ lfsub, float* __restrict__ hx_out,
-                                  float* __restrict__ rimg) {
-  const int pos = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (pos >= MP) return;
-  const int* pi = pinfo + 8 * tile_patch[pos / BM];
-  const int Li = pi[0], Lj = pi[1], LL = pi[2], pos0 = pi[3];
-  const int local = pos - pos0;
-  if (local >= LL) return;
-  const int q = (T - 1) / 2;
-  const int j = local / Li, i = local - (local / Li) * Li;
+// HX[j][i] = sum_{db,da} sum_split Y[split][t = db*T+da][(j+db-q)*Li + (i+da-q)] for every valid
+// position of every patch; ratio R = LF_sub ./ HX (non-finite -> 0).  A block covers 32
+// consecutive positions; its 8 warps take the tap rows db = w, w+8, ... (lanes = positions,
+// so each load of a warp is 32 consecutive floats of one tap's row), and the warps' partial
+// sums are added in a fixed order (deterministic).
+constexpr int COL2IM_WARPS = 8;
+__global__ void __launch_bounds__(32 * COL2IM_WARPS)
+k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, int T,
+                  const int* __restrict__ tile_patch, const int* __restrict__ pinfo,
+                  const float* __restrict__ lfsub, float* __restrict__ hx_out, float* __restrict__ rimg) {
+  __shared__ float part[COL2IM_WARPS][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pos = blockIdx.x * 32 + lane;
   float s = 0.f;
-  for (int t = lane; t < T * T; t += 32) {
-    const int db = t / T, da = t - (t / T) * T;
-    const int b = j + db - q, a = i + da - q;
-    if (b < 0 || b >= Lj || a < 0 || a >= Li) continue;
-    const int64_t p = (int64_t)pos0 + (int64_t)b * Li + a;
-    for (int sp = 0; sp < splits; ++sp) s += __ldg(ypart + ((int64_t)sp * MP + p) * NB + t);
+  bool valid = pos < MP;
+  int pos0 = 0, Li = 1, Lj = 0, j = 0, i = 0;
+  if (valid) {
+    const int* pi = pinfo + 8 * tile_patch[pos / BM];
+    Li = pi[0];
+    Lj = pi[1];
+    pos0 = pi[3];
+    const int local = pos - pos0;
+    valid = local < pi[2];
+    j = local / Li;
+    i = local - j * Li;
   }
+  if (valid) {
+    const int q = (T - 1) / 2;
+    for (int db = w; db < T; db += COL2IM_WARPS) {
+      const int b = j + db - q;
+      if (b < 0 || b >= Lj) continue;
+      for (int da = 0; da < T; ++da) {
+        const int a = i + da - q;
+        if (a < 0 || a >= Li) continue;
+        const float* y = ypart + (int64_t)(db * T + da) * MP + pos0 + (int64_t)b * Li + a;
+        for (int sp = 0; sp < splits; ++sp) s += __ldg(y + (int64_t)sp * NB * MP);
+      }
+    }
+  }
+  part[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && valid) {
+    float h = 0.f;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) {
-    if (hx_out) hx_out[pos] = s;
+    for (int k = 0; k < COL2IM_WARPS; ++k) h += part[k][lane];
+    if (hx_out) hx_out[pos] = h;
     if (rimg) {
-      float r = lfsub[pos] / s;
+      float r = lfsub[pos] / h;
       if (!isfinite(r)) r = 0.f;
       rimg[pos] = r;
     }
@@ -1108,7 +1121,7 @@ int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cud
 }
 
 int tc_col2im(const Psf* psf, TcSolverState* t, int view, bool ratio, float* hx_out, cudaStream_t st) {
-  k_tc_col2im_ratio<<<(t->MP + 7) / 8, 256, 0, st>>>(
+  k_tc_col2im_ratio<<<(t->MP + 31) / 32, 32 * COL2IM_WARPS, 0, st>>>(
       t->ypart.as<float>(), t->splits, t->MP, psf->tc->NB, psf->T, t->tile_patch.as<int>(), t->pinfo.as<int>(),
       t->lfs.as<float>() + (int64_t)view * t->MP, hx_out, ratio ? t->rimg.as<float>() : nullptr);
   MLF_LAUNCHED();
