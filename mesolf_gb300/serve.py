@@ -223,6 +223,15 @@ class SolveServer:
             "mean_batch": float(np.mean([len(b) for b in self._batches])) if self._batches else 0.0,
         }
 
+    def reset_stats(self):
+        """Forget the latencies and throughput recorded so far (e.g. after a warm-up)."""
+        with self._lock:
+            self._lat.clear()
+            self._voxels = 0
+            self._batches.clear()
+            self._t_first = None
+            self._t_last = 0.0
+
     def close(self):
         with self._lock:
             self._closing = True
