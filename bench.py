@@ -37,7 +37,7 @@ WORKLOAD_DESC = ("Nnum 15, 67x67 lenslets (1005x1005 px), 51 planes (0-200 um at
 
 
 KVIEW_DRAM_BYTES = 386.4e6     # k_view MODE_STEP launch, 1005x1005x51, FP32
-KTC_DRAM_BYTES = {"k_tc_bwd": 382.1e6, "k_tc_fwd": 220.9e6}   # per launch, same workload, bf16x2
+KTC_DRAM_BYTES = {"k_tc_bwd": 390.7e6, "k_tc_fwd": 220.5e6}   # per launch, same workload, bf16x2
 
 
 def max_over_ranks(x, ws, dev=None):
