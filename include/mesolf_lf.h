@@ -85,6 +85,14 @@ int mlf_last_error(char* buf, size_t len);
  * Synchronous (the reference calls cudaDeviceSynchronize, :406). */
 int mlf_conv_vec(const float* bitmap, int64_t W, int64_t H, int64_t n,
                  const float* kernels, int64_t kw, int32_t nnum, float* out, void* stream);
+/* The same projector with a choice of method: MLF_CONV_DIRECT (CUDA-core FP32 correlation),
+ * MLF_CONV_TENSOR (the correlation recast as the full forward projection of re-indexed
+ * kernels, batched over the slices on the tensor cores with both operands split,
+ * FP32-class accuracy; kernels up to 241 wide with a finite non-zero sum), MLF_CONV_AUTO
+ * (the tensor cores from 1e11 flop when they apply, else direct; what mlf_conv_vec does). */
+enum mlf_conv_method { MLF_CONV_AUTO = 0, MLF_CONV_DIRECT = 1, MLF_CONV_TENSOR = 2 };
+int mlf_conv_vec_ex(const float* bitmap, int64_t W, int64_t H, int64_t n, const float* kernels, int64_t kw,
+                    int32_t nnum, float* out, int32_t method, void* stream);
 
 /* ---------------------------------------------------------------------------------
  * Phase-space PSF.  Replaces recon_theory_phase_space_LFM_with_filter.m:13-40 and

@@ -67,13 +67,17 @@ def _stream_of(x, stream):
     return ctypes.c_void_p(0)
 
 
-def mex_lfm_convolution_vec(bitmap, kernels, stream=None):
+CONV_METHODS = {"auto": 0, "direct": 1, "tensor": 2}
+
+
+def mex_lfm_convolution_vec(bitmap, kernels, stream=None, method="auto"):
     """Drop-in for the MEX projector.
 
     bitmap: (W, H) or (W, H, n) float32; kernels: (kw, kw, 15, 15) float32.  Returns an
     array of the bitmap's shape, in the bitmap's memory kind.  Input checks follow
     ``mex_lfm_convolution_vec.cu:305-355`` and raise ``MesoLFError`` like its
-    ``mexErrMsgIdAndTxt``.
+    ``mexErrMsgIdAndTxt``.  ``method``: "direct" (CUDA-core FP32), "tensor" (the tensor-core
+    route, FP32-class accuracy), "auto" (tensor cores for large calls when they apply).
     """
     lib = _lib.load()
     shp = tuple(bitmap.shape)
@@ -87,7 +91,8 @@ def mex_lfm_convolution_vec(bitmap, kernels, stream=None):
     b_keep, bp = _fortran(bitmap)
     k_keep, kp = _fortran(kernels)
     out, op = _empty_like_kind(bitmap, shp)
-    check(lib.mlf_conv_vec(bp, W, Hh, n, kp, kw, int(kernels.shape[2]), op, _stream_of(bitmap, stream)))
+    check(lib.mlf_conv_vec_ex(bp, W, Hh, n, kp, kw, int(kernels.shape[2]), op, CONV_METHODS[method],
+                              _stream_of(bitmap, stream)))
     del b_keep, k_keep
     return out
 

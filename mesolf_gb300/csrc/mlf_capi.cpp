@@ -7,6 +7,7 @@
 // arrays are staged through device buffers owned by the call or the solver.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -155,9 +156,60 @@ int mlf_last_error(char* buf, size_t len) {
   return g_code;
 }
 
+// The MEX projector on the tensor cores: the correlation of mlf_conv_vec equals the full
+// forward projection of the re-indexed kernels (launch_mex_reindex), so a one-plane PSF made
+// of them, every slice a patch of a batch, and the batched forward projection in
+// MLF_PREC_BF16X3 (FP32-class accuracy) give the output after padding each slice to a
+// multiple of 15 and cropping back.  MLF_ERR_UNSUPPORTED when the route does not apply
+// (kernels wider than 241, kernel sum zero or not finite).
+static int conv_vec_tc(const float* db, int64_t W, int64_t H, int64_t n, const float* dk, int64_t kw, float* dout,
+                       cudaStream_t st) {
+  const int nn = 15;
+  int K0 = 15;
+  while (K0 < kw + 14) K0 += 30;
+  if (K0 > 255) return fail(MLF_ERR_UNSUPPORTED, "tensor-core MEX projector: kernels wider than 241");
+  if (n > (1 << 20)) return fail(MLF_ERR_UNSUPPORTED, "tensor-core MEX projector: too many slices");
+  DevBuf hp;
+  MLF_TRY(hp.alloc(sizeof(float) * K0 * K0 * nn * nn, "MEX re-indexed kernels"));
+  MLF_TRY(launch_mex_reindex(dk, (int)kw, K0, nn, hp.as<float>(), st));
+  mlf_psf* psf = nullptr;
+  MLF_TRY(mlf_psf_create(hp.as<float>(), hp.as<float>(), K0, nn, 1, &psf, st));
+  std::unique_ptr<mlf_psf> pg(psf);
+  const double hs = psf->hsum_z[0];
+  if (!std::isfinite(hs) || hs == 0.0)
+    return fail(MLF_ERR_UNSUPPORTED, "tensor-core MEX projector: kernel sum is zero or not finite");
+  const int64_t Wp = (W + nn - 1) / nn * nn, Hq = (H + nn - 1) / nn * nn;
+  std::vector<int64_t> xr(n, Wp), xc(n, Hq);
+  std::vector<int32_t> z0(n, 0), nz(n, 1);
+  mlf_batch* b = nullptr;
+  MLF_TRY(mlf_batch_create(psf, (int32_t)n, xr.data(), xc.data(), z0.data(), nz.data(), &b));
+  std::unique_ptr<mlf_batch> bg(b);
+  DevBuf pin, pout;
+  MLF_TRY(pin.alloc(sizeof(float) * Wp * Hq * n, "MEX padded slices"));
+  MLF_TRY(pout.alloc(sizeof(float) * Wp * Hq * n, "MEX padded output"));
+  MLF_TRY(launch_mex_pad(db, W, H, n, Wp, Hq, kw % 2 == 0, pin.as<float>(), st));
+  std::vector<const float*> vp(n);
+  std::vector<float*> op(n);
+  for (int64_t i = 0; i < n; ++i) {
+    vp[i] = pin.as<float>() + i * Wp * Hq;
+    op[i] = pout.as<float>() + i * Wp * Hq;
+  }
+  MLF_TRY(mlf_batch_forward_project(b, vp.data(), op.data(), 1, MLF_PREC_BF16X3, st));
+  MLF_TRY(launch_mex_crop(pout.as<float>(), Wp, Hq, W, H, n, dout, st));
+  MLF_CUDA(cudaStreamSynchronize(st));
+  return MLF_OK;
+}
+
 int mlf_conv_vec(const float* bitmap, int64_t W, int64_t H, int64_t n, const float* kernels,
                  int64_t kw, int32_t nnum, float* out, void* stream) {
+  return mlf_conv_vec_ex(bitmap, W, H, n, kernels, kw, nnum, out, MLF_CONV_AUTO, stream);
+}
+
+int mlf_conv_vec_ex(const float* bitmap, int64_t W, int64_t H, int64_t n, const float* kernels,
+                    int64_t kw, int32_t nnum, float* out, int32_t method, void* stream) {
   clear_error();
+  if (method != MLF_CONV_AUTO && method != MLF_CONV_DIRECT && method != MLF_CONV_TENSOR)
+    return fail(MLF_ERR_INVALID, "mlf_conv_vec_ex: unknown method");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // src/cuda/mex_lfm_convolution_vec.cu:313-347 -- 2-D/3-D single bitmap, n >= 1,
   // 4-D single kernels with kw <= 341; the kernel count per axis is fixed at 15 (:35).
@@ -173,7 +225,18 @@ int mlf_conv_vec(const float* bitmap, int64_t W, int64_t H, int64_t n, const flo
   MLF_TRY(stage_in(kernels, (size_t)(kw * kw * nnum * nnum), kin, &dk, st));
   OutStage o;
   MLF_TRY(stage_out(out, (size_t)(W * H * n), bout, &o));
-  MLF_TRY(conv_vec_run(db, W, H, n, dk, kw, nnum, o.dev, st));
+  const double flop = 2.0 * (double)W * H * n * kw * kw;
+  bool done = false;
+  if (method == MLF_CONV_TENSOR || (method == MLF_CONV_AUTO && flop >= 1e11)) {
+    const int rc = conv_vec_tc(db, W, H, n, dk, kw, o.dev, st);
+    if (rc == MLF_OK)
+      done = true;
+    else if (rc != MLF_ERR_UNSUPPORTED || method == MLF_CONV_TENSOR)
+      return rc;
+    else
+      clear_error();
+  }
+  if (!done) MLF_TRY(conv_vec_run(db, W, H, n, dk, kw, nnum, o.dev, st));
   MLF_TRY(finish_out(o, st));
   MLF_CUDA(cudaStreamSynchronize(st));
   return MLF_OK;

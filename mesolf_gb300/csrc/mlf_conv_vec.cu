@@ -62,7 +62,70 @@ k_conv_vec(const float* __restrict__ in, int W, int H, const float* __restrict__
   if (x < W && y < H) out[(int64_t)i * W * H + (int64_t)y * W + x] = acc;
 }
 
+// ---- tensor-core route: the correlation above (kernel slot from the OUTPUT pixel's phase)
+// equals the full light-field forward projection (PSF slice from the SOURCE pixel's phase,
+// forwardProjectGPU.m) of the re-indexed kernel
+//   H'[d][psi] = K[c - d + hk][(psi - (c - d)) mod 15]   per axis, c = (K0-1)/2, hk = kw/2,
+// embedded in K0 = 15 + 30 m >= kw + 14 so that every tap lies inside the phase-space crop.
+__global__ void k_mex_reindex(const float* __restrict__ K, int kw, int K0, int nn, float* __restrict__ Hp) {
+  const int c = (K0 - 1) / 2, hk = kw / 2;
+  const int64_t total = (int64_t)K0 * K0 * nn * nn;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int dx = (int)(e % K0);
+    const int dy = (int)((e / K0) % K0);
+    const int px = (int)((e / ((int64_t)K0 * K0)) % nn);
+    const int py = (int)(e / ((int64_t)K0 * K0 * nn));
+    const int kx = c - dx + hk, ky = c - dy + hk;
+    float v = 0.f;
+    if (kx >= 0 && kx < kw && ky >= 0 && ky < kw) {
+      const int fx = ((px - (c - dx)) % nn + nn) % nn, fy = ((py - (c - dy)) % nn + nn) % nn;
+      v = K[(int64_t)kx + (int64_t)kw * (ky + (int64_t)kw * (fx + (int64_t)nn * fy))];
+    }
+    Hp[e] = v;
+  }
+}
+
+// slices of the bitmap -> zero-padded Wp x Hq slices; for even kw the reference never reads
+// the last input row / column, so they are zeroed
+__global__ void k_mex_pad(const float* __restrict__ bm, int64_t W, int64_t H, int64_t n, int64_t Wp, int64_t Hq,
+                          int zero_last, float* __restrict__ dst) {
+  const int64_t total = Wp * Hq * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = e % Wp, y = (e / Wp) % Hq, i = e / (Wp * Hq);
+    float v = 0.f;
+    if (x < W && y < H && !(zero_last && (x == W - 1 || y == H - 1))) v = bm[x + W * (y + H * i)];
+    dst[e] = v;
+  }
+}
+
+__global__ void k_mex_crop(const float* __restrict__ src, int64_t Wp, int64_t Hq, int64_t W, int64_t H, int64_t n,
+                           float* __restrict__ out) {
+  const int64_t total = W * H * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = e % W, y = (e / W) % H, i = e / (W * H);
+    out[e] = src[x + Wp * (y + Hq * i)];
+  }
+}
+
 }  // namespace
+
+int launch_mex_reindex(const float* K, int kw, int K0, int nn, float* Hp, cudaStream_t st) {
+  k_mex_reindex<<<2048, 256, 0, st>>>(K, kw, K0, nn, Hp);
+  MLF_LAUNCHED();
+  return MLF_OK;
+}
+int launch_mex_pad(const float* bm, int64_t W, int64_t H, int64_t n, int64_t Wp, int64_t Hq, bool zero_last,
+                   float* dst, cudaStream_t st) {
+  k_mex_pad<<<2048, 256, 0, st>>>(bm, W, H, n, Wp, Hq, zero_last ? 1 : 0, dst);
+  MLF_LAUNCHED();
+  return MLF_OK;
+}
+int launch_mex_crop(const float* src, int64_t Wp, int64_t Hq, int64_t W, int64_t H, int64_t n, float* out,
+                    cudaStream_t st) {
+  k_mex_crop<<<2048, 256, 0, st>>>(src, Wp, Hq, W, H, n, out);
+  MLF_LAUNCHED();
+  return MLF_OK;
+}
 
 int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,
                  int64_t kw, int nnum, float* d_out, cudaStream_t st) {

@@ -218,6 +218,12 @@ size_t tc_work_plan_bytes(const Psf* psf, const std::vector<int>& Li, const std:
 int filter_run(Solver* s, cudaStream_t st);
 int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,
                  int64_t kw, int nnum, float* d_out, cudaStream_t st);
+// pieces of the tensor-core route of the MEX projector (mlf_conv_vec.cu)
+int launch_mex_reindex(const float* K, int kw, int K0, int nn, float* Hp, cudaStream_t st);
+int launch_mex_pad(const float* bm, int64_t W, int64_t H, int64_t n, int64_t Wp, int64_t Hq, bool zero_last,
+                   float* dst, cudaStream_t st);
+int launch_mex_crop(const float* src, int64_t Wp, int64_t Hq, int64_t W, int64_t H, int64_t n, float* out,
+                    cudaStream_t st);
 
 // view kernels (instantiated per tap count T in mlf_view_T*.cu)
 struct ViewArgs {

@@ -165,6 +165,34 @@ def test_sample_filter_zero_plane_stays_zero(cuda):
     assert rel_l2(got, ref) <= 1e-6
 
 
+@pytest.mark.parametrize("W,H,n,kw", [(40, 33, 3, 7), (31, 46, 2, 16), (64, 50, 2, 61), (90, 77, 1, 120),
+                                      (45, 60, 2, 241)])
+def test_conv_vec_tensor_route_matches_oracle_and_direct(cuda, W, H, n, kw):
+    """The MEX projector through the tensor-core route (the correlation recast as the full
+    forward projection of re-indexed kernels): 1e-5 of the FP64 oracle and of the direct
+    CUDA-core kernel (relative L2)."""
+    import torch
+    from mesolf_gb300 import mex_lfm_convolution_vec
+    rng = np.random.default_rng(W + 3 * kw)
+    bm = rng.random((W, H, n)).astype(np.float32)
+    K = rng.random((kw, kw, 15, 15)).astype(np.float32)
+    tc = mex_lfm_convolution_vec(bm, K, method="tensor")
+    direct = mex_lfm_convolution_vec(bm, K, method="direct")
+    if kw <= 61:
+        ref = R.lfm_conv_vec(bm, K)
+        assert rel_l2(tc, ref) <= 1e-5, rel_l2(tc, ref)
+    assert rel_l2(tc, direct) <= 1e-5, rel_l2(tc, direct)
+
+
+def test_conv_vec_tensor_route_rejects_wide_kernels(cuda):
+    from mesolf_gb300 import MesoLFError, mex_lfm_convolution_vec
+    bm = np.ones((30, 30), np.float32)
+    with pytest.raises(MesoLFError):
+        mex_lfm_convolution_vec(bm, np.ones((243, 243, 15, 15), np.float32), method="tensor")
+    out = mex_lfm_convolution_vec(bm, np.ones((243, 243, 15, 15), np.float32), method="auto")
+    assert out.shape == (30, 30)
+
+
 # ------------------------------------------------------------------------------ RL solve
 RL_CASES = [((5, 4), 61, 3, 2), ((4, 6), 91, 5, 2), ((3, 3), 231, 3, 1), ((8, 7), 61, 7, 3)]
 
