@@ -259,3 +259,42 @@ def test_phase_space_kept_mask_matches_impulses():
                 lf[u::N, v::N] = R.forward_ps(Hps[:, :, u, v, :], vol, N)
         same = np.abs(lf - full).max() <= 1e-9 * max(1.0, np.abs(full).max())
         assert same == bool(keep[i, j, a, b]), (i, j, a, b)
+
+
+@pytest.mark.parametrize("W,H,kw", [(31, 46, 16), (40, 33, 7), (47, 52, 21)])
+def test_mex_correlation_equals_forward_projection_of_reindexed_kernels(W, H, kw):
+    """The identity behind the tensor-core route of the MEX projector: the correlation with
+    the kernel slot taken from the output pixel's phase (mex_lfm_convolution_vec.cu:43-266)
+    equals the full forward projection (forwardProjectGPU.m, PSF slice from the source
+    pixel's phase) of H'[d][psi] = K[c-d+hk][(psi-(c-d)) mod 15], embedded in K0 = 15 + 30m
+    >= kw + 14, on the bitmap zero-padded to multiples of 15 (last row / column zeroed for
+    even kw) -- and so equals the interleaved phase-space views of H'."""
+    rng = np.random.default_rng(kw)
+    bm = rng.random((W, H))
+    K = rng.random((kw, kw, 15, 15))
+    ref = R.lfm_conv_vec(bm, K)
+    K0 = 15
+    while K0 < kw + 14:
+        K0 += 30
+    c, hk = (K0 - 1) // 2, kw // 2
+    Hp = np.zeros((K0, K0, 15, 15, 1))
+    for dx in range(K0):
+        kx = c - dx + hk
+        if not 0 <= kx < kw:
+            continue
+        for dy in range(K0):
+            ky = c - dy + hk
+            if not 0 <= ky < kw:
+                continue
+            ps = (np.arange(15) - (c - dx)) % 15
+            qs = (np.arange(15) - (c - dy)) % 15
+            Hp[dx, dy, :, :, 0] = K[kx, ky][np.ix_(ps, qs)]
+    b = bm.copy()
+    if kw % 2 == 0:
+        b[W - 1, :] = 0
+        b[:, H - 1] = 0
+    Wp, Hq = -(-W // 15) * 15, -(-H // 15) * 15
+    bp = np.zeros((Wp, Hq, 1))
+    bp[:W, :H, 0] = b
+    out = R.forward_project_full(Hp, bp)[:W, :H]
+    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
