@@ -156,6 +156,7 @@ struct Solver {
   int tev_used = 0;
   bool timing = false;
   bool lite = false;            // batch member: geometry, filter plan and filter scratch only
+  bool lite_ready = false;      // ... the latter two built by lite_prepare on the first solve
   int z0 = 0;                   // first PSF plane of this patch (batch members)
   TcSolverState* tc = nullptr;  // built on the first tensor-core solve
   ~Solver();
@@ -194,6 +195,8 @@ int rl_iteration_count_views(const std::vector<std::vector<double>>& w);
 int forward_view_prec(Solver* s, const float* d_vol, int u, int v, int precision, float* d_hx, cudaStream_t st);
 int sample_filter(Solver* s, float* d_vol, cudaStream_t st);
 int filter_init(Solver* s);
+// a batch member's filter plan and scratch, on first use (allocates: outside any capture)
+int lite_prepare(Solver* s);
 int timing_mark(Solver* s, cudaStream_t st);
 // tensor-core path (mlf_tc.cu).  A work set covers P patches (P = 1 for a single solver);
 // `members[p]` supplies each patch's geometry, filter plan and filter scratch.

@@ -467,12 +467,7 @@ int solver_init(Solver* s) {
                                          " not in {3,5,...,17} (K0 up to 255 at N = 15)");
   s->Pa = round_up(s->Li, 4);
   s->plane = (int64_t)s->Lj * s->Pa;
-  if (s->lite) {
-    // batch member: geometry, filter plan and filter scratch only
-    MLF_TRY(s->Xtmp.alloc((size_t)s->Xr * s->Xc * s->Z * sizeof(float), "filter scratch"));
-    MLF_TRY(s->red.alloc(4096 * sizeof(double), "reduction scratch"));
-    return filter_init(s);
-  }
+  if (s->lite) return MLF_OK;  // batch member: geometry now, filter plan and scratch on first solve
   s->tilesA = ceil_div(s->Li, 4);
   s->tilesB = ceil_div(s->Lj, 8);
   s->tps = s->tilesA * s->tilesB;
@@ -537,6 +532,15 @@ int solver_init(Solver* s) {
   MLF_CUDA(cudaMemset(s->Xtmp.p, 0, s->Xtmp.bytes));
   MLF_CUDA(cudaMemset(s->rpad.p, 0, s->rpad.bytes));
   MLF_TRY(filter_init(s));
+  return MLF_OK;
+}
+
+int lite_prepare(Solver* s) {
+  if (!s->lite || s->lite_ready) return MLF_OK;
+  MLF_TRY(s->Xtmp.alloc((size_t)s->Xr * s->Xc * s->Z * sizeof(float), "filter scratch"));
+  MLF_TRY(s->red.alloc(4096 * sizeof(double), "reduction scratch"));
+  MLF_TRY(filter_init(s));
+  s->lite_ready = true;
   return MLF_OK;
 }
 

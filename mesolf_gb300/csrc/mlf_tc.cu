@@ -1264,6 +1264,7 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
     MLF_CUDA(cudaEventCreate(&e1));
     MLF_CUDA(cudaEventRecord(e0, st));
   }
+  for (Solver* m : members) MLF_TRY(lite_prepare(m));  // filter plans of batch members (allocates)
   timer->timing = stats != nullptr;
   timer->tev_used = 0;
   int64_t launches = 0;
