@@ -302,6 +302,7 @@ def main():
                  "ms_per_step": mms, "speedup_vs_plain_fp32": ms / mms,
                  "rel_l2_vs_plain_fp32": float(d),
                  "gpu_launches": int(mlaunch),
+                 "launch_config": {k: st2[k] for k in ("fwd_splits", "fwd_stages", "bwd_xbufs", "tuned")},
                  "view_kernels_ms_per_view": mk_ms / max(1, mk_n),
                  "roofline": {"bound": "tensor", "achieved": mflop / (mk_ms * 1e-3) / 1e12,
                               "traffic": KTC_DRAM_BYTES if (Xr, Xc, Z) == (1005, 1005, 51) else None,

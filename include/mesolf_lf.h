@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define MLF_ABI_VERSION 1
+#define MLF_ABI_VERSION 2
 
 enum mlf_status_code {
   MLF_OK = 0,
@@ -58,6 +58,13 @@ typedef struct mlf_stats {
   double view_kernel_ms;        /* summed device time of the projector (view) kernel launches */
   int64_t view_kernel_launches; /* number of projector kernel launches timed */
   int64_t kernel_launches;      /* kernels launched by the solve */
+  /* tensor-core solves: the launch configuration in use, chosen by the autotuner on the
+   * first solve of the work set at this precision (timing candidates on one view step)
+   * unless the environment sets MLF_TUNE=0; 0 for FP32 solves */
+  int32_t fwd_splits;           /* split-K count of the forward GEMM over the channels */
+  int32_t fwd_stages;           /* shared-memory ring depth of the forward GEMM */
+  int32_t bwd_xbufs;            /* X-tile buffers per half in the back projection (1 or 2) */
+  int32_t tuned;                /* 1 if chosen by timing, 0 if the built-in heuristics */
 } mlf_stats;
 
 /* Library / ABI version (MLF_ABI_VERSION). */

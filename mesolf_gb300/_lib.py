@@ -62,7 +62,9 @@ SIGNATURES = {
 class MLFStats(ctypes.Structure):
     _fields_ = [("n_views", ctypes.c_int32), ("iterations", ctypes.c_int32), ("gpu_ms", ctypes.c_double),
                 ("view_ms", ctypes.c_double), ("view_kernel_ms", ctypes.c_double),
-                ("view_kernel_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+                ("view_kernel_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
+                ("fwd_splits", ctypes.c_int32), ("fwd_stages", ctypes.c_int32), ("bwd_xbufs", ctypes.c_int32),
+                ("tuned", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -592,6 +592,7 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     stats->view_kernel_ms = vk;
     stats->view_kernel_launches = s->tev_used / 2;
     stats->kernel_launches = launches;
+    stats->fwd_splits = stats->fwd_stages = stats->bwd_xbufs = stats->tuned = 0;
   }
   s->timing = false;
   s->tev_used = 0;

@@ -34,6 +34,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -860,6 +861,14 @@ struct TcPsfState {
 struct TcSolverState {
   int P = 0, MP = 0, Zch = 0, splits = 1, ks_per_split = 0, KSF = 0, nsm = 0;
   float d_eps = 0.f;  // the members' variant (all the same)
+  // launch configuration per precision: split-K count of the forward GEMM (the partials
+  // buffer holds splits_max), its ring depth, the back projection's X buffers per half
+  struct Tune {
+    int done = 0, tuned = 0, splits = 0, ksp = 0, fwd_stages = 0, xbufs = 0;
+  };
+  Tune tune[4];
+  int splits_max = 1, splits_def = 1, ksp_def = 0;
+  int fwd_stages = 0, xbufs = 0;  // in use (0: derive from shared memory)
   bool dtab_ok = false;  // every patch has >= 2q+2 lenslets per side: D from class tables
   std::vector<int> pos0, Li, Lj, LL, z0, nz;
   std::vector<int> views;   // union of the patches' active views, spiral order
@@ -1026,6 +1035,9 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   t->splits = std::max(1, std::min(t->KSF, t->nsm / std::max(1, mt)));
   t->ks_per_split = (t->KSF + t->splits - 1) / t->splits;
   t->splits = (t->KSF + t->ks_per_split - 1) / t->ks_per_split;
+  t->splits_def = t->splits;
+  t->ksp_def = t->ks_per_split;
+  t->splits_max = std::min(t->KSF, 2 * t->splits);
   const int64_t nch = psf->nch;
   MLF_TRY(t->X.alloc((size_t)nch * t->MP * 4, "tc volume (FP32)"));
   MLF_TRY(t->lfs.alloc((size_t)psf->N * psf->N * t->MP * 4, "tc sub-aperture images"));
@@ -1037,7 +1049,7 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_TRY(t->ar_hi.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->ar_lo.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->a1.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
-  MLF_TRY(t->ypart.alloc((size_t)t->splits * t->MP * tp->NB * 4, "tc forward partials"));
+  MLF_TRY(t->ypart.alloc((size_t)t->splits_max * t->MP * tp->NB * 4, "tc forward partials"));
   MLF_TRY(t->err.alloc(sizeof(int), "tc error flag"));
   t->dtab_ok = true;
   for (int p = 0; p < t->P; ++p)
@@ -1112,6 +1124,7 @@ int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cud
   a.NN = psf->N * psf->N;
   const size_t stage = (size_t)FWD_XTILE + (size_t)tp->NB * 128 * (blo ? 2 : 1);
   a.stages = (int)std::max<size_t>(2, std::min<size_t>(FWD_MAX_STAGES, (size_t)(tp->fwd_dyn_max - 1024) / stage));
+  if (t->fwd_stages > 0 && (size_t)t->fwd_stages * stage + 1024 <= (size_t)tp->fwd_dyn_max) a.stages = t->fwd_stages;
   const size_t fsmem = (size_t)a.stages * stage + 1024;
   if (fsmem > (size_t)tp->fwd_dyn_max)
     return fail(MLF_ERR_UNSUPPORTED, "tensor-core forward projection: taps tile exceeds shared memory");
@@ -1175,7 +1188,8 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   const int mt = t->MP / BM, nt = tp->CHP / BWD_BN;
   const int grid = std::min(mt * nt, t->nsm);
   // two X buffers when they fit (D from tables frees the A1 operand's ring slots)
-  const int xbufs = (!dgemm && bwd_smem_bytes(alo, blo, false, 2) <= (size_t)tp->bwd_dyn_max) ? 2 : 1;
+  int xbufs = (!dgemm && bwd_smem_bytes(alo, blo, false, 2) <= (size_t)tp->bwd_dyn_max) ? 2 : 1;
+  if (t->xbufs == 1) xbufs = 1;
   const size_t smem = bwd_smem_bytes(alo, blo, dgemm, xbufs);
   if (dgemm)
     k_tc_bwd<true, 1><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a, mt, nt);
@@ -1254,6 +1268,101 @@ int capture_iteration(const Psf* psf, TcSolverState* t, const std::vector<Solver
 
 }  // namespace
 
+// The launch configuration of this precision (tuned, or the heuristics) into effect.
+void tc_apply_tune(TcSolverState* t, int precision) {
+  const TcSolverState::Tune& g = t->tune[precision & 3];
+  if (g.done) {
+    t->splits = g.splits;
+    t->ks_per_split = g.ksp;
+    t->fwd_stages = g.fwd_stages;
+    t->xbufs = g.xbufs;
+  } else {
+    t->splits = t->splits_def;
+    t->ks_per_split = t->ksp_def;
+    t->fwd_stages = 0;
+    t->xbufs = 0;
+  }
+}
+
+// Autotuner: time the candidate launch configurations on the first view step of the work
+// set (forward GEMM: split-K count in {s/2, s, 2s} x ring depth in {2, 3, 4}; back
+// projection: one or two X buffers per half) and keep the fastest.  X is saved before and
+// restored after, so the solve is unaffected.  Runs once per work set and precision, before
+// the iteration is captured; MLF_TUNE=0 keeps the heuristics.
+int tc_autotune(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st) {
+  TcSolverState::Tune& g = t->tune[precision & 3];
+  if (g.done) return MLF_OK;
+  g.done = 1;
+  g.splits = t->splits_def;
+  g.ksp = t->ksp_def;
+  const char* env = std::getenv("MLF_TUNE");
+  if ((env && std::strcmp(env, "0") == 0) || t->views.empty()) return MLF_OK;
+  DevBuf xsave;
+  MLF_TRY(xsave.alloc(t->X.bytes, "autotune volume copy"));
+  MLF_CUDA(cudaMemcpyAsync(xsave.p, t->X.p, t->X.bytes, cudaMemcpyDeviceToDevice, st));
+  cudaEvent_t e0, e1;
+  MLF_CUDA(cudaEventCreate(&e0));
+  MLF_CUDA(cudaEventCreate(&e1));
+  auto timed = [&](auto&& launch, float* ms) -> int {
+    MLF_TRY(launch());  // warm
+    MLF_CUDA(cudaEventRecord(e0, st));
+    for (int r = 0; r < 2; ++r) MLF_TRY(launch());
+    MLF_CUDA(cudaEventRecord(e1, st));
+    MLF_CUDA(cudaEventSynchronize(e1));
+    MLF_CUDA(cudaEventElapsedTime(ms, e0, e1));
+    return MLF_OK;
+  };
+  const int v0 = t->views[0];
+  const float* w0 = t->wtab_dev.as<float>();
+  float best = 1e30f;
+  for (int s : {std::max(1, t->splits_def / 2), t->splits_def, t->splits_max}) {
+    const int ksp = (t->KSF + s - 1) / s;
+    const int sp = (t->KSF + ksp - 1) / ksp;
+    if (sp > t->splits_max) continue;
+    for (int stg = 2; stg <= FWD_MAX_STAGES; ++stg) {
+      t->splits = sp;
+      t->ks_per_split = ksp;
+      t->fwd_stages = stg;
+      float ms = 0.f;
+      MLF_TRY(timed([&] { return tc_fwd_launch(psf, t, precision, v0, st, w0); }, &ms));
+      if (ms < best) {
+        best = ms;
+        g.splits = sp;
+        g.ksp = ksp;
+        g.fwd_stages = stg;
+      }
+    }
+  }
+  // the back projection needs the ratio image of view 0 under the chosen forward
+  t->splits = g.splits;
+  t->ks_per_split = g.ksp;
+  t->fwd_stages = g.fwd_stages;
+  MLF_TRY(tc_fwd_launch(psf, t, precision, v0, st, w0));
+  MLF_TRY(tc_col2im(psf, t, v0, true, nullptr, st));
+  MLF_TRY(tc_im2col_ratio(psf, t, precision, st));
+  if (t->dtab_ok) {
+    best = 1e30f;
+    for (int xb = 1; xb <= 2; ++xb) {
+      t->xbufs = xb;
+      float ms = 0.f;
+      MLF_TRY(timed([&] {
+        MLF_CUDA(cudaMemcpyAsync(t->X.p, xsave.p, t->X.bytes, cudaMemcpyDeviceToDevice, st));
+        return tc_bwd_launch(psf, t, precision, v0, w0, st);
+      }, &ms));
+      if (ms < best) {
+        best = ms;
+        g.xbufs = xb;
+      }
+    }
+  }
+  MLF_CUDA(cudaMemcpyAsync(t->X.p, xsave.p, t->X.bytes, cudaMemcpyDeviceToDevice, st));
+  MLF_CUDA(cudaStreamSynchronize(st));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  g.tuned = 1;
+  return MLF_OK;
+}
+
 int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vector<const float*>& lf,
            const std::vector<const float*>& warm, const std::vector<float*>& out, int max_iter, int precision,
            mlf_stats* stats, Solver* timer, cudaStream_t st) {
@@ -1282,6 +1391,8 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
     }
   }
   if (max_iter > 0) {
+    MLF_TRY(tc_autotune(psf, t, precision, st));  // first solve at this precision only
+    tc_apply_tune(t, precision);
     TcSolverState::Iteration& g = t->iter[precision & 3][timer->timing ? 1 : 0];
     if (!g.exec) {
       timer->tev_used = 0;
@@ -1317,6 +1428,10 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
     stats->view_kernel_ms = vk * max_iter;
     stats->view_kernel_launches = (int64_t)(timer->tev_used / 2) * max_iter;
     stats->kernel_launches = launches;
+    stats->fwd_splits = t->splits;
+    stats->fwd_stages = t->fwd_stages;
+    stats->bwd_xbufs = t->xbufs ? t->xbufs : (t->dtab_ok ? 2 : 1);
+    stats->tuned = t->tune[precision & 3].tuned;
     MLF_TRY(tc_check_error(t));
   }
   timer->timing = false;
@@ -1327,6 +1442,7 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
 // Forward projection of one view with the tensor cores (parity tests), single solver.
 int tc_forward_view(Solver* s, int precision, const float* d_vol, int view, float* hx_out, cudaStream_t st) {
   TcSolverState* t = s->tc;
+  tc_apply_tune(t, precision);
   MLF_TRY(launch_to_phase(d_vol, work_geo(t, s, 0), t->X.as<float>(), st));
   MLF_TRY(tc_fwd_launch(s->psf, t, precision, view, st));
   return tc_col2im(s->psf, t, view, false, hx_out, st);
@@ -1336,6 +1452,7 @@ int tc_forward_project(TcSolverState* t, const std::vector<Solver*>& members, co
                        const std::vector<float*>& lf_out, int precision, const float* zscale, cudaStream_t st) {
   const Psf* psf = members[0]->psf;
   const int N = psf->N;
+  tc_apply_tune(t, precision);
   for (int p = 0; p < t->P; ++p)
     MLF_TRY(launch_to_phase(vols[p], work_geo(t, members[p], p), t->X.as<float>() + t->pos0[p], st,
                             zscale ? zscale + t->z0[p] : nullptr));
@@ -1351,6 +1468,7 @@ int tc_forward_project(TcSolverState* t, const std::vector<Solver*>& members, co
 // One RL view step on the tensor cores (parity tests), single solver.
 int tc_view_step(Solver* s, int precision, const float* d_lf, float* d_vol, int view, float w, cudaStream_t st) {
   TcSolverState* t = s->tc;
+  tc_apply_tune(t, precision);
   const PatchGeo g = work_geo(t, s, 0);
   MLF_TRY(launch_extract_views(d_lf, g, t->lfs.as<float>(), t->MP, 0, st));
   MLF_TRY(launch_to_phase(d_vol, g, t->X.as<float>(), st));

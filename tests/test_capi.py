@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol(lib):
     for name in header_functions():
         assert hasattr(lib, name), name
         assert name in _lib.SIGNATURES, f"{name} missing from the ctypes signature table"
-    assert lib.mlf_version() == 1
+    assert lib.mlf_version() == 2
 
 
 def _err(lib):

@@ -104,3 +104,25 @@ def test_tc_solve_small_uneven(cuda):
     # the FP32 path on the same solver still matches after tensor-core solves
     got = s.run(to_dev(LF), 2).cpu().numpy()
     assert rel_l2(got, ref) <= 1e-4
+
+
+def test_autotuned_solve_matches_heuristic_configuration(cuda, monkeypatch):
+    """The autotuner (first tensor-core solve of a work set) only changes launch parameters:
+    the tuned solve equals one with the built-in heuristics (MLF_TUNE=0) up to the summation
+    order of the split-K partials, and the stats report the configuration."""
+    import torch
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver
+    from mesolf_gb300.api import _fortran
+    w = synth.small_config(lenslets=(20, 18), K0=61, Z=5, seed=7)
+    H, Ht = w.psf()
+    lf = _fortran(torch.as_tensor(np.ascontiguousarray(w.measured(H, w.volume()))).cuda())[0]
+    psf = PhaseSpacePSF(H, Ht)
+    a = RLSolver(psf, lf.shape)
+    va = a.run(lf, 2, precision="bf16x2").cpu().numpy()
+    sa = a.last_stats
+    assert sa["tuned"] == 1 and sa["fwd_splits"] >= 1 and 2 <= sa["fwd_stages"] <= 4 and sa["bwd_xbufs"] in (1, 2)
+    monkeypatch.setenv("MLF_TUNE", "0")
+    b = RLSolver(psf, lf.shape)
+    vb = b.run(lf, 2, precision="bf16x2").cpu().numpy()
+    assert b.last_stats["tuned"] == 0
+    assert np.linalg.norm(va - vb) / np.linalg.norm(vb) <= 1e-5
