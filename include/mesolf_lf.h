@@ -100,6 +100,18 @@ int mlf_conv_vec(const float* bitmap, int64_t W, int64_t H, int64_t n,
 enum mlf_conv_method { MLF_CONV_AUTO = 0, MLF_CONV_DIRECT = 1, MLF_CONV_TENSOR = 2 };
 int mlf_conv_vec_ex(const float* bitmap, int64_t W, int64_t H, int64_t n, const float* kernels, int64_t kw,
                     int32_t nnum, float* out, int32_t method, void* stream);
+/* Sum of MEX projections in one pass, the "collect and forward-project" section of
+ * src/gen_seed_library_local_with_ring_bg_same_size.m:257-318 (per depth z: the slices of
+ * every segment at that depth projected with Ht(:,:,:,:,z), added to that segment's
+ * accumulator; four kinds of slices).  out[:,:,o] = sum over the input slices j with
+ * slot[j] = o of mex_lfm_convolution_vec(bitmaps[:,:,j], kernels[:,:,:,:,plane[j]]).
+ * bitmaps W x H x n, kernels kw x kw x 15 x 15 x Z, out W x H x n_out (host or device);
+ * plane[], slot[] host arrays of n.  On the tensor cores (one batched forward projection of
+ * the re-indexed kernels, FP32-class accuracy) when kw <= 241 and every plane's kernel sum is
+ * finite and non-zero; otherwise slice by slice with the direct kernel.  Synchronous. */
+int mlf_conv_vec_accumulate(const float* bitmaps, int64_t W, int64_t H, int64_t n, const int32_t* plane,
+                            const int32_t* slot, int64_t n_out, const float* kernels, int64_t kw, int32_t nnum,
+                            int64_t Z, float* out, void* stream);
 
 /* ---------------------------------------------------------------------------------
  * Phase-space PSF.  Replaces recon_theory_phase_space_LFM_with_filter.m:13-40 and

@@ -8,8 +8,10 @@ from ._lib import MesoLFError, load as load_library  # noqa: F401
 from .api import (BatchSolver, PhaseSpacePSF, RLSolver, mex_lfm_convolution_vec,  # noqa: F401
                   recon_theory_phase_space_LFM_with_filter,
                   recon_theory_phase_space_LFM_with_filter_simple_peeling, forwardProjectGPU,
-                  forwardProjectACC, forwardProjectGPU_discrete, forwardProjectGPU_skip_2D)
+                  forwardProjectACC, forwardProjectGPU_discrete, forwardProjectGPU_skip_2D,
+                  mex_lfm_convolution_vec_accumulate, seed_library_projections)
 
 __all__ = ["MesoLFError", "load_library", "BatchSolver", "PhaseSpacePSF", "RLSolver", "mex_lfm_convolution_vec",
            "recon_theory_phase_space_LFM_with_filter", "recon_theory_phase_space_LFM_with_filter_simple_peeling",
-           "forwardProjectGPU", "forwardProjectACC", "forwardProjectGPU_discrete", "forwardProjectGPU_skip_2D"]
+           "forwardProjectGPU", "forwardProjectACC", "forwardProjectGPU_discrete", "forwardProjectGPU_skip_2D",
+           "mex_lfm_convolution_vec_accumulate", "seed_library_projections"]

@@ -30,6 +30,8 @@ SIGNATURES = {
     "mlf_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "mlf_conv_vec": (ctypes.c_int, [_vp, _i64, _i64, _i64, _vp, _i64, _i32, _vp, _vp]),
     "mlf_conv_vec_ex": (ctypes.c_int, [_vp, _i64, _i64, _i64, _vp, _i64, _i32, _vp, _i32, _vp]),
+    "mlf_conv_vec_accumulate": (ctypes.c_int, [_vp, _i64, _i64, _i64, _vp, _vp, _i64, _vp, _i64, _i32, _i64,
+                                               _vp, _vp]),
     "mlf_psf_create": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i64, ctypes.POINTER(_vp), _vp]),
     "mlf_psf_destroy": (ctypes.c_int, [_vp]),
     "mlf_psf_info": (ctypes.c_int, [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),

@@ -97,6 +97,58 @@ def mex_lfm_convolution_vec(bitmap, kernels, stream=None, method="auto"):
     return out
 
 
+def mex_lfm_convolution_vec_accumulate(bitmaps, plane, slot, n_out, kernels, stream=None):
+    """``out[:, :, o] = sum over j with slot[j] == o of mex_lfm_convolution_vec(bitmaps[:, :, j],
+    kernels[:, :, :, :, plane[j]])`` in one pass (``mlf_conv_vec_accumulate``).  bitmaps
+    (W, H, n), kernels (kw, kw, 15, 15, Z); plane and slot 0-based integer sequences of n."""
+    lib = _lib.load()
+    W, Hh, n = bitmaps.shape
+    kw, Z = kernels.shape[0], kernels.shape[4]
+    pl = np.ascontiguousarray(np.asarray(plane, dtype=np.int32))
+    sl = np.ascontiguousarray(np.asarray(slot, dtype=np.int32))
+    if pl.size != n or sl.size != n:
+        raise _lib.MesoLFError(_lib.MLF_ERR_INVALID, "plane and slot must have one entry per slice")
+    bk, bp = _fortran(bitmaps)
+    kk, kp = _fortran(kernels)
+    out, op = _empty_like_kind(bitmaps, (W, Hh, int(n_out)))
+    check(lib.mlf_conv_vec_accumulate(bp, W, Hh, n, pl.ctypes.data, sl.ctypes.data, int(n_out), kp, kw,
+                                      int(kernels.shape[2]), Z, op, _stream_of(bitmaps, stream)))
+    del bk, kk
+    return out
+
+
+def seed_library_projections(Ht, sample, sample_mask, ring, ring_mask, unique_arrays):
+    """The "collect and forward-project" section of
+    ``src/gen_seed_library_local_with_ring_bg_same_size.m:257-318``: for every depth z, the
+    slices of every segment at that depth (``find(unique_array == z)``) are projected with
+    ``Ht(:,:,:,:,z)`` through ``mex_lfm_convolution_vec`` and added to the segment's
+    accumulator, for the sample, its mask (binarised, ``> 0``), the ring and its mask.
+
+    Segment i's volumes are (W, H, d_i) arrays, ``unique_arrays[i]`` the 1-based PSF plane
+    of each of its d_i slices.  Returns ``(m_spatial_init_ext, m_seg_mask_ext,
+    m_ring_init_ext, m_ring_mask_ext)``, each (W, H, N_seg), as host float32 arrays (the
+    reference gathers them).  One batched pass on the GPU instead of 4 MEX calls per depth."""
+    nseg = len(unique_arrays)
+    kinds = [sample, sample_mask, ring, ring_mask]
+    slices, plane, slot = [], [], []
+    for k, vols in enumerate(kinds):
+        for i in range(nseg):
+            v = np.asarray(vols[i], dtype=np.float32)
+            if v.ndim == 2:
+                v = v[:, :, None]
+            if k in (1, 3):
+                v = (v > 0).astype(np.float32)
+            ua = np.ravel(unique_arrays[i])
+            for s in range(v.shape[2]):
+                slices.append(v[:, :, s])
+                plane.append(int(ua[s]) - 1)
+                slot.append(k * nseg + i)
+    bm = np.asfortranarray(np.stack(slices, axis=2))
+    out = mex_lfm_convolution_vec_accumulate(bm, plane, slot, 4 * nseg, np.asfortranarray(Ht, dtype=np.float32))
+    out = np.asarray(out)
+    return tuple(np.asfortranarray(out[:, :, k * nseg:(k + 1) * nseg]) for k in range(4))
+
+
 class PhaseSpacePSF:
     """Normalised phase-space PSF resident in HBM (``…_with_filter.m:13-40``)."""
 

@@ -242,6 +242,104 @@ int mlf_conv_vec_ex(const float* bitmap, int64_t W, int64_t H, int64_t n, const 
   return MLF_OK;
 }
 
+int mlf_conv_vec_accumulate(const float* bitmaps, int64_t W, int64_t H, int64_t n, const int32_t* plane,
+                            const int32_t* slot, int64_t n_out, const float* kernels, int64_t kw, int32_t nnum,
+                            int64_t Z, float* out, void* stream) {
+  clear_error();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!bitmaps || !plane || !slot || !kernels || !out) return fail(MLF_ERR_INVALID, "mlf_conv_vec_accumulate: null pointer");
+  if (W < 1 || H < 1 || n < 1 || n_out < 1 || Z < 1) return fail(MLF_ERR_INVALID, "mlf_conv_vec_accumulate: empty input");
+  if (kw < 1 || kw > 341) return fail(MLF_ERR_INVALID, "mlf_conv_vec_accumulate: kernel_width exceeds kernel_width_limit=341");
+  if (nnum != 15) return fail(MLF_ERR_INVALID, "mlf_conv_vec_accumulate: the kernel grid must be 15 x 15");
+  std::vector<int> zmin(n_out, (int)Z), zmax(n_out, -1);
+  for (int64_t j = 0; j < n; ++j) {
+    if (plane[j] < 0 || plane[j] >= Z || slot[j] < 0 || slot[j] >= n_out)
+      return fail(MLF_ERR_INVALID, "mlf_conv_vec_accumulate: slice " + std::to_string(j) + ": plane or slot out of range");
+    zmin[slot[j]] = std::min(zmin[slot[j]], plane[j]);
+    zmax[slot[j]] = std::max(zmax[slot[j]], plane[j]);
+  }
+  const int64_t img = W * H, kz = kw * kw * nnum * nnum;
+  DevBuf bin, kin, bout;
+  const float *db = nullptr, *dk = nullptr;
+  MLF_TRY(stage_in(bitmaps, (size_t)(img * n), bin, &db, st));
+  MLF_TRY(stage_in(kernels, (size_t)(kz * Z), kin, &dk, st));
+  OutStage o;
+  MLF_TRY(stage_out(out, (size_t)(img * n_out), bout, &o));
+  MLF_CUDA(cudaMemsetAsync(o.dev, 0, sizeof(float) * img * n_out, st));
+  const bool even = kw % 2 == 0;
+  // tensor-core route: one PSF of the re-indexed kernels of every plane, one patch per output
+  // slot spanning its planes, one batched forward projection
+  int K0 = 15;
+  while (K0 < kw + 14) K0 += 30;
+  bool done = false;
+  if (K0 <= 255) {
+    const int nn = 15;
+    DevBuf hp;
+    MLF_TRY(hp.alloc(sizeof(float) * K0 * K0 * nn * nn * Z, "MEX re-indexed kernels"));
+    for (int64_t z = 0; z < Z; ++z)
+      MLF_TRY(launch_mex_reindex(dk + z * kz, (int)kw, K0, nn, hp.as<float>() + z * K0 * K0 * nn * nn, st));
+    mlf_psf* psf = nullptr;
+    MLF_TRY(mlf_psf_create(hp.as<float>(), hp.as<float>(), K0, nn, Z, &psf, st));
+    std::unique_ptr<mlf_psf> pg(psf);
+    bool sums_ok = true;
+    for (int64_t z = 0; z < Z; ++z) sums_ok = sums_ok && std::isfinite(psf->hsum_z[z]) && psf->hsum_z[z] != 0.0;
+    if (sums_ok) {
+      const int64_t Wp = (W + nn - 1) / nn * nn, Hq = (H + nn - 1) / nn * nn;
+      std::vector<int64_t> xr, xc;
+      std::vector<int32_t> z0, nz, patch_of(n_out, -1);
+      std::vector<int64_t> voff;
+      int64_t vtot = 0;
+      for (int64_t s = 0; s < n_out; ++s) {
+        if (zmax[s] < 0) continue;  // nothing projected into this slot: stays zero
+        patch_of[s] = (int32_t)xr.size();
+        xr.push_back(Wp);
+        xc.push_back(Hq);
+        z0.push_back(zmin[s]);
+        nz.push_back(zmax[s] - zmin[s] + 1);
+        voff.push_back(vtot);
+        vtot += Wp * Hq * nz.back();
+      }
+      mlf_batch* b = nullptr;
+      MLF_TRY(mlf_batch_create(psf, (int32_t)xr.size(), xr.data(), xc.data(), z0.data(), nz.data(), &b));
+      std::unique_ptr<mlf_batch> bg(b);
+      DevBuf vols, lfo;
+      MLF_TRY(vols.alloc(sizeof(float) * vtot, "accumulated slice volumes"));
+      MLF_TRY(lfo.alloc(sizeof(float) * Wp * Hq * xr.size(), "accumulated projections"));
+      MLF_CUDA(cudaMemsetAsync(vols.p, 0, sizeof(float) * vtot, st));
+      for (int64_t j = 0; j < n; ++j) {
+        const int p = patch_of[slot[j]];
+        float* dst = vols.as<float>() + voff[p] + Wp * Hq * (plane[j] - zmin[slot[j]]);
+        MLF_TRY(launch_mex_pad_add(db + j * img, W, H, Wp, Hq, even, dst, st));
+      }
+      std::vector<const float*> vp(xr.size());
+      std::vector<float*> op(xr.size());
+      for (size_t p = 0; p < xr.size(); ++p) {
+        vp[p] = vols.as<float>() + voff[p];
+        op[p] = lfo.as<float>() + (int64_t)p * Wp * Hq;
+      }
+      MLF_TRY(mlf_batch_forward_project(b, vp.data(), op.data(), 1, MLF_PREC_BF16X3, st));
+      for (int64_t s = 0; s < n_out; ++s)
+        if (patch_of[s] >= 0)
+          MLF_TRY(launch_mex_crop(lfo.as<float>() + (int64_t)patch_of[s] * Wp * Hq, Wp, Hq, W, H, 1,
+                                  o.dev + s * img, st));
+      MLF_CUDA(cudaStreamSynchronize(st));
+      done = true;
+    }
+  }
+  if (!done) {
+    // direct route: every slice projected on its own and added to its slot
+    DevBuf tmp;
+    MLF_TRY(tmp.alloc(sizeof(float) * img, "projection scratch"));
+    for (int64_t j = 0; j < n; ++j) {
+      MLF_TRY(conv_vec_run(db + j * img, W, H, 1, dk + plane[j] * kz, kw, nnum, tmp.as<float>(), st));
+      MLF_TRY(launch_mex_pad_add(tmp.as<float>(), W, H, W, H, false, o.dev + slot[j] * img, st));
+    }
+  }
+  MLF_TRY(finish_out(o, st));
+  MLF_CUDA(cudaStreamSynchronize(st));
+  return MLF_OK;
+}
+
 int mlf_psf_create(const float* H, const float* Ht, int64_t K0, int32_t N, int64_t Z, mlf_psf** out,
                    void* stream) {
   clear_error();

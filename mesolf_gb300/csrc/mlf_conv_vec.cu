@@ -98,6 +98,17 @@ __global__ void k_mex_pad(const float* __restrict__ bm, int64_t W, int64_t H, in
   }
 }
 
+// dst += src zero-padded to Wp x Hq (one slice; last row / column dropped for even kw)
+__global__ void k_mex_pad_add(const float* __restrict__ src, int64_t W, int64_t H, int64_t Wp, int64_t Hq,
+                              int zero_last, float* __restrict__ dst) {
+  const int64_t total = W * H;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = e % W, y = e / W;
+    if (zero_last && (x == W - 1 || y == H - 1)) continue;
+    dst[x + Wp * y] += src[e];
+  }
+}
+
 __global__ void k_mex_crop(const float* __restrict__ src, int64_t Wp, int64_t Hq, int64_t W, int64_t H, int64_t n,
                            float* __restrict__ out) {
   const int64_t total = W * H * n;
@@ -117,6 +128,12 @@ int launch_mex_reindex(const float* K, int kw, int K0, int nn, float* Hp, cudaSt
 int launch_mex_pad(const float* bm, int64_t W, int64_t H, int64_t n, int64_t Wp, int64_t Hq, bool zero_last,
                    float* dst, cudaStream_t st) {
   k_mex_pad<<<2048, 256, 0, st>>>(bm, W, H, n, Wp, Hq, zero_last ? 1 : 0, dst);
+  MLF_LAUNCHED();
+  return MLF_OK;
+}
+int launch_mex_pad_add(const float* src, int64_t W, int64_t H, int64_t Wp, int64_t Hq, bool zero_last, float* dst,
+                       cudaStream_t st) {
+  k_mex_pad_add<<<512, 256, 0, st>>>(src, W, H, Wp, Hq, zero_last ? 1 : 0, dst);
   MLF_LAUNCHED();
   return MLF_OK;
 }

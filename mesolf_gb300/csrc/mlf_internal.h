@@ -225,6 +225,8 @@ int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const f
 int launch_mex_reindex(const float* K, int kw, int K0, int nn, float* Hp, cudaStream_t st);
 int launch_mex_pad(const float* bm, int64_t W, int64_t H, int64_t n, int64_t Wp, int64_t Hq, bool zero_last,
                    float* dst, cudaStream_t st);
+int launch_mex_pad_add(const float* src, int64_t W, int64_t H, int64_t Wp, int64_t Hq, bool zero_last, float* dst,
+                       cudaStream_t st);
 int launch_mex_crop(const float* src, int64_t Wp, int64_t Hq, int64_t W, int64_t H, int64_t n, float* out,
                     cudaStream_t st);
 

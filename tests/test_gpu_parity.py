@@ -193,6 +193,32 @@ def test_conv_vec_tensor_route_rejects_wide_kernels(cuda):
     assert out.shape == (30, 30)
 
 
+@pytest.mark.parametrize("kw", [21, 16, 243])
+def test_seed_library_projections_match_the_reference_loop(cuda, kw):
+    """gen_seed_library_local_with_ring_bg_same_size.m:257-318 restated as a literal loop over
+    depths and segments on the FP64 oracle of the MEX projector, against the one-pass GPU
+    version (tensor-core route for kw <= 241, direct route for 243); relative L2 1e-5 per
+    accumulator."""
+    from mesolf_gb300 import seed_library_projections
+    rng = np.random.default_rng(kw)
+    W = H = 40 if kw <= 61 else 16   # the FP64 loop is slow for the widest kernel
+    Z = 4
+    Ht = rng.random((kw, kw, 15, 15, Z)).astype(np.float32)
+    ua = [[1, 2, 4], [3], [2, 3]]
+    vols = [[rng.random((W, H, len(u))).astype(np.float32) - 0.3 for u in ua] for _ in range(4)]
+    got = seed_library_projections(Ht, *vols, ua)
+    for k in range(4):
+        ref = np.zeros((W, H, len(ua)))
+        for z in range(1, Z + 1):
+            for i, u in enumerate(ua):
+                for s in [j for j, zz in enumerate(u) if zz == z]:
+                    v = vols[k][i][:, :, s]
+                    if k in (1, 3):
+                        v = (v > 0).astype(np.float32)
+                    ref[:, :, i] += R.lfm_conv_vec(v, Ht[:, :, :, :, z - 1])
+        assert rel_l2(got[k], ref) <= 1e-5, (k, rel_l2(got[k], ref))
+
+
 # ------------------------------------------------------------------------------ RL solve
 RL_CASES = [((5, 4), 61, 3, 2), ((4, 6), 91, 5, 2), ((3, 3), 231, 3, 1), ((8, 7), 61, 7, 3)]
 
