@@ -373,6 +373,7 @@ def main():
     # at N = 1 only
     if ws == 1:
         line["mex_projector"] = mex_block(dev, peak)
+        line["seed_library"] = seed_block(Ht, dev)
         solver.close()
         torch.cuda.empty_cache()
         line["precision_vs_fp64_oracle"] = precision_block(psf, dev)
@@ -671,6 +672,47 @@ def mex_block(dev, fp32_peak, steps=2):
             "rel_l2_tensor_vs_direct": d_rel,
             "rel_l2_vs_fp64_oracle_64_pixels": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
             "data": "seeded uniform bitmap and kernels of the fixture's shape"}
+
+
+def seed_block(Ht, dev, n_seg=128, side=396, depth=9):
+    """The seed library's "collect and forward-project" section on a synthetic segment set:
+    n_seg segments of side x side pixels, each `depth` consecutive planes of the PSF, four
+    kinds of slices (sample, mask, ring, ring mask), projected with Ht in one pass
+    (seed_library_projections).  The reference makes 4 MEX calls per depth over the slices at
+    that depth; its time is estimated from one direct MEX slice projection."""
+    import torch
+    from mesolf_gb300 import mex_lfm_convolution_vec, seed_library_projections
+    Z = Ht.shape[4]
+    rng = np.random.default_rng(21)
+    ua, vols = [], [[] for _ in range(4)]
+    for i in range(n_seg):
+        z0 = int(rng.integers(0, Z - depth + 1))
+        ua.append(list(range(z0 + 1, z0 + depth + 1)))
+        base = rng.random((side, side, depth)).astype(np.float32)
+        for k in range(4):
+            vols[k].append(base if k % 2 == 0 else (base > 0.7).astype(np.float32))
+    seed_library_projections(Ht, *vols, ua)      # warm (PSF set-up paths, allocations)
+    t0 = time.perf_counter()
+    out = seed_library_projections(Ht, *vols, ua)
+    t_pass = time.perf_counter() - t0
+    one = torch.as_tensor(vols[0][0][:, :, :1]).to(dev)
+    Kz = torch.as_tensor(np.ascontiguousarray(Ht[:, :, :, :, 0])).to(dev)
+    mex_lfm_convolution_vec(one, Kz, method="direct")
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    mex_lfm_convolution_vec(one, Kz, method="direct")
+    torch.cuda.synchronize()
+    t_slice = time.perf_counter() - t1
+    n_proj = 4 * n_seg * depth
+    kw = Ht.shape[0]
+    return {"workload": f"seed_library_{n_seg}seg_{side}px_{depth}planes_kw{kw}", "segments": n_seg,
+            "slice_projections": n_proj, "one_pass_s": t_pass,
+            "per_depth_mex_loop_estimate_s": t_slice * n_proj,
+            "speedup_vs_per_depth_loop": t_slice * n_proj / t_pass,
+            "tflops_algorithmic": 2.0 * side * side * kw * kw * n_proj / t_pass / 1e12,
+            "all_finite": bool(all(np.isfinite(o).all() for o in out)),
+            "note": "host arrays in and out, as the reference gathers its accumulators; the loop estimate is the "
+                    "direct MEX kernel's time for one slice times the number of slice projections"}
 
 
 def _measured_bf16():
