@@ -130,20 +130,25 @@ def seed_library_projections(Ht, sample, sample_mask, ring, ring_mask, unique_ar
     reference gathers them).  One batched pass on the GPU instead of 4 MEX calls per depth."""
     nseg = len(unique_arrays)
     kinds = [sample, sample_mask, ring, ring_mask]
-    slices, plane, slot = [], [], []
+    depth = [np.asarray(v).shape[2] if np.asarray(v).ndim == 3 else 1 for v in sample]
+    W, Hh = np.asarray(sample[0]).shape[:2]
+    n = 4 * sum(depth)
+    bm = np.empty((W, Hh, n), dtype=np.float32, order="F")   # every slice copied once, in place
+    plane, slot = np.empty(n, np.int32), np.empty(n, np.int32)
+    j = 0
     for k, vols in enumerate(kinds):
         for i in range(nseg):
-            v = np.asarray(vols[i], dtype=np.float32)
+            v = np.asarray(vols[i])
             if v.ndim == 2:
                 v = v[:, :, None]
+            d = v.shape[2]
             if k in (1, 3):
-                v = (v > 0).astype(np.float32)
-            ua = np.ravel(unique_arrays[i])
-            for s in range(v.shape[2]):
-                slices.append(v[:, :, s])
-                plane.append(int(ua[s]) - 1)
-                slot.append(k * nseg + i)
-    bm = np.asfortranarray(np.stack(slices, axis=2))
+                np.greater(v, 0, out=bm[:, :, j:j + d], casting="unsafe")
+            else:
+                bm[:, :, j:j + d] = v
+            plane[j:j + d] = np.ravel(unique_arrays[i])[:d].astype(np.int32) - 1
+            slot[j:j + d] = k * nseg + i
+            j += d
     out = mex_lfm_convolution_vec_accumulate(bm, plane, slot, 4 * nseg, np.asfortranarray(Ht, dtype=np.float32))
     out = np.asarray(out)
     return tuple(np.asfortranarray(out[:, :, k * nseg:(k + 1) * nseg]) for k in range(4))
