@@ -374,6 +374,7 @@ def main():
     if ws == 1:
         line["mex_projector"] = mex_block(dev, peak)
         line["seed_library"] = seed_block(Ht, dev)
+        line["summary_image"] = summary_block(dev, cpu=not args.no_cpu_baseline)
         solver.close()
         torch.cuda.empty_cache()
         line["precision_vs_fp64_oracle"] = precision_block(psf, dev)
@@ -713,6 +714,85 @@ def seed_block(Ht, dev, n_seg=128, side=396, depth=9):
             "all_finite": bool(all(np.isfinite(o).all() for o in out)),
             "note": "host arrays in and out, as the reference gathers its accumulators; the loop estimate is the "
                     "direct MEX kernel's time for one slice times the number of slice projections"}
+
+
+def summary_block(dev, side=1005, T=2000, steps=3, cpu=True, cpu_pixels=8192):
+    """The step before the reconstruction: the summary image (LFIMG) of a side x side-pixel,
+    T-frame sensor movie with the reference's default parameters (pixelwise detrend,
+    bg_iter 5, windows 100 and 20 frames, poly_index 3), movie resident in HBM (`value`) and
+    from pinned host memory (`e2e`).  The movie is 4 B x pixels x frames (8.08 GB at 1005^2 x
+    2000, larger than L2); every pass streams it once: 2 x bg_iter passes per call."""
+    import torch
+    from mesolf_gb300 import synth
+    from mesolf_gb300.api import summary_image
+    from oracle import mesolf_ref as R
+    P = side * side
+    prm = ("pixelwise", 5, 100, 20, 3)
+    Y = synth.sensor_movie(P, T, seed=17, device=dev)
+    img, _, _ = summary_image(Y, *prm)  # warm
+    pm, acc = np.zeros(5), np.zeros(5)
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        img, bs, bt = summary_image(Y, *prm, pass_ms=pm)
+        acc += pm
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    acc /= steps
+    movie_bytes = 4.0 * P * T
+    passes = 2 * prm[1]
+    hbm = _measured_hbm()
+    gbs = lambda t_ms: movie_bytes / (t_ms * 1e-3) / 1e9 if t_ms > 0 else None
+    last_gbs = gbs(acc[3])
+    # end to end from pinned host memory: H2D of the movie, D2H of the three outputs
+    host = torch.empty((T, P), dtype=torch.float32, pin_memory=True)
+    host.copy_(Y.T)
+    hmov = host.T
+    summary_image(hmov, *prm)
+    t0 = time.perf_counter()
+    for _ in range(2):
+        himg, _, _ = summary_image(hmov, *prm)
+    t_e2e = (time.perf_counter() - t0) / 2
+    same = bool(torch.equal(himg, img.cpu()))
+    out = {"workload": f"summary_image_{side}x{side}px_{T}frames_pixelwise_bg5_w100_w20_p3",
+           "value": T / (ms * 1e-3), "unit": "frames/s", "ms_per_call": ms,
+           "movie_gb": movie_bytes / 1e9, "movie_passes": passes,
+           "pass_ms": {"first_column_with_max": acc[0], "column": acc[1], "row": acc[2],
+                       "last_pixelwise": acc[3], "finalise": acc[4]},
+           "stream_gbs": {"column": gbs(acc[1]), "row": gbs(acc[2]), "last_pixelwise": last_gbs,
+                          "whole_call": movie_bytes * passes / (ms * 1e-3) / 1e9},
+           "roofline": {"bound": "hbm", "kernel": "k_si_pixelwise (last pass: s, moving means, power, std)",
+                        "achieved": last_gbs, "peak": hbm, "unit": "GB/s",
+                        "frac": last_gbs / hbm if (hbm and last_gbs) else None,
+                        "algorithmic_bytes_per_launch": movie_bytes, "traffic": None,
+                        "note": "achieved = movie bytes / last-pass time (CUDA events around the launch); "
+                                "peak = measured copy bandwidth"},
+           "e2e": {"value": T / t_e2e, "unit": "frames/s", "s_per_call": t_e2e,
+                   "h2d_bytes_per_step": int(movie_bytes), "d2h_bytes_per_step": int(4 * (2 * P + T)),
+                   "same_result_as_device_input": same},
+           "kernel_launches_per_call": 3 * prm[1] + 2,
+           "data": "synthetic: per-pixel baselines, 20% bleaching trend, calcium-like transients, noise "
+                   "(mesolf_gb300/synth.py sensor_movie)"}
+    if cpu:
+        idx = torch.arange(0, P, P // cpu_pixels, device=dev)[:cpu_pixels]
+        sub = Y[idx].cpu().numpy()
+        t0 = time.perf_counter()
+        ri, _, _ = R.summary_image(sub, *prm)
+        t_cpu = time.perf_counter() - t0
+        got = img[idx].double().cpu().numpy()
+        scale = float(np.dot(got, ri) / np.dot(ri, ri))
+        out["cpu_baseline"] = {"value": T / (t_cpu * P / len(idx)), "unit": "frames/s", "cores": 1,
+                               "kind": "port",
+                               "sample": f"the FP64 numpy oracle on {len(idx)} of the {P} pixels, all {T} frames "
+                                         f"({t_cpu:.2f} s), scaled by the pixel count"}
+        out["rel_l2_vs_fp64_oracle_sampled_pixels"] = float(np.linalg.norm(got / scale - ri) / np.linalg.norm(ri))
+    del Y, host, hmov
+    torch.cuda.empty_cache()
+    return out
 
 
 def _measured_bf16():

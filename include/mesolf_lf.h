@@ -114,6 +114,31 @@ int mlf_conv_vec_accumulate(const float* bitmaps, int64_t W, int64_t H, int64_t 
                             int64_t Z, float* out, void* stream);
 
 /* ---------------------------------------------------------------------------------
+ * Summary image, the step that produces LFIMG.  Replaces
+ * summary_image_generation_module(sensor_movie, patch_info, SI)
+ * (src/module/summary_image_generation_module.m:43-133, with src/rank_1_factorization.m and
+ * src/compute_std_image.m): rank-1 background by bg_iter alternating iterations, then
+ *   MLF_DETREND_PIXELWISE: per pixel y = movie/max, y - movmean(y, window_1), movmean(., window_2),
+ *                          .^poly_index, population std over the frames;
+ *   MLF_DETREND_GLOBAL:    compute_std_image(movie/max, bg_spatial, bg_temporal) as written;
+ * summary = image / max(image).  movie: P pixels x T frames, column-major (frame-contiguous),
+ * host or device.  Outputs (host or device): summary P, bg_spatial P (Y t / max, not normalised
+ * in the last iteration), bg_temporal T (unit norm); bg_spatial / bg_temporal may be NULL.
+ * A negative std radicand (possible through compute_std_image's expansion) gives 0 where
+ * MATLAB gives a complex value.  The global mode's Savitzky-Golay baseline is only plotted by
+ * the reference and is not computed.  Synchronous. */
+enum mlf_detrend_mode { MLF_DETREND_PIXELWISE = 0, MLF_DETREND_GLOBAL = 1 };
+int mlf_summary_image(const float* movie, int64_t P, int64_t T, int32_t mode, int32_t bg_iter, int32_t window_1,
+                      int32_t window_2, int32_t poly_index, float* summary_out, float* bg_spatial_out,
+                      float* bg_temporal_out, void* stream);
+/* The same, with the device time of each pass (CUDA events on `stream`) in pass_ms[5]:
+ * first column pass (with the max), mean later column pass, mean row pass, last pass (the
+ * image), finalisation (image max and scale); pass_ms may be NULL. */
+int mlf_summary_image_ex(const float* movie, int64_t P, int64_t T, int32_t mode, int32_t bg_iter,
+                         int32_t window_1, int32_t window_2, int32_t poly_index, float* summary_out,
+                         float* bg_spatial_out, float* bg_temporal_out, double* pass_ms, void* stream);
+
+/* ---------------------------------------------------------------------------------
  * Phase-space PSF.  Replaces recon_theory_phase_space_LFM_with_filter.m:13-40 and
  * gen_phasespace_PSF_theory.m:1-31: per-depth FP64 normalisation of H and Ht, the
  * phase-space realignment of H, the crop of Ht, and the view weights (weight_cut 0.2,

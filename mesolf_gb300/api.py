@@ -5,6 +5,8 @@
 * :func:`recon_theory_phase_space_LFM_with_filter` --
   ``Xguess = recon_theory_phase_space_LFM_with_filter(LFIMG, H, Ht, maxIter, gpuFlag, gpu_id)``
   (``src/recon/recon_theory_phase_space_LFM_with_filter.m:10``).
+* :func:`summary_image_generation_module` -- the step that produces ``LFIMG``
+  (``src/module/summary_image_generation_module.m:1-133``).
 * :class:`PhaseSpacePSF` / :class:`RLSolver` -- the same solve split into a resident PSF
   and a reusable per-image-size context (what a serving loop keeps in HBM).
 
@@ -115,6 +117,63 @@ def mex_lfm_convolution_vec_accumulate(bitmaps, plane, slot, n_out, kernels, str
                                       int(kernels.shape[2]), Z, op, _stream_of(bitmaps, stream)))
     del bk, kk
     return out
+
+
+DETREND_MODES = {"pixelwise": _lib.MLF_DETREND_PIXELWISE, "global": _lib.MLF_DETREND_GLOBAL}
+
+#: Defaults of the summary-image parameters (``src/mesolf_set_params.m:114-132``).
+SUMMARY_DEFAULTS = {"detrend_mode": "pixelwise", "bg_iter": 5, "pixelwise_window_1": 100,
+                    "pixelwise_window_2": 20, "pixelwise_poly_index": 3}
+
+
+def summary_image(movie, detrend_mode="pixelwise", bg_iter=5, window_1=100, window_2=20, poly_index=3,
+                  stream=None, pass_ms=None):
+    """Summary image of a (pixels, frames) movie (``mlf_summary_image``): returns
+    ``(summary, bg_spatial, bg_temporal)`` with shapes (P,), (P,), (T,), host arrays for a host
+    movie and CUDA tensors for a CUDA tensor.  ``pass_ms``: an optional float64 array of 5
+    that receives the device time of the passes (``mlf_summary_image_ex``)."""
+    lib = _lib.load()
+    if detrend_mode not in DETREND_MODES:
+        raise _lib.MesoLFError(_lib.MLF_ERR_INVALID, 'Invalid value for param "detrend_mode"')
+    shape = tuple(movie.shape)
+    if len(shape) != 2:
+        raise _lib.MesoLFError(_lib.MLF_ERR_INVALID, "the movie must be (pixels, frames)")
+    P, T = shape
+    keep, mp = _fortran(movie)
+    img, ip = _empty_like_kind(movie, (P,))
+    bs, sp = _empty_like_kind(movie, (P,))
+    bt, tp = _empty_like_kind(movie, (T,))
+    pm = None
+    if pass_ms is not None:
+        if not (isinstance(pass_ms, np.ndarray) and pass_ms.dtype == np.float64 and pass_ms.size >= 5):
+            raise _lib.MesoLFError(_lib.MLF_ERR_INVALID, "pass_ms must be a float64 array of 5")
+        pm = pass_ms.ctypes.data
+    check(lib.mlf_summary_image_ex(mp, P, T, DETREND_MODES[detrend_mode], int(bg_iter), int(window_1),
+                                   int(window_2), int(poly_index), ip, sp, tp, pm, _stream_of(movie, stream)))
+    del keep
+    return img, bs, bt
+
+
+def summary_image_generation_module(sensor_movie, patch_info, SI):
+    """``[summary_image, bg_spatial_init, bg_temporal_init] =
+    summary_image_generation_module(sensor_movie, patch_info, SI)``
+    (``src/module/summary_image_generation_module.m:1-133``).  sensor_movie is
+    (size_h * size_w, frames) or (size_h, size_w, frames); patch_info["size"] gives
+    (size_h, size_w); SI is a dict with the keys of :data:`SUMMARY_DEFAULTS` (missing keys take
+    those defaults).  Returns the (size_h, size_w) summary image normalised to its maximum,
+    the (size_h, size_w) rank-1 spatial background and the (1, frames) temporal background.
+    The reference's TIFF/PNG outputs and trend plot are not produced."""
+    prm = dict(SUMMARY_DEFAULTS)
+    prm.update({k: v for k, v in dict(SI).items() if k in SUMMARY_DEFAULTS})
+    h, w = (int(v) for v in patch_info["size"][:2])
+    T = sensor_movie.shape[-1]
+    mov = sensor_movie.reshape((h * w, T), order="F") if not _is_torch(sensor_movie) else \
+        sensor_movie.permute(*reversed(range(sensor_movie.dim()))).reshape(T, h * w).T
+    img, bs, bt = summary_image(mov, prm["detrend_mode"], prm["bg_iter"], prm["pixelwise_window_1"],
+                                prm["pixelwise_window_2"], prm["pixelwise_poly_index"])
+    if _is_torch(img):
+        return (img.reshape(w, h).T, bs.reshape(w, h).T, bt.reshape(1, T))
+    return img.reshape((h, w), order="F"), bs.reshape((h, w), order="F"), bt.reshape(1, T)
 
 
 def seed_library_projections(Ht, sample, sample_mask, ring, ring_mask, unique_arrays):

@@ -242,6 +242,56 @@ int mlf_conv_vec_ex(const float* bitmap, int64_t W, int64_t H, int64_t n, const 
   return MLF_OK;
 }
 
+int mlf_summary_image(const float* movie, int64_t P, int64_t T, int32_t mode, int32_t bg_iter, int32_t window_1,
+                      int32_t window_2, int32_t poly_index, float* summary_out, float* bg_spatial_out,
+                      float* bg_temporal_out, void* stream) {
+  return mlf_summary_image_ex(movie, P, T, mode, bg_iter, window_1, window_2, poly_index, summary_out,
+                              bg_spatial_out, bg_temporal_out, nullptr, stream);
+}
+
+int mlf_summary_image_ex(const float* movie, int64_t P, int64_t T, int32_t mode, int32_t bg_iter,
+                         int32_t window_1, int32_t window_2, int32_t poly_index, float* summary_out,
+                         float* bg_spatial_out, float* bg_temporal_out, double* pass_ms, void* stream) {
+  clear_error();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!movie || !summary_out) return fail(MLF_ERR_INVALID, "mlf_summary_image: null pointer");
+  if (P < 1 || T < 1) return fail(MLF_ERR_INVALID, "mlf_summary_image: empty movie");
+  if (T > INT32_MAX / 8) return fail(MLF_ERR_INVALID, "mlf_summary_image: too many frames");
+  if (mode != MLF_DETREND_PIXELWISE && mode != MLF_DETREND_GLOBAL)
+    return fail(MLF_ERR_INVALID, "mlf_summary_image: Invalid value for param \"detrend_mode\"");
+  if (bg_iter < 1) return fail(MLF_ERR_INVALID, "mlf_summary_image: bg_iter must be at least 1");
+  if (mode == MLF_DETREND_PIXELWISE && (window_1 < 1 || window_2 < 1 || poly_index < 0))
+    return fail(MLF_ERR_INVALID, "mlf_summary_image: windows must be positive and poly_index non-negative");
+  DevBuf bin, bimg, bs, bt;
+  const float* dy = nullptr;
+  MLF_TRY(stage_in(movie, (size_t)(P * T), bin, &dy, st));
+  OutStage oi, os, ot;
+  MLF_TRY(stage_out(summary_out, (size_t)P, bimg, &oi));
+  DevBuf s_own, t_own;
+  float* ds = nullptr;
+  float* dt = nullptr;
+  if (bg_spatial_out) {
+    MLF_TRY(stage_out(bg_spatial_out, (size_t)P, bs, &os));
+    ds = os.dev;
+  } else {
+    MLF_TRY(s_own.alloc(sizeof(float) * P, "summary: spatial background"));
+    ds = s_own.as<float>();
+  }
+  if (bg_temporal_out) {
+    MLF_TRY(stage_out(bg_temporal_out, (size_t)T, bt, &ot));
+    dt = ot.dev;
+  } else {
+    MLF_TRY(t_own.alloc(sizeof(float) * T, "summary: temporal background"));
+    dt = t_own.as<float>();
+  }
+  MLF_TRY(summary_run(dy, P, T, mode, bg_iter, window_1, window_2, poly_index, oi.dev, ds, dt, pass_ms, st));
+  MLF_TRY(finish_out(oi, st));
+  if (bg_spatial_out) MLF_TRY(finish_out(os, st));
+  if (bg_temporal_out) MLF_TRY(finish_out(ot, st));
+  MLF_CUDA(cudaStreamSynchronize(st));
+  return MLF_OK;
+}
+
 int mlf_conv_vec_accumulate(const float* bitmaps, int64_t W, int64_t H, int64_t n, const int32_t* plane,
                             const int32_t* slot, int64_t n_out, const float* kernels, int64_t kw, int32_t nnum,
                             int64_t Z, float* out, void* stream) {

@@ -222,6 +222,8 @@ int filter_run(Solver* s, cudaStream_t st);
 int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,
                  int64_t kw, int nnum, float* d_out, cudaStream_t st);
 // pieces of the tensor-core route of the MEX projector (mlf_conv_vec.cu)
+int summary_run(const float* dY, int64_t P, int64_t T, int mode, int bg_iter, int w1, int w2, int poly,
+                float* d_img, float* d_s, float* d_t, double* pass_ms, cudaStream_t st);
 int launch_mex_reindex(const float* K, int kw, int K0, int nn, float* Hp, cudaStream_t st);
 int launch_mex_pad(const float* bm, int64_t W, int64_t H, int64_t n, int64_t Wp, int64_t Hq, bool zero_last,
                    float* dst, cudaStream_t st);

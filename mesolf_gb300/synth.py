@@ -261,3 +261,35 @@ class SomaStream:
         v = self._blur_last(v.permute(1, 2, 0).contiguous(), self.gz, self.rz).permute(2, 0, 1)  # Z
         v = v.contiguous() + self.background
         return v.permute(2, 1, 0)
+
+
+def sensor_movie(P, T, seed=0, device=None, n_spike=0.004, tau=8.0):
+    """Synthetic sensor movie, (P pixels, T frames) float32 column-major (frame-contiguous):
+    per-pixel baseline (100..600) with a slow bleaching trend, calcium-like transients
+    (events with probability ``n_spike`` per frame, exponential decay ``tau`` frames, amplitude
+    up to 300) and Gaussian noise (sigma 8).  numpy on the host when ``device`` is None, else
+    a torch tensor built on that device (same distribution, torch's generator)."""
+    if device is None:
+        rng = np.random.default_rng(seed)
+        base = (100 + 500 * rng.random(P)).astype(np.float32)
+        trend = (1 - 0.2 * np.arange(T) / max(T, 1)).astype(np.float32)
+        Y = np.empty((P, T), np.float32, order="F")
+        c = np.zeros(P, np.float32)
+        decay = np.float32(np.exp(-1.0 / tau))
+        for j in range(T):
+            ev = rng.random(P) < n_spike
+            c = c * decay + ev * (300 * rng.random(P)).astype(np.float32)
+            Y[:, j] = base * trend[j] + c + rng.normal(0, 8, P).astype(np.float32)
+        return Y
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    base = 100 + 500 * torch.rand(P, generator=g, device=device)
+    Yt = torch.empty((T, P), dtype=torch.float32, device=device)  # row j = frame j
+    c = torch.zeros(P, device=device)
+    decay = float(np.exp(-1.0 / tau))
+    for j in range(T):
+        ev = torch.rand(P, generator=g, device=device) < n_spike
+        c = c * decay + ev * 300 * torch.rand(P, generator=g, device=device)
+        Yt[j] = base * (1 - 0.2 * j / max(T, 1)) + c + 8 * torch.randn(P, generator=g, device=device)
+    return Yt.T  # (P, T), column-major

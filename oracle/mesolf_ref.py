@@ -654,3 +654,77 @@ def forward_project_skip_2d(H, img, step, cc):
             ts[a::N, b::N] = img[a::N, b::N]
             acc += np.fft.rfft2(ts, E) * np.fft.rfft2(H[:, :, a, b, int(cc) - 1], E)
     return np.fft.irfft2(acc, E)[m:m + Xr, m:m + Xc]
+
+
+# ----------------------------------------------------------------------------- f3 summary image
+def movmean(x, k, axis=-1):
+    """MATLAB ``movmean`` / ``smoothdata(..., 'movmean', k)`` with shrinking end windows:
+    the window of element i spans ``i - floor(k/2)`` .. ``i + k - 1 - floor(k/2)`` (for even k
+    it is centred on the current and previous elements).  Each window is summed directly
+    (left to right), with no running-sum cancellation."""
+    x = np.moveaxis(np.asarray(x, dtype=np.float64), axis, -1)
+    n = x.shape[-1]
+    before = min(int(k) // 2, n - 1)
+    after = min(int(k) - 1 - int(k) // 2, n - 1)
+    s = np.zeros_like(x)
+    cnt = np.zeros(n)
+    for d in range(-before, after + 1):
+        lo, hi = max(0, -d), min(n, n - d)
+        s[..., lo:hi] += x[..., lo + d:hi + d]
+        cnt[lo:hi] += 1
+    return np.moveaxis(s / cnt, -1, axis)
+
+
+def rank_1_factorization(Y, maxIter=1, divisor=1.0):
+    """``rank_1_factorization.m:32-45``: Y ~ bg_spatial * bg_temporal (pixels x frames)."""
+    Y = np.asarray(Y, dtype=np.float64)
+    s = np.ones(Y.shape[0]) / np.sqrt(Y.shape[0])
+    t = None
+    for it in range(1, maxIter + 1):
+        t = (s @ Y) / divisor
+        t = t / np.linalg.norm(t)
+        s = (Y @ t) / divisor
+        if it < maxIter:
+            s = s / np.linalg.norm(s)
+    return s, t
+
+
+def compute_std_image(Y, y1=None, y2=None):
+    """``compute_std_image.m:22-26`` as written:
+    ``sqrt((A - y1.^2)/length(y2) - B.^2 + 2*B.*y1*C - y1.^2*C^2)`` with A = sum(Y.^2, 2),
+    B = mean(Y, 2), C = mean(y2).  A negative radicand (possible through the expansion) gives
+    a complex value in MATLAB; it is clamped to 0 here."""
+    Y = np.asarray(Y, dtype=np.float64)
+    if y1 is None:
+        y1 = np.zeros(Y.shape[0])
+        y2 = np.zeros(Y.shape[1])
+    A = (Y ** 2).sum(axis=1)
+    B = Y.mean(axis=1)
+    C = np.mean(y2)
+    v = (A - y1 ** 2) / len(y2) - B ** 2 + 2 * B * y1 * C - y1 ** 2 * C ** 2
+    return np.sqrt(np.maximum(v, 0.0))
+
+
+def summary_image(movie, mode="pixelwise", bg_iter=5, window_1=100, window_2=20, poly_index=3):
+    """``summary_image_generation_module.m:43-133`` on a (pixels x frames) movie: returns
+    ``(summary_image / max(summary_image), bg_spatial, bg_temporal)``.  Defaults are
+    ``mesolf_set_params.m:120-132``.  'global' (``:43-61``): Y = movie / max, rank-1 (s, t)
+    with divisor 1, compute_std_image(Y, s, t).  'pixelwise' (``:62-97``): rank-1 of the raw
+    movie with the max as divisor; per pixel y = movie / max, y - movmean(y, window_1),
+    movmean(., window_2), .^poly_index, compute_std_image with zero backgrounds.  The global
+    mode's Savitzky-Golay baseline (``:46-50``) only feeds a plot and is not computed."""
+    Y = np.asarray(movie, dtype=np.float64)
+    M = Y.max()
+    if mode == "global":
+        Yn = Y / M
+        s, t = rank_1_factorization(Yn, bg_iter)
+        img = compute_std_image(Yn, s, t)
+    elif mode == "pixelwise":
+        s, t = rank_1_factorization(Y, bg_iter, M)
+        y = Y / M
+        z = y - movmean(y, window_1, axis=1)
+        z = movmean(z, window_2, axis=1) ** poly_index
+        img = compute_std_image(z)
+    else:
+        raise ValueError('Invalid value for param "detrend_mode"')
+    return img / img.max(), s, t

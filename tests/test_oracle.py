@@ -298,3 +298,41 @@ def test_mex_correlation_equals_forward_projection_of_reindexed_kernels(W, H, kw
     bp[:W, :H, 0] = b
     out = R.forward_project_full(Hp, bp)[:W, :H]
     assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_movmean_matches_matlab_window_rule():
+    x = np.arange(10, dtype=float)
+    # k = 4 (even): window of element i is [i-2, i+1], shrunk at the ends
+    assert np.allclose(R.movmean(x, 4), [np.mean(x[max(0, i - 2):i + 2]) for i in range(10)])
+    # k = 3 (odd): [i-1, i+1]
+    assert np.allclose(R.movmean(x, 3), [np.mean(x[max(0, i - 1):i + 2]) for i in range(10)])
+
+
+def test_summary_image_std_and_rank1():
+    rng = np.random.default_rng(0)
+    mov = rng.random((50, 300)) + np.linspace(0, 1, 300)[None, :]
+    img, s, t = R.summary_image(mov, "pixelwise", bg_iter=2, window_1=40, window_2=5, poly_index=2)
+    assert img.shape == (50,) and np.isclose(img.max(), 1.0) and (img >= 0).all()
+    assert np.isclose(np.linalg.norm(t), 1.0)
+    # rank-1 fit of an exact rank-1 matrix recovers its factors' directions
+    a, b = rng.random(30), rng.random(80)
+    s1, t1 = R.rank_1_factorization(np.outer(a, b), 3)
+    assert np.allclose(np.abs(s1 / np.linalg.norm(s1)), a / np.linalg.norm(a))
+    assert np.allclose(np.abs(t1), b / np.linalg.norm(b))
+
+
+def test_summary_image_known_answers():
+    # pixels with a linear ramp: the moving mean of a ramp equals the ramp away from the ends
+    # (odd window), so the detrended series is zero there; a constant pixel has zero std
+    T = 200
+    ramp = np.arange(T, dtype=float)
+    mov = np.stack([1 + 0 * ramp, 5 + 0.01 * ramp, 3 + np.sin(ramp / 7)])
+    img, _, _ = R.summary_image(mov, "pixelwise", bg_iter=1, window_1=11, window_2=1, poly_index=1)
+    assert img[0] < 1e-12 and img[2] == 1.0 and 0 < img[1] < 0.1
+    # compute_std_image as written (not the residual std of Y - s t)
+    Y = np.outer(np.arange(1, 5.0), np.ones(7))
+    s, t = R.rank_1_factorization(Y, 1)
+    A, B, C = (Y ** 2).sum(1), Y.mean(1), t.mean()
+    v = (A - s ** 2) / 7 - B ** 2 + 2 * B * s * C - s ** 2 * C ** 2
+    assert (v < 0).any()  # the expansion can go negative: MATLAB gives a complex value, 0 here
+    assert np.allclose(R.compute_std_image(Y, s, t), np.sqrt(np.maximum(v, 0)))
