@@ -212,12 +212,31 @@ k_si_rowdot1(const float* __restrict__ Y, int64_t P, int64_t T, const float* __r
   s[p] = (a + b) * scal[SC_INVM];
 }
 
+template <int POLY>
+__device__ __forceinline__ float powi(float m, int poly) {
+  if (POLY >= 0) {
+    if (POLY == 0) return 1.f;
+    float x = m;
+#pragma unroll
+    for (int q = 1; q < POLY; ++q) x *= m;
+    return x;
+  }
+  float x = 1.f;
+  for (int q = 0; q < poly; ++q) x *= m;
+  return x;
+}
+
 // Last pass, 'pixelwise': s (as k_si_rowdot1) and the detrended std image of each pixel.
-// Shared memory: ring1[R1][blockDim] (last y values), ring2[R2][blockDim] (last z values),
-// R = min(window, T).  Unified step k = 0 .. T-1+a1+a2: y[k] enters window 1 (k < T),
-// y[k-w1] leaves it; z[i1] (i1 = k - a1) enters window 2, z[i1-w2] leaves it; the mean of
+// Shared memory: ring1[R1][blockDim] (last raw values), ring2[R2][blockDim] (last z values),
+// R = min(window, T).  Unified step k = 0 .. T-1+a1+a2: Y[k] enters window 1 (k < T),
+// Y[k-w1] leaves it; z[i1] (i1 = k - a1) enters window 2, z[i1-w2] leaves it; the mean of
 // window 2 around i2 = i1 - a2 gives x[i2].  Window of element i: [i-b, i+a] clipped to
-// [0, T-1], b = floor(w/2), a = w-1-b (MATLAB movmean / smoothdata 'movmean').
+// [0, T-1], b = floor(w/2), a = w-1-b (MATLAB movmean / smoothdata 'movmean').  The rings
+// hold raw movie values; 1/M is applied to the window-2 mean (the detrend is linear).
+// Steps k in [max(w1, a1 + w2), T) have full windows on both sides and every add and drop:
+// they run a branch-free form (R1 = w1, R2 = w2 there, so drop slot = write slot).  POLY >= 0
+// fixes the power at compile time; -1 takes it from `poly`.
+template <int POLY>
 __global__ void __launch_bounds__(128)
 k_si_pixelwise(const float* __restrict__ Y, int64_t P, int T, const float* __restrict__ t,
                const float* __restrict__ scal, int w1, int w2, int R1, int R2, int poly,
@@ -232,83 +251,128 @@ k_si_pixelwise(const float* __restrict__ Y, int64_t P, int T, const float* __res
   if (p < P) {
     const float invM = scal[SC_INVM];
     const int b1 = w1 / 2, a1 = w1 - 1 - b1, b2 = w2 / 2, a2 = w2 - 1 - b2;
-    const float rw1 = 1.f / (float)w1, rw2 = 1.f / (float)w2;
+    const float rw1 = 1.f / (float)w1, rw2i = invM / (float)w2;
+    const int R1n = R1 * nt, R2n = R2 * nt;
     const float* y = Y + p;
     float S1 = 0.f, L1 = 0.f, S2 = 0.f, sx = 0.f, sxx = 0.f, sa = 0.f, sb = 0.f;
-    // ring slots: in1 = k % R1, dr1 = (k - w1) % R1, c1 = (k - a1) % R1,
-    //             in2 = i1 % R2, dr2 = (i1 - w2) % R2
+    // ring offsets (slot * nt): in1 = k % R1, dr1 = (k - w1) % R1, c1 = (k - a1) % R1,
+    //                           in2 = i1 % R2, dr2 = (i1 - w2) % R2
     int in1 = 0, dr1 = 0, c1 = 0, in2 = 0, dr2 = 0;
+    auto adv = [](int& o, int nt_, int Rn) {
+      o += nt_;
+      if (o == Rn) o = 0;
+    };
     const int K = T + a1 + a2;
-    auto step = [&](int k, float yraw) {
-      // window 1 over y
+    auto step = [&](int k, float raw) {
+      // window 1
       if (k < T) {
-        const float yv = yraw * invM;
         if (k >= w1) {  // R1 == w1 here: the dropped value sits in the slot being written
           float s, e;
-          two_sum(S1, -ring1[(int64_t)in1 * nt], s, e);
+          two_sum(S1, -ring1[in1], s, e);
           S1 = s;
           L1 += e;
         }
-        ring1[(int64_t)in1 * nt] = yv;
+        ring1[in1] = raw;
         float s, e;
-        two_sum(S1, yv, s, e);
+        two_sum(S1, raw, s, e);
         S1 = s;
         L1 += e;
-        if (++in1 == R1) in1 = 0;
+        adv(in1, nt, R1n);
       } else if (k >= w1 && k - w1 < T) {
         float s, e;
-        two_sum(S1, -ring1[(int64_t)dr1 * nt], s, e);
+        two_sum(S1, -ring1[dr1], s, e);
         S1 = s;
         L1 += e;
       }
-      if (k >= w1 && ++dr1 == R1) dr1 = 0;
+      if (k >= w1) adv(dr1, nt, R1n);
       const int i1 = k - a1;
       if (i1 < 0) return;
-      // z[i1] and window 2 over z
+      // z[i1], window 2
       if (i1 < T) {
         const int cnt = min(i1 + a1, T - 1) - max(i1 - b1, 0) + 1;
         const float rc = cnt == w1 ? rw1 : 1.f / (float)cnt;
-        const float z = ring1[(int64_t)c1 * nt] - (S1 + L1) * rc;
-        if (++c1 == R1) c1 = 0;
+        const float z = fmaf(-(S1 + L1), rc, ring1[c1]);
+        adv(c1, nt, R1n);
         float zd = 0.f;
-        if (i1 >= w2) zd = ring2[(int64_t)in2 * nt];  // R2 == w2 here
-        ring2[(int64_t)in2 * nt] = z;
+        if (i1 >= w2) zd = ring2[in2];  // R2 == w2 here
+        ring2[in2] = z;
         S2 += z - zd;
-        if (++in2 == R2) in2 = 0;
+        adv(in2, nt, R2n);
       } else if (i1 >= w2 && i1 - w2 < T) {
-        S2 -= ring2[(int64_t)dr2 * nt];
+        S2 -= ring2[dr2];
       }
-      if (i1 >= w2 && ++dr2 == R2) dr2 = 0;
+      if (i1 >= w2) adv(dr2, nt, R2n);
       const int i2 = i1 - a2;
       if (i2 < 0 || i2 >= T) return;
       const int cnt = min(i2 + a2, T - 1) - max(i2 - b2, 0) + 1;
-      const float m = S2 * (cnt == w2 ? rw2 : 1.f / (float)cnt);
-      float x = 1.f;
-      for (int q = 0; q < poly; ++q) x *= m;
+      const float m = S2 * (cnt == w2 ? rw2i : invM / (float)cnt);
+      const float x = powi<POLY>(m, poly);
       sx += x;
       sxx = fmaf(x, x, sxx);
     };
-    int k = 0;
+    const int k_bulk = max(w1, a1 + w2);
     float cur[SI_PIX_U];
 #pragma unroll
     for (int u = 0; u < SI_PIX_U; ++u) cur[u] = u < T ? __ldcs(y + (int64_t)u * P) : 0.f;
+    int k = 0;
     for (; k < T; k += SI_PIX_U) {
       float nxt[SI_PIX_U];
+      if (k + 2 * SI_PIX_U <= T) {
 #pragma unroll
-      for (int u = 0; u < SI_PIX_U; ++u) {
-        const int kk = k + SI_PIX_U + u;
-        nxt[u] = kk < T ? __ldcs(y + (int64_t)kk * P) : 0.f;
+        for (int u = 0; u < SI_PIX_U; ++u) nxt[u] = __ldcs(y + (int64_t)(k + SI_PIX_U + u) * P);
+      } else {
+#pragma unroll
+        for (int u = 0; u < SI_PIX_U; ++u) {
+          const int kk = k + SI_PIX_U + u;
+          nxt[u] = kk < T ? __ldcs(y + (int64_t)kk * P) : 0.f;
+        }
       }
+      if (k >= k_bulk && k + SI_PIX_U <= T) {
+        // bulk: both windows full, every add and drop present
+        float4 tq[SI_PIX_U / 4];
 #pragma unroll
-      for (int u = 0; u < SI_PIX_U; ++u) {
-        const int kk = k + u;
-        if (kk < T) {
-          const float tj = __ldg(t + kk);
+        for (int q = 0; q < SI_PIX_U / 4; ++q) tq[q] = __ldg(reinterpret_cast<const float4*>(t + k) + q);
+#pragma unroll
+        for (int u = 0; u < SI_PIX_U; ++u) {
+          const float raw = cur[u];
+          const float4 tv = tq[u / 4];
+          const float tj = (u & 3) == 0 ? tv.x : (u & 3) == 1 ? tv.y : (u & 3) == 2 ? tv.z : tv.w;
           if (u & 1)
-            sb = fmaf(cur[u], tj, sb);
+            sb = fmaf(raw, tj, sb);
           else
-            sa = fmaf(cur[u], tj, sa);
-          step(kk, cur[u]);
+            sa = fmaf(raw, tj, sa);
+          const float d = ring1[in1];
+          ring1[in1] = raw;
+          float dd, ed, s1, e1;
+          two_sum(raw, -d, dd, ed);
+          two_sum(S1, dd, s1, e1);
+          S1 = s1;
+          L1 += e1 + ed;
+          adv(in1, nt, R1n);
+          const float z = fmaf(-(S1 + L1), rw1, ring1[c1]);
+          adv(c1, nt, R1n);
+          const float zd = ring2[in2];
+          ring2[in2] = z;
+          S2 += z - zd;
+          adv(in2, nt, R2n);
+          const float x = powi<POLY>(S2 * rw2i, poly);
+          sx += x;
+          sxx = fmaf(x, x, sxx);
+        }
+        dr1 = in1;  // R1 == w1, R2 == w2: the drop slots follow the write slots
+        dr2 = in2;
+      } else {
+#pragma unroll
+        for (int u = 0; u < SI_PIX_U; ++u) {
+          const int kk = k + u;
+          if (kk < T) {
+            const float tj = __ldg(t + kk);
+            if (u & 1)
+              sb = fmaf(cur[u], tj, sb);
+            else
+              sa = fmaf(cur[u], tj, sa);
+            step(kk, cur[u]);
+          }
         }
       }
 #pragma unroll
@@ -439,7 +503,6 @@ int summary_run(const float* dY, int64_t P, int64_t T, int mode, int bg_iter, in
   // a window of 2T or more covers the whole series for every element: same result as 2T
   w1 = (int)std::min<int64_t>(w1, 2 * T);
   w2 = (int)std::min<int64_t>(w2, 2 * T);
-  MLF_TRY(allow_max_dyn_smem((const void*)k_si_pixelwise));
   int dev = 0, optin = 0;
   MLF_CUDA(cudaGetDevice(&dev));
   MLF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -455,7 +518,9 @@ int summary_run(const float* dY, int64_t P, int64_t T, int mode, int bg_iter, in
   int64_t chunk = (cdiv(P, ps) + 3) / 4 * 4;
   ps = cdiv(P, chunk);
   const int64_t nrow = cdiv(P, nt);
-  DevBuf tpart, maxpart, scal, imgpart, sbuf;
+  DevBuf tpart, maxpart, scal, imgpart, sbuf, tbuf;
+  MLF_TRY(tbuf.alloc(sizeof(float) * (T + 4), "summary: temporal background"));  // 16-byte aligned
+  float* tb = tbuf.as<float>();
   MLF_TRY(tpart.alloc(sizeof(float) * ps * T, "summary: column partial sums"));
   MLF_TRY(maxpart.alloc(sizeof(float) * ps * ngrp, "summary: max partials"));
   MLF_TRY(scal.alloc(sizeof(float) * SC_N, "summary: scalars"));
@@ -482,14 +547,14 @@ int summary_run(const float* dY, int64_t P, int64_t T, int mode, int bg_iter, in
     }
     MLF_LAUNCHED();
     k_si_tnorm<<<1, SI_RED_THREADS, 0, st>>>(tpart.as<float>(), (int)ps, T, maxpart.as<float>(),
-                                             it == 0 ? ps * ngrp : 0, d_t, sc);
+                                             it == 0 ? ps * ngrp : 0, tb, sc);
     MLF_LAUNCHED();
     MLF_TRY(clk.mark(st));
     if (it + 1 < bg_iter) {
       if (vec)
-        k_si_rowdot4<<<(unsigned)cdiv(P / 4, SI_ROW_THREADS), SI_ROW_THREADS, 0, st>>>(dY, P, T, d_t, sc, s_tmp);
+        k_si_rowdot4<<<(unsigned)cdiv(P / 4, SI_ROW_THREADS), SI_ROW_THREADS, 0, st>>>(dY, P, T, tb, sc, s_tmp);
       else
-        k_si_rowdot1<<<(unsigned)cdiv(P, SI_ROW_THREADS), SI_ROW_THREADS, 0, st>>>(dY, P, T, d_t, sc, s_tmp);
+        k_si_rowdot1<<<(unsigned)cdiv(P, SI_ROW_THREADS), SI_ROW_THREADS, 0, st>>>(dY, P, T, tb, sc, s_tmp);
       MLF_LAUNCHED();
       MLF_TRY(clk.mark(st));
     }
@@ -497,12 +562,14 @@ int summary_run(const float* dY, int64_t P, int64_t T, int mode, int bg_iter, in
   int64_t nparts;
   if (mode == MLF_DETREND_PIXELWISE) {
     const int R1 = (int)std::min<int64_t>(w1, T), R2 = (int)std::min<int64_t>(w2, T);
-    k_si_pixelwise<<<(unsigned)nrow, nt, smem, st>>>(dY, P, (int)T, d_t, sc, w1, w2, R1, R2, poly, d_s, d_img,
-                                                      imgpart.as<float>());
+    auto kp = poly == 1 ? k_si_pixelwise<1> : poly == 2 ? k_si_pixelwise<2> : poly == 3 ? k_si_pixelwise<3>
+                                                                                      : k_si_pixelwise<-1>;
+    MLF_TRY(allow_max_dyn_smem((const void*)kp));
+    kp<<<(unsigned)nrow, nt, smem, st>>>(dY, P, (int)T, tb, sc, w1, w2, R1, R2, poly, d_s, d_img, imgpart.as<float>());
     nparts = nrow;
   } else {
     nparts = cdiv(P, SI_ROW_THREADS);
-    k_si_global<<<(unsigned)nparts, SI_ROW_THREADS, 0, st>>>(dY, P, T, d_t, sc, d_s, d_img, imgpart.as<float>());
+    k_si_global<<<(unsigned)nparts, SI_ROW_THREADS, 0, st>>>(dY, P, T, tb, sc, d_s, d_img, imgpart.as<float>());
   }
   MLF_LAUNCHED();
   MLF_TRY(clk.mark(st));
@@ -510,6 +577,7 @@ int summary_run(const float* dY, int64_t P, int64_t T, int mode, int bg_iter, in
   k_si_scale<<<(unsigned)cdiv(P, 256), 256, 0, st>>>(d_img, P, sc);
   MLF_LAUNCHED();
   MLF_TRY(clk.mark(st));
+  MLF_CUDA(cudaMemcpyAsync(d_t, tb, sizeof(float) * T, cudaMemcpyDeviceToDevice, st));
   MLF_CUDA(cudaStreamSynchronize(st));  // the scratch above is released on return
   if (pass_ms) {
     // marks: start, then per iteration: after column pass (+ t normalisation), after row pass

@@ -29,6 +29,8 @@ def rel_l2(a, b):
     (300, 50, 3, 1, 1, 1),          # unit window 2, power 1
     (256, 41, 4, 6, 3, 2),          # even windows
     (96, 1, 100, 20, 3, 1),         # one frame
+    (2048, 700, 60, 10, 4, 2),      # power 4 (runtime power), bulk steps
+    (1500, 1000, 33, 7, 2, 1),      # odd windows, power 2
 ])
 def test_pixelwise_matches_oracle(cuda, P, T, w1, w2, poly, it):
     from mesolf_gb300.api import summary_image
