@@ -33,7 +33,7 @@ constexpr int SI_COL_THREADS = 512;
 constexpr int SI_FPB = 4;           // frames per column-pass block
 constexpr int SI_ROW_THREADS = 256;
 constexpr int SI_ROW_U = 8;         // float4 frames prefetched per plain row-pass group
-constexpr int SI_PIX_U = 16;        // frames prefetched per pixelwise group
+constexpr int SI_PIX_U = 32;        // frames prefetched per pixelwise group
 constexpr int SI_RED_THREADS = 1024;
 
 // scal[]: 0 M, 1 1/M, 2 mean(t), 3 max(img)
@@ -234,8 +234,9 @@ __device__ __forceinline__ float powi(float m, int poly) {
 // [0, T-1], b = floor(w/2), a = w-1-b (MATLAB movmean / smoothdata 'movmean').  The rings
 // hold raw movie values; 1/M is applied to the window-2 mean (the detrend is linear).
 // Steps k in [max(w1, a1 + w2), T) have full windows on both sides and every add and drop:
-// they run a branch-free form (R1 = w1, R2 = w2 there, so drop slot = write slot).  POLY >= 0
-// fixes the power at compile time; -1 takes it from `poly`.
+// they run a branch-free form (R1 = w1, R2 = w2 there, so drop slot = write slot) that adds
+// (new - dropped) to the window-1 sum with one TwoSum.  POLY >= 0 fixes the power at compile
+// time; -1 takes it from `poly`.
 template <int POLY>
 __global__ void __launch_bounds__(128)
 k_si_pixelwise(const float* __restrict__ Y, int64_t P, int T, const float* __restrict__ t,
@@ -343,11 +344,10 @@ k_si_pixelwise(const float* __restrict__ Y, int64_t P, int T, const float* __res
             sa = fmaf(raw, tj, sa);
           const float d = ring1[in1];
           ring1[in1] = raw;
-          float dd, ed, s1, e1;
-          two_sum(raw, -d, dd, ed);
-          two_sum(S1, dd, s1, e1);
+          float s1, e1;
+          two_sum(S1, raw - d, s1, e1);  // (raw - d) rounds relative to the values, not to S1
           S1 = s1;
-          L1 += e1 + ed;
+          L1 += e1;
           adv(in1, nt, R1n);
           const float z = fmaf(-(S1 + L1), rw1, ring1[c1]);
           adv(c1, nt, R1n);

@@ -31,6 +31,9 @@ def rel_l2(a, b):
     (96, 1, 100, 20, 3, 1),         # one frame
     (2048, 700, 60, 10, 4, 2),      # power 4 (runtime power), bulk steps
     (1500, 1000, 33, 7, 2, 1),      # odd windows, power 2
+    (1000, 400, 500, 100, 3, 1),    # long windows: 64 pixels per block
+    (500, 600, 1000, 200, 3, 1),    # longer windows: 32 pixels per block, one per thread
+    (700, 90, 30, 8, 0, 1),         # power 0: a constant series, zero image
 ])
 def test_pixelwise_matches_oracle(cuda, P, T, w1, w2, poly, it):
     from mesolf_gb300.api import summary_image
@@ -39,7 +42,7 @@ def test_pixelwise_matches_oracle(cuda, P, T, w1, w2, poly, it):
     ri, rs, rt = R.summary_image(Y, "pixelwise", it, w1, w2, poly)
     if np.isfinite(ri).all():
         assert rel_l2(img, ri) <= TOL_IMG
-    else:  # one frame: a zero image, 0/0 as in MATLAB
+    else:  # one frame or power 0: a zero image, 0/0 as in MATLAB
         assert np.isnan(img).all()
     assert rel_l2(s, rs) <= TOL_BG
     assert rel_l2(t, rt) <= TOL_BG
