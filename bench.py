@@ -385,6 +385,7 @@ def main():
         line["mex_projector"] = mex_block(dev, peak)
         line["seed_library"] = seed_block(Ht, dev)
         line["summary_image"] = summary_block(dev, cpu=not args.no_cpu_baseline)
+        line["rectification"] = rectify_block(dev, cpu=not args.no_cpu_baseline)
         solver.close()
         torch.cuda.empty_cache()
         line["precision_vs_fp64_oracle"] = precision_block(psf, dev)
@@ -804,6 +805,73 @@ def summary_block(dev, side=1005, T=2000, steps=3, cpu=True, cpu_pixels=8192, e2
                                          f"({t_cpu:.2f} s), scaled by the pixel count"}
         out["rel_l2_vs_fp64_oracle_sampled_pixels"] = float(np.linalg.norm(got / scale - ri) / np.linalg.norm(ri))
     del Y
+    torch.cuda.empty_cache()
+    return out
+
+
+def rectify_block(dev, frame=1100, T=2000, steps=3, cpu=True):
+    """The input step: raw uint16 frames (frame x frame pixels, T frames) cut and rectified onto
+    the lenslet grid (image_load_module_aug: Nnum 15, pitch 15.27 px, one patch with a
+    one-lenslet border crop, 1050 x 1050 rectified pixels), movie left unnormalised in HBM for
+    the summary image.  `value`: frames resident in HBM; `e2e`: frames from pinned host memory
+    (cut region copied per frame inside the timed region), movie in HBM.  Algorithmic bytes per
+    frame: the raw cut read once (2 B/px) + the rectified frame written (4 B/px)."""
+    import torch
+    from mesolf_gb300 import rectify as RC
+    from oracle import mesolf_ref as R
+    SI = dict(Nnum=15, frames_dx=15.27, frames_x_offset=frame / 2 + 0.3, frames_y_offset=frame / 2 - 0.4,
+              frames_crop_border_microlenses=[1, 1, 1, 1], patch_mode="carpet", n_patches=1)
+    info = RC.determine_patch_info_aug(SI, (frame, frame))[0]
+    g = torch.Generator(device=dev)
+    g.manual_seed(23)
+    fr16 = (torch.rand((T, frame, frame), generator=g, device=dev) * 4000).to(torch.int16)
+    fr = fr16.view(torch.uint16)                       # values < 4000: the same bits
+    frames = fr.permute(2, 1, 0)                       # (rows, cols, T), column-major
+    mov = RC.image_load_module_aug(info, SI, frames, normalize=False)
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        mov = RC.image_load_module_aug(info, SI, frames, normalize=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    (y0, y1), (x0, x1) = info["raw_cut"]
+    h, w = info["size"]
+    alg = T * (2.0 * (y1 - y0 + 1) * (x1 - x0 + 1) + 4.0 * h * w)
+    hbm = _measured_hbm()
+    ach = alg / (ms * 1e-3) / 1e9
+    host = fr16.cpu().pin_memory().view(torch.uint16).permute(2, 1, 0)
+    RC.image_load_module_aug(info, SI, host, normalize=False, out_device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hm = RC.image_load_module_aug(info, SI, host, normalize=False, out_device=dev)
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    out = {"workload": f"rectify_{frame}x{frame}_u16_{T}frames_to_{h}x{w}", "value": T / (ms * 1e-3),
+           "unit": "frames/s", "ms_per_call": ms,
+           "roofline": {"bound": "hbm", "kernel": "k_rectify", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                        "frac": ach / hbm if hbm else None, "algorithmic_bytes_per_launch": alg, "traffic": None,
+                        "note": "achieved = (raw cut read + rectified movie written) / call time"},
+           "e2e": {"value": T / t_e2e, "unit": "frames/s", "s_per_call": t_e2e,
+                   "h2d_bytes_per_step": int(2 * T * (y1 - y0 + 1) * (x1 - x0 + 1)), "d2h_bytes_per_step": 0,
+                   "same_result_as_device_input": bool(torch.equal(hm, mov)),
+                   "note": "movie kept in HBM for the summary image"},
+           "data": "seeded uniform uint16 frames"}
+    if cpu:
+        sub = 8
+        fh = fr16[:sub].permute(2, 1, 0).cpu().numpy().astype(np.uint16)
+        t0 = time.perf_counter()
+        ref = R.image_load(fh, info, dict(SI, frames_end=sub))
+        t_cpu = time.perf_counter() - t0
+        got = mov[:, :sub].cpu().numpy()
+        out["cpu_baseline"] = {"value": sub / t_cpu, "unit": "frames/s", "cores": 1, "kind": "port",
+                               "sample": f"the FP64 numpy oracle (bilinear on the same grids) on {sub} frames "
+                                         f"({t_cpu:.2f} s)"}
+        out["rel_l2_vs_fp64_oracle_8_frames"] = float(np.linalg.norm(got / got.max() - ref) / np.linalg.norm(ref))
+    del frames, fr, fr16, mov, host, hm
     torch.cuda.empty_cache()
     return out
 

@@ -139,6 +139,31 @@ int mlf_summary_image_ex(const float* movie, int64_t P, int64_t T, int32_t mode,
                          float* bg_spatial_out, float* bg_temporal_out, double* pass_ms, void* stream);
 
 /* ---------------------------------------------------------------------------------
+ * Frame rectification, the step that produces the sensor movie.  Replaces the per-patch
+ * part of image_load_module_aug(patch_info, SI) (src/module/image_load_module_aug.m:19-164)
+ * on frames already in memory (reading the TIFF files stays with the caller):
+ *   output frames i = 0 .. n_final-1, n_final = numel(frames_start:frames_step:min(n_frames, frames_end));
+ *   frames_average != 0: output i is the mean of input frames
+ *       frames_start + i*frames_step + j, j < frames_step (stopping at the last frame);
+ *   otherwise output i is input frame frames_start + i*frames_step (frame numbers 1-based);
+ *   each cut to raw_cut = {y0, y1, x0, x1} (1-based, inclusive; rows y, columns x) and
+ *   rectified by img_rectify_mod (:126-164: griddedInterpolant bilinear with linear
+ *   extrapolation onto the dx/Nnum grid anchored at (raw_cut_yCenter, raw_cut_xCenter),
+ *   first lenslet aligned, cut to whole lenslets), which must give size_h x size_w
+ *   (MLF_ERR_INVALID with the reference's message otherwise);
+ *   normalize != 0: the movie is divided by its maximum (as the reference does).
+ * frames: H x W x n_frames, column-major, MLF_DTYPE_U16 or MLF_DTYPE_F32, host or device
+ * (from host memory only the cut region of the frames used is copied).  frames_end < 0 means
+ * no end.  movie_out: (size_h*size_w) x n_final floats, column-major, host or device;
+ * *n_out receives n_final (may be NULL).  Synchronous. */
+enum mlf_dtype { MLF_DTYPE_F32 = 0, MLF_DTYPE_U16 = 1 };
+int mlf_rectify_frames(const void* frames, int32_t dtype, int64_t H, int64_t W, int64_t n_frames,
+                       const int64_t* raw_cut, double raw_cut_xCenter, double raw_cut_yCenter, int32_t Nnum,
+                       double frames_dx, int64_t size_h, int64_t size_w, int64_t frames_start, int64_t frames_step,
+                       int64_t frames_end, int32_t frames_average, int32_t normalize, float* movie_out,
+                       int64_t* n_out, void* stream);
+
+/* ---------------------------------------------------------------------------------
  * Phase-space PSF.  Replaces recon_theory_phase_space_LFM_with_filter.m:13-40 and
  * gen_phasespace_PSF_theory.m:1-31: per-depth FP64 normalisation of H and Ht, the
  * phase-space realignment of H, the crop of Ht, and the view weights (weight_cut 0.2,

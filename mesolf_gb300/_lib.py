@@ -21,6 +21,8 @@ MLF_PREC_BF16 = 2
 MLF_PREC_BF16X2 = 3
 MLF_DETREND_PIXELWISE = 0
 MLF_DETREND_GLOBAL = 1
+MLF_DTYPE_F32 = 0
+MLF_DTYPE_U16 = 1
 
 #: Every symbol declared in include/mesolf_lf.h, with (restype, argtypes).
 _vp = ctypes.c_void_p
@@ -60,6 +62,9 @@ SIGNATURES = {
     "mlf_batch_plan_bytes": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, ctypes.POINTER(_i64)]),
     "mlf_forward_project": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _vp]),
     "mlf_batch_forward_project": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _vp]),
+    "mlf_rectify_frames": (ctypes.c_int, [_vp, _i32, _i64, _i64, _i64, _vp, ctypes.c_double, ctypes.c_double, _i32,
+                                          ctypes.c_double, _i64, _i64, _i64, _i64, _i64, _i32, _i32, _vp,
+                                          ctypes.POINTER(_i64), _vp]),
     "mlf_summary_image": (ctypes.c_int, [_vp, _i64, _i64, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     "mlf_summary_image_ex": (ctypes.c_int, [_vp, _i64, _i64, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _vp,
                                             _vp]),

@@ -5,6 +5,8 @@
 * :func:`recon_theory_phase_space_LFM_with_filter` --
   ``Xguess = recon_theory_phase_space_LFM_with_filter(LFIMG, H, Ht, maxIter, gpuFlag, gpu_id)``
   (``src/recon/recon_theory_phase_space_LFM_with_filter.m:10``).
+* :func:`determine_patch_info_aug`, :func:`image_load_module_aug`, :func:`img_rectify_mod`
+  -- raw frames to the per-patch sensor movie (``mesolf_gb300/rectify.py``).
 * :func:`summary_image_generation_module` -- the step that produces ``LFIMG``
   (``src/module/summary_image_generation_module.m:1-133``).
 * :class:`PhaseSpacePSF` / :class:`RLSolver` -- the same solve split into a resident PSF
@@ -23,6 +25,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import MLFStats, check
+from .rectify import determine_patch_info_aug, image_load_module_aug, img_rectify_mod  # noqa: F401
 
 PRECISIONS = {"fp32": _lib.MLF_PREC_FP32, "bf16x3": _lib.MLF_PREC_BF16X3, "bf16": _lib.MLF_PREC_BF16,
               "bf16x2": _lib.MLF_PREC_BF16X2}

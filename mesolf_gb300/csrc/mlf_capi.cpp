@@ -292,6 +292,59 @@ int mlf_summary_image_ex(const float* movie, int64_t P, int64_t T, int32_t mode,
   return MLF_OK;
 }
 
+int mlf_rectify_frames(const void* frames, int32_t dtype, int64_t H, int64_t W, int64_t n_frames,
+                       const int64_t* raw_cut, double raw_cut_xCenter, double raw_cut_yCenter, int32_t Nnum,
+                       double frames_dx, int64_t size_h, int64_t size_w, int64_t frames_start, int64_t frames_step,
+                       int64_t frames_end, int32_t frames_average, int32_t normalize, float* movie_out,
+                       int64_t* n_out, void* stream) {
+  clear_error();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!frames || !raw_cut || !movie_out) return fail(MLF_ERR_INVALID, "mlf_rectify_frames: null pointer");
+  if (dtype != MLF_DTYPE_F32 && dtype != MLF_DTYPE_U16) return fail(MLF_ERR_INVALID, "mlf_rectify_frames: dtype");
+  if (H < 1 || W < 1 || n_frames < 1) return fail(MLF_ERR_INVALID, "mlf_rectify_frames: empty frames");
+  const int64_t y0 = raw_cut[0], y1 = raw_cut[1], x0 = raw_cut[2], x1 = raw_cut[3];
+  if (y0 < 1 || y1 > H || x0 < 1 || x1 > W || y1 - y0 < 1 || x1 - x0 < 1)
+    return fail(MLF_ERR_INVALID, "mlf_rectify_frames: raw_cut outside the frame or narrower than 2 pixels");
+  if (Nnum < 1 || !(frames_dx > 0) || !std::isfinite(raw_cut_xCenter) || !std::isfinite(raw_cut_yCenter))
+    return fail(MLF_ERR_INVALID, "mlf_rectify_frames: Nnum, frames_dx or the lenslet centre");
+  if (size_h < 1 || size_w < 1 || frames_start < 1 || frames_step < 1)
+    return fail(MLF_ERR_INVALID, "mlf_rectify_frames: size or frame range");
+  const int64_t last = frames_end < 0 ? n_frames : std::min(n_frames, frames_end);  // 1-based
+  if (last < frames_start) return fail(MLF_ERR_INVALID, "mlf_rectify_frames: no frame selected");
+  const int64_t n_final = (last - frames_start) / frames_step + 1;
+  const int navg = frames_average ? (int)std::min<int64_t>(frames_step, INT32_MAX) : 1;
+  const int64_t h = y1 - y0 + 1, w = x1 - x0 + 1;
+  const size_t es = dtype == MLF_DTYPE_U16 ? 2 : 4;
+  const int64_t P = size_h * size_w;
+  OutStage o;
+  DevBuf bout, bin;
+  MLF_TRY(stage_out(movie_out, (size_t)(P * n_final), bout, &o));
+  if (is_device_ptr(frames)) {
+    // read the frames in place: 0-based first frame, step, last frame
+    MLF_TRY(rectify_run(frames, dtype, H * W, H, y0 - 1, x0 - 1, h, w, raw_cut_xCenter, raw_cut_yCenter, Nnum,
+                        frames_dx, size_h, size_w, frames_start - 1, frames_step, navg, last - 1, n_final, o.dev,
+                        normalize != 0, st));
+  } else {
+    // copy the cut region of the frames used (every frame of the range when averaging)
+    const int64_t n_used = frames_average ? last - frames_start + 1 : n_final;
+    MLF_TRY(bin.alloc(es * h * w * n_used, "rectification input staging"));
+    const char* src = static_cast<const char*>(frames);
+    for (int64_t k = 0; k < n_used; ++k) {
+      const int64_t f = frames_average ? frames_start - 1 + k : frames_start - 1 + k * frames_step;
+      const char* s0 = src + es * ((size_t)f * H * W + (size_t)(x0 - 1) * H + (size_t)(y0 - 1));
+      MLF_CUDA(cudaMemcpy2DAsync(static_cast<char*>(bin.p) + es * h * w * k, es * h, s0, es * H, es * h, w,
+                                 cudaMemcpyHostToDevice, st));
+    }
+    MLF_TRY(rectify_run(bin.p, dtype, h * w, h, 0, 0, h, w, raw_cut_xCenter, raw_cut_yCenter, Nnum, frames_dx,
+                        size_h, size_w, 0, frames_average ? frames_step : 1, navg, n_used - 1, n_final, o.dev,
+                        normalize != 0, st));
+  }
+  MLF_TRY(finish_out(o, st));
+  MLF_CUDA(cudaStreamSynchronize(st));
+  if (n_out) *n_out = n_final;
+  return MLF_OK;
+}
+
 int mlf_conv_vec_accumulate(const float* bitmaps, int64_t W, int64_t H, int64_t n, const int32_t* plane,
                             const int32_t* slot, int64_t n_out, const float* kernels, int64_t kw, int32_t nnum,
                             int64_t Z, float* out, void* stream) {

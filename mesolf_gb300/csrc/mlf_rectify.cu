@@ -1,0 +1,180 @@
+// Rectification of raw sensor frames onto the lenslet-aligned grid, the input step of the
+// pipeline: src/module/image_load_module_aug.m:19-164 (frame selection and averaging,
+// raw-patch cut, img_rectify_mod, division by the movie max).
+//
+// img_rectify_mod (:126-164) resamples a raw patch with griddedInterpolant (bilinear, linear
+// extrapolation, 1-based sample coordinates 1..H, 1..W) onto the grid
+//   R = [fliplr(c : -dx/M : -dx/M), c+dx/M : dx/M : size+0.9]
+// per axis (c = lenslet centre inside the patch), drops the first mod(idx(c) - floor(M/2), M)
+// grid points so that lenslets start on a multiple of M, evaluates, and keeps the first
+// M*floor(n/M) rows and columns.  The grids are computed here on the host in FP64 and turned
+// into per-row and per-column (cell, weight) tables; the kernel gathers the four neighbours of
+// every output pixel of every output frame, averaging the selected input frames first (the
+// interpolation is linear, so this is the reference's mean-then-rectify).
+//
+// One launch covers all output frames: thread per output pixel (coalesced along the fast
+// axis of the output, which maps to near-consecutive raw rows), grid.y over frames.  The raw
+// data is read once from HBM; the four-neighbour reuse is served by L1/L2.  HBM-bound.
+#include "mlf_internal.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace mlf {
+
+namespace {
+
+constexpr int RC_THREADS = 256;
+
+template <typename TIn>
+__device__ __forceinline__ float ldv(const TIn* p) {
+  return (float)__ldg(p);
+}
+
+// out[(r + oh*c) + P*i] = bilinear(mean of frames f0 + i*fstep + j, j < navg_i) at row cell
+// iy[r] (weight wy[r]) and column cell ix[c] (weight wx[c]).  Frame f of the input is at
+// raw + f*fstride; element (row, col) of the cut at (row0 + row) + cstride*(col0 + col).
+template <typename TIn>
+__global__ void __launch_bounds__(RC_THREADS)
+k_rectify(const TIn* __restrict__ raw, int64_t fstride, int64_t cstride, int64_t row0, int64_t col0,
+          const int* __restrict__ iy, const float* __restrict__ wy, int oh, const int* __restrict__ ix,
+          const float* __restrict__ wx, int ow, int64_t f0, int64_t fstep, int navg, int64_t flast, int64_t n_out,
+          float* __restrict__ out) {
+  const int64_t P = (int64_t)oh * ow;
+  const int64_t p = (int64_t)blockIdx.x * RC_THREADS + threadIdx.x;
+  if (p >= P) return;
+  const int r = (int)(p % oh), c = (int)(p / oh);
+  const int i0 = iy[r], j0 = ix[c];
+  const float fy = wy[r], fx = wx[c];
+  const int64_t o00 = (row0 + i0) + cstride * (col0 + j0);
+  const int64_t o10 = o00 + 1, o01 = o00 + cstride, o11 = o01 + 1;
+  for (int64_t i = blockIdx.y; i < n_out; i += gridDim.y) {
+    const int64_t fa = f0 + i * fstep;
+    const int64_t fb = min(fa + navg - 1, flast);
+    float v00 = 0.f, v10 = 0.f, v01 = 0.f, v11 = 0.f;
+    for (int64_t f = fa; f <= fb; ++f) {
+      const TIn* fr = raw + f * fstride;
+      v00 += ldv(fr + o00);
+      v10 += ldv(fr + o10);
+      v01 += ldv(fr + o01);
+      v11 += ldv(fr + o11);
+    }
+    const float rn = 1.f / (float)(fb - fa + 1);
+    const float a = fmaf(fx, v01 - v00, v00), b = fmaf(fx, v11 - v10, v10);
+    out[p + P * i] = fmaf(fy, b - a, a) * rn;
+  }
+}
+
+__global__ void k_rc_max(const float* __restrict__ a, int64_t n, float* __restrict__ part) {
+  __shared__ float sh[32];
+  float m = -INFINITY;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, a[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, sh[w]);
+    part[blockIdx.x] = m;
+  }
+}
+
+__global__ void k_rc_scale(float* __restrict__ a, int64_t n, const float* __restrict__ part, int nparts) {
+  __shared__ float mx;
+  if (threadIdx.x == 0) {
+    float m = -INFINITY;
+    for (int i = 0; i < nparts; ++i) m = fmaxf(m, part[i]);
+    mx = m;
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = a[i] / mx;
+}
+
+// MATLAB a:d:b (d != 0): count floor((b-a)/d) + 1 with a relative tolerance of 1e-10
+int64_t colon_count(double a, double d, double b) {
+  const double q = (b - a) / d;
+  const double tol = 1e-10 * std::max(1.0, std::fabs(q));
+  if (q < -tol) return 0;
+  return (int64_t)std::floor(q + tol) + 1;
+}
+
+}  // namespace
+
+// One axis of img_rectify_mod: query coordinates of the kept grid (before the cut to whole
+// lenslets), 1-based.  lo = -dx/M, hi = n + 0.9.
+std::vector<double> rectify_axis_query(double center, double lo, double hi, int M, double dx) {
+  const double s = dx / M;
+  const int64_t nl = colon_count(center, -s, lo), nr = colon_count(center + s, s, hi);
+  std::vector<double> R;
+  R.reserve((size_t)(nl + nr));
+  for (int64_t k = nl - 1; k >= 0; --k) R.push_back(center - s * (double)k);
+  for (int64_t k = 0; k < nr; ++k) R.push_back(center + s + s * (double)k);
+  const int64_t c0 = nl - M / 2;  // find(R == center) = nl (1-based)
+  const int64_t qinit = c0 - (int64_t)M * (int64_t)std::floor((double)c0 / M);
+  if (qinit > (int64_t)R.size()) return {};
+  return std::vector<double>(R.begin() + qinit, R.end());
+}
+
+int rectify_run(const void* d_raw, int dtype, int64_t fstride, int64_t cstride, int64_t row0, int64_t col0,
+                int64_t h, int64_t w, double xc, double yc, int M, double dx, int64_t out_h, int64_t out_w,
+                int64_t f0, int64_t fstep, int navg, int64_t flast, int64_t n_out, float* d_out, bool normalize,
+                cudaStream_t st) {
+  std::vector<double> xq = rectify_axis_query(xc, -dx / M, (double)w + 0.9, M, dx);
+  std::vector<double> yq = rectify_axis_query(yc, -dx / M, (double)h + 0.9, M, dx);
+  const int64_t kh = M * ((int64_t)yq.size() / M), kw = M * ((int64_t)xq.size() / M);
+  if (kh != out_h || kw != out_w)
+    return fail(MLF_ERR_INVALID, "After raw patch read and rectification, the shape is different from what was "
+                                 "expected. (" + std::to_string(kh) + " x " + std::to_string(kw) + " vs " +
+                                 std::to_string(out_h) + " x " + std::to_string(out_w) + ")");
+  // per-row / per-column cell (0-based, clamped to [0, n-2]) and weight inside the cell
+  std::vector<int> iy(out_h), ix(out_w);
+  std::vector<float> wy(out_h), wx(out_w);
+  for (int64_t r = 0; r < out_h; ++r) {
+    const double c = std::min(std::max(std::floor(yq[r]), 1.0), (double)(h - 1));
+    iy[r] = (int)c - 1;
+    wy[r] = (float)(yq[r] - c);
+  }
+  for (int64_t c = 0; c < out_w; ++c) {
+    const double cc = std::min(std::max(std::floor(xq[c]), 1.0), (double)(w - 1));
+    ix[c] = (int)cc - 1;
+    wx[c] = (float)(xq[c] - cc);
+  }
+  DevBuf tabs;
+  const size_t tb = sizeof(int) * (out_h + out_w) + sizeof(float) * (out_h + out_w);
+  MLF_TRY(tabs.alloc(tb, "rectification tables"));
+  char* base = static_cast<char*>(tabs.p);
+  int* d_iy = reinterpret_cast<int*>(base);
+  int* d_ix = d_iy + out_h;
+  float* d_wy = reinterpret_cast<float*>(d_ix + out_w);
+  float* d_wx = d_wy + out_h;
+  MLF_CUDA(cudaMemcpyAsync(d_iy, iy.data(), sizeof(int) * out_h, cudaMemcpyHostToDevice, st));
+  MLF_CUDA(cudaMemcpyAsync(d_ix, ix.data(), sizeof(int) * out_w, cudaMemcpyHostToDevice, st));
+  MLF_CUDA(cudaMemcpyAsync(d_wy, wy.data(), sizeof(float) * out_h, cudaMemcpyHostToDevice, st));
+  MLF_CUDA(cudaMemcpyAsync(d_wx, wx.data(), sizeof(float) * out_w, cudaMemcpyHostToDevice, st));
+  const int64_t P = out_h * out_w;
+  const dim3 grid((unsigned)((P + RC_THREADS - 1) / RC_THREADS), (unsigned)std::min<int64_t>(n_out, 65535));
+  if (dtype == MLF_DTYPE_U16)
+    k_rectify<uint16_t><<<grid, RC_THREADS, 0, st>>>(static_cast<const uint16_t*>(d_raw), fstride, cstride, row0,
+                                                     col0, d_iy, d_wy, (int)out_h, d_ix, d_wx, (int)out_w, f0, fstep,
+                                                     navg, flast, n_out, d_out);
+  else
+    k_rectify<float><<<grid, RC_THREADS, 0, st>>>(static_cast<const float*>(d_raw), fstride, cstride, row0, col0,
+                                                  d_iy, d_wy, (int)out_h, d_ix, d_wx, (int)out_w, f0, fstep, navg,
+                                                  flast, n_out, d_out);
+  MLF_LAUNCHED();
+  if (normalize) {
+    constexpr int NB = 1024;
+    DevBuf part;
+    MLF_TRY(part.alloc(sizeof(float) * NB, "rectification max partials"));
+    k_rc_max<<<NB, 256, 0, st>>>(d_out, P * n_out, part.as<float>());
+    k_rc_scale<<<NB, 256, 0, st>>>(d_out, P * n_out, part.as<float>(), NB);
+    MLF_LAUNCHED();
+    MLF_CUDA(cudaStreamSynchronize(st));
+  } else {
+    MLF_CUDA(cudaStreamSynchronize(st));  // tables are released on return
+  }
+  return MLF_OK;
+}
+
+}  // namespace mlf

@@ -728,3 +728,197 @@ def summary_image(movie, mode="pixelwise", bg_iter=5, window_1=100, window_2=20,
     else:
         raise ValueError('Invalid value for param "detrend_mode"')
     return img / img.max(), s, t
+
+
+# ----------------------------------------------------------------------------- f4 rectification
+def matlab_round(x):
+    """MATLAB ``round``: half away from zero."""
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+def matlab_colon(a, d, b):
+    """MATLAB ``a:d:b`` for a non-zero double step: a + k*d for k = 0 .. floor((b-a)/d), with a
+    relative tolerance of 1e-10 on the count (MATLAB's colon also tolerates rounding at the end
+    point; its exact rule is not published, so end points within that tolerance are unpinned)."""
+    q = (b - a) / d
+    if q < -1e-10 * max(1.0, abs(q)):
+        return np.zeros(0)
+    n = int(np.floor(q + 1e-10 * max(1.0, abs(q)))) + 1
+    return a + d * np.arange(n, dtype=np.float64)
+
+
+def rectify_axis(center, lo, hi, M, dx):
+    """One axis of the rectification grid (``image_load_module_aug.m:130-143`` with
+    lo = -dx/M, hi = size + 0.9; ``determine_patch_info_aug.m:50-68`` with lo = 1, hi = size):
+    ``R = [fliplr(center:-dx/M:lo), center+dx/M:dx/M:hi]``, the 1-based index of ``center`` in
+    R, the left cut ``qinit = mod(idx - floor(M/2), M)`` and the kept query vector
+    ``R(qinit+1:end)``.  Returns ``(R, idx, qinit, Rq)``."""
+    s = dx / M
+    left = matlab_colon(center, -s, lo)[::-1]
+    right = matlab_colon(center + s, s, hi)
+    R = np.concatenate([left, right])
+    idx = len(left)                       # find(R == center), 1-based
+    c0 = idx - M // 2
+    qinit = c0 - M * int(np.floor(c0 / M))
+    return R, idx, qinit, R[qinit:]
+
+
+def interp2_linear(img, yq, xq):
+    """``griddedInterpolant({1:H, 1:W}, img)`` evaluated on the grid (yq, xq): bilinear with
+    linear extrapolation (the interpolant's default method and extrapolation), 1-based
+    coordinates.  Every query uses the cell [i, i+1] x [j, j+1] with i = floor(y) clamped to
+    [1, H-1] (and j likewise), so that outside the samples the boundary cell extends linearly."""
+    img = np.asarray(img, dtype=np.float64)
+    H, W = img.shape
+    if H < 2 or W < 2:
+        raise ValueError("griddedInterpolant needs at least 2 samples per dimension")
+    yq = np.asarray(yq, np.float64)
+    xq = np.asarray(xq, np.float64)
+    i = np.clip(np.floor(yq), 1, H - 1).astype(np.int64)
+    j = np.clip(np.floor(xq), 1, W - 1).astype(np.int64)
+    fy = (yq - i)[:, None]
+    fx = (xq - j)[None, :]
+    v00 = img[i - 1][:, j - 1]
+    v10 = img[i][:, j - 1]
+    v01 = img[i - 1][:, j]
+    v11 = img[i][:, j]
+    return (1 - fy) * ((1 - fx) * v00 + fx * v01) + fy * ((1 - fx) * v10 + fx * v11)
+
+
+def img_rectify_mod(img, x_center, y_center, M, dx):
+    """``image_load_module_aug.m:126-164``: resample a raw patch onto the lenslet-aligned grid
+    of pitch dx/M (query grids from ``rectify_axis`` with lo = -dx/M, hi = size + 0.9), then cut
+    the right / bottom to whole lenslets."""
+    H, W = np.shape(img)
+    _, _, _, xq = rectify_axis(x_center, -dx / M, W + 0.9, M, dx)
+    _, _, _, yq = rectify_axis(y_center, -dx / M, H + 0.9, M, dx)
+    out = interp2_linear(img, yq, xq)
+    return out[:M * (out.shape[0] // M), :M * (out.shape[1] // M)]
+
+
+def image_load(frames, patch_info, SI):
+    """``image_load_module_aug.m:19-123`` on frames already in memory (``frames`` H x W x n,
+    MATLAB order, the files in ``dir`` order; the TIFF reading is out of scope): frame
+    selection ``frames_start:frames_step:min(n, frames_end)``, mean of ``frames_step``
+    consecutive frames when ``frames_average`` (the last group may be shorter), cut to
+    ``raw_cut``, rectification, and division by the movie max.  Returns (pixels, frames)."""
+    frames = np.asarray(frames)
+    n_files = frames.shape[2]
+    start, step = int(SI.get("frames_start", 1)), int(SI.get("frames_step", 1))
+    end = SI.get("frames_end", np.inf)
+    last = int(min(n_files, end))
+    if SI.get("frames_average", True):
+        navg = step
+        idx = np.arange(start, last + 1)
+    else:
+        navg = 1
+        idx = np.arange(start, last + 1, step)
+    n_final = len(np.arange(start, last + 1, step))
+    (ys, ye), (xs, xe) = np.asarray(patch_info["raw_cut"], dtype=np.int64)
+    h, w = (int(v) for v in patch_info["size"])
+    M = int(SI["Nnum"])
+    out = np.empty((h * w, n_final), dtype=np.float64)
+    for i in range(n_final):
+        sel = idx[i * navg:min((i + 1) * navg, len(idx))]
+        patch = frames[ys - 1:ye, xs - 1:xe, sel - 1].astype(np.float64).mean(axis=2)
+        r = img_rectify_mod(patch, patch_info["raw_cut_xCenter"], patch_info["raw_cut_yCenter"], M,
+                            float(SI["frames_dx"]))
+        if r.shape != (h, w):
+            raise ValueError("After raw patch read and rectification, the shape is different from what was expected.")
+        out[:, i] = r.reshape(-1, order="F")
+    return out / out.max()
+
+
+def determine_patch_info(SI, frame_shape):
+    """``determine_patch_info_aug.m:12-290`` (no plotting): the rectified full-frame size from
+    the grids (lo = 1, hi = size), the lenslet-border crop, the patches ('carpet' or 'roi'),
+    and for each patch its raw cut and the lenslet centre inside the cut.  ``frame_shape`` is
+    the (rows, cols) of the first frame.  Returns a list of dicts with keys location (2x2,
+    1-based [top, left; bottom, right]), size, raw_cut (2x2: [y0, y1; x0, x1]),
+    raw_cut_xCenter, raw_cut_yCenter."""
+    Hf, Wf = (int(v) for v in frame_shape)
+    M = int(SI["Nnum"])
+    dx = float(SI["frames_dx"])
+    xC, yC = float(SI["frames_x_offset"]), float(SI["frames_y_offset"])
+    cut = list(SI.get("frames_crop_border_microlenses", [0, 0, 0, 0]))
+    XcutLeft, XcutRight, YcutUp, YcutDown = cut[0], cut[1], cut[2], cut[3]
+    Xr, pre_cx, XqInit, Xq = rectify_axis(xC, 1.0, float(Wf), M, dx)
+    Yr, pre_cy, YqInit, Yq = rectify_axis(yC, 1.0, float(Hf), M, dx)
+    size_y, size_x = M * (len(Yq) // M), M * (len(Xq) // M)
+    XsizeML, YsizeML = size_x // M, size_y // M
+    if XcutLeft + XcutRight >= XsizeML:
+        raise ValueError("X-cut range is larger than the x-size of image")
+    if YcutUp + YcutDown >= YsizeML:
+        raise ValueError("Y-cut range is larger than the y-size of image")
+    Xrange = np.arange(1 + XcutLeft, XsizeML - XcutRight + 1)
+    Yrange = np.arange(1 + YcutUp, YsizeML - YcutDown + 1)
+    gh, gw = len(Yrange) * M, len(Xrange) * M
+    patches = []
+    mode = SI.get("patch_mode", "carpet")
+
+    def add(top_left, bottom_right):
+        ph = bottom_right[0] - top_left[0] + 1
+        pw = bottom_right[1] - top_left[1] + 1
+        ph -= ph % M
+        pw -= pw % M
+        if ph < 50 or pw < 50:
+            return
+        patches.append({"location": np.array([[top_left[0], top_left[1]],
+                                              [top_left[0] + ph - 1, top_left[1] + pw - 1]]),
+                        "size": (int(ph), int(pw))})
+
+    if mode == "carpet":
+        n = SI.get("n_patches", 1)
+        n = [n, n] if np.isscalar(n) else list(n)
+        psh = int(np.ceil((gh // n[0]) / M)) * M
+        psw = int(np.ceil((gw // n[1]) / M)) * M
+        for k in range(n[0] * n[1]):
+            ci, cj = k % n[0] + 1, k // n[0] + 1          # ind2sub, column-major
+            tl = [(ci - 1) * psh + 1, (cj - 1) * psw + 1]
+            br = [min(ci * psh, gh), min(cj * psw, gw)]
+            add(tl, br)
+    elif mode == "roi":
+        rps = int(SI["ROI_patch_size"])
+        rps -= rps % M
+        for roi in np.atleast_2d(np.asarray(SI["ROI_list"])):
+            tl0, br0 = [int(roi[0]), int(roi[1])], [int(roi[2]), int(roi[3])]
+            rs = [br0[0] - tl0[0] + 1, br0[1] - tl0[1] + 1]
+            nh, nw = int(np.ceil(rs[0] / rps)), int(np.ceil(rs[1] / rps))
+            sh_, sw_ = rps, rps
+            if rs[0] < rps:
+                sh_, nh = rs[0], 1
+            if rs[1] < rps:
+                sw_, nw = rs[1], 1
+            for k in range(nh * nw):
+                ci, cj = k % nh + 1, k // nh + 1
+                tl = [(ci - 1) * sh_ + tl0[0], (cj - 1) * sw_ + tl0[1]]
+                br = [min(ci * sh_, rs[0]) + tl0[0] - 1, min(cj * sw_, rs[1]) + tl0[1] - 1]
+                add(tl, br)
+    else:
+        raise ValueError("patch_mode should be either 'carpet' or 'roi'")
+    Y_after_top = (Yrange[0] - 1) * M + 1
+    X_after_left = (Xrange[0] - 1) * M + 1
+    margin = int(np.ceil(M / 2)) - 2
+    for p in patches:
+        (top, left), (bottom, right) = p["location"]
+        pt = top + Y_after_top - 1 + YqInit - 1 - margin
+        pl = left + X_after_left - 1 + XqInit - 1 - margin
+        pb = bottom + Y_after_top - 1 + YqInit - 1 + margin - 1
+        pr = right + X_after_left - 1 + XqInit - 1 + margin - 1
+        for v, R in ((pt, Yr), (pb, Yr), (pl, Xr), (pr, Xr)):
+            if v < 1 or v > len(R):
+                raise IndexError("Index exceeds the number of array elements")
+        y0 = max(int(np.floor(Yr[pt - 1])), 1)
+        y1 = min(int(np.ceil(Yr[pb - 1])), Hf)
+        x0 = max(int(np.floor(Xr[pl - 1])), 1)
+        x1 = min(int(np.ceil(Xr[pr - 1])), Wf)
+        cy = int(matlab_round((pt + pb) / 2))
+        cx = int(matlab_round((pl + pr) / 2))
+        my = (pre_cy - cy) % M
+        mx = (pre_cx - cx) % M
+        yc = Yr[cy - (M - my) - 1] if my >= int(np.ceil(M / 2)) else Yr[cy + my - 1]
+        xc = Xr[cx - (M - mx) - 1] if mx >= int(np.ceil(M / 2)) else Xr[cx + mx - 1]
+        p["raw_cut"] = np.array([[y0, y1], [x0, x1]])
+        p["raw_cut_yCenter"] = float(yc - Yr[pt - 1])
+        p["raw_cut_xCenter"] = float(xc - Xr[pl - 1])
+    return patches
