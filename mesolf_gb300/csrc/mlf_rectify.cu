@@ -12,8 +12,9 @@
 // every output pixel of every output frame, averaging the selected input frames first (the
 // interpolation is linear, so this is the reference's mean-then-rectify).
 //
-// One launch covers all output frames: thread per output pixel (coalesced along the fast
-// axis of the output, which maps to near-consecutive raw rows), grid.y over frames.  The raw
+// One launch covers all output frames: thread per output row of one column (coalesced along
+// the fast axis of the output, which maps to near-consecutive raw rows) and 8 output frames,
+// with all 32 neighbour loads of the 8 frames in flight before the interpolation.  The raw
 // data is read once from HBM; the four-neighbour reuse is served by L1/L2.  HBM-bound.
 #include "mlf_internal.h"
 
@@ -24,7 +25,6 @@ namespace mlf {
 
 namespace {
 
-constexpr int RC_THREADS = 256;
 
 template <typename TIn>
 __device__ __forceinline__ float ldv(const TIn* p) {
@@ -34,34 +34,66 @@ __device__ __forceinline__ float ldv(const TIn* p) {
 // out[(r + oh*c) + P*i] = bilinear(mean of frames f0 + i*fstep + j, j < navg_i) at row cell
 // iy[r] (weight wy[r]) and column cell ix[c] (weight wx[c]).  Frame f of the input is at
 // raw + f*fstride; element (row, col) of the cut at (row0 + row) + cstride*(col0 + col).
+// Block: RC_ROWS output rows x RC_COLS columns (threadIdx.y), output frames in chunks of
+// RC_FCH (all 4*RC_FCH neighbour loads of a chunk in flight before the interpolation), RC_NCH
+// chunks per block; the tables are read once per thread.
+constexpr int RC_ROWS = 128, RC_COLS = 4, RC_FCH = 8, RC_NCH = 8;
+
 template <typename TIn>
-__global__ void __launch_bounds__(RC_THREADS)
+__global__ void __launch_bounds__(RC_ROWS * RC_COLS)
 k_rectify(const TIn* __restrict__ raw, int64_t fstride, int64_t cstride, int64_t row0, int64_t col0,
           const int* __restrict__ iy, const float* __restrict__ wy, int oh, const int* __restrict__ ix,
           const float* __restrict__ wx, int ow, int64_t f0, int64_t fstep, int navg, int64_t flast, int64_t n_out,
           float* __restrict__ out) {
+  const int r = blockIdx.x * RC_ROWS + threadIdx.x;
+  const int c = blockIdx.y * RC_COLS + threadIdx.y;
+  if (r >= oh || c >= ow) return;
   const int64_t P = (int64_t)oh * ow;
-  const int64_t p = (int64_t)blockIdx.x * RC_THREADS + threadIdx.x;
-  if (p >= P) return;
-  const int r = (int)(p % oh), c = (int)(p / oh);
-  const int i0 = iy[r], j0 = ix[c];
-  const float fy = wy[r], fx = wx[c];
+  const int i0 = __ldg(iy + r), j0 = __ldg(ix + c);
+  const float fy = __ldg(wy + r), fx = __ldg(wx + c);
   const int64_t o00 = (row0 + i0) + cstride * (col0 + j0);
-  const int64_t o10 = o00 + 1, o01 = o00 + cstride, o11 = o01 + 1;
-  for (int64_t i = blockIdx.y; i < n_out; i += gridDim.y) {
-    const int64_t fa = f0 + i * fstep;
-    const int64_t fb = min(fa + navg - 1, flast);
-    float v00 = 0.f, v10 = 0.f, v01 = 0.f, v11 = 0.f;
-    for (int64_t f = fa; f <= fb; ++f) {
-      const TIn* fr = raw + f * fstride;
-      v00 += ldv(fr + o00);
-      v10 += ldv(fr + o10);
-      v01 += ldv(fr + o01);
-      v11 += ldv(fr + o11);
+  const int64_t o01 = o00 + cstride;
+  float* op = out + r + (int64_t)oh * c;
+  for (int ch = 0; ch < RC_NCH; ++ch) {
+    const int64_t ib = ((int64_t)blockIdx.z * RC_NCH + ch) * RC_FCH;
+    if (ib >= n_out) return;
+    const int ni = (int)(n_out - ib < RC_FCH ? n_out - ib : RC_FCH);
+    if (navg == 1) {
+      float v[RC_FCH][4];
+#pragma unroll
+      for (int q = 0; q < RC_FCH; ++q) {
+        if (q < ni) {
+          const TIn* fr = raw + (f0 + (ib + q) * fstep) * fstride;
+          v[q][0] = ldv(fr + o00);
+          v[q][1] = ldv(fr + o00 + 1);
+          v[q][2] = ldv(fr + o01);
+          v[q][3] = ldv(fr + o01 + 1);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RC_FCH; ++q) {
+        if (q < ni) {
+          const float a = fmaf(fx, v[q][2] - v[q][0], v[q][0]), b = fmaf(fx, v[q][3] - v[q][1], v[q][1]);
+          __stcs(op + P * (ib + q), fmaf(fy, b - a, a));
+        }
+      }
+      continue;
     }
-    const float rn = 1.f / (float)(fb - fa + 1);
-    const float a = fmaf(fx, v01 - v00, v00), b = fmaf(fx, v11 - v10, v10);
-    out[p + P * i] = fmaf(fy, b - a, a) * rn;
+    for (int q = 0; q < ni; ++q) {
+      const int64_t fa = f0 + (ib + q) * fstep;
+      const int64_t fb = min(fa + navg - 1, flast);
+      float v00 = 0.f, v10 = 0.f, v01 = 0.f, v11 = 0.f;
+      for (int64_t f = fa; f <= fb; ++f) {
+        const TIn* fr = raw + f * fstride;
+        v00 += ldv(fr + o00);
+        v10 += ldv(fr + o00 + 1);
+        v01 += ldv(fr + o01);
+        v11 += ldv(fr + o01 + 1);
+      }
+      const float rn = 1.f / (float)(fb - fa + 1);
+      const float a = fmaf(fx, v01 - v00, v00), b = fmaf(fx, v11 - v10, v10);
+      __stcs(op + P * (ib + q), fmaf(fy, b - a, a) * rn);
+    }
   }
 }
 
@@ -153,15 +185,20 @@ int rectify_run(const void* d_raw, int dtype, int64_t fstride, int64_t cstride, 
   MLF_CUDA(cudaMemcpyAsync(d_wy, wy.data(), sizeof(float) * out_h, cudaMemcpyHostToDevice, st));
   MLF_CUDA(cudaMemcpyAsync(d_wx, wx.data(), sizeof(float) * out_w, cudaMemcpyHostToDevice, st));
   const int64_t P = out_h * out_w;
-  const dim3 grid((unsigned)((P + RC_THREADS - 1) / RC_THREADS), (unsigned)std::min<int64_t>(n_out, 65535));
+  const int64_t per_block = (int64_t)RC_FCH * RC_NCH;
+  if ((n_out + per_block - 1) / per_block > 65535 || (out_w + RC_COLS - 1) / RC_COLS > 65535)
+    return fail(MLF_ERR_UNSUPPORTED, "mlf_rectify_frames: too many output frames or columns for one launch");
+  const dim3 grid((unsigned)((out_h + RC_ROWS - 1) / RC_ROWS), (unsigned)((out_w + RC_COLS - 1) / RC_COLS),
+                  (unsigned)((n_out + per_block - 1) / per_block));
+  const dim3 block(RC_ROWS, RC_COLS);
   if (dtype == MLF_DTYPE_U16)
-    k_rectify<uint16_t><<<grid, RC_THREADS, 0, st>>>(static_cast<const uint16_t*>(d_raw), fstride, cstride, row0,
-                                                     col0, d_iy, d_wy, (int)out_h, d_ix, d_wx, (int)out_w, f0, fstep,
-                                                     navg, flast, n_out, d_out);
-  else
-    k_rectify<float><<<grid, RC_THREADS, 0, st>>>(static_cast<const float*>(d_raw), fstride, cstride, row0, col0,
+    k_rectify<uint16_t><<<grid, block, 0, st>>>(static_cast<const uint16_t*>(d_raw), fstride, cstride, row0, col0,
                                                   d_iy, d_wy, (int)out_h, d_ix, d_wx, (int)out_w, f0, fstep, navg,
                                                   flast, n_out, d_out);
+  else
+    k_rectify<float><<<grid, block, 0, st>>>(static_cast<const float*>(d_raw), fstride, cstride, row0, col0, d_iy,
+                                               d_wy, (int)out_h, d_ix, d_wx, (int)out_w, f0, fstep, navg, flast, n_out,
+                                               d_out);
   MLF_LAUNCHED();
   if (normalize) {
     constexpr int NB = 1024;
