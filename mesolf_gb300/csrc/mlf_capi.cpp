@@ -321,7 +321,7 @@ int mlf_rectify_frames(const void* frames, int32_t dtype, int64_t H, int64_t W, 
   MLF_TRY(stage_out(movie_out, (size_t)(P * n_final), bout, &o));
   if (is_device_ptr(frames)) {
     // read the frames in place: 0-based first frame, step, last frame
-    MLF_TRY(rectify_run(frames, dtype, H * W, H, y0 - 1, x0 - 1, h, w, raw_cut_xCenter, raw_cut_yCenter, Nnum,
+    MLF_TRY(rectify_run(frames, dtype, H * W * n_frames, H * W, H, y0 - 1, x0 - 1, h, w, raw_cut_xCenter, raw_cut_yCenter, Nnum,
                         frames_dx, size_h, size_w, frames_start - 1, frames_step, navg, last - 1, n_final, o.dev,
                         normalize != 0, st));
   } else {
@@ -335,7 +335,7 @@ int mlf_rectify_frames(const void* frames, int32_t dtype, int64_t H, int64_t W, 
       MLF_CUDA(cudaMemcpy2DAsync(static_cast<char*>(bin.p) + es * h * w * k, es * h, s0, es * H, es * h, w,
                                  cudaMemcpyHostToDevice, st));
     }
-    MLF_TRY(rectify_run(bin.p, dtype, h * w, h, 0, 0, h, w, raw_cut_xCenter, raw_cut_yCenter, Nnum, frames_dx,
+    MLF_TRY(rectify_run(bin.p, dtype, h * w * n_used, h * w, h, 0, 0, h, w, raw_cut_xCenter, raw_cut_yCenter, Nnum, frames_dx,
                         size_h, size_w, 0, frames_average ? frames_step : 1, navg, n_used - 1, n_final, o.dev,
                         normalize != 0, st));
   }

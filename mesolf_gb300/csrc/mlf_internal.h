@@ -224,7 +224,7 @@ int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const f
 // pieces of the tensor-core route of the MEX projector (mlf_conv_vec.cu)
 int summary_run(const float* dY, int64_t P, int64_t T, int mode, int bg_iter, int w1, int w2, int poly,
                 float* d_img, float* d_s, float* d_t, double* pass_ms, cudaStream_t st);
-int rectify_run(const void* d_raw, int dtype, int64_t fstride, int64_t cstride, int64_t row0, int64_t col0,
+int rectify_run(const void* d_raw, int dtype, int64_t total, int64_t fstride, int64_t cstride, int64_t row0, int64_t col0,
                 int64_t h, int64_t w, double xc, double yc, int M, double dx, int64_t out_h, int64_t out_w,
                 int64_t f0, int64_t fstep, int navg, int64_t flast, int64_t n_out, float* d_out, bool normalize,
                 cudaStream_t st);

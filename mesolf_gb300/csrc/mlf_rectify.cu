@@ -97,6 +97,73 @@ k_rectify(const TIn* __restrict__ raw, int64_t fstride, int64_t cstride, int64_t
   }
 }
 
+// The same for one input frame per output frame (navg = 1), with the raw tile of each block
+// staged in shared memory by 16-byte loads: block = RC_ROWS x RC_COLS output pixels, chunks of
+// SF output frames (blockIdx.z).  For frame q and raw column k of the block's footprint (raw
+// columns ix[c0] .. ix[c1]+1, rows iy[r0] .. iy[r1]+1) the column segment is loaded from the
+// 16-byte boundary at or below its first element into slot [q][k] (`slot` elements), its
+// start at off[q][k] inside the slot.  A few wide loads per thread replace four narrow
+// gathers per output pixel and frame.  raw must be 16-byte aligned; `total` = elements of
+// the frame buffer (vectors that would cross its end are loaded per element).
+constexpr int SF = 16;
+
+// exact uint16 -> float with one logic op and one add: the bits 0x4B000000 | x are the float
+// 2^23 + x (x < 2^23 fits the mantissa)
+__device__ __forceinline__ float to_f(uint16_t x) { return __uint_as_float(0x4B000000u | x) - 8388608.f; }
+__device__ __forceinline__ float to_f(float x) { return x; }
+
+template <typename TIn>
+__global__ void __launch_bounds__(RC_ROWS * RC_COLS, 4)
+k_rectify_staged(const TIn* __restrict__ raw, int64_t total, int64_t fstride, int64_t cstride, int64_t row0,
+                 int64_t col0, const int* __restrict__ iy, const float* __restrict__ wy, int oh,
+                 const int* __restrict__ ix, const float* __restrict__ wx, int ow, int64_t f0, int64_t fstep,
+                 int64_t n_out, int slot, int maxc, float* __restrict__ out) {
+  constexpr int VEC = 16 / sizeof(TIn);
+  extern __shared__ __align__(16) unsigned char rc_smem[];
+  TIn* tile = reinterpret_cast<TIn*>(rc_smem);  // [SF][maxc][slot]
+  __shared__ int off[SF][8];
+  const int tid = threadIdx.y * RC_ROWS + threadIdx.x;
+  const int r0 = blockIdx.x * RC_ROWS, c0 = blockIdx.y * RC_COLS;
+  const int r1 = min(r0 + RC_ROWS, oh) - 1, c1 = min(c0 + RC_COLS, ow) - 1;
+  const int rlo = __ldg(iy + r0), nrow = __ldg(iy + r1) + 2 - rlo;
+  const int clo = __ldg(ix + c0), ncol = __ldg(ix + c1) + 2 - clo;  // <= maxc (host bound)
+  const int nv = (nrow + 2 * VEC - 2) / VEC;                         // vectors per column segment
+  const int64_t ib = (int64_t)blockIdx.z * SF;
+  const int nf = (int)(n_out - ib < SF ? n_out - ib : SF);
+  const int nload = nf * ncol * nv;
+  for (int idx = tid; idx < nload; idx += RC_ROWS * RC_COLS) {
+    const int q = idx / (ncol * nv), rem = idx - q * (ncol * nv);
+    const int k = rem / nv, v = rem - k * nv;
+    const int64_t e = (f0 + (ib + q) * fstep) * fstride + (row0 + rlo) + cstride * (col0 + clo + k);
+    const int64_t ea = e & ~(int64_t)(VEC - 1);
+    if (v == 0) off[q][k] = (int)(e - ea);
+    TIn* dst = tile + ((int64_t)q * maxc + k) * slot + (int64_t)v * VEC;
+    const int64_t src = ea + (int64_t)v * VEC;
+    if (src + VEC <= total) {
+      *reinterpret_cast<uint4*>(dst) = __ldcs(reinterpret_cast<const uint4*>(raw + src));
+    } else {
+#pragma unroll
+      for (int u = 0; u < VEC; ++u) dst[u] = src + u < total ? raw[src + u] : TIn(0);
+    }
+  }
+  __syncthreads();
+  const int r = r0 + threadIdx.x, c = c0 + threadIdx.y;
+  if (r >= oh || c >= ow) return;
+  const int lr = __ldg(iy + r) - rlo, lc = __ldg(ix + c) - clo;
+  const float fy = __ldg(wy + r), fx = __ldg(wx + c);
+  const int64_t P = (int64_t)oh * ow;
+  float* op = out + r + (int64_t)oh * c + P * ib;
+  const TIn* base = tile + (int64_t)lc * slot + lr;
+#pragma unroll 4
+  for (int q = 0; q < nf; ++q) {
+    const TIn* ca = base + (int64_t)q * maxc * slot + off[q][lc];
+    const TIn* cb = base + (int64_t)q * maxc * slot + slot + off[q][lc + 1];
+    const float v00 = to_f(ca[0]), v10 = to_f(ca[1]), v01 = to_f(cb[0]), v11 = to_f(cb[1]);
+    const float a = fmaf(fx, v01 - v00, v00), b = fmaf(fx, v11 - v10, v10);
+    __stcs(op + P * q, fmaf(fy, b - a, a));
+  }
+}
+
 __global__ void k_rc_max(const float* __restrict__ a, int64_t n, float* __restrict__ part) {
   __shared__ float sh[32];
   float m = -INFINITY;
@@ -148,7 +215,7 @@ std::vector<double> rectify_axis_query(double center, double lo, double hi, int 
   return std::vector<double>(R.begin() + qinit, R.end());
 }
 
-int rectify_run(const void* d_raw, int dtype, int64_t fstride, int64_t cstride, int64_t row0, int64_t col0,
+int rectify_run(const void* d_raw, int dtype, int64_t total, int64_t fstride, int64_t cstride, int64_t row0, int64_t col0,
                 int64_t h, int64_t w, double xc, double yc, int M, double dx, int64_t out_h, int64_t out_w,
                 int64_t f0, int64_t fstep, int navg, int64_t flast, int64_t n_out, float* d_out, bool normalize,
                 cudaStream_t st) {
@@ -185,12 +252,40 @@ int rectify_run(const void* d_raw, int dtype, int64_t fstride, int64_t cstride, 
   MLF_CUDA(cudaMemcpyAsync(d_wy, wy.data(), sizeof(float) * out_h, cudaMemcpyHostToDevice, st));
   MLF_CUDA(cudaMemcpyAsync(d_wx, wx.data(), sizeof(float) * out_w, cudaMemcpyHostToDevice, st));
   const int64_t P = out_h * out_w;
+  // largest raw tile of a block (rows and columns of the four-neighbour footprint)
+  int maxr = 0, maxc = 0;
+  for (int64_t r0 = 0; r0 < out_h; r0 += RC_ROWS)
+    maxr = std::max(maxr, iy[std::min<int64_t>(r0 + RC_ROWS, out_h) - 1] + 2 - iy[r0]);
+  for (int64_t c0 = 0; c0 < out_w; c0 += RC_COLS)
+    maxc = std::max(maxc, ix[std::min<int64_t>(c0 + RC_COLS, out_w) - 1] + 2 - ix[c0]);
+  const int es = dtype == MLF_DTYPE_U16 ? 2 : 4, vec = 16 / es;
+  const int slot = ((maxr + 2 * vec - 2) / vec) * vec;
+  const size_t smem = (size_t)SF * maxc * slot * es;
+  const bool staged = navg == 1 && reinterpret_cast<uintptr_t>(d_raw) % 16 == 0 && maxc <= 8 &&
+                      smem <= 96 * 1024 && (out_w + RC_COLS - 1) / RC_COLS <= 65535;
+  const dim3 block(RC_ROWS, RC_COLS);
+  if (staged) {
+    const void* kf = dtype == MLF_DTYPE_U16 ? (const void*)k_rectify_staged<uint16_t> : (const void*)k_rectify_staged<float>;
+    MLF_TRY(allow_max_dyn_smem(kf));
+    const int64_t chunks = (n_out + SF - 1) / SF;
+    if (chunks > 65535) return fail(MLF_ERR_UNSUPPORTED, "mlf_rectify_frames: more than 1048560 output frames");
+    const dim3 grid((unsigned)((out_h + RC_ROWS - 1) / RC_ROWS), (unsigned)((out_w + RC_COLS - 1) / RC_COLS),
+                    (unsigned)chunks);
+    if (dtype == MLF_DTYPE_U16)
+      k_rectify_staged<uint16_t><<<grid, block, smem, st>>>(static_cast<const uint16_t*>(d_raw), total, fstride,
+                                                            cstride, row0, col0, d_iy, d_wy, (int)out_h, d_ix, d_wx,
+                                                            (int)out_w, f0, fstep, n_out, slot, maxc, d_out);
+    else
+      k_rectify_staged<float><<<grid, block, smem, st>>>(static_cast<const float*>(d_raw), total, fstride, cstride,
+                                                         row0, col0, d_iy, d_wy, (int)out_h, d_ix, d_wx, (int)out_w,
+                                                         f0, fstep, n_out, slot, maxc, d_out);
+    MLF_LAUNCHED();
+  } else {
   const int64_t per_block = (int64_t)RC_FCH * RC_NCH;
   if ((n_out + per_block - 1) / per_block > 65535 || (out_w + RC_COLS - 1) / RC_COLS > 65535)
     return fail(MLF_ERR_UNSUPPORTED, "mlf_rectify_frames: too many output frames or columns for one launch");
   const dim3 grid((unsigned)((out_h + RC_ROWS - 1) / RC_ROWS), (unsigned)((out_w + RC_COLS - 1) / RC_COLS),
                   (unsigned)((n_out + per_block - 1) / per_block));
-  const dim3 block(RC_ROWS, RC_COLS);
   if (dtype == MLF_DTYPE_U16)
     k_rectify<uint16_t><<<grid, block, 0, st>>>(static_cast<const uint16_t*>(d_raw), fstride, cstride, row0, col0,
                                                   d_iy, d_wy, (int)out_h, d_ix, d_wx, (int)out_w, f0, fstep, navg,
@@ -199,6 +294,7 @@ int rectify_run(const void* d_raw, int dtype, int64_t fstride, int64_t cstride, 
     k_rectify<float><<<grid, block, 0, st>>>(static_cast<const float*>(d_raw), fstride, cstride, row0, col0, d_iy,
                                                d_wy, (int)out_h, d_ix, d_wx, (int)out_w, f0, fstep, navg, flast, n_out,
                                                d_out);
+  }
   MLF_LAUNCHED();
   if (normalize) {
     constexpr int NB = 1024;
