@@ -261,7 +261,7 @@ ViewArgs view_args(Solver* s) {
   a.plane = s->plane; a.nch = s->nch;
   a.tilesA = s->tilesA; a.tilesB = s->tilesB; a.tps = s->tps; a.slots = s->slots;
   a.RP = s->RP; a.RProws = s->RProws; a.XP = s->XP; a.XProws = s->XProws; a.maxc = s->maxc;
-  a.slot_floats = round_up(s->XProws * s->XP + 4 * s->T * s->T + s->maxc * s->maxc + s->T * s->maxc, 4);
+  a.slot_floats = round_up(s->XProws * s->XP + 4 * s->T * view_tap_pitch(s->T) + s->maxc * s->maxc + s->T * s->maxc, 4);
   return a;
 }
 
@@ -504,13 +504,15 @@ int solver_init(Solver* s) {
   MLF_TRY(s->cls.alloc(tab.size() * sizeof(int), "class tables"));
   MLF_CUDA(cudaMemcpy(s->cls.p, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
 
-  const int slot_floats = round_up(s->XProws * s->XP + 4 * s->T * s->T + s->maxc * s->maxc + s->T * s->maxc, 4);
-  s->slots = s->tps >= 128 ? 1 : std::max(1, std::min(32, 192 / s->tps));
-  s->threads = round_up(s->slots * s->tps, 32);
-  s->smem = sizeof(float) * ((size_t)s->RProws * s->RP + (size_t)s->slots * slot_floats);
+  const int slot_floats = round_up(s->XProws * s->XP + 4 * s->T * view_tap_pitch(s->T) + s->maxc * s->maxc + s->T * s->maxc, 4);
   int dev_smem = 0, nsm = 0;
   MLF_CUDA(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
   MLF_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device));
+  // small patches: several channel slots per CTA, as many as the shared memory holds
+  const int64_t fit = ((int64_t)dev_smem / (int64_t)sizeof(float) - (int64_t)s->RProws * s->RP) / slot_floats;
+  s->slots = s->tps >= 128 ? 1 : std::max(1, std::min({32, 192 / s->tps, (int)std::max<int64_t>(1, fit)}));
+  s->threads = round_up(s->slots * s->tps, 32);
+  s->smem = sizeof(float) * ((size_t)s->RProws * s->RP + (size_t)s->slots * slot_floats);
   if ((int)s->smem > dev_smem) return fail(MLF_ERR_UNSUPPORTED, "view kernel shared memory exceeds the device limit");
   MLF_TRY(prepare_view_kernels(s->T, s->smem));
   int per_sm = 1;

@@ -734,38 +734,46 @@ __global__ void k_tc_build_wft(const float* __restrict__ wf, int N, int Z, int T
 }
 
 // im2col of the ratio images (or of ones when R == nullptr) over the (T+2)^2 window, for
-// all patches: row = global position, R indexed by global position.
-__global__ void k_tc_im2col(const float* __restrict__ R, const int* __restrict__ tile_patch,
-                            const int* __restrict__ pinfo, int MP, int T, int KB, bf16* __restrict__ hi,
-                            bf16* __restrict__ lo) {
-  const int T2 = T + 2, q = (T - 1) / 2;
-  const int64_t total = (int64_t)MP * KB;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(e % KB);
-    const int pos = (int)(e / KB);
+// all patches: row = global position, R indexed by global position.  One warp per row; the
+// lanes walk the row's KB columns (columns past (T+2)^2 and rows past a patch's positions
+// are zero).
+constexpr int IM2COL_WARPS = 8;
+__global__ void __launch_bounds__(32 * IM2COL_WARPS)
+k_tc_im2col(const float* __restrict__ R, const int* __restrict__ tile_patch, const int* __restrict__ pinfo,
+            int MP, int T, int KB, bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  const int T2 = T + 2, q = (T - 1) / 2, KK = T2 * T2;
+  const int lane = threadIdx.x & 31;
+  for (int pos = blockIdx.x * IM2COL_WARPS + (threadIdx.x >> 5); pos < MP; pos += gridDim.x * IM2COL_WARPS) {
     const int* pi = pinfo + 8 * tile_patch[pos / BM];
-    const int Li = pi[0], Lj = pi[1], LL = pi[2], pos0 = pi[3];
+    const int Li = pi[0], Lj = pi[1], pos0 = pi[3];
     const int local = pos - pos0;
-    float val = 0.f;
-    if (local < LL && k < T2 * T2) {
-      const int b = local / Li, a = local - (local / Li) * Li;
-      const int j = b + k / T2 - q - 1, i = a + k % T2 - q - 1;
-      if (j >= 0 && j < Lj && i >= 0 && i < Li) val = R ? R[pos0 + j * Li + i] : 1.f;
+    const bool row_ok = local < pi[2];
+    const int b = row_ok ? local / Li : 0;
+    const int a = local - b * Li;
+    bf16* hrow = hi + (int64_t)pos * KB;
+    bf16* lrow = lo ? lo + (int64_t)pos * KB : nullptr;
+    for (int k = lane; k < KB; k += 32) {
+      float val = 0.f;
+      if (row_ok && k < KK) {
+        const int dj = k / T2;
+        const int j = b + dj - q - 1, i = a + (k - dj * T2) - q - 1;
+        if (j >= 0 && j < Lj && i >= 0 && i < Li) val = R ? __ldg(R + pos0 + j * Li + i) : 1.f;
+      }
+      bf16 h16, l16;
+      split_bf16(val, h16, l16);
+      hrow[k] = h16;
+      if (lrow) lrow[k] = l16;
     }
-    bf16 h16, l16;
-    split_bf16(val, h16, l16);
-    hi[e] = h16;
-    if (lo) lo[e] = l16;
   }
 }
 
 // HX[j][i] = sum_{db,da} sum_split Y[split][t = db*T+da][(j+db-q)*Li + (i+da-q)] for every valid
 // position of every patch; ratio R = LF_sub ./ HX (non-finite -> 0).  A block covers 32
-// consecutive positions; its 8 warps take the tap rows db = w, w+8, ... (lanes = positions,
-// so each load of a warp is 32 consecutive floats of one tap's row), and the warps' partial
-// sums are added in a fixed order (deterministic).
-constexpr int COL2IM_WARPS = 8;
+// consecutive positions (lanes); warp w takes the tap rows db = w, w+16, ..., so each load of
+// a warp is 32 consecutive floats of one tap's row.  Four split partials are loaded before
+// they are added, so every thread keeps several loads in flight; the warps' sums are added
+// in a fixed order (deterministic).
+constexpr int COL2IM_WARPS = 16;
 __global__ void __launch_bounds__(32 * COL2IM_WARPS)
 k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, int T,
                   const int* __restrict__ tile_patch, const int* __restrict__ pinfo,
@@ -788,14 +796,23 @@ k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, i
   }
   if (valid) {
     const int q = (T - 1) / 2;
+    const int64_t sstride = (int64_t)NB * MP;
+    const int da_lo = max(0, q - i), da_hi = min(T - 1, Li - 1 - i + q);  // 0 <= i + da - q < Li
     for (int db = w; db < T; db += COL2IM_WARPS) {
       const int b = j + db - q;
       if (b < 0 || b >= Lj) continue;
-      for (int da = 0; da < T; ++da) {
-        const int a = i + da - q;
-        if (a < 0 || a >= Li) continue;
-        const float* y = ypart + (int64_t)(db * T + da) * MP + pos0 + (int64_t)b * Li + a;
-        for (int sp = 0; sp < splits; ++sp) s += __ldg(y + (int64_t)sp * NB * MP);
+      // element (db, da): (db*T + da)*MP + pos0 + b*Li + i + da - q
+      const float* yrow = ypart + (int64_t)(db * T) * MP + pos0 + (int64_t)b * Li + (i - q);
+#pragma unroll 2
+      for (int da = da_lo; da <= da_hi; ++da) {
+        const float* y = yrow + (int64_t)da * (MP + 1);
+        int sp = 0;
+        for (; sp + 4 <= splits; sp += 4) {
+          const float v0 = __ldg(y + sp * sstride), v1 = __ldg(y + (sp + 1) * sstride);
+          const float v2 = __ldg(y + (sp + 2) * sstride), v3 = __ldg(y + (sp + 3) * sstride);
+          s += (v0 + v1) + (v2 + v3);
+        }
+        for (; sp < splits; ++sp) s += __ldg(y + sp * sstride);
       }
     }
   }
@@ -1061,8 +1078,8 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_CUDA(cudaMemsetAsync(t->X.p, 0, t->X.bytes, st));
   MLF_CUDA(cudaMemsetAsync(t->lfs.p, 0, t->lfs.bytes, st));
   MLF_CUDA(cudaMemsetAsync(t->err.p, 0, sizeof(int), st));
-  k_tc_im2col<<<2048, 256, 0, st>>>(nullptr, t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP, psf->T, tp->KB,
-                                    t->a1.as<bf16>(), nullptr);
+  k_tc_im2col<<<(t->MP + IM2COL_WARPS - 1) / IM2COL_WARPS, 32 * IM2COL_WARPS, 0, st>>>(
+      nullptr, t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP, psf->T, tp->KB, t->a1.as<bf16>(), nullptr);
   MLF_LAUNCHED();
   MLF_TRY(make_map(&t->mARh, t->ar_hi.p, t->MP, tp->KB, BM));
   MLF_TRY(make_map(&t->mARl, t->ar_lo.p, t->MP, tp->KB, BM));
@@ -1142,7 +1159,8 @@ int tc_col2im(const Psf* psf, TcSolverState* t, int view, bool ratio, float* hx_
 }
 
 int tc_im2col_ratio(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st) {
-  k_tc_im2col<<<2048, 256, 0, st>>>(t->rimg.as<float>(), t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP,
+  k_tc_im2col<<<(t->MP + IM2COL_WARPS - 1) / IM2COL_WARPS, 32 * IM2COL_WARPS, 0, st>>>(
+      t->rimg.as<float>(), t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP,
                                     psf->T, psf->tc->KB, t->ar_hi.as<bf16>(),
                                     act_split(precision) ? t->ar_lo.as<bf16>() : nullptr);
   MLF_LAUNCHED();

@@ -28,9 +28,11 @@ namespace mlf {
 constexpr int VT_TY = 8;  // tile rows (b direction)
 constexpr int VT_TX = 4;  // tile cols (a direction)
 
-// acc[ty][tx] += sum_{dy<T, dx<T} in[(ty+dy)*pitch + OFF + tx + dx] * w[dy*T+dx]
-// `in` must be 16-byte aligned and pitch a multiple of 4.
-template <int T, int OFF>
+// acc[ty][tx] += sum_{dy<T, dx<T} in[(ty+dy)*pitch + OFF + tx + dx] * w[dy*WP+dx]
+// `in` must be 16-byte aligned and pitch a multiple of 4.  Tap rows are WP floats apart;
+// when WP is a multiple of 4 a row is read with 16-byte loads (the padding is not used).
+// For a fixed output the products are added in the order dy, then dx.
+template <int T, int OFF, int WP = T>
 __device__ __forceinline__ void conv_tile(const float* __restrict__ in, int pitch,
                                           const float* __restrict__ w,
                                           float (&acc)[VT_TY][VT_TX]) {
@@ -39,8 +41,20 @@ __device__ __forceinline__ void conv_tile(const float* __restrict__ in, int pitc
 #pragma unroll 1
   for (int dy = 0; dy < T; ++dy) {
     float wr[T];
+    if constexpr (WP % 4 == 0) {
+      const float4* w4 = reinterpret_cast<const float4*>(w + dy * WP);
 #pragma unroll
-    for (int dx = 0; dx < T; ++dx) wr[dx] = w[dy * T + dx];
+      for (int k = 0; k < (T + 3) / 4; ++k) {
+        const float4 t4 = w4[k];
+        wr[4 * k] = t4.x;
+        if (4 * k + 1 < T) wr[4 * k + 1] = t4.y;
+        if (4 * k + 2 < T) wr[4 * k + 2] = t4.z;
+        if (4 * k + 3 < T) wr[4 * k + 3] = t4.w;
+      }
+    } else {
+#pragma unroll
+      for (int dx = 0; dx < T; ++dx) wr[dx] = w[dy * WP + dx];
+    }
     const float* rowp = in + dy * pitch;
 #pragma unroll
     for (int ty = 0; ty < VT_TY; ++ty) {
@@ -80,6 +94,8 @@ template <int T, int MODE>
 __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
   extern __shared__ __align__(16) float sm[];
   constexpr int TT = T * T;
+  constexpr int TW = view_tap_pitch(T);  // tap-row pitch in shared memory
+  constexpr int TTW = T * TW;
   constexpr int Q = (T - 1) / 2;
   constexpr int QP = view_qpad(Q);      // column of the forward-input interior
   constexpr bool BWD = (MODE != MODE_FWD);
@@ -98,7 +114,7 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
   float* slot_base = rs + (BWD ? A.RProws * A.RP : 0);
   float* xin = slot_base + (slot_ok ? slot : 0) * A.slot_floats;  // [XProws][XP]
   float* taps = xin + A.XProws * A.XP;                         // [2 buffers][wb | wf]
-  float* dtab = taps + 4 * TT;                                 // [maxc][maxc]
+  float* dtab = taps + 4 * TTW;                                // [maxc][maxc]
   float* rowp = dtab + A.maxc * A.maxc;                        // [T][maxc]
 
   // ---- zero the slots (halos must be zero), stage R
@@ -126,8 +142,9 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
   // taps of the first channel into buffer 0
   if (slot_ok && first < A.nch) {
     for (int i = lt; i < TT; i += A.tps) {
-      if (BWD) taps[i] = __ldg(A.wb + first * TT + i);
-      if (XIN) taps[TT + i] = __ldg(A.wf + first * TT + i);
+      const int j = (i / T) * TW + i % T;
+      if (BWD) taps[j] = __ldg(A.wb + first * TT + i);
+      if (XIN) taps[TTW + j] = __ldg(A.wf + first * TT + i);
     }
   }
   int buf = 0;
@@ -138,8 +155,8 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
     const int beta = active ? (int)(ch / ((int64_t)A.Z * A.N)) : 0;
     const int sa = floor_div(alpha - A.u + h, A.N);
     const int sb = floor_div(beta - A.v + h, A.N);
-    const float* wbs = taps + buf * 2 * TT;
-    const float* wfs = wbs + TT;
+    const float* wbs = taps + buf * 2 * TTW;
+    const float* wfs = wbs + TTW;
 
     // ---- X tile -> forward-input plane (interior at rows +Q, cols +QP), asynchronously
     if (XIN && active && lt < A.tps) {
@@ -159,7 +176,7 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
         const int dj = i / A.maxc, ca = i - dj * A.maxc;
         const int lo = rA[2 * ca], hi = rA[2 * ca + 1];
         float s = 0.f;
-        for (int di = lo; di <= hi; ++di) s += wbs[dj * T + di];
+        for (int di = lo; di <= hi; ++di) s += wbs[dj * TW + di];
         rowp[i] = s;
       }
     }
@@ -176,70 +193,85 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
     }
     __syncthreads();
 
-    if (active && lt < A.tps) {
-      if (BWD) {
+    // One correlation call site for both phases (back projection of view k, forward
+    // projection of view k+1), so that a single unrolled body per window offset is hot.
+#pragma unroll 1
+    for (int ph = 0; ph < 2; ++ph) {
+      if (ph == 1 && !(XIN && (MODE == MODE_FWD || A.do_fwd))) break;
+      if (active && lt < A.tps && ph == 0 && !BWD) {
+        cp_async_wait_all();  // forward only: this thread's X tile has landed in xin
+      } else if (active && lt < A.tps) {
         float acc[VT_TY][VT_TX];
 #pragma unroll
         for (int y = 0; y < VT_TY; ++y)
 #pragma unroll
           for (int x = 0; x < VT_TX; ++x) acc[y][x] = 0.f;
-        const float* rin = rs + (b0 + sb + 1) * A.RP + a0;
-        switch (sa + 1) {
-          case 0: conv_tile<T, 0>(rin, A.RP, wbs, acc); break;
-          case 1: conv_tile<T, 1>(rin, A.RP, wbs, acc); break;
-          default: conv_tile<T, 2>(rin, A.RP, wbs, acc); break;
+        const float* in = ph == 0 ? rs + (b0 + sb + 1) * A.RP + a0 : xin + b0 * A.XP + a0;
+        const int pitch = ph == 0 ? A.RP : A.XP;
+        const float* wsel = ph == 0 ? wbs : wfs;
+        switch (ph == 0 ? sa + 1 : QP - Q) {
+          case 0: conv_tile<T, 0, TW>(in, pitch, wsel, acc); break;
+          case 1: conv_tile<T, 1, TW>(in, pitch, wsel, acc); break;
+          case 2: conv_tile<T, 2, TW>(in, pitch, wsel, acc); break;
+          default:
+            if constexpr (QP - Q == 3) conv_tile<T, 3, TW>(in, pitch, wsel, acc);
+            break;
         }
-        if (MODE == MODE_BWDC) {
+        if (ph == 0) {
+          if (MODE == MODE_BWDC) {
 #pragma unroll
-          for (int y = 0; y < VT_TY; ++y) {
-            const int b = b0 + y;
-            if (b >= A.Lj) continue;
+            for (int y = 0; y < VT_TY; ++y) {
+              const int b = b0 + y;
+              if (b >= A.Lj) continue;
 #pragma unroll
-            for (int x = 0; x < VT_TX; ++x)
-              if (a0 + x < A.Li) A.Cout[ch * A.plane + (int64_t)b * A.Pa + a0 + x] = acc[y][x];
-          }
-        } else {
-          cp_async_wait_all();  // this thread's X tile has landed in xin
-          const int* cA = A.clsA + (sa + 1) * A.Li;
-          const int* cB = A.clsB + (sb + 1) * A.Lj;
-          float* Xch = A.X + ch * A.plane;
+              for (int x = 0; x < VT_TX; ++x)
+                if (a0 + x < A.Li) A.Cout[ch * A.plane + (int64_t)b * A.Pa + a0 + x] = acc[y][x];
+            }
+          } else {
+            cp_async_wait_all();  // this thread's X tile has landed in xin
+            const int* cA = A.clsA + (sa + 1) * A.Li;
+            const int* cB = A.clsB + (sb + 1) * A.Lj;
+            float* Xch = A.X + ch * A.plane;
 #pragma unroll
-          for (int y = 0; y < VT_TY; ++y) {
-            const int b = b0 + y;
-            if (b >= A.Lj) continue;
-            const int cb = __ldg(cB + b);
-            float* xrow = xin + (b + Q) * A.XP + a0 + QP;
+            for (int y = 0; y < VT_TY; ++y) {
+              const int b = b0 + y;
+              if (b >= A.Lj) continue;
+              const int cb = __ldg(cB + b);
+              float* xrow = xin + (b + Q) * A.XP + a0 + QP;
 #pragma unroll
-            for (int x = 0; x < VT_TX; ++x) {
-              const int a = a0 + x;
-              if (a >= A.Li) continue;
-              const float c = acc[y][x];
-              const float d = dtab[cb * A.maxc + __ldg(cA + a)];
-              const float xo = xrow[x];
-              float xc = xo * c / (d + A.d_eps);           // :130  X .* C ./ D
-              if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;     // :132-134 NaN, Inf, < 0
-              float xn = xc * A.w + (1.f - A.w) * xo;       // :136
-              if (xn < 0.f) xn = 0.f;                      // :137
-              xrow[x] = xn;
-              Xch[(int64_t)b * A.Pa + a] = xn;
+              for (int x = 0; x < VT_TX; ++x) {
+                const int a = a0 + x;
+                if (a >= A.Li) continue;
+                const float c = acc[y][x];
+                const float d = dtab[cb * A.maxc + __ldg(cA + a)];
+                const float xo = xrow[x];
+                float xc = xo * c / (d + A.d_eps);           // :130  X .* C ./ D
+                if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;     // :132-134 NaN, Inf, < 0
+                float xn = __fmaf_rn(xc, A.w, __fmul_rn(1.f - A.w, xo));  // :136
+                if (xn < 0.f) xn = 0.f;                      // :137
+                xrow[x] = xn;
+                Xch[(int64_t)b * A.Pa + a] = xn;
+              }
             }
           }
+        } else {
+#pragma unroll
+          for (int y = 0; y < VT_TY; ++y)
+#pragma unroll
+            for (int x = 0; x < VT_TX; ++x) hx[y][x] += acc[y][x];
         }
-      } else {
-        cp_async_wait_all();
       }
+      if (ph == 0) __syncthreads();
     }
-    __syncthreads();
-    if (XIN && (MODE == MODE_FWD || A.do_fwd) && active && lt < A.tps)
-      conv_tile<T, QP - Q>(xin + b0 * A.XP + a0, A.XP, wfs, hx);
     // taps of the next channel into the other buffer (read after the barrier below)
     {
       const int64_t nxt = ch + step;
-      float* nb = taps + (buf ^ 1) * 2 * TT;
+      float* nb = taps + (buf ^ 1) * 2 * TTW;
       if (slot_ok && nxt < A.nch) {
         for (int i = lt; i < TT; i += A.tps) {
-          if (BWD) nb[i] = __ldg(A.wb + nxt * TT + i);
-          if (XIN) nb[TT + i] = __ldg(A.wf + nxt * TT + i);
+          const int j = (i / T) * TW + i % T;
+          if (BWD) nb[j] = __ldg(A.wb + nxt * TT + i);
+          if (XIN) nb[TTW + j] = __ldg(A.wf + nxt * TT + i);
         }
       }
     }
