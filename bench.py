@@ -116,10 +116,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(device, rank):
+def make_workload(device, rank, planes=None):
     import torch
     from mesolf_gb300 import synth
     w = synth.config2(seed=rank)
+    if planes:
+        # the deepest planes of the same workload: lateral size, PSF array side and the
+        # per-plane kernel windows unchanged, fewer planes (and somas in proportion)
+        k = w.z_idx[-planes:]
+        w = synth.Workload(f"lf1005x1005x{planes}_k231_it3_deepest", w.N, w.lenslets, w.K0, k,
+                           np.asarray(w.plane_sides)[-planes:], max(1, w.n_obj * planes // len(w.z_idx)),
+                           w.sigma, w.peaks, w.background, w.photons, w.iters, w.seed)
     H, Ht = w.psf()
     vol = w.volume()
     lf = w.measured(H, vol, device=str(device))
@@ -206,6 +213,9 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="one solve of --iters iterations and exit (for ncu captures)")
     ap.add_argument("--iters", type=int, default=None)
+    ap.add_argument("--planes", type=int, default=None,
+                    help="with --profile: the deepest PLANES planes of the workload only (a smaller "
+                         "device footprint for full ncu captures; same lateral size and kernel widths)")
     ap.add_argument("--mixed", default="bf16x2", help="tensor-core precision timed beside plain FP32 ('' to skip)")
     ap.add_argument("--serve-frames", type=int, default=4,
                     help="frames of the 36-patch 18 Hz serving stream (0 to skip)")
@@ -242,7 +252,7 @@ def main():
     from mesolf_gb300 import PhaseSpacePSF, RLSolver, _lib
     from mesolf_gb300.api import _fortran
 
-    w, H, Ht, lf = make_workload(dev, rank)
+    w, H, Ht, lf = make_workload(dev, rank, args.planes if args.profile else None)
     torch.cuda.empty_cache()
     Xr, Xc = w.image_shape
     Z = w.Z

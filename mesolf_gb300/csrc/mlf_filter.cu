@@ -24,74 +24,107 @@ namespace {
 constexpr int kLines = 32;      // lines per CTA (one per lane)
 constexpr int kPad = 33;        // shared-memory row stride (bank-conflict free)
 constexpr int kChunk = 8;       // consecutive outputs per thread
-constexpr int kFiltThreads = 256;
+constexpr int kFiltThreads = 512;
+constexpr int kLoadUnroll = 8;   // loads in flight per thread while staging lines
+constexpr int kRephaseLines = 4; // lines per block of k_rephase
 
 struct FGeo {
   int64_t Xr, Xc;
   int Z;
 };
 
-__device__ __forceinline__ int64_t unphase_index(const PatchGeo& g, int64_t e) {
-  const int64_t r = e % g.Xr;
-  const int64_t c = (e / g.Xr) % g.Xc;
-  const int z = (int)(e / (g.Xr * g.Xc));
-  const int64_t ch = geo_channel(g, (int)(r % g.N), (int)(c % g.N), z);
-  return ch * g.plane + (c / g.N) * g.Pa + (r / g.N);
+// Phase-major -> MATLAB layout for one line (c, z) of length Xr = N*Li:
+// line[N*a + alpha] = X[ch(alpha, beta, z)][b][a], beta = c mod N, b = c / N.  `f(i, off)` is
+// called for i in [0, Xr) with the X offset of element i's source, i = alpha*Li + a, so that
+// consecutive i read consecutive floats of one channel row.
+__device__ __forceinline__ int64_t line_src(const PatchGeo& g, int c, int z, int i) {
+  const int alpha = i / g.Li, a = i - alpha * g.Li;
+  return geo_channel(g, alpha, c % g.N, z) * g.plane + (int64_t)(c / g.N) * g.Pa + a;
 }
 
-// Phase-major -> MATLAB layout for the patch's planes (into the scratch volume).
-__global__ void k_unphase(const float* __restrict__ X, PatchGeo g, float* __restrict__ V) {
-  const int64_t n = g.Xr * g.Xc * g.Z;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x)
-    V[e] = X[unphase_index(g, e)];
-}
-
-// MATLAB layout -> phase-major, scaling each plane by scale[z].
-__global__ void k_rephase(const float* __restrict__ V, const double* __restrict__ scale, PatchGeo g,
-                          float* __restrict__ X) {
-  const int64_t n = g.Xr * g.Xc * g.Z;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int z = (int)(e / (g.Xr * g.Xc));
-    X[unphase_index(g, e)] = (float)((double)V[e] * scale[z]);
+// MATLAB layout -> phase-major for the filtered planes, scaling each plane by scale[z]: one
+// block per kRephaseLines lines (c, zlist[blockIdx.y]); the lines are staged in shared
+// memory so that both the read of V and the write of X's channel rows are coalesced.
+__global__ void k_rephase(const float* __restrict__ V, const double* __restrict__ scale,
+                          const int* __restrict__ zlist, PatchGeo g, float* __restrict__ X) {
+  extern __shared__ float lines[];  // [kRephaseLines][Xr]
+  const int c0 = blockIdx.x * kRephaseLines, z = zlist[blockIdx.y];
+  const int Xr = (int)g.Xr;
+  const int nl = (int)(g.Xc - c0 < kRephaseLines ? g.Xc - c0 : kRephaseLines);
+  const int total = nl * Xr;
+  const float* src = V + ((int64_t)z * g.Xc + c0) * g.Xr;  // nl consecutive lines
+  for (int e0 = threadIdx.x; e0 < total; e0 += kLoadUnroll * blockDim.x) {
+    float v[kLoadUnroll];
+#pragma unroll
+    for (int u = 0; u < kLoadUnroll; ++u) {
+      const int e = e0 + u * blockDim.x;
+      v[u] = e < total ? src[e] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadUnroll; ++u) {
+      const int e = e0 + u * blockDim.x;
+      if (e < total) lines[e] = v[u];
+    }
+  }
+  __syncthreads();
+  const double sc = scale[z];
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int l = e / Xr, i = e - l * Xr;
+    const int alpha = i / g.Li, a = i - alpha * g.Li;
+    X[line_src(g, c0 + l, z, i)] = (float)((double)lines[l * Xr + g.N * a + alpha] * sc);
   }
 }
 
 // Circular 1-D filtering of kLines lines of length L held in shared memory as
-// buf[i * kPad + line].  taps[k] = c[(k - wlo) mod L], k < nt:
+// buf[i * kPad + line].  taps[k] = c[(k - wlo) mod L] for k < nt, zero for nt <= k < ntp
+// (ntp a multiple of 8, taps in shared memory, 16-byte aligned):
 //   y[i] = sum_k taps[k] * x[(i + wlo - k) mod L]
-// Each thread produces kChunk consecutive outputs of one line (lane = line).
+// Each thread produces kChunk = 8 consecutive outputs of one line (lane = line) and walks the
+// taps in groups of 8 over a 16-value register window, so one group costs 8 window loads
+// and 2 tap loads for 64 FMAs.  Every output adds its products in the order k = 0, 1, ...
+// (the zero taps add exactly nothing).
 // `emit(line, i, value)` stores an output; returns the thread's FP64 sum of outputs.
 template <class Emit>
 __device__ double filter_lines(const float* __restrict__ buf, int L, const float* __restrict__ taps,
-                               int nt, int wlo, int nlines, Emit emit) {
+                               int ntp, int wlo, int nlines, Emit emit) {
+  static_assert(kChunk == 8, "the register window assumes 8 outputs per thread");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   double s = 0.0;
   const int nchunks = (L + kChunk - 1) / kChunk;
   for (int chk = warp; chk < nchunks; chk += nwarps) {
     if (lane >= nlines) continue;
     const int i0 = chk * kChunk;
-    float win[kChunk];
-    int j = (i0 + wlo) % L;  // index of x for output i0 at k = 0
+    const int j = (i0 + wlo) % L;  // index of x for output i0 at k = 0
+    float w[16];                    // w[m] = x[(j - k0 - 8 + m) mod L] within the group at k0
 #pragma unroll
-    for (int t = 0; t < kChunk; ++t) {
+    for (int t = 0; t < 8; ++t) {
       int jt = j + t;
       if (jt >= L) jt -= L;
-      win[t] = buf[jt * kPad + lane];
+      w[8 + t] = buf[jt * kPad + lane];
     }
+    int jb = j - 8;
+    while (jb < 0) jb += L;
     float acc[kChunk];
 #pragma unroll
     for (int t = 0; t < kChunk; ++t) acc[t] = 0.f;
-    for (int k = 0; k < nt; ++k) {
-      const float c = taps[k];
+    for (int k0 = 0; k0 < ntp; k0 += 8) {
 #pragma unroll
-      for (int t = 0; t < kChunk; ++t) acc[t] = fmaf(c, win[t], acc[t]);
-      // slide: next k needs x[(i + wlo - k - 1) mod L]
+      for (int m = 0; m < 8; ++m) {
+        int jm = jb + m;
+        if (jm >= L) jm -= L;
+        w[m] = buf[jm * kPad + lane];
+      }
+      const float4 c0 = *reinterpret_cast<const float4*>(taps + k0);
+      const float4 c1 = *reinterpret_cast<const float4*>(taps + k0 + 4);
+      const float c[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
 #pragma unroll
-      for (int t = kChunk - 1; t > 0; --t) win[t] = win[t - 1];
-      j = (j == 0) ? L - 1 : j - 1;
-      win[0] = buf[j * kPad + lane];
+      for (int sk = 0; sk < 8; ++sk)
+#pragma unroll
+        for (int t = 0; t < kChunk; ++t) acc[t] = fmaf(c[sk], w[8 + t - sk], acc[t]);
+#pragma unroll
+      for (int m = 0; m < 8; ++m) w[8 + m] = w[m];
+      jb -= 8;
+      while (jb < 0) jb += L;
     }
 #pragma unroll
     for (int t = 0; t < kChunk; ++t) {
@@ -105,6 +138,16 @@ __device__ double filter_lines(const float* __restrict__ buf, int L, const float
   return s;
 }
 
+// Stage the taps of bank entry e in shared memory, zero-padded to a multiple of 8.
+__device__ __forceinline__ int stage_taps(float* tsm, const float* __restrict__ taps, int nt) {
+  const int ntp = (nt + 7) & ~7;
+  for (int k = threadIdx.x; k < ntp; k += blockDim.x) tsm[k] = k < nt ? taps[k] : 0.f;
+  return ntp;
+}
+
+// shared-memory offset (floats) of the staged taps, after a line buffer of L lines
+__host__ __device__ constexpr int taps_offset(int L) { return (L * kPad + 3) & ~3; }
+
 __device__ void block_reduce_store(double s, double* out) {
   __shared__ double sh[32];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -117,31 +160,50 @@ __device__ void block_reduce_store(double s, double* out) {
   }
 }
 
-// Pass along r (contiguous): grid (ceil(Xc / kLines), Zf).  Lines = columns c of plane z.
-// Also accumulates the plane's input sum (sum_before).
-__global__ void k_filter_r(float* __restrict__ V, FGeo g, const int* __restrict__ zlist,
-                           const int* __restrict__ plane_entry, const float* __restrict__ cx,
-                           const int* __restrict__ wlo_e, const int* __restrict__ nt_e, int tap_stride,
-                           double* sums_in) {
-  extern __shared__ float buf[];  // [Xr][kPad]
+// Pass along r: grid (ceil(Xc / kLines), Zf).  Lines = columns c of plane z, gathered
+// straight from the phase-major volume X (line_src); the row-filtered lines are written to
+// V in MATLAB layout.  Also accumulates the plane's input sum (sum_before).
+__global__ void k_filter_r(const float* __restrict__ X, PatchGeo pg, float* __restrict__ V, FGeo g,
+                           const int* __restrict__ zlist, const int* __restrict__ plane_entry,
+                           const float* __restrict__ cx, const int* __restrict__ wlo_e,
+                           const int* __restrict__ nt_e, int tap_stride, double* sums_in) {
+  extern __shared__ __align__(16) float buf[];  // [Xr][kPad], then the taps
   const int z = zlist[blockIdx.y];
   const int e = plane_entry[z];
-  const int64_t c0 = (int64_t)blockIdx.x * kLines;
+  const int c0 = blockIdx.x * kLines;
   const int nlines = (int)(g.Xc - c0 < kLines ? g.Xc - c0 : kLines);
   float* plane = V + (int64_t)z * g.Xr * g.Xc;
+  const int L = (int)g.Xr;
+  float* tsm = buf + taps_offset(L);
+  const int ntp = stage_taps(tsm, cx + (int64_t)e * tap_stride, nt_e[e]);
+  // element e = l * L + i of the block's lines; 8 loads in flight per thread
   double sin = 0.0;
-  for (int l = 0; l < nlines; ++l) {
-    const float* line = plane + (c0 + l) * g.Xr;
-    for (int64_t i = threadIdx.x; i < g.Xr; i += blockDim.x) {
-      const float x = line[i];
-      buf[i * kPad + l] = x;
-      sin += (double)x;
+  const int total = nlines * L;
+  for (int e0 = threadIdx.x; e0 < total; e0 += kLoadUnroll * blockDim.x) {
+    float v[kLoadUnroll];
+#pragma unroll
+    for (int u = 0; u < kLoadUnroll; ++u) {
+      const int e = e0 + u * blockDim.x;
+      v[u] = 0.f;
+      if (e < total) {
+        const int l = e / L;
+        v[u] = X[line_src(pg, c0 + l, z, e - l * L)];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadUnroll; ++u) {
+      const int e = e0 + u * blockDim.x;
+      if (e < total) {
+        const int l = e / L, i = e - l * L;
+        const int alpha = i / pg.Li, a = i - alpha * pg.Li;
+        buf[(pg.N * a + alpha) * kPad + l] = v[u];
+        sin += (double)v[u];
+      }
     }
   }
   __syncthreads();
-  const int L = (int)g.Xr;
-  double sout = filter_lines(buf, L, cx + (int64_t)e * tap_stride, nt_e[e], wlo_e[e], nlines,
-                             [&](int l, int i, float y) { plane[(c0 + l) * g.Xr + i] = y; });
+  double sout = filter_lines(buf, L, tsm, ntp, wlo_e[e], nlines,
+                             [&](int l, int i, float y) { plane[(int64_t)(c0 + l) * g.Xr + i] = y; });
   (void)sout;
   block_reduce_store(sin, sums_in + (int64_t)blockIdx.y * gridDim.x + blockIdx.x);
 }
@@ -152,18 +214,32 @@ __global__ void k_filter_c(float* __restrict__ V, FGeo g, const int* __restrict_
                            const int* __restrict__ plane_entry, const float* __restrict__ cy,
                            const int* __restrict__ wlo_e, const int* __restrict__ nt_e, int tap_stride,
                            double* sums_out) {
-  extern __shared__ float buf[];  // [Xc][kPad]
+  extern __shared__ __align__(16) float buf[];  // [Xc][kPad], then the taps
   const int z = zlist[blockIdx.y];
   const int e = plane_entry[z];
   const int64_t r0 = (int64_t)blockIdx.x * kLines;
+  float* tsm = buf + taps_offset((int)g.Xc);
+  const int ntp = stage_taps(tsm, cy + (int64_t)e * tap_stride, nt_e[e]);
   const int nlines = (int)(g.Xr - r0 < kLines ? g.Xr - r0 : kLines);
   float* plane = V + (int64_t)z * g.Xr * g.Xc;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int64_t c = warp; c < g.Xc; c += nwarps)
-    if (lane < nlines) buf[c * kPad + lane] = plane[c * g.Xr + r0 + lane];
+  // 8 column loads in flight per thread
+  for (int c0 = warp; c0 < (int)g.Xc; c0 += kLoadUnroll * nwarps) {
+    float v[kLoadUnroll];
+#pragma unroll
+    for (int u = 0; u < kLoadUnroll; ++u) {
+      const int c = c0 + u * nwarps;
+      v[u] = (c < g.Xc && lane < nlines) ? plane[(int64_t)c * g.Xr + r0 + lane] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadUnroll; ++u) {
+      const int c = c0 + u * nwarps;
+      if (c < g.Xc && lane < nlines) buf[c * kPad + lane] = v[u];
+    }
+  }
   __syncthreads();
   const int L = (int)g.Xc;
-  double s = filter_lines(buf, L, cy + (int64_t)e * tap_stride, nt_e[e], wlo_e[e], nlines,
+  double s = filter_lines(buf, L, tsm, ntp, wlo_e[e], nlines,
                           [&](int l, int i, float y) { plane[(int64_t)i * g.Xr + r0 + l] = y; });
   block_reduce_store(s, sums_out + (int64_t)blockIdx.y * gridDim.x + blockIdx.x);
 }
@@ -329,7 +405,8 @@ int filter_init(Solver* s) {
   const int gr = (int)((s->Xc + kLines - 1) / kLines), gc = (int)((s->Xr + kLines - 1) / kLines);
   f.max_blocks = std::max(gr, gc);
   MLF_TRY(f.sums.alloc(sizeof(double) * (2 * (size_t)std::max(1, nzf) * f.max_blocks + Z), "filter sums"));
-  const size_t smem_r = sizeof(float) * (size_t)Lr * kPad, smem_c = sizeof(float) * (size_t)Lc * kPad;
+  const size_t smem_r = sizeof(float) * ((size_t)taps_offset(Lr) + ((Lr + 7) & ~7));
+  const size_t smem_c = sizeof(float) * ((size_t)taps_offset(Lc) + ((Lc + 7) & ~7));
   int dev_smem = 0;
   MLF_CUDA(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
   if ((int)std::max(smem_r, smem_c) > dev_smem)
@@ -355,20 +432,19 @@ int filter_run_geo(Solver* s, const PatchGeo& g, float* X, cudaStream_t st) {
   const int* wlo_y = nt_x + ne;
   const int* nt_y = wlo_y + ne;
   const FGeo fg{s->Xr, s->Xc, Z};
-  const int64_t n = s->Xr * s->Xc * Z;
-  const int eg = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
   float* V = s->Xtmp.as<float>();
-  k_unphase<<<eg, 256, 0, st>>>(X, g, V);
   const int gr = (int)((s->Xc + kLines - 1) / kLines), gc = (int)((s->Xr + kLines - 1) / kLines);
   double* sin = f.sums.as<double>();
   double* sout = sin + (size_t)nzf * f.max_blocks;
   double* scale = sout + (size_t)nzf * f.max_blocks;
-  k_filter_r<<<dim3(gr, nzf), kFiltThreads, sizeof(float) * s->Xr * kPad, st>>>(
-      V, fg, zl, pe, f.cx.as<float>(), wlo_x, nt_x, (int)s->Xr, sin);
-  k_filter_c<<<dim3(gc, nzf), kFiltThreads, sizeof(float) * s->Xc * kPad, st>>>(
-      V, fg, zl, pe, f.cy.as<float>(), wlo_y, nt_y, (int)s->Xc, sout);
+  const int Lr = (int)s->Xr, Lc = (int)s->Xc;
+  k_filter_r<<<dim3(gr, nzf), kFiltThreads, sizeof(float) * ((size_t)taps_offset(Lr) + ((Lr + 7) & ~7)), st>>>(
+      X, g, V, fg, zl, pe, f.cx.as<float>(), wlo_x, nt_x, Lr, sin);
+  k_filter_c<<<dim3(gc, nzf), kFiltThreads, sizeof(float) * ((size_t)taps_offset(Lc) + ((Lc + 7) & ~7)), st>>>(
+      V, fg, zl, pe, f.cy.as<float>(), wlo_y, nt_y, Lc, sout);
   k_filter_scale<<<(Z + 255) / 256, 256, 0, st>>>(sin, gr, sout, gc, zl, nzf, Z, scale);
-  k_rephase<<<eg, 256, 0, st>>>(V, scale, g, X);
+  k_rephase<<<dim3((Lc + kRephaseLines - 1) / kRephaseLines, nzf), 256, sizeof(float) * kRephaseLines * Lr, st>>>(
+      V, scale, zl, g, X);
   MLF_LAUNCHED();
   return MLF_OK;
 }

@@ -202,22 +202,36 @@ __global__ void k_scatter_views(const float* __restrict__ lfs, PatchGeo g, float
 // HX = sum of the per-CTA forward partials (fixed order).  Optionally writes HX and the
 // ratio image R = LF_sub ./ HX with non-finite -> 0 (recon_…_with_filter.m:116-117) into
 // the halo-padded buffer read by the next view kernel.
-__global__ void k_reduce_ratio(const float* __restrict__ part, int nparts, int Li, int Lj,
-                               const float* __restrict__ lfsub, float* __restrict__ hx_out,
-                               float* __restrict__ rpad, int RP, int off) {
+// One block covers 32 positions (lanes); its 8 warps take the partials k = w, w+8, ... with
+// four accumulators each, and the warps' sums are added in a fixed order (deterministic).
+constexpr int kReduceGroups = 8;
+__global__ void __launch_bounds__(32 * kReduceGroups)
+k_reduce_ratio(const float* __restrict__ part, int nparts, int Li, int Lj,
+               const float* __restrict__ lfsub, float* __restrict__ hx_out,
+               float* __restrict__ rpad, int RP, int off) {
+  __shared__ float sh[kReduceGroups][32];
   const int LL = Li * Lj;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= LL) return;
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-  int k = 0;
-  for (; k + 4 <= nparts; k += 4) {
-    s0 += part[(int64_t)(k + 0) * LL + i];
-    s1 += part[(int64_t)(k + 1) * LL + i];
-    s2 += part[(int64_t)(k + 2) * LL + i];
-    s3 += part[(int64_t)(k + 3) * LL + i];
+  const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  float s = 0.f;
+  if (i < LL) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int k = grp;
+    for (; k + 3 * kReduceGroups < nparts; k += 4 * kReduceGroups) {
+      s0 += part[(int64_t)k * LL + i];
+      s1 += part[(int64_t)(k + kReduceGroups) * LL + i];
+      s2 += part[(int64_t)(k + 2 * kReduceGroups) * LL + i];
+      s3 += part[(int64_t)(k + 3 * kReduceGroups) * LL + i];
+    }
+    for (; k < nparts; k += kReduceGroups) s0 += part[(int64_t)k * LL + i];
+    s = (s0 + s1) + (s2 + s3);
   }
-  for (; k < nparts; ++k) s0 += part[(int64_t)k * LL + i];
-  const float hx = (s0 + s1) + (s2 + s3);
+  sh[grp][lane] = s;
+  __syncthreads();
+  if (grp != 0 || i >= LL) return;
+  float hx = 0.f;
+#pragma unroll
+  for (int g = 0; g < kReduceGroups; ++g) hx += sh[g][lane];
   if (hx_out) hx_out[i] = hx;
   if (rpad) {
     float r = lfsub[i] / hx;
@@ -342,7 +356,7 @@ int run_view(Solver* s, int mode, int view_cur, int view_next, float w, bool do_
 int run_reduce(Solver* s, int view, float* hx_out, bool ratio, cudaStream_t st) {
   const int LL = s->Li * s->Lj;
   const float* lfsub = s->lfs.as<float>() + (int64_t)view * LL;
-  k_reduce_ratio<<<ceil_div(LL, 256), 256, 0, st>>>(
+  k_reduce_ratio<<<ceil_div(LL, 32), 32 * kReduceGroups, 0, st>>>(
       s->part.as<float>(), s->grid, s->Li, s->Lj, lfsub, hx_out,
       ratio ? s->rpad.as<float>() : nullptr, s->RP, s->q + 1);
   MLF_LAUNCHED();
