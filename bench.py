@@ -329,6 +329,7 @@ def main():
         mixed = {"precision": args.mixed, "value": replica_value(w.voxels, ws, mms), "unit": "voxels/s",
                  "ms_per_step": mms, "speedup_vs_plain_fp32": ms / mms,
                  "rel_l2_vs_plain_fp32": float(d),
+                 "rel_change_last_iteration": st2.get("rel_change"),
                  "gpu_launches": int(mlaunch),
                  "launch_config": {k: st2[k] for k in ("fwd_splits", "fwd_stages", "bwd_xbufs", "tuned")},
                  "view_kernels_ms_per_view": mk_ms / max(1, mk_n),
@@ -382,7 +383,9 @@ def main():
                        "views_per_iteration": n_views, "parallelism": f"replicas x{ws}",
                        "l2": "inputs larger than L2 (projector taps 4.6 GB, volume 206 MB)"},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks,
-            "impl": "ours", "mixed": mixed}
+            "impl": "ours", "mixed": mixed,
+            "convergence": {"rel_change_last_iteration": st.get("rel_change"),
+                            "note": "||X_k - X_(k-1)|| / ||X_k|| of the last RL iteration, FP64 on the device"}}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         t, thr, planes = cpu_baseline_sample(H, Ht, lf.astype(np.float64))
         t_solve = t * n_views * w.iters

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define MLF_ABI_VERSION 2
+#define MLF_ABI_VERSION 3
 
 enum mlf_status_code {
   MLF_OK = 0,
@@ -65,6 +65,9 @@ typedef struct mlf_stats {
   int32_t fwd_stages;           /* shared-memory ring depth of the forward GEMM */
   int32_t bwd_xbufs;            /* X-tile buffers per half in the back projection (1 or 2) */
   int32_t tuned;                /* 1 if chosen by timing, 0 if the built-in heuristics */
+  /* convergence monitor (ABI 3): ||X_k - X_(k-1)||_2 / ||X_k||_2 of the last iteration k,
+   * both sums in FP64 on the device (over all patches of a batch); 0 when no iteration ran */
+  double rel_change;
 } mlf_stats;
 
 /* Library / ABI version (MLF_ABI_VERSION). */
@@ -230,7 +233,8 @@ int mlf_batch_create(mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int6
                      const int32_t* nz, mlf_batch** out);
 int mlf_batch_destroy(mlf_batch* b);
 /* Device bytes mlf_batch_create would allocate for these patches (an upper bound, for
- * admission by free HBM before creating the work set).  No allocation. */
+ * admission by free HBM before creating the work set; it includes the convergence-monitor
+ * volume that the first solve with stats allocates).  No allocation. */
 int mlf_batch_plan_bytes(const mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int64_t* Xc,
                          const int32_t* z0, const int32_t* nz, int64_t* bytes);
 int64_t mlf_batch_device_bytes(const mlf_batch* b);

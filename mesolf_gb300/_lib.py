@@ -76,7 +76,7 @@ class MLFStats(ctypes.Structure):
                 ("view_ms", ctypes.c_double), ("view_kernel_ms", ctypes.c_double),
                 ("view_kernel_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
                 ("fwd_splits", ctypes.c_int32), ("fwd_stages", ctypes.c_int32), ("bwd_xbufs", ctypes.c_int32),
-                ("tuned", ctypes.c_int32)]
+                ("tuned", ctypes.c_int32), ("rel_change", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

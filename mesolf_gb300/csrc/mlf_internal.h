@@ -150,6 +150,8 @@ struct Solver {
   DevBuf cls;        // int tables: clsA[3][Li], clsB[3][Lj], rngA[3][maxc][2], rngB[3][maxc][2]
   DevBuf red;        // double scratch for reductions
   DevBuf stage_in, stage_out;  // device staging for host arrays
+  DevBuf Xprev;      // float [nch][plane]      volume at the start of the iteration (stats only)
+  DevBuf relbuf;     // double: block partials and the relative change of the last iteration
   FilterPlan filt;
   // optional per-launch timing of the projector kernels (enabled when stats are requested)
   std::vector<cudaEvent_t> tev;
@@ -188,6 +190,13 @@ inline float solver_d_eps(const Solver* s) { return s->variant == MLF_VARIANT_PE
 int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st);
 // flat initial guess sum(lf)/(Xr*Xc*Z) on the patch's planes, 0 on the other channels
 int launch_init_flat(const float* d_lf, const PatchGeo& g, float* X, double* scratch, cudaStream_t st);
+// Convergence monitor: rel = ||X - Xprev||_2 / ||X||_2 over n floats, both sums in FP64
+// (fixed-order reductions), then Xprev <- X.  `buf` holds kRelChangeBufDoubles doubles; the
+// result is buf[0].  rel_change_prepare allocates Xprev / buf (not during a graph capture).
+constexpr int kRelChangeBlocks = 512;
+constexpr int kRelChangeBufDoubles = 2 * kRelChangeBlocks + 8;
+int launch_rel_change(const float* X, float* Xprev, int64_t n, double* buf, cudaStream_t st);
+int rel_change_read(const double* buf, double* out);
 int filter_run_geo(Solver* s, const PatchGeo& g, float* X, cudaStream_t st);
 PatchGeo solver_geo(const Solver* s);
 std::vector<double> psf_range_weights(const Psf* p, int z0, int nz);

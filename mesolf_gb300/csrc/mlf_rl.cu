@@ -399,8 +399,8 @@ Solver::~Solver() {
 
 size_t Solver::bytes() const {
   return X.bytes + Xtmp.bytes + lfs.bytes + rpad.bytes + part.bytes + hx.bytes + cls.bytes +
-         red.bytes + stage_in.bytes + stage_out.bytes + filt.cx.bytes + filt.cy.bytes +
-         filt.sums.bytes + tc_solver_bytes(this);
+         red.bytes + stage_in.bytes + stage_out.bytes + Xprev.bytes + relbuf.bytes + filt.cx.bytes +
+         filt.cy.bytes + filt.sums.bytes + tc_solver_bytes(this);
 }
 
 size_t Psf::bytes() const { return wf.bytes + wb.bytes + tc_psf_bytes(this); }
@@ -433,6 +433,77 @@ int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStrea
   MLF_LAUNCHED();
   return MLF_OK;
 }
+// ------------------------------------------------------------------ convergence monitor
+// Block b of kRelChangeBlocks takes the float4 groups b*256 + tid, + grid*256, ... (a fixed
+// partition), sums (x - xp)^2 and x^2 in FP64 in a fixed order, and copies X into Xprev.
+__global__ void __launch_bounds__(256) k_rel_change_partial(const float* __restrict__ X,
+                                                           float* __restrict__ Xprev, int64_t n,
+                                                           double* __restrict__ part) {
+  __shared__ double sh[2][8];
+  double d2 = 0.0, x2 = 0.0;
+  const int64_t n4 = n / 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const float4* x4 = reinterpret_cast<const float4*>(X);
+  float4* p4 = reinterpret_cast<float4*>(Xprev);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+    const float4 x = x4[i], xp = p4[i];
+    const double a = (double)x.x - xp.x, b = (double)x.y - xp.y, c = (double)x.z - xp.z,
+                 d = (double)x.w - xp.w;
+    d2 += a * a + b * b + c * c + d * d;
+    x2 += (double)x.x * x.x + (double)x.y * x.y + (double)x.z * x.z + (double)x.w * x.w;
+    p4[i] = x;
+  }
+  for (int64_t i = 4 * n4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double a = (double)X[i] - Xprev[i];
+    d2 += a * a;
+    x2 += (double)X[i] * X[i];
+    Xprev[i] = X[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    d2 += __shfl_down_sync(0xffffffffu, d2, o);
+    x2 += __shfl_down_sync(0xffffffffu, x2, o);
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][w] = d2;
+    sh[1][w] = x2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      a += sh[0][k];
+      b += sh[1][k];
+    }
+    part[2 + 2 * blockIdx.x] = a;
+    part[3 + 2 * blockIdx.x] = b;
+  }
+}
+
+__global__ void k_rel_change_final(double* buf, int nb) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double a = 0.0, b = 0.0;
+  for (int k = 0; k < nb; ++k) {
+    a += buf[2 + 2 * k];
+    b += buf[3 + 2 * k];
+  }
+  buf[0] = b > 0.0 ? sqrt(a / b) : 0.0;
+}
+
+int launch_rel_change(const float* X, float* Xprev, int64_t n, double* buf, cudaStream_t st) {
+  if (reinterpret_cast<uintptr_t>(X) % 16 != 0 || reinterpret_cast<uintptr_t>(Xprev) % 16 != 0)
+    return fail(MLF_ERR_INVALID, "relative change: volume buffers must be 16-byte aligned");
+  k_rel_change_partial<<<kRelChangeBlocks, 256, 0, st>>>(X, Xprev, n, buf);
+  k_rel_change_final<<<1, 32, 0, st>>>(buf, kRelChangeBlocks);
+  MLF_LAUNCHED();
+  return MLF_OK;
+}
+
+int rel_change_read(const double* buf, double* out) {
+  MLF_CUDA(cudaMemcpy(out, buf, sizeof(double), cudaMemcpyDeviceToHost));
+  return MLF_OK;
+}
+
 int launch_init_flat(const float* d_lf, const PatchGeo& g, float* X, double* scratch, cudaStream_t st) {
   const int nb = 256;
   k_sum_partial<<<nb, 256, 0, st>>>(d_lf, g.Xr * g.Xc, scratch);
@@ -585,7 +656,20 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     MLF_TRY(launch_init_flat(d_lf, g, s->X.as<float>(), s->red.as<double>(), st));
     launches += 2;
   }
-  for (int it = 0; it < max_iter; ++it) MLF_TRY(enqueue_iteration(s, &launches, st));
+  const bool monitor = stats != nullptr && max_iter > 0;
+  if (monitor) {
+    if (!s->Xprev.p) MLF_TRY(s->Xprev.alloc(s->X.bytes, "convergence monitor volume"));
+    if (!s->relbuf.p) MLF_TRY(s->relbuf.alloc(kRelChangeBufDoubles * sizeof(double), "convergence monitor sums"));
+    MLF_CUDA(cudaMemcpyAsync(s->Xprev.p, s->X.p, s->X.bytes, cudaMemcpyDeviceToDevice, st));
+  }
+  for (int it = 0; it < max_iter; ++it) {
+    MLF_TRY(enqueue_iteration(s, &launches, st));
+    if (monitor) {
+      MLF_TRY(launch_rel_change(s->X.as<float>(), s->Xprev.as<float>(), (int64_t)(s->X.bytes / sizeof(float)),
+                                s->relbuf.as<double>(), st));
+      launches += 2;
+    }
+  }
   MLF_TRY(launch_from_phase(s->X.as<float>(), g, d_out, st));
   ++launches;
   if (stats) {
@@ -609,6 +693,8 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     stats->view_kernel_launches = s->tev_used / 2;
     stats->kernel_launches = launches;
     stats->fwd_splits = stats->fwd_stages = stats->bwd_xbufs = stats->tuned = 0;
+    stats->rel_change = 0.0;
+    if (monitor) MLF_TRY(rel_change_read(s->relbuf.as<double>(), &stats->rel_change));
   }
   s->timing = false;
   s->tev_used = 0;

@@ -891,6 +891,7 @@ struct TcSolverState {
   std::vector<int> views;   // union of the patches' active views, spiral order
   std::vector<float> wtab;  // [views][P]
   DevBuf X, lfs, rimg, tile_patch, pinfo, wtab_dev, wscratch, ar_hi, ar_lo, a1, ypart, err;
+  DevBuf Xprev, relbuf;  // convergence monitor (solves with stats only)
   CUtensorMap mARh, mARl, mA1, mXv;
   // One RL iteration (view loop + filters of every patch) as an instantiated CUDA graph,
   // per precision and with / without per-view timing nodes.  All buffers above are fixed
@@ -980,7 +981,7 @@ size_t tc_work_bytes(const TcSolverState* t) {
   if (!t) return 0;
   return t->X.bytes + t->lfs.bytes + t->rimg.bytes + t->tile_patch.bytes + t->pinfo.bytes + t->wtab_dev.bytes +
          t->wscratch.bytes + t->ar_hi.bytes + t->ar_lo.bytes + t->a1.bytes +
-         t->ypart.bytes + t->err.bytes;
+         t->ypart.bytes + t->err.bytes + t->Xprev.bytes + t->relbuf.bytes;
 }
 
 size_t tc_solver_bytes(const Solver* s) { return tc_work_bytes(s->tc); }
@@ -1003,7 +1004,9 @@ size_t tc_work_plan_bytes(const Psf* psf, const std::vector<int>& Li, const std:
   const int64_t P = (int64_t)Li.size();
   return (size_t)(psf->nch * MP * 4 + (int64_t)psf->N * psf->N * MP * 4 + MP * 4 + tiles * 4 + 8 * P * 4 +
                   (int64_t)psf->N * psf->N * P * 4 + P * 4 + 3 * MP * KB * 2 +
-                  (int64_t)splits * MP * NB * 4 + 4);
+                  (int64_t)splits * MP * NB * 4 + 4 +
+                  // convergence monitor, allocated by the first solve that asks for stats
+                  psf->nch * MP * 4 + (int64_t)kRelChangeBufDoubles * 8);
 }
 
 int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState** out, cudaStream_t st) {
@@ -1263,6 +1266,12 @@ int capture_iteration(const Psf* psf, TcSolverState* t, const std::vector<Solver
     rc = filter_run_geo(members[p], work_geo(t, members[p], p), t->X.as<float>() + t->pos0[p], st);
     launches += 5;
   }
+  // the instrumented variant (stats requested) also measures the iteration's relative change
+  if (rc == MLF_OK && timer->timing && t->Xprev.p) {
+    rc = launch_rel_change(t->X.as<float>(), t->Xprev.as<float>(), (int64_t)(t->X.bytes / sizeof(float)),
+                           t->relbuf.as<double>(), st);
+    launches += 2;
+  }
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(st, &g);
   if (rc != MLF_OK) {
@@ -1408,9 +1417,15 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
       launches += 3;
     }
   }
+  const bool monitor = stats != nullptr && max_iter > 0;
+  if (monitor) {  // before any capture: these allocate
+    if (!t->Xprev.p) MLF_TRY(t->Xprev.alloc(t->X.bytes, "convergence monitor volume"));
+    if (!t->relbuf.p) MLF_TRY(t->relbuf.alloc(kRelChangeBufDoubles * sizeof(double), "convergence monitor sums"));
+  }
   if (max_iter > 0) {
     MLF_TRY(tc_autotune(psf, t, precision, st));  // first solve at this precision only
     tc_apply_tune(t, precision);
+    if (monitor) MLF_CUDA(cudaMemcpyAsync(t->Xprev.p, t->X.p, t->X.bytes, cudaMemcpyDeviceToDevice, st));
     TcSolverState::Iteration& g = t->iter[precision & 3][timer->timing ? 1 : 0];
     if (!g.exec) {
       timer->tev_used = 0;
@@ -1450,6 +1465,8 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
     stats->fwd_stages = t->fwd_stages;
     stats->bwd_xbufs = t->xbufs ? t->xbufs : (t->dtab_ok ? 2 : 1);
     stats->tuned = t->tune[precision & 3].tuned;
+    stats->rel_change = 0.0;
+    if (monitor) MLF_TRY(rel_change_read(t->relbuf.as<double>(), &stats->rel_change));
     MLF_TRY(tc_check_error(t));
   }
   timer->timing = false;

@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol(lib):
     for name in header_functions():
         assert hasattr(lib, name), name
         assert name in _lib.SIGNATURES, f"{name} missing from the ctypes signature table"
-    assert lib.mlf_version() == 2
+    assert lib.mlf_version() == 3
 
 
 def _err(lib):
@@ -74,3 +74,26 @@ def test_python_api_no_cpu_fallback():
     with pytest.raises(MesoLFError):
         recon_theory_phase_space_LFM_with_filter(np.zeros((15, 15)), np.zeros((15, 15, 15, 15, 1)),
                                                  np.zeros((15, 15, 15, 15, 1)), 1, gpuFlag=False)
+
+
+def test_stats_struct_layout_matches_the_header(tmp_path):
+    """The ctypes mirror of mlf_stats has the size and field offsets the C compiler gives
+    the header's struct (a mismatch would make the library write past the caller's struct)."""
+    import shutil
+    import subprocess
+    from mesolf_gb300._lib import MLFStats
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    inc = os.path.join(ROOT, "include")
+    fields = [f for f, _ in MLFStats._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"mesolf_lf.h\"\nint main(void){\n"
+                   "printf(\"%zu\\n\", sizeof(mlf_stats));\n" +
+                   "".join(f"printf(\"%zu\\n\", offsetof(mlf_stats, {f}));\n" for f in fields) +
+                   "return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert out[0] == ctypes.sizeof(MLFStats)
+    assert out[1:] == [getattr(MLFStats, f).offset for f in fields]
