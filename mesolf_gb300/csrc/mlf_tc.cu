@@ -382,7 +382,10 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
         set_abort(&abort_flag);
         break;
       }
-      const int pz0 = __ldg(pi + 4), pnz = __ldg(pi + 5);
+      // channels are plane-major (ch = z*NN + ...): the patch's planes [z0, z0+nz) are the
+      // channel range [z0*NN, (z0+nz)*NN), cut at the real channel count
+      const int ch_lo = __ldg(pi + 4) * a.NN;
+      const unsigned ch_n = (unsigned)(min(a.nch, (__ldg(pi + 4) + __ldg(pi + 5)) * a.NN) - ch_lo);
       const float wv = __ldg(a.wrow + pp);
       const uint32_t tC = tmem_base + buf * 256 + lane_off, tD = tC + 128;
 #pragma unroll
@@ -404,12 +407,11 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           float* xp = xh + ((sub * 2 + cc) * 16 + j) * BM + row;
-          const int zr = (chb + j) / a.NN - pz0;
-          if (pos_ok && chb + j < a.nch && zr >= 0 && zr < pnz) {
+          if (pos_ok && (unsigned)(chb + j - ch_lo) < ch_n) {
             const float xo = *xp;
             float xc = __fdividef(xo * cv[j], dv[j] + a.d_eps);   // :130  X .* C ./ D
             if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;       // :132-134
-            float xn = xc * wv + (1.f - wv) * xo;          // :136
+            float xn = __fmaf_rn(xc, wv, __fmul_rn(1.f - wv, xo));  // :136
             if (xn < 0.f) xn = 0.f;                        // :137
             *xp = xn;
           }
