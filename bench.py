@@ -13,6 +13,17 @@ Multi-GPU: patches are independent (replicas); each rank solves its own patch, n
 collective on the data path; value = all ranks' voxels / max rank time.
 The reference arm (--impl reference) times the CPU restatement of the reference's
 algorithm (the oracle port; the MATLAB original cannot run here) on the host cores.
+
+At N = 1 the line also carries: `roofline` (the fused view kernel against the FP32 FMA rate
+measured live), `clocks`, `convergence` (the last iteration's FP64 relative change),
+`mixed` (the same workload on the tensor cores, bf16x2, timed on iteration graphs without
+timing nodes; its kernel times come from one instrumented solve after the timed region),
+`precision_vs_fp64_oracle`, `serving` (36-patch carpet at 18 Hz), `batched` (64 uneven
+patches), `mex_projector`, `seed_library`, `summary_image`, `rectification` and
+`cpu_baseline`.
+
+    python bench.py --profile --iters 1 [--planes P] [--precision bf16x2]   # one solve, for ncu
+    python bench.py --only summary|rectify --frames F                      # one block, for ncu
 """
 from __future__ import annotations
 
