@@ -79,6 +79,13 @@ int mlf_version(void);
  * reference. */
 int mlf_probe_fp32_peak(double ms, double* tflops, void* stream);
 
+/* Failure-detection check: one thread waits, with the bounded mbarrier wait every
+ * tensor-core kernel uses, on a barrier that nothing arrives at, for `limit` polls
+ * (1..2^20, ~64 ns apart).  The wait gives up, the kernel records the timeout and returns,
+ * and this returns MLF_ERR_TIMEOUT with the context still usable.  No counterpart in the
+ * reference. */
+int mlf_probe_wait_timeout(uint32_t limit, void* stream);
+
 /* Copy the calling thread's last error message into buf (always NUL-terminated).
  * Returns the status code of that error. */
 int mlf_last_error(char* buf, size_t len);

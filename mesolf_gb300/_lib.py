@@ -31,6 +31,7 @@ _i64 = ctypes.c_int64
 SIGNATURES = {
     "mlf_version": (ctypes.c_int, []),
     "mlf_probe_fp32_peak": (ctypes.c_int, [ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]),
+    "mlf_probe_wait_timeout": (ctypes.c_int, [ctypes.c_uint32, _vp]),
     "mlf_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "mlf_conv_vec": (ctypes.c_int, [_vp, _i64, _i64, _i64, _vp, _i64, _i32, _vp, _vp]),
     "mlf_conv_vec_ex": (ctypes.c_int, [_vp, _i64, _i64, _i64, _vp, _i64, _i32, _vp, _i32, _vp]),

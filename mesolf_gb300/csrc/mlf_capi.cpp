@@ -6,6 +6,7 @@
 // per-thread message instead of aborting.  Pointers may be device or host memory: host
 // arrays are staged through device buffers owned by the call or the solver.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cmath>
 #include <cstring>
@@ -16,6 +17,15 @@
 #include "mlf_internal.h"
 
 namespace mlf {
+
+namespace {
+// NVTX range for the duration of an entry point (visible to nsys / ncu --nvtx; a no-op
+// when no tool is attached).
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
+}  // namespace
 
 namespace {
 thread_local int g_code = MLF_OK;
@@ -207,6 +217,7 @@ int mlf_conv_vec(const float* bitmap, int64_t W, int64_t H, int64_t n, const flo
 
 int mlf_conv_vec_ex(const float* bitmap, int64_t W, int64_t H, int64_t n, const float* kernels,
                     int64_t kw, int32_t nnum, float* out, int32_t method, void* stream) {
+  mlf::Range nvtx_range("mlf_conv_vec_ex");
   clear_error();
   if (method != MLF_CONV_AUTO && method != MLF_CONV_DIRECT && method != MLF_CONV_TENSOR)
     return fail(MLF_ERR_INVALID, "mlf_conv_vec_ex: unknown method");
@@ -252,6 +263,7 @@ int mlf_summary_image(const float* movie, int64_t P, int64_t T, int32_t mode, in
 int mlf_summary_image_ex(const float* movie, int64_t P, int64_t T, int32_t mode, int32_t bg_iter,
                          int32_t window_1, int32_t window_2, int32_t poly_index, float* summary_out,
                          float* bg_spatial_out, float* bg_temporal_out, double* pass_ms, void* stream) {
+  mlf::Range nvtx_range("mlf_summary_image_ex");
   clear_error();
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (!movie || !summary_out) return fail(MLF_ERR_INVALID, "mlf_summary_image: null pointer");
@@ -297,6 +309,7 @@ int mlf_rectify_frames(const void* frames, int32_t dtype, int64_t H, int64_t W, 
                        double frames_dx, int64_t size_h, int64_t size_w, int64_t frames_start, int64_t frames_step,
                        int64_t frames_end, int32_t frames_average, int32_t normalize, float* movie_out,
                        int64_t* n_out, void* stream) {
+  mlf::Range nvtx_range("mlf_rectify_frames");
   clear_error();
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (!frames || !raw_cut || !movie_out) return fail(MLF_ERR_INVALID, "mlf_rectify_frames: null pointer");
@@ -348,6 +361,7 @@ int mlf_rectify_frames(const void* frames, int32_t dtype, int64_t H, int64_t W, 
 int mlf_conv_vec_accumulate(const float* bitmaps, int64_t W, int64_t H, int64_t n, const int32_t* plane,
                             const int32_t* slot, int64_t n_out, const float* kernels, int64_t kw, int32_t nnum,
                             int64_t Z, float* out, void* stream) {
+  mlf::Range nvtx_range("mlf_conv_vec_accumulate");
   clear_error();
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (!bitmaps || !plane || !slot || !kernels || !out) return fail(MLF_ERR_INVALID, "mlf_conv_vec_accumulate: null pointer");
@@ -445,6 +459,7 @@ int mlf_conv_vec_accumulate(const float* bitmaps, int64_t W, int64_t H, int64_t 
 
 int mlf_psf_create(const float* H, const float* Ht, int64_t K0, int32_t N, int64_t Z, mlf_psf** out,
                    void* stream) {
+  mlf::Range nvtx_range("mlf_psf_create");
   clear_error();
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (!H || !Ht || !out) return fail(MLF_ERR_INVALID, "mlf_psf_create: null pointer");
@@ -536,6 +551,7 @@ int mlf_solver_create_variant(mlf_psf* psf, int64_t Xr, int64_t Xc, int32_t vari
 
 int mlf_solver_run_peeling(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t precision, float* vol_out,
                            float* lf_peeled_out, float* proj_sensor_out, mlf_stats* stats, void* stream) {
+  mlf::Range nvtx_range("mlf_solver_run_peeling");
   clear_error();
   if (!s || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: null pointer");
   if (max_iter < 0) return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: maxIter must be >= 0");
@@ -557,6 +573,7 @@ int64_t mlf_solver_device_bytes(const mlf_solver* s) { return s ? (int64_t)s->by
 
 int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t precision,
                    const float* warm_start, float* vol_out, mlf_stats* stats, void* stream) {
+  mlf::Range nvtx_range("mlf_solver_run");
   clear_error();
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (!s || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_solver_run: null pointer");
@@ -650,6 +667,7 @@ int64_t mlf_batch_device_bytes(const mlf_batch* b) {
 
 int mlf_batch_run(mlf_batch* b, const float* const* lfimg, int32_t max_iter, int32_t precision,
                   const float* const* warm, float* const* vol_out, mlf_stats* stats, void* stream) {
+  mlf::Range nvtx_range("mlf_batch_run");
   clear_error();
   if (!b || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_batch_run: null pointer");
   if (max_iter < 0) return fail(MLF_ERR_INVALID, "mlf_batch_run: maxIter must be >= 0");
@@ -675,6 +693,7 @@ int mlf_batch_run(mlf_batch* b, const float* const* lfimg, int32_t max_iter, int
 int mlf_rl_solve(const float* lfimg, int64_t Xr, int64_t Xc, const float* H, const float* Ht,
                  int64_t K0, int32_t N, int64_t Z, int32_t max_iter, int32_t precision, float* vol_out,
                  mlf_stats* stats, void* stream) {
+  mlf::Range nvtx_range("mlf_rl_solve");
   mlf_psf* psf = nullptr;
   MLF_TRY(mlf_psf_create(H, Ht, K0, N, Z, &psf, stream));
   std::unique_ptr<mlf_psf> guard(psf);
@@ -729,6 +748,7 @@ int mlf_forward_view_prec(mlf_solver* s, const float* vol, int32_t u, int32_t v,
 
 int mlf_forward_project(mlf_solver* s, const float* vol, float* lf_out, int32_t raw_psf, int32_t precision,
                         void* stream) {
+  mlf::Range nvtx_range("mlf_forward_project");
   clear_error();
   if (!s || !vol || !lf_out) return fail(MLF_ERR_INVALID, "mlf_forward_project: null pointer");
   if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2) return fail(MLF_ERR_INVALID, "mlf_forward_project: unknown precision");
@@ -739,6 +759,7 @@ int mlf_forward_project(mlf_solver* s, const float* vol, float* lf_out, int32_t 
 
 int mlf_batch_forward_project(mlf_batch* b, const float* const* vols, float* const* lf_out, int32_t raw_psf,
                               int32_t precision, void* stream) {
+  mlf::Range nvtx_range("mlf_batch_forward_project");
   clear_error();
   if (!b || !vols || !lf_out) return fail(MLF_ERR_INVALID, "mlf_batch_forward_project: null pointer");
   if (precision != MLF_PREC_BF16 && precision != MLF_PREC_BF16X2 && precision != MLF_PREC_BF16X3)

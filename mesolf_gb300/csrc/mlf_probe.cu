@@ -4,6 +4,7 @@
 // loop) sized to fill every SM; the rate it reaches under the current clocks is the
 // denominator used for the plain FP32 projector's roofline fraction.
 #include "mlf_internal.h"
+#include "mlf_tc.cuh"
 
 namespace mlf {
 namespace {
@@ -22,8 +23,36 @@ __global__ void __launch_bounds__(256) k_fma_probe(float* sink, int iters, float
   if (r == 123.456f) sink[blockIdx.x] = r;  // keeps the chains alive
 }
 
+// One thread waits, with the same bounded mbarrier wait the tensor-core kernels use, on a
+// barrier that nothing arrives at; when the wait gives up it records the timeout in
+// `status` and the kernel returns normally.
+__global__ void k_wait_probe(int* status, uint32_t limit) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  tc::mbar_init(&bar, 1);
+  tc::fence_mbar_init();
+  *status = tc::mbar_wait(&bar, 0, limit) ? 0 : 1;
+}
+
 }  // namespace
 }  // namespace mlf
+
+extern "C" int mlf_probe_wait_timeout(uint32_t limit, void* stream) {
+  using namespace mlf;
+  clear_error();
+  if (limit == 0 || limit > (1u << 20)) return fail(MLF_ERR_INVALID, "mlf_probe_wait_timeout: limit outside [1, 2^20]");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  DevBuf status;
+  MLF_TRY(status.alloc(sizeof(int), "wait probe status"));
+  MLF_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+  k_wait_probe<<<1, 32, 0, st>>>(status.as<int>(), limit);
+  MLF_LAUNCHED();
+  int h = 0;
+  MLF_CUDA(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MLF_CUDA(cudaStreamSynchronize(st));
+  if (h) return fail(MLF_ERR_TIMEOUT, "mlf_probe_wait_timeout: the bounded wait expired (as intended)");
+  return MLF_OK;
+}
 
 extern "C" int mlf_probe_fp32_peak(double ms, double* tflops, void* stream) {
   using namespace mlf;

@@ -7,6 +7,7 @@
 // one launch of the partial-sum reduction that forms the next ratio image.  The
 // mixed-precision (tensor-core) forms are in mlf_tc.cu; this file keeps the layout
 // kernels, which take a PatchGeo so they also serve the patches of a batch.
+#include <nvtx3/nvToolsExt.h>
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -663,7 +664,10 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     MLF_CUDA(cudaMemcpyAsync(s->Xprev.p, s->X.p, s->X.bytes, cudaMemcpyDeviceToDevice, st));
   }
   for (int it = 0; it < max_iter; ++it) {
-    MLF_TRY(enqueue_iteration(s, &launches, st));
+    nvtxRangePushA("RL iteration (enqueue)");
+    const int rc_it = enqueue_iteration(s, &launches, st);
+    nvtxRangePop();
+    MLF_TRY(rc_it);
     if (monitor) {
       MLF_TRY(launch_rel_change(s->X.as<float>(), s->Xprev.as<float>(), (int64_t)(s->X.bytes / sizeof(float)),
                                 s->relbuf.as<double>(), st));

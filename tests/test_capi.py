@@ -97,3 +97,9 @@ def test_stats_struct_layout_matches_the_header(tmp_path):
     out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert out[0] == ctypes.sizeof(MLFStats)
     assert out[1:] == [getattr(MLFStats, f).offset for f in fields]
+
+
+def test_wait_probe_rejects_limits_before_any_device_work(lib):
+    from mesolf_gb300 import _lib
+    assert lib.mlf_probe_wait_timeout(0, None) == _lib.MLF_ERR_INVALID
+    assert lib.mlf_probe_wait_timeout((1 << 20) + 1, None) == _lib.MLF_ERR_INVALID
