@@ -33,9 +33,9 @@ struct FGeo {
   int Z;
 };
 
-// Phase-major -> MATLAB layout for one line (c, z) of length Xr = N*Li:
-// line[N*a + alpha] = X[ch(alpha, beta, z)][b][a], beta = c mod N, b = c / N.  `f(i, off)` is
-// called for i in [0, Xr) with the X offset of element i's source, i = alpha*Li + a, so that
+// Offset in the phase-major volume X of the source of line (c, z) of the MATLAB layout
+// (length Xr = N*Li), element i enumerated as i = alpha*Li + a: that element is
+// line[N*a + alpha] = X[ch(alpha, beta, z)][b][a], beta = c mod N, b = c / N, so that
 // consecutive i read consecutive floats of one channel row.
 __device__ __forceinline__ int64_t line_src(const PatchGeo& g, int c, int z, int i) {
   const int alpha = i / g.Li, a = i - alpha * g.Li;
