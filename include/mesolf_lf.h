@@ -305,10 +305,14 @@ int mlf_sample_filter(mlf_solver* s, float* vol, void* stream);
  *   hx (dev, Xr/N x Xc/N) = (sum_z conv2(vol_z, Hps(:,:,u,v,z), 'same'))((N+1)/2:N:end, ...)
  * for vol (dev, Xr x Xc x Z, MATLAB layout), with the PSF's resident taps.
  * Scratch: a static device array of 2 Mi floats (8 MiB) that every GPU loading the
- * library holds until exit; (Xr/N)*(Xc/N) must not exceed it (MLF_ERR_INVALID otherwise).
- * The first call on a device looks the array up with that device current: make it before
- * any stream capture.  Calls share the array, so calls whose kernels overlap on the GPU
- * (other streams or threads) race and must be serialised by the caller. */
+ * library holds until exit.  Limit: one CTA covers the whole lenslet grid in 4 x 8 tiles,
+ * so ceil((Xr/N)/4) * ceil((Xc/N)/8) must not exceed 256 (e.g. 67 x 67 lenslets: 17 * 9 =
+ * 153; 64 x 128 at most) -- MLF_ERR_UNSUPPORTED otherwise.  The array's address is looked
+ * up on every call with the caller's device current (a reset device may place it
+ * elsewhere); the first call on a device, and the first after a cudaDeviceReset, loads the
+ * library's device code: make it before any stream capture.  Calls share the array, so
+ * calls whose kernels overlap on the GPU (other streams or threads) race and must be
+ * serialised by the caller. */
 int mlf_forward_view_static(const mlf_psf* psf, const float* vol, int64_t Xr, int64_t Xc, int32_t u,
                             int32_t v, float* hx, void* stream);
 

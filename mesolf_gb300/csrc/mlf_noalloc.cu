@@ -11,17 +11,25 @@
 // This variant reads the volume in its MATLAB layout directly (no phase-major copy) and
 // keeps the per-CTA partial sums in a file-scope static device array,
 // g_static_partials, of kStaticPartialFloats floats (8 MiB).  Every GPU that loads this
-// library holds that array until the process exits.  Its device address is looked up
-// once per device with cudaGetSymbolAddress on the first call made with that device
-// current, so the first call on a device must come before any stream capture.  All calls
-// on a device share the one array: every CTA overwrites the whole partial plane it owns
-// before the reduction reads it, so no clearing is needed, but two calls whose kernels
-// overlap on the GPU (different streams, or different host threads) race on the array
-// and must be serialised by the caller.
+// library holds that array until the process exits.  Its device address is looked up with
+// cudaGetSymbolAddress on every call, with the caller's device current: the lookup
+// allocates nothing, and a cached address would go stale when the caller resets the device
+// (MATLAB's reset(gpuDevice) runs cudaDeviceReset; the next context loads the module again,
+// possibly at another address).  The first call on a device, and the first after a reset,
+// makes the runtime load this library's device code, so it must come before any stream
+// capture.  All calls on a device share the one array: every CTA overwrites the whole
+// partial plane it owns before the reduction reads it, so no clearing is needed, but two
+// calls whose kernels overlap on the GPU (different streams, or different host threads)
+// race on the array and must be serialised by the caller.
+//
+// The projection itself is the MODE_FWD correlation of k_view (mlf_view.cuh), restaged:
+// the plane is gathered from the MATLAB-layout volume and the taps have pitch T.  A change
+// to k_view's tile geometry (VT_TX x VT_TY tiles, view_nw, view_qpad, conv_tile) must be
+// carried into k_fwd_static; tests/test_zz_no_alloc.py compares the two on every tap count
+// it covers.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
 
 #include "mlf_view.cuh"
 
@@ -33,23 +41,13 @@ namespace {
 constexpr int64_t kStaticPartialFloats = int64_t(2) << 20;  // 2 Mi floats = 8 MiB
 static __device__ __align__(256) float g_static_partials[kStaticPartialFloats];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-float* g_partials_addr[kMaxDevices] = {};
-
-// Device address of g_static_partials for device `dev` (must be current).
-int static_partials(int dev, float** out) {
-  if (dev < 0 || dev >= kMaxDevices) return fail(MLF_ERR_UNSUPPORTED, "device index out of range");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_partials_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_static_partials);
-    if (e != cudaSuccess || p == nullptr)
-      return fail(MLF_ERR_CUDA, std::string("cudaGetSymbolAddress(g_static_partials): ") +
-                                    cudaGetErrorString(e));
-    g_partials_addr[dev] = static_cast<float*>(p);
-  }
-  *out = g_partials_addr[dev];
+// Device address of g_static_partials in the current context.
+int static_partials(float** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_static_partials);
+  if (e != cudaSuccess || p == nullptr)
+    return fail(MLF_ERR_CUDA, std::string("cudaGetSymbolAddress(g_static_partials): ") + cudaGetErrorString(e));
+  *out = static_cast<float*>(p);
   return MLF_OK;
 }
 
@@ -191,7 +189,9 @@ extern "C" int mlf_forward_view_static(const mlf_psf* psf_handle, const float* v
   a.tilesB = (Lj + 7) / 8;
   a.tps = a.tilesA * a.tilesB;
   if (a.tps > 256)
-    return fail(MLF_ERR_UNSUPPORTED, "mlf_forward_view_static: lenslet grid larger than the per-CTA tile limit");
+    return fail(MLF_ERR_UNSUPPORTED, "mlf_forward_view_static: " + std::to_string(Li) + " x " + std::to_string(Lj) +
+                                         " lenslets need ceil(Li/4)*ceil(Lj/8) = " + std::to_string(a.tps) +
+                                         " tiles per CTA; the limit is 256");
   const int NW = view_nw(T);
   a.XP = ((4 * (a.tilesA - 1) + 4 * NW) + 3) / 4 * 4;
   a.XProws = a.tilesB * 8 + T - 1;
@@ -200,7 +200,7 @@ extern "C" int mlf_forward_view_static(const mlf_psf* psf_handle, const float* v
   const int threads = (a.slots * a.tps + 31) / 32 * 32;
   const size_t smem = sizeof(float) * (size_t)a.slots * std::max<int64_t>(a.slot_floats, LL);
   if ((int)smem > dev_smem) return fail(MLF_ERR_UNSUPPORTED, "mlf_forward_view_static: shared memory limit");
-  MLF_TRY(static_partials(dev, &a.part));
+  MLF_TRY(static_partials(&a.part));
   const int max_grid = (int)(kStaticPartialFloats / LL);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int grid = 0;

@@ -571,6 +571,39 @@ def lfm_conv_vec(bitmap, kernels):
     return out[:, :, 0] if squeeze else out
 
 
+def mex_slot_overlap_kernels(kernels):
+    """The kernel set the reference MEX kernel computes with when, on every kernel row, its
+    out-of-range fill group wins the shared-memory race (``src/cuda/mex_lfm_convolution_vec.cu``
+    ``:114-117,130,139-141,161-182``).
+
+    Each row the 1024 threads copy one row of all 15 kernels of the output row's phase into
+    15 shared slots of ``kw`` floats; thread group ``g = t // 15`` copies elements
+    ``[kw*g//68, kw*(g+1)//68)`` of slot ``t % 15``.  Group 68 (threads 1020-1023, slots 0-3)
+    gets ``[kw, kw + kw//68)``: it writes the first ``kw//68`` elements of the NEXT slot with
+    the next row's first elements of its own kernel, while group 0 writes the same cells of
+    slots 1-4 with their proper values, with no barrier between the two.  So for
+    ``a = x mod 15`` in 1..4 and ``kx < kw//68`` the tap used is either ``K(kx, ky, a, b)``
+    or, if group 68 stored last, flat element ``kw*kw*(a-1 + 15 b) + kw*(ky+1) + kx`` of the
+    kernel array (``K(kx, ky+1, a-1, b)``; for the last row the next kernel's first row).
+    This returns the kernel set of the second outcome for every row; ``lfm_conv_vec`` with
+    it gives that outcome's output.  For ``kw < 68`` nothing overlaps and the set is
+    ``kernels`` itself."""
+    K = np.asarray(kernels)
+    kw = K.shape[0]
+    nover = kw // 68
+    out = K.copy()
+    if nover == 0:
+        return out
+    flat = np.asfortranarray(K).reshape(-1, order="F")
+    for b in range(K.shape[3]):
+        for a in range(1, 5):
+            base = kw * kw * (a - 1 + K.shape[2] * b)
+            for ky in range(kw):
+                for kx in range(nover):
+                    out[kx, ky, a, b] = flat[base + kw * (ky + 1) + kx]
+    return out
+
+
 def lfm_conv_vec_points(bitmap, kernels, pts):
     """``lfm_conv_vec`` evaluated only at the (x, y, i) triples ``pts`` -- for large
     shapes where the full FP64 evaluation is too slow."""
