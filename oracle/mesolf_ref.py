@@ -19,11 +19,14 @@ followed by lenslet sampling, sparse up-sampling followed by ``conv2 'same'``), 
 the polyphase form that the CUDA kernels use, so the kernels' index algebra is checked
 independently.
 
-PARITY UNPINNED: the reference ships no golden vectors or known-answer tests for this
-path, and neither MATLAB nor its CUDA MEX (legacy texture references) can run here.
-The oracle is pinned instead by self-consistency checks (FFT path == direct path,
-literal MATLAB-semantics transcription == closed form, adjointness, flux conservation)
-and by committed golden vectors generated from it.
+PARITY: the MEX projector's semantics (``lfm_conv_vec``) are pinned to the reference's own
+kernel: ``oracle/refbuild.py`` compiles ``src/cuda/mex_lfm_convolution_vec.cu`` unchanged
+(texture fetches stood in for by plain loads) and ``tests/test_gpu_ref_mex.py`` runs it on
+the reference's own input fixture.  The RL loop and the other MATLAB functions are
+PARITY UNPINNED: the reference ships no golden vectors or known-answer tests for them, and
+MATLAB/Octave cannot run here.  They are pinned by self-consistency checks (FFT path ==
+direct path, literal MATLAB-semantics transcription == closed form, adjointness, flux
+conservation) and by committed golden vectors generated from this oracle.
 
 Arrays use MATLAB index order: ``LFIMG[r, c]``, ``X[r, c, z]``, ``H[x, y, a, b, z]``.
 All indices in this file are 0-based unless a comment says "1-based".
@@ -178,9 +181,38 @@ def phasespace_view(H, Ht, u, v):
 # ----------------------------------------------------------------------------- a4
 def view_weights(Hps):
     """View weights, ``recon_theory_phase_space_LFM_with_filter.m:20,30-38``."""
+    return view_weights_from_sums(Hps.sum(axis=(0, 1, 4)))        # :30 sum over x, y, z
+
+
+def view_sums(H):
+    """Per-view sums of ``Hps`` over x, y and z (the input of ``:31-38``) for the per-depth
+    normalised ``H`` of ``:13-16``, computed from the raw ``H`` without building ``Hps``: the
+    closed form of :func:`gen_phasespace_psf` puts ``H[r, c, a, b, z]`` at view ``(u, v)``
+    exactly when ``r = i1 + p + u - h`` for a ``p`` in ``[0, S)`` with ``p mod N = N-1-a``
+    and ``p + u - h`` in ``[0, S)`` (likewise ``c``), so each sum is a masked sum of the raw
+    planes divided by the plane's total.  Equals ``Hps.sum(axis=(0, 1, 4))``."""
+    K0, N, Z = H.shape[0], H.shape[2], H.shape[4]
+    S, i1 = phase_space_size(K0, N)
+    h = (N - 1) // 2
+    mask = np.zeros((N, K0, N))                  # mask[u, r, a]
+    for u in range(N):
+        for p in range(S):
+            if 0 <= p + u - h < S:
+                mask[u, i1 + p + u - h, N - 1 - (p % N)] = 1.0
+    out = np.zeros((N, N))
+    for z in range(Z):
+        Hz = np.asarray(H[:, :, :, :, z], dtype=np.float64)                 # (r, c, a, b)
+        tot = Hz.sum()
+        rows = np.einsum("ura,rcab->ucb", mask, Hz, optimize=True)         # (u, c, b)
+        out += np.einsum("ucb,vcb->uv", rows, mask, optimize=True) / tot
+    return out
+
+
+def view_weights_from_sums(sums):
+    """``:31-38`` applied to the per-view sums of ``Hps`` over x, y and z."""
     weight_cut = 0.2
     with np.errstate(invalid="ignore", divide="ignore"):
-        w = Hps.sum(axis=(0, 1, 4))                      # :30 sum over x, y, z
+        w = np.array(sums, dtype=np.float64)
         w[np.isnan(w)] = 0                               # :31
         w = w / w.sum()                                  # :32
         w = w - w.min()                                  # :33
