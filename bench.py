@@ -760,7 +760,7 @@ def precision_block(psf, dev):
     s = RLSolver(psf, g["lf"].shape)
     lf = _fortran(torch.as_tensor(g["lf"].astype(np.float32)).to(dev))[0]
     rows = []
-    for prec in ("fp32", "bf16x3", "bf16x2", "bf16"):
+    for prec in ("fp32", "bf16x3", "fp16x3", "bf16x2", "fp16x2", "bf16", "fp16"):
         for it in (3, 10):
             if f"x{it}" not in g:
                 continue

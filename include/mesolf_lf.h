@@ -42,8 +42,17 @@ enum mlf_precision {
   MLF_PREC_FP32 = 0,       /* plain FP32 FMA projector (the drop-in path) */
   MLF_PREC_BF16X3 = 1,     /* tensor cores: taps and activations split hi+lo BF16 (3 passes) */
   MLF_PREC_BF16 = 2,       /* tensor cores: single BF16 operands (1 pass) */
-  MLF_PREC_BF16X2 = 3      /* tensor cores: activations split hi+lo, taps single BF16 (2 passes) */
-  /* all tensor-core modes accumulate in FP32; ratio, update, filter and sums stay FP32 */
+  MLF_PREC_BF16X2 = 3,     /* tensor cores: activations split hi+lo, taps single BF16 (2 passes) */
+  MLF_PREC_FP16 = 4,       /* tensor cores: single FP16 operands (1 pass) */
+  MLF_PREC_FP16X2 = 5,     /* tensor cores: activations split hi+lo FP16, taps single FP16 (2 passes) */
+  MLF_PREC_FP16X3 = 6      /* tensor cores: taps and activations split hi+lo FP16 (3 passes) */
+  /* all tensor-core modes accumulate in FP32; ratio, update, filter and sums stay FP32.
+   * FP16 operands carry power-of-two scales so that FP16's range (6.1e-5 .. 65504) holds
+   * them: each back-projection tap row (view, channel) and each forward tap column (view,
+   * tap) is scaled to a maximum in [2^14, 2^15) on the device when the FP16 tables are
+   * built; the ratio image by its per-view maximum; the volume by a running maximum kept
+   * on the device (every back projection raises it).  Powers of two are exact, and the
+   * FP32 epilogues remove them (the tap-row scale cancels in C/D). */
 };
 
 typedef struct mlf_psf mlf_psf;       /* phase-space PSF resident in HBM */
@@ -234,7 +243,7 @@ int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t 
  * (per-depth normalisation makes a plane range a PSF of its own; the view weights are
  * recomputed for the range).  Each view step of all patches is one launch of the
  * tensor-core GEMMs over the concatenated lenslet positions; precision must be one of the
- * MLF_PREC_BF16* modes.  lfimg[k], warm[k] (warm may be NULL or hold NULLs) and vol_out[k]
+ * tensor-core modes (MLF_PREC_BF16*, MLF_PREC_FP16*).  lfimg[k], warm[k] (warm may be NULL or hold NULLs) and vol_out[k]
  * (Xr[k] x Xc[k] x nz[k]) are device pointers.  Synchronous when stats != NULL. */
 int mlf_batch_create(mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int64_t* Xc, const int32_t* z0,
                      const int32_t* nz, mlf_batch** out);
@@ -273,7 +282,7 @@ int mlf_backward_view(mlf_solver* s, const float* proj, int32_t u, int32_t v, fl
 int mlf_rl_view_step(mlf_solver* s, const float* lfimg, float* vol, int32_t u, int32_t v, double w,
                      void* stream);
 /* The same view step and forward projection at a given enum mlf_precision (the
- * tensor-core forms for MLF_PREC_BF16*). */
+ * tensor-core forms for MLF_PREC_BF16* and MLF_PREC_FP16*). */
 int mlf_rl_view_step_prec(mlf_solver* s, const float* lfimg, float* vol, int32_t u, int32_t v, double w,
                           int32_t precision, void* stream);
 int mlf_forward_view_prec(mlf_solver* s, const float* vol, int32_t u, int32_t v, int32_t precision,
@@ -290,7 +299,7 @@ int mlf_forward_view_prec(mlf_solver* s, const float* vol, int32_t u, int32_t v,
 int mlf_forward_project(mlf_solver* s, const float* vol, float* lf_out, int32_t raw_psf, int32_t precision,
                         void* stream);
 /* The same for every patch of a batch (vols[k]: Xr[k] x Xc[k] x nz[k], projected with
- * the PSF planes [z0[k], z0[k] + nz[k])), on the tensor cores (MLF_PREC_BF16*). */
+ * the PSF planes [z0[k], z0[k] + nz[k])), on the tensor cores (MLF_PREC_BF16*, MLF_PREC_FP16*). */
 int mlf_batch_forward_project(mlf_batch* b, const float* const* vols, float* const* lf_out, int32_t raw_psf,
                               int32_t precision, void* stream);
 /* The per-iteration flux-preserving NIP low-pass, sample_filter (recon_…_with_filter.m:222-240,

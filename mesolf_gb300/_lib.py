@@ -19,6 +19,9 @@ MLF_PREC_FP32 = 0
 MLF_PREC_BF16X3 = 1
 MLF_PREC_BF16 = 2
 MLF_PREC_BF16X2 = 3
+MLF_PREC_FP16 = 4
+MLF_PREC_FP16X2 = 5
+MLF_PREC_FP16X3 = 6
 MLF_DETREND_PIXELWISE = 0
 MLF_DETREND_GLOBAL = 1
 MLF_DTYPE_F32 = 0

@@ -28,7 +28,8 @@ from ._lib import MLFStats, check
 from .rectify import determine_patch_info_aug, image_load_module_aug, img_rectify_mod  # noqa: F401
 
 PRECISIONS = {"fp32": _lib.MLF_PREC_FP32, "bf16x3": _lib.MLF_PREC_BF16X3, "bf16": _lib.MLF_PREC_BF16,
-              "bf16x2": _lib.MLF_PREC_BF16X2}
+              "bf16x2": _lib.MLF_PREC_BF16X2, "fp16": _lib.MLF_PREC_FP16, "fp16x2": _lib.MLF_PREC_FP16X2,
+              "fp16x3": _lib.MLF_PREC_FP16X3}
 
 
 def _is_torch(x):

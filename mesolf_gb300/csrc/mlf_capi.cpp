@@ -555,7 +555,7 @@ int mlf_solver_run_peeling(mlf_solver* s, const float* lfimg, int32_t max_iter, 
   clear_error();
   if (!s || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: null pointer");
   if (max_iter < 0) return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: maxIter must be >= 0");
-  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2)
+  if (!prec_valid(precision))
     return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: unknown precision");
   for (const void* p : {(const void*)lfimg, (const void*)vol_out, (const void*)lf_peeled_out, (const void*)proj_sensor_out})
     if (p && !is_device_ptr(p)) return fail(MLF_ERR_INVALID, "mlf_solver_run_peeling: device pointers required");
@@ -578,7 +578,7 @@ int mlf_solver_run(mlf_solver* s, const float* lfimg, int32_t max_iter, int32_t 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (!s || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_solver_run: null pointer");
   if (max_iter < 0) return fail(MLF_ERR_INVALID, "mlf_solver_run: maxIter must be >= 0");
-  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2)
+  if (!prec_valid(precision))
     return fail(MLF_ERR_INVALID, "mlf_solver_run: unknown precision");
   const size_t n_img = (size_t)(s->Xr * s->Xc), n_vol = n_img * s->Z;
   const float *dlf = nullptr, *dwarm = nullptr;
@@ -671,9 +671,9 @@ int mlf_batch_run(mlf_batch* b, const float* const* lfimg, int32_t max_iter, int
   clear_error();
   if (!b || !lfimg || !vol_out) return fail(MLF_ERR_INVALID, "mlf_batch_run: null pointer");
   if (max_iter < 0) return fail(MLF_ERR_INVALID, "mlf_batch_run: maxIter must be >= 0");
-  if (precision != MLF_PREC_BF16 && precision != MLF_PREC_BF16X2 && precision != MLF_PREC_BF16X3)
-    return fail(MLF_ERR_UNSUPPORTED, "mlf_batch_run: batches run on the tensor cores (MLF_PREC_BF16*); "
-                                     "use mlf_solver_run per patch for MLF_PREC_FP32");
+  if (!prec_tensor(precision))
+    return fail(MLF_ERR_UNSUPPORTED, "mlf_batch_run: batches run on the tensor cores (MLF_PREC_BF16* / "
+                                     "MLF_PREC_FP16*); use mlf_solver_run per patch for MLF_PREC_FP32");
   const size_t P = b->members.size();
   std::vector<const float*> lf(P), wm(P);
   std::vector<float*> out(P);
@@ -731,7 +731,7 @@ int mlf_rl_view_step_prec(mlf_solver* s, const float* lfimg, float* vol, int32_t
   clear_error();
   if (!s || !lfimg || !vol) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: null pointer");
   if (u < 0 || v < 0 || u >= s->N || v >= s->N) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: view out of range");
-  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: unknown precision");
+  if (!prec_valid(precision)) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: unknown precision");
   if (!is_device_ptr(lfimg) || !is_device_ptr(vol)) return fail(MLF_ERR_INVALID, "mlf_rl_view_step: device pointers required");
   return rl_view_step(s, lfimg, vol, u, v, w, precision, static_cast<cudaStream_t>(stream));
 }
@@ -741,7 +741,7 @@ int mlf_forward_view_prec(mlf_solver* s, const float* vol, int32_t u, int32_t v,
   clear_error();
   if (!s || !vol || !hx) return fail(MLF_ERR_INVALID, "mlf_forward_view_prec: null pointer");
   if (u < 0 || v < 0 || u >= s->N || v >= s->N) return fail(MLF_ERR_INVALID, "mlf_forward_view_prec: view out of range");
-  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2) return fail(MLF_ERR_INVALID, "mlf_forward_view_prec: unknown precision");
+  if (!prec_valid(precision)) return fail(MLF_ERR_INVALID, "mlf_forward_view_prec: unknown precision");
   if (!is_device_ptr(vol) || !is_device_ptr(hx)) return fail(MLF_ERR_INVALID, "mlf_forward_view_prec: device pointers required");
   return forward_view_prec(s, vol, u, v, precision, hx, static_cast<cudaStream_t>(stream));
 }
@@ -751,7 +751,7 @@ int mlf_forward_project(mlf_solver* s, const float* vol, float* lf_out, int32_t 
   mlf::Range nvtx_range("mlf_forward_project");
   clear_error();
   if (!s || !vol || !lf_out) return fail(MLF_ERR_INVALID, "mlf_forward_project: null pointer");
-  if (precision < MLF_PREC_FP32 || precision > MLF_PREC_BF16X2) return fail(MLF_ERR_INVALID, "mlf_forward_project: unknown precision");
+  if (!prec_valid(precision)) return fail(MLF_ERR_INVALID, "mlf_forward_project: unknown precision");
   if (!is_device_ptr(vol) || !is_device_ptr(lf_out)) return fail(MLF_ERR_INVALID, "mlf_forward_project: device pointers required");
   return forward_project(s, vol, lf_out, raw_psf ? s->psf->hsum_dev.as<float>() : nullptr, precision,
                          static_cast<cudaStream_t>(stream));
@@ -762,8 +762,9 @@ int mlf_batch_forward_project(mlf_batch* b, const float* const* vols, float* con
   mlf::Range nvtx_range("mlf_batch_forward_project");
   clear_error();
   if (!b || !vols || !lf_out) return fail(MLF_ERR_INVALID, "mlf_batch_forward_project: null pointer");
-  if (precision != MLF_PREC_BF16 && precision != MLF_PREC_BF16X2 && precision != MLF_PREC_BF16X3)
-    return fail(MLF_ERR_UNSUPPORTED, "mlf_batch_forward_project: batches run on the tensor cores (MLF_PREC_BF16*)");
+  if (!prec_tensor(precision))
+    return fail(MLF_ERR_UNSUPPORTED, "mlf_batch_forward_project: batches run on the tensor cores "
+                                     "(MLF_PREC_BF16* / MLF_PREC_FP16*)");
   const size_t P = b->members.size();
   std::vector<const float*> v(P);
   std::vector<float*> o(P);

@@ -33,6 +33,12 @@ void clear_error();
                                            cudaGetErrorString(e_));                              \
   } while (0)
 
+// precision modes (enum mlf_precision)
+inline bool prec_valid(int p) { return p >= MLF_PREC_FP32 && p <= MLF_PREC_FP16X3; }
+inline bool prec_tensor(int p) { return prec_valid(p) && p != MLF_PREC_FP32; }
+inline bool prec_f16(int p) { return p >= MLF_PREC_FP16 && p <= MLF_PREC_FP16X3; }
+constexpr int kPrecModes = MLF_PREC_FP16X3 + 1;
+
 #define MLF_TRY(call)             \
   do {                            \
     int st_ = (call);             \

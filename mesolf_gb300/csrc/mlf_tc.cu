@@ -37,6 +37,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <type_traits>
 #include <vector>
 
 #include "mlf_internal.h"
@@ -69,6 +70,33 @@ __device__ __forceinline__ void split_bf16(float x, bf16& hi, bf16& lo) {
   lo = __float2bfloat16_rn(x - __bfloat162float(hi));
 }
 
+// FP16 operands (MLF_PREC_FP16*): the same hi + lo split in FP16, applied to values that
+// carry a power-of-two scale putting their largest magnitude in [2^14, 2^15).
+using f16 = __half;
+__device__ __forceinline__ void split_f16(float x, f16& hi, f16& lo) {
+  hi = __float2half_rn(x);
+  lo = __float2half_rn(x - __half2float(hi));
+}
+__device__ __forceinline__ void split2(float x, bf16& hi, bf16& lo) { split_bf16(x, hi, lo); }
+__device__ __forceinline__ void split2(float x, f16& hi, f16& lo) { split_f16(x, hi, lo); }
+__device__ __forceinline__ float to_f32(bf16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ float to_f32(f16 v) { return __half2float(v); }
+
+// 2^k with m * 2^k in [2^14, 2^15) -- the scale that puts an FP16 operand's largest
+// magnitude m just below FP16's maximum (65504) -- or 1 for m = 0 or a non-finite m.
+__host__ __device__ inline float f16_scale(float m) {
+  if (!(m > 0.f) || !(m <= 3.0e38f)) return 1.f;
+  int e = 0;
+  frexpf(m, &e);  // m = f * 2^e, f in [0.5, 1)
+  int k = 15 - e;
+  k = k < -126 ? -126 : (k > 126 ? 126 : k);
+  return ldexpf(1.f, k);
+}
+// maximum of non-negative floats through their bit patterns (which order like unsigned ints)
+__device__ __forceinline__ void atomic_max_nonneg(float* addr, float v) {
+  atomicMax(reinterpret_cast<unsigned*>(addr), __float_as_uint(v));
+}
+
 // ------------------------------------------------------------------ back projection + update
 struct TcBwdArgs {
   int* err;
@@ -81,6 +109,11 @@ struct TcBwdArgs {
   float d_eps;                      // added to D (peeling variant)
   const float* dtab;                // D from class tables of the current view: [ncls][ncls][CHP]
   int q, ncls;                      // (T-1)/2 and 2q+3 classes per axis
+  // FP16 modes only (null otherwise)
+  const float* rmax;    // |R| maximum of this view: AR carries f16_scale(rmax), removed here
+  float* rmax_next;     // the next view's slot, reset to 0 here for its col2im
+  float* xmax;          // running maximum of X (the forward GEMM's scale), raised by the update
+  const float* bscale;  // scale of each tap row of this view [CHP] (to scale d_eps with D)
 };
 
 constexpr int BWD_BN = 128;                            // channels per tile
@@ -154,7 +187,8 @@ __device__ __forceinline__ int dtab_class(int i, int L, int q) {
 // class), then the table entries per (channel, class pair), written channel-contiguous.
 constexpr int DTAB_THREADS = 128;
 __host__ __device__ inline int dtab_ch_words(int T) { return ((T + 2) * (T + 2)) | 1; }
-__global__ void __launch_bounds__(DTAB_THREADS) k_tc_dtab(const bf16* __restrict__ hi, const bf16* __restrict__ lo,
+template <typename E>
+__global__ void __launch_bounds__(DTAB_THREADS) k_tc_dtab(const E* __restrict__ hi, const E* __restrict__ lo,
                                                           int CHP, int KB, int T, float* __restrict__ dtab) {
   extern __shared__ float dsh[];
   const int T2 = T + 2, q = (T - 1) / 2, nc = 2 * q + 3;
@@ -166,7 +200,7 @@ __global__ void __launch_bounds__(DTAB_THREADS) k_tc_dtab(const bf16* __restrict
   for (int e = threadIdx.x; e < 32 * T2 * T2; e += DTAB_THREADS) {
     const int c = e / (T2 * T2), k = e - c * (T2 * T2);
     const int64_t r = (row0 + c) * (int64_t)KB + k;
-    W[c * stride + k] = __bfloat162float(hi[r]) + (lo ? __bfloat162float(lo[r]) : 0.f);
+    W[c * stride + k] = to_f32(hi[r]) + (lo ? to_f32(lo[r]) : 0.f);
   }
   __syncthreads();
   for (int e = threadIdx.x; e < 32 * T2 * nc; e += DTAB_THREADS) {
@@ -218,7 +252,7 @@ __device__ __forceinline__ int bwd_next(const TcBwdArgs& a, int t, int total, in
 // of the next tile is in flight while the current one is computed.
 // Epilogue warp e (warp e+2) covers TMEM lanes 32*((e+2)%4).., channel half e/8 and the
 // 32-channel quarter ((e%8)/4).
-template <bool DGEMM, int XB>
+template <bool DGEMM, int XB, bool F16>
 __global__ void __launch_bounds__(BWD_THREADS, 1)
 k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
          const __grid_constant__ CUtensorMap mA1, const __grid_constant__ CUtensorMap mBh,
@@ -257,6 +291,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
     if (DGEMM) tc::tma_prefetch_desc(&mA1);
     tc::tma_prefetch_desc(&mBh);
     tc::tma_prefetch_desc(&mX);
+    if (F16 && blockIdx.x == 0) *a.rmax_next = 0.f;
   }
   if (warp == 1) tc::tmem_alloc(&tmem_base, 512);
   tc::tc_fence_before();
@@ -295,7 +330,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------- MMA issuer
-      const uint32_t idesc = tc::idesc_bf16_f32(BM, BWD_BN);
+      const uint32_t idesc = F16 ? tc::idesc_f16_f32(BM, BWD_BN) : tc::idesc_bf16_f32(BM, BWD_BN);
       int it = 0, ti = 0;
       for (int t = bwd_next(a, blockIdx.x, total, mtiles); t < total && !aborted(&abort_flag);
            t = bwd_next(a, t + gridDim.x, total, mtiles), ++ti) {
@@ -354,6 +389,9 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
     const int quad = warp & 3;                 // TMEM lanes 32*quad .. 32*quad+31
     const int row = quad * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    // FP16: C carries the ratio image's scale; 1/scale is a power of two (exact)
+    const float rinv = F16 ? 1.f / f16_scale(*a.rmax) : 1.f;
+    float xm = 0.f;  // FP16: largest updated value (for the running maximum of X)
     int ti = 0;
     for (int t = bwd_next(a, blockIdx.x, total, mtiles); t < total; t = bwd_next(a, t + gridDim.x, total, mtiles), ++ti) {
       const int buf = ti & 1;
@@ -387,6 +425,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       const int ch_lo = __ldg(pi + 4) * a.NN;
       const unsigned ch_n = (unsigned)(min(a.nch, (__ldg(pi + 4) + __ldg(pi + 5)) * a.NN) - ch_lo);
       const float wv = __ldg(a.wrow + pp);
+      const float wc = wv * rinv;  // weight of the X .* C ./ D term (== wv outside FP16 modes)
       const uint32_t tC = tmem_base + buf * 256 + lane_off, tD = tC + 128;
 #pragma unroll
       for (int cc = 0; cc < 2; ++cc) {
@@ -404,16 +443,22 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
           }
           tc::tmem_ld16(tC + c * 16, cv);
         }
+        // D of the FP16 modes carries the tap row's scale: d_eps is scaled with it
+        if (F16 && a.d_eps != 0.f) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) dv[j] += a.d_eps * __ldg(a.bscale + chb + j);
+        }
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           float* xp = xh + ((sub * 2 + cc) * 16 + j) * BM + row;
           if (pos_ok && (unsigned)(chb + j - ch_lo) < ch_n) {
             const float xo = *xp;
-            float xc = __fdividef(xo * cv[j], dv[j] + a.d_eps);   // :130  X .* C ./ D
+            float xc = __fdividef(xo * cv[j], F16 ? dv[j] : dv[j] + a.d_eps);   // :130  X .* C ./ D
             if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;       // :132-134
-            float xn = __fmaf_rn(xc, wv, __fmul_rn(1.f - wv, xo));  // :136
+            float xn = __fmaf_rn(xc, wc, __fmul_rn(1.f - wv, xo));  // :136
             if (xn < 0.f) xn = 0.f;                        // :137
             *xp = xn;
+            if (F16) xm = fmaxf(xm, xn);
           }
         }
       }
@@ -425,6 +470,11 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
         tc::mbar_arrive(&tempty[buf]);
         tc::mbar_arrive(&hdone[buf][half]);
       }
+    }
+    if (F16) {
+      const unsigned active = __activemask();
+      const unsigned m = __reduce_max_sync(active, __float_as_uint(xm));
+      if (lane == __ffs(active) - 1 && m != 0u) atomicMax(reinterpret_cast<unsigned*>(a.xmax), m);
     }
   } else if (warp == BWD_IO_WARP) {
     if (lane == 0) {
@@ -495,6 +545,9 @@ struct TcFwdArgs {
   const int* tile_patch;   // patch of each position tile
   const int* pinfo;        // per patch: Li, Lj, LL, pos0, z0, nz, -, -
   int NN;                  // N*N channels per plane (plane-major channels)
+  // FP16 modes only (null otherwise)
+  const float* xmax;       // running maximum of X: the operand is X * f16_scale(xmax)
+  const float* fsinv;      // inverse scales of the view's tap columns [NB]
 };
 
 // The forward GEMM reads the FP32 volume directly: each stage's 32 KB region receives the
@@ -507,6 +560,7 @@ struct TcFwdArgs {
 constexpr int FWD_THREADS = 256;
 constexpr int FWD_XTILE = BM * BK * 4;  // 32 KB: FP32 X tile, then A hi | A lo (16 KB each)
 
+template <bool F16>
 __global__ void __launch_bounds__(FWD_THREADS, 1)
 k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtensorMap mBh,
          const __grid_constant__ CUtensorMap mBl, TcFwdArgs a) {
@@ -576,7 +630,7 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtenso
     for (int i = std::max(0, issued - S); i < issued; ++i)
       tc::mbar_wait(&full[i % S], (i / S) & 1, WAIT_LIMIT);
   } else if (warp == 1 && lane == 0) {
-    const uint32_t idesc = tc::idesc_bf16_f32(BM, a.NH);
+    const uint32_t idesc = F16 ? tc::idesc_f16_f32(BM, a.NH) : tc::idesc_bf16_f32(BM, a.NH);
     for (int ks = ks0; ks < ks1; ++ks) {
       const int i = ks - ks0, s = i % S;
       const uint32_t ph = (i / S) & 1;
@@ -610,8 +664,9 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtenso
     }
     tc::mma_commit(&accb);
   } else if (warp >= 4) {
-    // converters: FP32 X tile -> BF16 hi / lo operand, in place
+    // converters: FP32 X tile -> BF16 (FP16: scaled) hi / lo operand, in place
     const int p = threadIdx.x - 128;  // position row of the tile
+    const float sx = F16 ? f16_scale(*a.xmax) : 1.f;
     for (int ks = ks0; ks < ks1; ++ks) {
       const int i = ks - ks0, s = i % S;
       const uint32_t ph = (i / S) & 1;
@@ -635,10 +690,11 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtenso
       }
 #pragma unroll
       for (int c8 = 0; c8 < BK / 8; ++c8) {
-        __align__(16) bf16 hi[8];
-        __align__(16) bf16 lo[8];
+        using E = typename std::conditional<F16, f16, bf16>::type;
+        __align__(16) E hi[8];
+        __align__(16) E lo[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) split_bf16(x[c8 * 8 + j], hi[j], lo[j]);
+        for (int j = 0; j < 8; ++j) split2(F16 ? x[c8 * 8 + j] * sx : x[c8 * 8 + j], hi[j], lo[j]);
         const int off = p * 128 + ((c8 ^ (p & 7)) << 4);
         *reinterpret_cast<uint4*>(st + off) = *reinterpret_cast<const uint4*>(hi);
         if (a.use_alo) *reinterpret_cast<uint4*>(st + offAl + off) = *reinterpret_cast<const uint4*>(lo);
@@ -658,11 +714,17 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtenso
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     float* out = a.ypart + (int64_t)split * a.NB * a.MP + m0 + row;  // + t * MP
     const bool empty_split = ks1 <= ks0;
+    // FP16: remove the volume's and the tap column's scales (powers of two: exact)
+    const float xinv = F16 ? 1.f / f16_scale(*a.xmax) : 1.f;
     if (ok) {
       for (int c = 0; c < (a.nparts * a.NH) / 16; ++c) {
         float v[16];
         tc::tmem_ld16(tY + lane_off + c * 16, v);
         if (aborted(&abort_flag)) continue;
+        if (F16) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] *= xinv * __ldg(a.fsinv + c * 16 + j);
+        }
 #pragma unroll
         for (int j = 0; j < 16; ++j) out[(int64_t)(c * 16 + j) * a.MP] = empty_split ? 0.f : v[j];
       }
@@ -685,8 +747,10 @@ __device__ __forceinline__ int64_t tc_to_fp32_channel(int64_t ch, int N, int Z, 
 
 // Extended back-projection taps, BF16 hi/lo:  Wb'[view][ch][t'] for the (T+2)^2 window,
 // t' = dj'*(T+2) + di', holding wb[view][ch][(dj'-sb-1)*T + (di'-sa-1)] (0 elsewhere).
+// FP16 tables: each row scaled by rowscale[view * CHP + ch] (nullable: unscaled).
+template <typename E>
 __global__ void k_tc_build_wbx(const float* __restrict__ wb, int N, int Z, int T, int64_t nch, int CHP, int KB,
-                               bf16* __restrict__ hi, bf16* __restrict__ lo) {
+                               const float* __restrict__ rowscale, E* __restrict__ hi, E* __restrict__ lo) {
   const int T2 = T + 2, h = (N - 1) / 2;
   const int64_t total = (int64_t)N * N * CHP * KB;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -704,17 +768,21 @@ __global__ void k_tc_build_wbx(const float* __restrict__ wb, int N, int Z, int T
       const int dj = k / T2 - sb - 1, di = k % T2 - sa - 1;
       if (dj >= 0 && dj < T && di >= 0 && di < T)
         val = wb[((int64_t)view * nch + chf) * T * T + dj * T + di];
+      if (rowscale) val *= rowscale[r];
     }
-    bf16 h16, l16;
-    split_bf16(val, h16, l16);
+    E h16, l16;
+    split2(val, h16, l16);
     hi[e] = h16;
     lo[e] = l16;
   }
 }
 
 // Forward taps transposed, BF16 hi/lo: Wf'[view][t][ch] = wf[view][ch][t] (t < T^2).
+// FP16 tables: each tap column t of a view scaled by 1 / colscale_inv[view * NB + t]
+// (nullable: unscaled).
+template <typename E>
 __global__ void k_tc_build_wft(const float* __restrict__ wf, int N, int Z, int T, int64_t nch, int CHP, int NB,
-                               bf16* __restrict__ hi, bf16* __restrict__ lo) {
+                               const float* __restrict__ colscale_inv, E* __restrict__ hi, E* __restrict__ lo) {
   const int64_t total = (int64_t)N * N * NB * CHP;
   const int TT = T * T;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -727,24 +795,80 @@ __global__ void k_tc_build_wft(const float* __restrict__ wf, int N, int Z, int T
     if (ch < nch && t < TT) {
       int alpha, beta;
       val = wf[((int64_t)view * nch + tc_to_fp32_channel(ch, N, Z, &alpha, &beta)) * TT + t];
+      if (colscale_inv) val *= 1.f / colscale_inv[r];
     }
-    bf16 h16, l16;
-    split_bf16(val, h16, l16);
+    E h16, l16;
+    split2(val, h16, l16);
     hi[e] = h16;
     lo[e] = l16;
   }
+}
+
+// Scales of the FP16 tap tables, one warp per row or column: bscale[view][ch] =
+// f16_scale(max_t |wb[view][ch][t]|) for the back-projection rows (it cancels in C / D);
+// fsinv[view][t] = 1 / f16_scale(max_ch |wf[view][ch][t]|) for the forward GEMM's columns
+// (the forward epilogue multiplies by it).
+__global__ void k_tc_f16_scales(const float* __restrict__ wb, const float* __restrict__ wf, int N, int Z, int T,
+                                int64_t nch, int CHP, int NB, float* __restrict__ bscale, float* __restrict__ fsinv) {
+  const int TT = T * T;
+  const int64_t nbr = (int64_t)N * N * CHP, nfr = (int64_t)N * N * NB;
+  const int lane = threadIdx.x & 31;
+  const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nbr + nfr; r += wstride) {
+    float m = 0.f;
+    int alpha, beta;
+    if (r < nbr) {
+      const int view = (int)(r / CHP);
+      const int64_t ch = r % CHP;
+      if (ch < nch) {
+        const float* row = wb + ((int64_t)view * nch + tc_to_fp32_channel(ch, N, Z, &alpha, &beta)) * TT;
+        for (int t = lane; t < TT; t += 32) m = fmaxf(m, fabsf(row[t]));
+      }
+    } else {
+      const int view = (int)((r - nbr) / NB), t = (int)((r - nbr) % NB);
+      if (t < TT)
+        for (int64_t ch = lane; ch < nch; ch += 32)
+          m = fmaxf(m, fabsf(wf[((int64_t)view * nch + tc_to_fp32_channel(ch, N, Z, &alpha, &beta)) * TT + t]));
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) {
+      if (r < nbr)
+        bscale[r] = f16_scale(m);
+      else
+        fsinv[r - nbr] = 1.f / f16_scale(m);
+    }
+  }
+}
+
+// *amax = max(*amax, max |x[i]|) over n floats (amax holds a non-negative float).
+__global__ void k_tc_absmax(const float* __restrict__ x, int64_t n, float* amax) {
+  float m = 0.f;
+  const int64_t n4 = n / 4;
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 v = __ldg(x4 + i);
+    m = fmaxf(fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y))), fmaxf(fabsf(v.z), fabsf(v.w)));
+  }
+  for (int64_t i = 4 * n4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[i]));
+  const unsigned w = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
+  if ((threadIdx.x & 31) == 0 && w != 0u) atomicMax(reinterpret_cast<unsigned*>(amax), w);
 }
 
 // im2col of the ratio images (or of ones when R == nullptr) over the (T+2)^2 window, for
 // all patches: row = global position, R indexed by global position.  One warp per row; the
 // lanes walk the row's KB columns (columns past (T+2)^2 and rows past a patch's positions
 // are zero).
+// FP16 (rmax non-null): values scaled by f16_scale(*rmax), the ratio image's maximum.
 constexpr int IM2COL_WARPS = 8;
+template <typename E>
 __global__ void __launch_bounds__(32 * IM2COL_WARPS)
 k_tc_im2col(const float* __restrict__ R, const int* __restrict__ tile_patch, const int* __restrict__ pinfo,
-            int MP, int T, int KB, bf16* __restrict__ hi, bf16* __restrict__ lo) {
+            int MP, int T, int KB, const float* __restrict__ rmax, E* __restrict__ hi, E* __restrict__ lo) {
   const int T2 = T + 2, q = (T - 1) / 2, KK = T2 * T2;
   const int lane = threadIdx.x & 31;
+  const float sc = rmax ? f16_scale(*rmax) : 1.f;
   for (int pos = blockIdx.x * IM2COL_WARPS + (threadIdx.x >> 5); pos < MP; pos += gridDim.x * IM2COL_WARPS) {
     const int* pi = pinfo + 8 * tile_patch[pos / BM];
     const int Li = pi[0], Lj = pi[1], pos0 = pi[3];
@@ -752,17 +876,17 @@ k_tc_im2col(const float* __restrict__ R, const int* __restrict__ tile_patch, con
     const bool row_ok = local < pi[2];
     const int b = row_ok ? local / Li : 0;
     const int a = local - b * Li;
-    bf16* hrow = hi + (int64_t)pos * KB;
-    bf16* lrow = lo ? lo + (int64_t)pos * KB : nullptr;
+    E* hrow = hi + (int64_t)pos * KB;
+    E* lrow = lo ? lo + (int64_t)pos * KB : nullptr;
     for (int k = lane; k < KB; k += 32) {
       float val = 0.f;
       if (row_ok && k < KK) {
         const int dj = k / T2;
         const int j = b + dj - q - 1, i = a + (k - dj * T2) - q - 1;
-        if (j >= 0 && j < Lj && i >= 0 && i < Li) val = R ? __ldg(R + pos0 + j * Li + i) : 1.f;
+        if (j >= 0 && j < Lj && i >= 0 && i < Li) val = R ? __ldg(R + pos0 + j * Li + i) * sc : 1.f;
       }
-      bf16 h16, l16;
-      split_bf16(val, h16, l16);
+      E h16, l16;
+      split2(val, h16, l16);
       hrow[k] = h16;
       if (lrow) lrow[k] = l16;
     }
@@ -774,12 +898,13 @@ k_tc_im2col(const float* __restrict__ R, const int* __restrict__ tile_patch, con
 // consecutive positions (lanes); warp w takes the tap rows db = w, w+16, ..., so each load of
 // a warp is 32 consecutive floats of one tap's row.  Four split partials are loaded before
 // they are added, so every thread keeps several loads in flight; the warps' sums are added
-// in a fixed order (deterministic).
+// in a fixed order (deterministic).  rmax (nullable, FP16 modes) receives max |R|.
 constexpr int COL2IM_WARPS = 16;
 __global__ void __launch_bounds__(32 * COL2IM_WARPS)
 k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, int T,
                   const int* __restrict__ tile_patch, const int* __restrict__ pinfo,
-                  const float* __restrict__ lfsub, float* __restrict__ hx_out, float* __restrict__ rimg) {
+                  const float* __restrict__ lfsub, float* __restrict__ hx_out, float* __restrict__ rimg,
+                  float* __restrict__ rmax) {
   __shared__ float part[COL2IM_WARPS][32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int pos = blockIdx.x * 32 + lane;
@@ -820,6 +945,7 @@ k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, i
   }
   part[w][lane] = s;
   __syncthreads();
+  float rabs = 0.f;
   if (w == 0 && valid) {
     float h = 0.f;
 #pragma unroll
@@ -829,7 +955,12 @@ k_tc_col2im_ratio(const float* __restrict__ ypart, int splits, int MP, int NB, i
       float r = lfsub[pos] / h;
       if (!isfinite(r)) r = 0.f;
       rimg[pos] = r;
+      rabs = fabsf(r);
     }
+  }
+  if (rmax && w == 0) {
+    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(rabs));
+    if (lane == 0 && m != 0u) atomicMax(reinterpret_cast<unsigned*>(rmax), m);
   }
 }
 
@@ -847,14 +978,15 @@ int get_encoder() {
   return MLF_OK;
 }
 
-// 2-D BF16 matrix [rows][cols] (cols contiguous, multiple of 64), box 64 x box_rows, SW128.
-int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+// 2-D BF16 (or FP16) matrix [rows][cols] (cols contiguous, multiple of 64), box 64 x box_rows, SW128.
+int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows, bool fp16 = false) {
   MLF_TRY(get_encoder());
   cuuint64_t dims[2] = {cols, rows};
   cuuint64_t strides[1] = {cols * 2};
   cuuint32_t box[2] = {64, box_rows};
   cuuint32_t es[2] = {1, 1};
-  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+  CUresult r = g_encode(m, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                        const_cast<void*>(base), dims, strides, box, es,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(MLF_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
@@ -872,6 +1004,12 @@ struct TcPsfState {
   DevBuf dtab[2];       // D class tables of every view, [view][ncls][ncls][CHP]; taps hi / hi + lo
   DevBuf wbx_hi, wbx_lo, wft_hi, wft_lo;
   CUtensorMap mBh, mBl, mFh, mFl;
+  // FP16 forms, built on the first use of an MLF_PREC_FP16* mode: the scaled tap tables,
+  // the back-projection row scales [view][CHP], the forward columns' inverse scales
+  // [view][NB] and their D class tables
+  bool f16_ready = false;
+  DevBuf wbx16_hi, wbx16_lo, wft16_hi, wft16_lo, bscale, fsinv, dtab16[2];
+  CUtensorMap mBh16, mBl16, mFh16, mFl16;
 };
 
 // Work set of P patches sharing one PSF: positions of all patches concatenated (each
@@ -885,7 +1023,7 @@ struct TcSolverState {
   struct Tune {
     int done = 0, tuned = 0, splits = 0, ksp = 0, fwd_stages = 0, xbufs = 0;
   };
-  Tune tune[4];
+  Tune tune[kPrecModes];
   int splits_max = 1, splits_def = 1, ksp_def = 0;
   int fwd_stages = 0, xbufs = 0;  // in use (0: derive from shared memory)
   bool dtab_ok = false;  // every patch has >= 2q+2 lenslets per side: D from class tables
@@ -894,7 +1032,10 @@ struct TcSolverState {
   std::vector<float> wtab;  // [views][P]
   DevBuf X, lfs, rimg, tile_patch, pinfo, wtab_dev, wscratch, ar_hi, ar_lo, a1, ypart, err;
   DevBuf Xprev, relbuf;  // convergence monitor (solves with stats only)
-  CUtensorMap mARh, mARl, mA1, mXv;
+  // FP16 modes: the im2col of ones in FP16, and the operand scales' state: [0] running
+  // maximum of X, [1], [2] max |R| of the even / odd view steps of an iteration
+  DevBuf a1h, f16s;
+  CUtensorMap mARh, mARl, mA1, mA1h, mXv;
   // One RL iteration (view loop + filters of every patch) as an instantiated CUDA graph,
   // per precision and with / without per-view timing nodes.  All buffers above are fixed
   // for the life of the work set, so a captured iteration stays valid.
@@ -903,7 +1044,7 @@ struct TcSolverState {
     int64_t launches = 0;  // kernel nodes
     int tev_used = 0;      // timing events recorded by one replay
   };
-  Iteration iter[4][2];
+  Iteration iter[kPrecModes][2];
   // Captures run on this private stream (the legacy default stream cannot be captured);
   // the instantiated graph is then launched on the caller's stream.
   cudaStream_t capture_stream = nullptr;
@@ -940,10 +1081,10 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
   MLF_TRY(t->wbx_lo.alloc(nb * 2, "tc back-projection taps"));
   MLF_TRY(t->wft_hi.alloc(nf * 2, "tc forward taps"));
   MLF_TRY(t->wft_lo.alloc(nf * 2, "tc forward taps"));
-  k_tc_build_wbx<<<4096, 256, 0, st>>>(p->wb.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP, t->KB,
-                                       t->wbx_hi.as<bf16>(), t->wbx_lo.as<bf16>());
-  k_tc_build_wft<<<4096, 256, 0, st>>>(p->wf.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP, t->NB,
-                                       t->wft_hi.as<bf16>(), t->wft_lo.as<bf16>());
+  k_tc_build_wbx<bf16><<<4096, 256, 0, st>>>(p->wb.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP, t->KB,
+                                             nullptr, t->wbx_hi.as<bf16>(), t->wbx_lo.as<bf16>());
+  k_tc_build_wft<bf16><<<4096, 256, 0, st>>>(p->wf.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP, t->NB,
+                                             nullptr, t->wft_hi.as<bf16>(), t->wft_lo.as<bf16>());
   MLF_LAUNCHED();
   MLF_TRY(make_map(&t->mBh, t->wbx_hi.p, (uint64_t)V * t->CHP, t->KB, BWD_BN));
   MLF_TRY(make_map(&t->mBl, t->wbx_lo.p, (uint64_t)V * t->CHP, t->KB, BWD_BN));
@@ -954,36 +1095,71 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
     MLF_CUDA(cudaGetDevice(&dev));
     MLF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     cudaFuncAttributes fb, ff;
-    MLF_CUDA(cudaFuncGetAttributes(&ff, k_tc_fwd));
-    int bmax = optin;
-    for (const void* f : {(const void*)k_tc_bwd<true, 1>, (const void*)k_tc_bwd<false, 1>,
-                          (const void*)k_tc_bwd<false, 2>}) {
+    int bmax = optin, fstat = 0;
+    for (const void* f : {(const void*)k_tc_bwd<true, 1, false>, (const void*)k_tc_bwd<false, 1, false>,
+                          (const void*)k_tc_bwd<false, 2, false>, (const void*)k_tc_bwd<true, 1, true>,
+                          (const void*)k_tc_bwd<false, 1, true>, (const void*)k_tc_bwd<false, 2, true>}) {
       MLF_CUDA(cudaFuncGetAttributes(&fb, f));
       MLF_TRY(allow_max_dyn_smem(f));
       bmax = std::min(bmax, optin - (int)fb.sharedSizeBytes);
     }
-    MLF_TRY(allow_max_dyn_smem((const void*)k_tc_dtab));
+    MLF_TRY(allow_max_dyn_smem((const void*)k_tc_dtab<bf16>));
+    MLF_TRY(allow_max_dyn_smem((const void*)k_tc_dtab<f16>));
     t->bwd_dyn_max = bmax;
     if (bwd_smem_bytes(1, 1, true, 1) > (size_t)bmax)
       return fail(MLF_ERR_UNSUPPORTED, "tensor-core back projection needs more shared memory than the device offers");
-    t->fwd_dyn_max = optin - (int)ff.sharedSizeBytes;
-    MLF_CUDA(cudaFuncSetAttribute(k_tc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, t->fwd_dyn_max));
+    for (const void* f : {(const void*)k_tc_fwd<false>, (const void*)k_tc_fwd<true>}) {
+      MLF_CUDA(cudaFuncGetAttributes(&ff, f));
+      fstat = std::max(fstat, (int)ff.sharedSizeBytes);
+    }
+    t->fwd_dyn_max = optin - fstat;
+    MLF_CUDA(cudaFuncSetAttribute(k_tc_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, t->fwd_dyn_max));
+    MLF_CUDA(cudaFuncSetAttribute(k_tc_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, t->fwd_dyn_max));
   }
   p->tc = t.release();
   return MLF_OK;
 }
 
+// The FP16 tap tables (scaled, see k_tc_f16_scales), built once per PSF on first use.
+int tc_f16_prepare(const Psf* p, cudaStream_t st) {
+  TcPsfState* t = p->tc;
+  if (t->f16_ready) return MLF_OK;
+  const int V = p->N * p->N;
+  const size_t nb = (size_t)V * t->CHP * t->KB, nf = (size_t)V * t->NB * t->CHP;
+  MLF_TRY(t->wbx16_hi.alloc(nb * 2, "tc FP16 back-projection taps"));
+  MLF_TRY(t->wbx16_lo.alloc(nb * 2, "tc FP16 back-projection taps"));
+  MLF_TRY(t->wft16_hi.alloc(nf * 2, "tc FP16 forward taps"));
+  MLF_TRY(t->wft16_lo.alloc(nf * 2, "tc FP16 forward taps"));
+  MLF_TRY(t->bscale.alloc((size_t)V * t->CHP * 4, "tc FP16 tap scales"));
+  MLF_TRY(t->fsinv.alloc((size_t)V * t->NB * 4, "tc FP16 tap scales"));
+  k_tc_f16_scales<<<2048, 256, 0, st>>>(p->wb.as<float>(), p->wf.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP,
+                                        t->NB, t->bscale.as<float>(), t->fsinv.as<float>());
+  k_tc_build_wbx<f16><<<4096, 256, 0, st>>>(p->wb.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP, t->KB,
+                                            t->bscale.as<float>(), t->wbx16_hi.as<f16>(), t->wbx16_lo.as<f16>());
+  k_tc_build_wft<f16><<<4096, 256, 0, st>>>(p->wf.as<float>(), p->N, p->Z, p->T, p->nch, t->CHP, t->NB,
+                                            t->fsinv.as<float>(), t->wft16_hi.as<f16>(), t->wft16_lo.as<f16>());
+  MLF_LAUNCHED();
+  MLF_TRY(make_map(&t->mBh16, t->wbx16_hi.p, (uint64_t)V * t->CHP, t->KB, BWD_BN, true));
+  MLF_TRY(make_map(&t->mBl16, t->wbx16_lo.p, (uint64_t)V * t->CHP, t->KB, BWD_BN, true));
+  MLF_TRY(make_map(&t->mFh16, t->wft16_hi.p, (uint64_t)V * t->NB, t->CHP, t->NH, true));
+  MLF_TRY(make_map(&t->mFl16, t->wft16_lo.p, (uint64_t)V * t->NB, t->CHP, t->NH, true));
+  t->f16_ready = true;
+  return MLF_OK;
+}
+
 size_t tc_psf_bytes(const Psf* p) {
   if (!p->tc) return 0;
-  return p->tc->wbx_hi.bytes + p->tc->wbx_lo.bytes + p->tc->wft_hi.bytes + p->tc->wft_lo.bytes +
-         p->tc->dtab[0].bytes + p->tc->dtab[1].bytes;
+  const TcPsfState* t = p->tc;
+  return t->wbx_hi.bytes + t->wbx_lo.bytes + t->wft_hi.bytes + t->wft_lo.bytes + t->dtab[0].bytes +
+         t->dtab[1].bytes + t->wbx16_hi.bytes + t->wbx16_lo.bytes + t->wft16_hi.bytes + t->wft16_lo.bytes +
+         t->bscale.bytes + t->fsinv.bytes + t->dtab16[0].bytes + t->dtab16[1].bytes;
 }
 
 size_t tc_work_bytes(const TcSolverState* t) {
   if (!t) return 0;
   return t->X.bytes + t->lfs.bytes + t->rimg.bytes + t->tile_patch.bytes + t->pinfo.bytes + t->wtab_dev.bytes +
          t->wscratch.bytes + t->ar_hi.bytes + t->ar_lo.bytes + t->a1.bytes +
-         t->ypart.bytes + t->err.bytes + t->Xprev.bytes + t->relbuf.bytes;
+         t->ypart.bytes + t->err.bytes + t->Xprev.bytes + t->relbuf.bytes + t->a1h.bytes + t->f16s.bytes;
 }
 
 size_t tc_solver_bytes(const Solver* s) { return tc_work_bytes(s->tc); }
@@ -1005,7 +1181,7 @@ size_t tc_work_plan_bytes(const Psf* psf, const std::vector<int>& Li, const std:
   splits = (KSF + ksp - 1) / ksp;
   const int64_t P = (int64_t)Li.size();
   return (size_t)(psf->nch * MP * 4 + (int64_t)psf->N * psf->N * MP * 4 + MP * 4 + tiles * 4 + 8 * P * 4 +
-                  (int64_t)psf->N * psf->N * P * 4 + P * 4 + 3 * MP * KB * 2 +
+                  (int64_t)psf->N * psf->N * P * 4 + P * 4 + 4 * MP * KB * 2 + 16 +
                   (int64_t)splits * MP * NB * 4 + 4 +
                   // convergence monitor, allocated by the first solve that asks for stats
                   psf->nch * MP * 4 + (int64_t)kRelChangeBufDoubles * 8);
@@ -1071,6 +1247,8 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_TRY(t->ar_hi.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->ar_lo.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->a1.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
+  MLF_TRY(t->a1h.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
+  MLF_TRY(t->f16s.alloc(4 * sizeof(float), "tc FP16 operand scales"));
   MLF_TRY(t->ypart.alloc((size_t)t->splits_max * t->MP * tp->NB * 4, "tc forward partials"));
   MLF_TRY(t->err.alloc(sizeof(int), "tc error flag"));
   t->dtab_ok = true;
@@ -1083,12 +1261,19 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_CUDA(cudaMemsetAsync(t->X.p, 0, t->X.bytes, st));
   MLF_CUDA(cudaMemsetAsync(t->lfs.p, 0, t->lfs.bytes, st));
   MLF_CUDA(cudaMemsetAsync(t->err.p, 0, sizeof(int), st));
-  k_tc_im2col<<<(t->MP + IM2COL_WARPS - 1) / IM2COL_WARPS, 32 * IM2COL_WARPS, 0, st>>>(
-      nullptr, t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP, psf->T, tp->KB, t->a1.as<bf16>(), nullptr);
+  MLF_CUDA(cudaMemsetAsync(t->f16s.p, 0, t->f16s.bytes, st));
+  k_tc_im2col<bf16><<<(t->MP + IM2COL_WARPS - 1) / IM2COL_WARPS, 32 * IM2COL_WARPS, 0, st>>>(
+      nullptr, t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP, psf->T, tp->KB, nullptr, t->a1.as<bf16>(),
+      (bf16*)nullptr);
+  k_tc_im2col<f16><<<(t->MP + IM2COL_WARPS - 1) / IM2COL_WARPS, 32 * IM2COL_WARPS, 0, st>>>(
+      nullptr, t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP, psf->T, tp->KB, nullptr, t->a1h.as<f16>(),
+      (f16*)nullptr);
   MLF_LAUNCHED();
+  // the im2col buffers hold BF16 or FP16 values by mode: the maps only move 2-byte elements
   MLF_TRY(make_map(&t->mARh, t->ar_hi.p, t->MP, tp->KB, BM));
   MLF_TRY(make_map(&t->mARl, t->ar_lo.p, t->MP, tp->KB, BM));
   MLF_TRY(make_map(&t->mA1, t->a1.p, t->MP, tp->KB, BM));
+  MLF_TRY(make_map(&t->mA1h, t->a1h.p, t->MP, tp->KB, BM, true));
   {
     MLF_TRY(get_encoder());
     cuuint64_t dims[2] = {(cuuint64_t)t->MP, (cuuint64_t)nch};
@@ -1113,10 +1298,26 @@ namespace {
 
 // (activation split, tap split) per precision mode
 void splits_of(int precision, int* alo, int* blo) {
-  *alo = (precision == MLF_PREC_BF16X2 || precision == MLF_PREC_BF16X3) ? 1 : 0;
-  *blo = (precision == MLF_PREC_BF16X3) ? 1 : 0;
+  *alo = (precision == MLF_PREC_BF16X2 || precision == MLF_PREC_BF16X3 || precision == MLF_PREC_FP16X2 ||
+          precision == MLF_PREC_FP16X3) ? 1 : 0;
+  *blo = (precision == MLF_PREC_BF16X3 || precision == MLF_PREC_FP16X3) ? 1 : 0;
 }
-bool act_split(int precision) { return precision == MLF_PREC_BF16X2 || precision == MLF_PREC_BF16X3; }
+bool act_split(int precision) {
+  int alo, blo;
+  splits_of(precision, &alo, &blo);
+  return alo != 0;
+}
+
+// FP16 modes: reset the operand scales' state and take the running maximum of X from the
+// whole work-set volume (the start of an iteration, or of a stand-alone projection).
+int tc_f16_begin(TcSolverState* t, int precision, cudaStream_t st, int64_t* launches = nullptr) {
+  if (!prec_f16(precision)) return MLF_OK;
+  MLF_CUDA(cudaMemsetAsync(t->f16s.p, 0, t->f16s.bytes, st));
+  k_tc_absmax<<<2 * t->nsm, 512, 0, st>>>(t->X.as<float>(), (int64_t)(t->X.bytes / sizeof(float)), t->f16s.as<float>());
+  MLF_LAUNCHED();
+  if (launches) ++*launches;
+  return MLF_OK;
+}
 
 PatchGeo work_geo(const TcSolverState* t, const Solver* m, int p) {
   return PatchGeo{m->N, t->nz[p], t->Zch, t->z0[p], t->Li[p], t->Lj[p], t->Li[p], (int64_t)t->MP, m->Xr, m->Xc, 1};
@@ -1144,30 +1345,46 @@ int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cud
   a.tile_patch = t->tile_patch.as<int>();
   a.pinfo = t->pinfo.as<int>();
   a.NN = psf->N * psf->N;
+  const bool use16 = prec_f16(precision);
+  if (use16) {
+    a.xmax = t->f16s.as<float>();
+    a.fsinv = tp->fsinv.as<float>() + (int64_t)view * tp->NB;
+  }
   const size_t stage = (size_t)FWD_XTILE + (size_t)tp->NB * 128 * (blo ? 2 : 1);
   a.stages = (int)std::max<size_t>(2, std::min<size_t>(FWD_MAX_STAGES, (size_t)(tp->fwd_dyn_max - 1024) / stage));
   if (t->fwd_stages > 0 && (size_t)t->fwd_stages * stage + 1024 <= (size_t)tp->fwd_dyn_max) a.stages = t->fwd_stages;
   const size_t fsmem = (size_t)a.stages * stage + 1024;
   if (fsmem > (size_t)tp->fwd_dyn_max)
     return fail(MLF_ERR_UNSUPPORTED, "tensor-core forward projection: taps tile exceeds shared memory");
-  k_tc_fwd<<<dim3(t->MP / BM, t->splits), FWD_THREADS, fsmem, st>>>(t->mXv, tp->mFh, tp->mFl, a);
+  if (use16)
+    k_tc_fwd<true><<<dim3(t->MP / BM, t->splits), FWD_THREADS, fsmem, st>>>(t->mXv, tp->mFh16, tp->mFl16, a);
+  else
+    k_tc_fwd<false><<<dim3(t->MP / BM, t->splits), FWD_THREADS, fsmem, st>>>(t->mXv, tp->mFh, tp->mFl, a);
   MLF_LAUNCHED();
   return MLF_OK;
 }
 
-int tc_col2im(const Psf* psf, TcSolverState* t, int view, bool ratio, float* hx_out, cudaStream_t st) {
+// slot (FP16 modes): the max |R| slot of this view step (its parity within the iteration)
+int tc_col2im(const Psf* psf, TcSolverState* t, int view, bool ratio, float* hx_out, cudaStream_t st,
+              int precision = MLF_PREC_BF16X2, int slot = 0) {
+  float* rmax = (ratio && prec_f16(precision)) ? t->f16s.as<float>() + 1 + slot : nullptr;
   k_tc_col2im_ratio<<<(t->MP + 31) / 32, 32 * COL2IM_WARPS, 0, st>>>(
       t->ypart.as<float>(), t->splits, t->MP, psf->tc->NB, psf->T, t->tile_patch.as<int>(), t->pinfo.as<int>(),
-      t->lfs.as<float>() + (int64_t)view * t->MP, hx_out, ratio ? t->rimg.as<float>() : nullptr);
+      t->lfs.as<float>() + (int64_t)view * t->MP, hx_out, ratio ? t->rimg.as<float>() : nullptr, rmax);
   MLF_LAUNCHED();
   return MLF_OK;
 }
 
-int tc_im2col_ratio(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st) {
-  k_tc_im2col<<<(t->MP + IM2COL_WARPS - 1) / IM2COL_WARPS, 32 * IM2COL_WARPS, 0, st>>>(
-      t->rimg.as<float>(), t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP,
-                                    psf->T, psf->tc->KB, t->ar_hi.as<bf16>(),
-                                    act_split(precision) ? t->ar_lo.as<bf16>() : nullptr);
+int tc_im2col_ratio(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st, int slot = 0) {
+  const dim3 grid((t->MP + IM2COL_WARPS - 1) / IM2COL_WARPS), block(32 * IM2COL_WARPS);
+  if (prec_f16(precision))
+    k_tc_im2col<f16><<<grid, block, 0, st>>>(t->rimg.as<float>(), t->tile_patch.as<int>(), t->pinfo.as<int>(), t->MP,
+                                             psf->T, psf->tc->KB, t->f16s.as<float>() + 1 + slot,
+                                             t->ar_hi.as<f16>(), act_split(precision) ? t->ar_lo.as<f16>() : nullptr);
+  else
+    k_tc_im2col<bf16><<<grid, block, 0, st>>>(t->rimg.as<float>(), t->tile_patch.as<int>(), t->pinfo.as<int>(),
+                                              t->MP, psf->T, psf->tc->KB, nullptr, t->ar_hi.as<bf16>(),
+                                              act_split(precision) ? t->ar_lo.as<bf16>() : nullptr);
   MLF_LAUNCHED();
   return MLF_OK;
 }
@@ -1178,24 +1395,32 @@ int tc_dtab_prepare(const Psf* psf, int precision, cudaStream_t st) {
   int alo, blo;
   splits_of(precision, &alo, &blo);
   TcPsfState* tp = psf->tc;
-  if (tp->dtab[blo].p) return MLF_OK;
+  const bool use16 = prec_f16(precision);
+  DevBuf& dt = use16 ? tp->dtab16[blo] : tp->dtab[blo];
+  if (dt.p) return MLF_OK;
   const int nc = 2 * psf->q + 3, V = psf->N * psf->N;
-  MLF_TRY(tp->dtab[blo].alloc((size_t)V * nc * nc * tp->CHP * sizeof(float), "tc D class tables"));
+  MLF_TRY(dt.alloc((size_t)V * nc * nc * tp->CHP * sizeof(float), "tc D class tables"));
   const size_t dsm = sizeof(float) * 64 * (size_t)dtab_ch_words(psf->T);
-  k_tc_dtab<<<dim3(tp->CHP / 32, V), DTAB_THREADS, dsm, st>>>(tp->wbx_hi.as<bf16>(),
-                                                              blo ? tp->wbx_lo.as<bf16>() : nullptr, tp->CHP,
-                                                              tp->KB, psf->T, tp->dtab[blo].as<float>());
+  if (use16)
+    k_tc_dtab<f16><<<dim3(tp->CHP / 32, V), DTAB_THREADS, dsm, st>>>(
+        tp->wbx16_hi.as<f16>(), blo ? tp->wbx16_lo.as<f16>() : nullptr, tp->CHP, tp->KB, psf->T, dt.as<float>());
+  else
+    k_tc_dtab<bf16><<<dim3(tp->CHP / 32, V), DTAB_THREADS, dsm, st>>>(
+        tp->wbx_hi.as<bf16>(), blo ? tp->wbx_lo.as<bf16>() : nullptr, tp->CHP, tp->KB, psf->T, dt.as<float>());
   MLF_LAUNCHED();
   return MLF_OK;
 }
 
-int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, const float* wrow, cudaStream_t st) {
+int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, const float* wrow, cudaStream_t st,
+                  int slot = 0) {
   const TcPsfState* tp = psf->tc;
   int alo, blo;
   splits_of(precision, &alo, &blo);
   const bool dgemm = !t->dtab_ok;
+  const bool use16 = prec_f16(precision);
   const int q = psf->q, nc = 2 * q + 3;
-  if (!dgemm && !tp->dtab[blo].p) return fail(MLF_ERR_INVALID, "tensor-core D class tables not prepared");
+  const DevBuf& dt = use16 ? tp->dtab16[blo] : tp->dtab[blo];
+  if (!dgemm && !dt.p) return fail(MLF_ERR_INVALID, "tensor-core D class tables not prepared");
   TcBwdArgs a{};
   a.err = t->err.as<int>();
   a.tile_patch = t->tile_patch.as<int>();
@@ -1205,21 +1430,40 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   a.use_alo = alo;
   a.use_blo = blo;
   a.d_eps = t->d_eps;
-  a.dtab = dgemm ? nullptr : tp->dtab[blo].as<float>() + (int64_t)view * nc * nc * tp->CHP;
+  a.dtab = dgemm ? nullptr : dt.as<float>() + (int64_t)view * nc * nc * tp->CHP;
   a.q = q;
   a.ncls = nc;
+  if (use16) {
+    a.rmax = t->f16s.as<float>() + 1 + slot;
+    a.rmax_next = t->f16s.as<float>() + 1 + (slot ^ 1);
+    a.xmax = t->f16s.as<float>();
+    a.bscale = tp->bscale.as<float>() + (int64_t)view * tp->CHP;
+  }
   const int mt = t->MP / BM, nt = tp->CHP / BWD_BN;
   const int grid = std::min(mt * nt, t->nsm);
   // two X buffers when they fit (D from tables frees the A1 operand's ring slots)
   int xbufs = (!dgemm && bwd_smem_bytes(alo, blo, false, 2) <= (size_t)tp->bwd_dyn_max) ? 2 : 1;
   if (t->xbufs == 1) xbufs = 1;
   const size_t smem = bwd_smem_bytes(alo, blo, dgemm, xbufs);
-  if (dgemm)
-    k_tc_bwd<true, 1><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a, mt, nt);
-  else if (xbufs == 2)
-    k_tc_bwd<false, 2><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a, mt, nt);
-  else
-    k_tc_bwd<false, 1><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a, mt, nt);
+  if (use16) {
+    const CUtensorMap &mBh = tp->mBh16, &mBl = tp->mBl16;
+    if (dgemm)
+      k_tc_bwd<true, 1, true><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1h, mBh, mBl, t->mXv, a, mt, nt);
+    else if (xbufs == 2)
+      k_tc_bwd<false, 2, true><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1h, mBh, mBl, t->mXv, a, mt, nt);
+    else
+      k_tc_bwd<false, 1, true><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1h, mBh, mBl, t->mXv, a, mt, nt);
+  } else {
+    if (dgemm)
+      k_tc_bwd<true, 1, false><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a,
+                                                                mt, nt);
+    else if (xbufs == 2)
+      k_tc_bwd<false, 2, false><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a,
+                                                                 mt, nt);
+    else
+      k_tc_bwd<false, 1, false><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, t->mA1, tp->mBh, tp->mBl, t->mXv, a,
+                                                                 mt, nt);
+  }
   MLF_LAUNCHED();
   return MLF_OK;
 }
@@ -1231,21 +1475,22 @@ int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* ti
   const int V = (int)t->views.size();
   if (V == 0) return MLF_OK;
   int64_t n = 0;
+  MLF_TRY(tc_f16_begin(t, precision, st, &n));
   MLF_TRY(timing_mark(timer, st));
   MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[0], st, t->wtab_dev.as<float>()));
   MLF_TRY(timing_mark(timer, st));
-  MLF_TRY(tc_col2im(psf, t, t->views[0], true, nullptr, st));
-  MLF_TRY(tc_im2col_ratio(psf, t, precision, st));
+  MLF_TRY(tc_col2im(psf, t, t->views[0], true, nullptr, st, precision, 0));
+  MLF_TRY(tc_im2col_ratio(psf, t, precision, st, 0));
   n += 3;
   for (int k = 0; k < V; ++k) {
     MLF_TRY(timing_mark(timer, st));
-    MLF_TRY(tc_bwd_launch(psf, t, precision, t->views[k], t->wtab_dev.as<float>() + (size_t)k * t->P, st));
+    MLF_TRY(tc_bwd_launch(psf, t, precision, t->views[k], t->wtab_dev.as<float>() + (size_t)k * t->P, st, k & 1));
     ++n;
     if (k + 1 < V) {
       MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[k + 1], st, t->wtab_dev.as<float>() + (size_t)(k + 1) * t->P));
       MLF_TRY(timing_mark(timer, st));
-      MLF_TRY(tc_col2im(psf, t, t->views[k + 1], true, nullptr, st));
-      MLF_TRY(tc_im2col_ratio(psf, t, precision, st));
+      MLF_TRY(tc_col2im(psf, t, t->views[k + 1], true, nullptr, st, precision, (k + 1) & 1));
+      MLF_TRY(tc_im2col_ratio(psf, t, precision, st, (k + 1) & 1));
       n += 3;
     } else {
       MLF_TRY(timing_mark(timer, st));
@@ -1299,7 +1544,7 @@ int capture_iteration(const Psf* psf, TcSolverState* t, const std::vector<Solver
 
 // The launch configuration of this precision (tuned, or the heuristics) into effect.
 void tc_apply_tune(TcSolverState* t, int precision) {
-  const TcSolverState::Tune& g = t->tune[precision & 3];
+  const TcSolverState::Tune& g = t->tune[precision];
   if (g.done) {
     t->splits = g.splits;
     t->ks_per_split = g.ksp;
@@ -1319,7 +1564,7 @@ void tc_apply_tune(TcSolverState* t, int precision) {
 // restored after, so the solve is unaffected.  Runs once per work set and precision, before
 // the iteration is captured; MLF_TUNE=0 keeps the heuristics.
 int tc_autotune(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st) {
-  TcSolverState::Tune& g = t->tune[precision & 3];
+  TcSolverState::Tune& g = t->tune[precision];
   if (g.done) return MLF_OK;
   g.done = 1;
   g.splits = t->splits_def;
@@ -1329,6 +1574,7 @@ int tc_autotune(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st
   DevBuf xsave;
   MLF_TRY(xsave.alloc(t->X.bytes, "autotune volume copy"));
   MLF_CUDA(cudaMemcpyAsync(xsave.p, t->X.p, t->X.bytes, cudaMemcpyDeviceToDevice, st));
+  MLF_TRY(tc_f16_begin(t, precision, st));
   cudaEvent_t e0, e1;
   MLF_CUDA(cudaEventCreate(&e0));
   MLF_CUDA(cudaEventCreate(&e1));
@@ -1367,8 +1613,8 @@ int tc_autotune(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st
   t->ks_per_split = g.ksp;
   t->fwd_stages = g.fwd_stages;
   MLF_TRY(tc_fwd_launch(psf, t, precision, v0, st, w0));
-  MLF_TRY(tc_col2im(psf, t, v0, true, nullptr, st));
-  MLF_TRY(tc_im2col_ratio(psf, t, precision, st));
+  MLF_TRY(tc_col2im(psf, t, v0, true, nullptr, st, precision, 0));
+  MLF_TRY(tc_im2col_ratio(psf, t, precision, st, 0));
   if (t->dtab_ok) {
     best = 1e30f;
     for (int xb = 1; xb <= 2; ++xb) {
@@ -1406,6 +1652,7 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
   timer->timing = stats != nullptr;
   timer->tev_used = 0;
   int64_t launches = 0;
+  if (prec_f16(precision)) MLF_TRY(tc_f16_prepare(psf, st));
   if (t->dtab_ok) MLF_TRY(tc_dtab_prepare(psf, precision, st));
   for (int p = 0; p < t->P; ++p) {
     const PatchGeo g = work_geo(t, members[p], p);
@@ -1428,7 +1675,7 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
     MLF_TRY(tc_autotune(psf, t, precision, st));  // first solve at this precision only
     tc_apply_tune(t, precision);
     if (monitor) MLF_CUDA(cudaMemcpyAsync(t->Xprev.p, t->X.p, t->X.bytes, cudaMemcpyDeviceToDevice, st));
-    TcSolverState::Iteration& g = t->iter[precision & 3][timer->timing ? 1 : 0];
+    TcSolverState::Iteration& g = t->iter[precision][timer->timing ? 1 : 0];
     if (!g.exec) {
       timer->tev_used = 0;
       MLF_TRY(capture_iteration(psf, t, members, precision, timer, &g));
@@ -1466,7 +1713,7 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
     stats->fwd_splits = t->splits;
     stats->fwd_stages = t->fwd_stages;
     stats->bwd_xbufs = t->xbufs ? t->xbufs : (t->dtab_ok ? 2 : 1);
-    stats->tuned = t->tune[precision & 3].tuned;
+    stats->tuned = t->tune[precision].tuned;
     stats->rel_change = 0.0;
     if (monitor) MLF_TRY(rel_change_read(t->relbuf.as<double>(), &stats->rel_change));
     MLF_TRY(tc_check_error(t));
@@ -1480,7 +1727,9 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
 int tc_forward_view(Solver* s, int precision, const float* d_vol, int view, float* hx_out, cudaStream_t st) {
   TcSolverState* t = s->tc;
   tc_apply_tune(t, precision);
+  if (prec_f16(precision)) MLF_TRY(tc_f16_prepare(s->psf, st));
   MLF_TRY(launch_to_phase(d_vol, work_geo(t, s, 0), t->X.as<float>(), st));
+  MLF_TRY(tc_f16_begin(t, precision, st));
   MLF_TRY(tc_fwd_launch(s->psf, t, precision, view, st));
   return tc_col2im(s->psf, t, view, false, hx_out, st);
 }
@@ -1490,9 +1739,11 @@ int tc_forward_project(TcSolverState* t, const std::vector<Solver*>& members, co
   const Psf* psf = members[0]->psf;
   const int N = psf->N;
   tc_apply_tune(t, precision);
+  if (prec_f16(precision)) MLF_TRY(tc_f16_prepare(psf, st));
   for (int p = 0; p < t->P; ++p)
     MLF_TRY(launch_to_phase(vols[p], work_geo(t, members[p], p), t->X.as<float>() + t->pos0[p], st,
                             zscale ? zscale + t->z0[p] : nullptr));
+  MLF_TRY(tc_f16_begin(t, precision, st));
   for (int view = 0; view < N * N; ++view) {
     MLF_TRY(tc_fwd_launch(psf, t, precision, view, st));
     MLF_TRY(tc_col2im(psf, t, view, false, t->lfs.as<float>() + (int64_t)view * t->MP, st));
@@ -1510,11 +1761,13 @@ int tc_view_step(Solver* s, int precision, const float* d_lf, float* d_vol, int 
   MLF_TRY(launch_extract_views(d_lf, g, t->lfs.as<float>(), t->MP, 0, st));
   MLF_TRY(launch_to_phase(d_vol, g, t->X.as<float>(), st));
   MLF_CUDA(cudaMemcpyAsync(t->wscratch.p, &w, sizeof(float), cudaMemcpyHostToDevice, st));
+  if (prec_f16(precision)) MLF_TRY(tc_f16_prepare(s->psf, st));
   if (t->dtab_ok) MLF_TRY(tc_dtab_prepare(s->psf, precision, st));
+  MLF_TRY(tc_f16_begin(t, precision, st));
   MLF_TRY(tc_fwd_launch(s->psf, t, precision, view, st));
-  MLF_TRY(tc_col2im(s->psf, t, view, true, nullptr, st));
-  MLF_TRY(tc_im2col_ratio(s->psf, t, precision, st));
-  MLF_TRY(tc_bwd_launch(s->psf, t, precision, view, t->wscratch.as<float>(), st));
+  MLF_TRY(tc_col2im(s->psf, t, view, true, nullptr, st, precision, 0));
+  MLF_TRY(tc_im2col_ratio(s->psf, t, precision, st, 0));
+  MLF_TRY(tc_bwd_launch(s->psf, t, precision, view, t->wscratch.as<float>(), st, 0));
   MLF_TRY(launch_from_phase(t->X.as<float>(), g, d_vol, st));
   MLF_CUDA(cudaStreamSynchronize(st));
   return MLF_OK;

@@ -1,11 +1,12 @@
 // Inline-PTX building blocks for the sm_103a tensor-core (tcgen05) kernels: mbarriers with
-// bounded waits, TMA tile loads, TMEM allocation, tcgen05.mma (kind::f16, BF16 inputs,
-// FP32 accumulators), commits and TMEM loads, and the shared-memory / instruction
+// bounded waits, TMA tile loads, TMEM allocation, tcgen05.mma (kind::f16, BF16 or FP16
+// inputs -- both operands of one MMA the same type -- FP32 accumulators), commits and TMEM loads, and the shared-memory / instruction
 // descriptors for K-major operands in the 128-byte swizzled layout.
 #pragma once
 
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -163,6 +164,14 @@ __device__ __forceinline__ uint64_t desc_kmajor_sw128(uint32_t saddr) {
   d |= (uint64_t)1 << 46;                    // descriptor version (tcgen05)
   d |= (uint64_t)2 << 61;                    // SWIZZLE_128B
   return d;
+}
+
+// Instruction descriptor, kind::f16: FP16 x FP16 -> FP32, both operands K-major (A and B
+// formats 0 = F16).
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
+  return (1u << 4)                      // D format: F32
+         | ((uint32_t)(N >> 3) << 17)   // N / 8
+         | ((uint32_t)(M >> 4) << 24);  // M / 16
 }
 
 // Instruction descriptor, kind::f16: BF16 x BF16 -> FP32, both operands K-major.

@@ -40,7 +40,7 @@ def _patches(seed=0, K0=61, Z=7):
     return H, Ht, lfs
 
 
-@pytest.mark.parametrize("prec", ["bf16x2", "bf16x3"])
+@pytest.mark.parametrize("prec", ["bf16x2", "bf16x3", "fp16x2"])
 def test_batch_matches_single_solves(cuda, prec):
     from mesolf_gb300 import BatchSolver, PhaseSpacePSF, RLSolver
     H, Ht, lfs = _patches()

@@ -1,8 +1,8 @@
 """The 1005 x 1005 x 51 workload against its FP64 oracle fixture (tests/golden/
 lf1005x1005x51_k231.npz, made by make_golden_c2.py): relative L2 and max-abs error of the
 solve on the fixture's sample of 131072 voxels, per precision, after 3 (and 10, when the
-fixture holds it) iterations.  Bars: 1e-4 for FP32 and bf16x3, 1e-3 for bf16x2, 2e-3 for
-bf16 (single BF16 operands)."""
+fixture holds it) iterations.  Bars: 1e-4 for FP32, bf16x3 and fp16x3, 1e-3 for bf16x2, fp16x2 and fp16,
+2e-3 for bf16 (single BF16 operands)."""
 import os
 
 import numpy as np
@@ -13,7 +13,7 @@ from mesolf_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 FIX = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "lf1005x1005x51_k231.npz")
-BARS = {"fp32": 1e-4, "bf16x3": 1e-4, "bf16x2": 1e-3, "bf16": 2e-3}
+BARS = {"fp32": 1e-4, "bf16x3": 1e-4, "bf16x2": 1e-3, "bf16": 2e-3, "fp16x3": 1e-4, "fp16x2": 1e-3, "fp16": 1e-3}
 
 
 def errors(vol, g, it):
@@ -38,7 +38,7 @@ def setup(cuda):
     return g, s, lf
 
 
-@pytest.mark.parametrize("prec", ["fp32", "bf16x3", "bf16x2", "bf16"])
+@pytest.mark.parametrize("prec", ["fp32", "bf16x3", "bf16x2", "bf16", "fp16x3", "fp16x2", "fp16"])
 def test_against_fp64_oracle(setup, prec):
     g, s, lf = setup
     for it in (3, 10):

@@ -1,12 +1,16 @@
-"""Tensor-core (tcgen05, BF16 operands, FP32 accumulation) RL path against the FP64 oracle.
+"""Tensor-core (tcgen05, BF16 or FP16 operands, FP32 accumulation) RL path against the FP64
+oracle.
 
 Tolerances (relative L2), from the operand rounding of each mode:
-  bf16x3  (hi+lo split of taps and activations, 3 MMA passes)  1e-5 per projection,
-          1e-4 for a whole solve (the FP32 bar);
-  bf16x2  (activations split, taps single BF16)                 5e-3 per view step,
+  bf16x3 / fp16x3  (hi+lo split of taps and activations, 3 MMA passes)  1e-5 per projection,
+                   1e-4 for a whole solve (the FP32 bar);
+  bf16x2  (activations split, taps single BF16, 8 bits)     2e-3 per view step,
           1e-3 for a whole solve (the mixed-precision bar);
-  bf16    (single BF16)                                         5e-3 per view step,
-          2e-3 for a whole solve.
+  fp16x2  (activations split, taps single FP16, 11 bits)    5e-4 per view step, 1e-3 per solve;
+  bf16    (single BF16)                                     5e-3 per view step, 2e-3 per solve;
+  fp16    (single FP16)                                     1e-3 per view step, 1e-3 per solve.
+The FP16 modes scale every operand by a power of two into FP16's range (exact) and remove
+the scales in the FP32 epilogues.
 """
 import os
 
@@ -19,8 +23,9 @@ from mesolf_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-STEP_TOL = {"bf16x3": 1e-5, "bf16x2": 2e-3, "bf16": 5e-3}
-SOLVE_TOL = {"bf16x3": 1e-4, "bf16x2": 1e-3, "bf16": 2e-3}
+STEP_TOL = {"bf16x3": 1e-5, "bf16x2": 2e-3, "bf16": 5e-3, "fp16x3": 1e-5, "fp16x2": 5e-4, "fp16": 1e-3}
+SOLVE_TOL = {"bf16x3": 1e-4, "bf16x2": 1e-3, "bf16": 2e-3, "fp16x3": 1e-4, "fp16x2": 1e-3, "fp16": 1e-3}
+PRECS = ["bf16x3", "bf16x2", "bf16", "fp16x3", "fp16x2", "fp16"]
 
 
 def rel_l2(a, b):
@@ -39,7 +44,7 @@ CASES = [((5, 4), 61, 3), ((9, 8), 91, 2), ((6, 7), 231, 2), ((3, 3), 255, 2), (
 
 
 @pytest.mark.parametrize("lenslets,K0,Z", CASES)
-@pytest.mark.parametrize("prec", ["bf16x3", "bf16x2", "bf16"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_tc_forward_view(cuda, lenslets, K0, Z, prec):
     from mesolf_gb300 import PhaseSpacePSF, RLSolver
     w = synth.small_config(lenslets=lenslets, K0=K0, Z=Z)
@@ -54,12 +59,11 @@ def test_tc_forward_view(cuda, lenslets, K0, Z, prec):
     for (u, v) in [(7, 7), (0, 14), (13, 2)]:
         hx = s.forward_view(to_dev(vol), u, v, precision=prec).cpu().numpy()
         ref = R.forward_ps(Hps[:, :, u, v, :], vol.astype(np.float64), 15)
-        tol = STEP_TOL[prec] if prec != "bf16x3" else 1e-5
-        assert rel_l2(hx, ref) <= tol, (u, v, rel_l2(hx, ref))
+        assert rel_l2(hx, ref) <= STEP_TOL[prec], (u, v, rel_l2(hx, ref))
 
 
 @pytest.mark.parametrize("lenslets,K0,Z", CASES)
-@pytest.mark.parametrize("prec", ["bf16x3", "bf16x2", "bf16"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_tc_view_step(cuda, lenslets, K0, Z, prec):
     from mesolf_gb300 import PhaseSpacePSF, RLSolver
     w = synth.small_config(lenslets=lenslets, K0=K0, Z=Z)
@@ -77,7 +81,7 @@ def test_tc_view_step(cuda, lenslets, K0, Z, prec):
         assert rel_l2(got, ref) <= STEP_TOL[prec], (u, v, rel_l2(got, ref))
 
 
-@pytest.mark.parametrize("prec", ["bf16x3", "bf16x2", "bf16"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_tc_config1_solve_matches_golden(cuda, prec):
     """Nnum 15, 11x11 lenslets, 21 planes, K0 61, 8 RL iterations vs the FP64 oracle."""
     from mesolf_gb300 import PhaseSpacePSF, RLSolver
@@ -87,6 +91,7 @@ def test_tc_config1_solve_matches_golden(cuda, prec):
     s = RLSolver(psf, (165, 165))
     x8 = s.run(g["lf"], 8, precision=prec)
     err = rel_l2(x8, g["x8"])
+    print(f"config 1, 8 iterations, {prec}: rel L2 {err:.3e}")
     assert err <= SOLVE_TOL[prec], (prec, err)
 
 
@@ -98,7 +103,7 @@ def test_tc_solve_small_uneven(cuda):
     ref = R.recon_phase_space(LF, H, Ht, 2)
     psf = PhaseSpacePSF(H, Ht)
     s = RLSolver(psf, LF.shape)
-    for prec in ("bf16x3", "bf16x2"):
+    for prec in ("bf16x3", "bf16x2", "fp16x3", "fp16x2", "fp16"):
         got = s.run(to_dev(LF), 2, precision=prec).cpu().numpy()
         assert rel_l2(got, ref) <= SOLVE_TOL[prec], (prec, rel_l2(got, ref))
     # the FP32 path on the same solver still matches after tensor-core solves
