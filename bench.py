@@ -760,16 +760,29 @@ def precision_block(psf, dev):
     s = RLSolver(psf, g["lf"].shape)
     lf = _fortran(torch.as_tensor(g["lf"].astype(np.float32)).to(dev))[0]
     rows = []
+    stream = torch.cuda.current_stream()
     for prec in ("fp32", "bf16x3", "fp16x3", "bf16x2", "fp16x2", "bf16", "fp16"):
         for it in (3, 10):
             if f"x{it}" not in g:
                 continue
-            vol = s.run(lf, it, precision=prec, want_stats=False).cpu().numpy()
+            vol = s.run(lf, it, precision=prec, want_stats=False)
+            row = {"precision": prec, "iterations": it}
+            if it == 3:
+                # device time of this solve (image in HBM), 3 timed solves after this one
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(3):
+                    s.run(lf, it, precision=prec, out=vol, want_stats=False)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                row["ms_per_solve"] = e0.elapsed_time(e1) / 3
+            vol = vol.cpu().numpy()
             ref = g[f"x{it}"].astype(np.float64)
             got = vol.astype(np.float64).reshape(-1, order="F")[g["idx"]]
-            rows.append({"precision": prec, "iterations": it,
-                         "rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
-                         "max_abs": float(np.abs(got - ref).max()), "ref_max": float(np.abs(ref).max())})
+            row.update({"rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+                        "max_abs": float(np.abs(got - ref).max()), "ref_max": float(np.abs(ref).max())})
+            rows.append(row)
     s.close()
     return {"available": True, "sample_voxels": int(g["idx"].size), "vs": "FP64 oracle", "rows": rows}
 

@@ -55,7 +55,14 @@ constexpr int STAGES = 2;
 constexpr int TILE_A = BM * BK * 2;  // 16 KB
 constexpr uint32_t WAIT_LIMIT = 1u << 22;  // polls; ~0.3-1 s with the back-off sleep
 
-enum TcErr { TC_ERR_TIMEOUT_PRODUCER = 1, TC_ERR_TIMEOUT_MMA = 2, TC_ERR_TIMEOUT_EPILOGUE = 3 };
+// Device status word values (tc_check_error turns any of them into MLF_ERR_TIMEOUT).
+// TC_ERR_TIMEOUT_DRAIN: a wait for copies or MMAs already issued gave up while the CTA was
+// finishing.  The CTA still frees its TMEM: an MMA completes within microseconds, so a
+// commit that has not arrived after the wait limit (about a second) means the barrier
+// itself failed, and a CTA that exits holding TMEM would block the allocation of every
+// later CTA on its SM.
+enum TcErr { TC_ERR_TIMEOUT_PRODUCER = 1, TC_ERR_TIMEOUT_MMA = 2, TC_ERR_TIMEOUT_EPILOGUE = 3,
+             TC_ERR_TIMEOUT_DRAIN = 4 };
 
 // shared abort flag written by one role and polled by the others
 __device__ __forceinline__ bool aborted(const int* f) { return *reinterpret_cast<const volatile int*>(f) != 0; }
@@ -325,7 +332,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       }
       // drain: every issued copy must have landed before the CTA can exit
       for (int i = std::max(0, it - STAGES); i < it; ++i)
-        tc::mbar_wait(&full[i % STAGES], (i / STAGES) & 1, WAIT_LIMIT);
+        if (!tc::mbar_wait(&full[i % STAGES], (i / STAGES) & 1, WAIT_LIMIT)) atomicExch(a.err, TC_ERR_TIMEOUT_DRAIN);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -379,7 +386,7 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       }
       // every issued MMA must have completed before TMEM is released
       tc::mma_commit(&mdone);
-      tc::mbar_wait(&mdone, 0, WAIT_LIMIT);
+      if (!tc::mbar_wait(&mdone, 0, WAIT_LIMIT)) atomicExch(a.err, TC_ERR_TIMEOUT_DRAIN);
     }
     // ---------------- epilogue: update X in shared memory
   } else if (warp < BWD_IO_WARP) {
@@ -525,7 +532,8 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
       // loads not consumed (after an abort) must land before the CTA exits; a tile whose
       // stores were issued had its loads consumed
       for (int k = ti; k < issued; ++k)
-        for (int h = 0; h < 2; ++h) tc::mbar_wait(&xfull[k % XB][h], (k / XB) & 1, WAIT_LIMIT);
+        for (int h = 0; h < 2; ++h)
+          if (!tc::mbar_wait(&xfull[k % XB][h], (k / XB) & 1, WAIT_LIMIT)) atomicExch(a.err, TC_ERR_TIMEOUT_DRAIN);
     }
   }
   tc::tc_fence_before();
@@ -628,7 +636,7 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtenso
       ++issued;
     }
     for (int i = std::max(0, issued - S); i < issued; ++i)
-      tc::mbar_wait(&full[i % S], (i / S) & 1, WAIT_LIMIT);
+      if (!tc::mbar_wait(&full[i % S], (i / S) & 1, WAIT_LIMIT)) atomicExch(a.err, TC_ERR_TIMEOUT_DRAIN);
   } else if (warp == 1 && lane == 0) {
     const uint32_t idesc = F16 ? tc::idesc_f16_f32(BM, a.NH) : tc::idesc_bf16_f32(BM, a.NH);
     for (int ks = ks0; ks < ks1; ++ks) {
