@@ -284,6 +284,12 @@ constexpr int view_qpad(int q) { return (q + 3) & ~3; }
 constexpr int view_offmax(int q) { return (view_qpad(q) - q) > 2 ? (view_qpad(q) - q) : 2; }
 // float4 loads per window row: 4 outputs + T - 1 taps + the largest offset
 constexpr int view_nw(int T) { return (4 + T - 1 + view_offmax((T - 1) / 2) + 3) / 4; }
+// The view kernel's own tile (conv_rows in mlf_view.cuh): 4 b x 8 a, and its float4 loads
+// per window row (8 outputs + T - 1 taps + the largest offset).  The tile of conv_tile
+// above (8 b x 4 a) is the allocation-free forward projection's.
+constexpr int VW_TY = 4;
+constexpr int VW_TX = 8;
+constexpr int view_nw8(int T) { return (VW_TX + T - 1 + view_offmax((T - 1) / 2) + 3) / 4; }
 int prepare_view_kernels(int T, size_t smem);
 int occupancy_view_kernel(int T, int threads, size_t smem, int* blocks);
 int launch_view_kernel(int T, int mode, const ViewArgs& a, int grid, int threads, size_t smem,

@@ -554,18 +554,18 @@ int solver_init(Solver* s) {
   s->Pa = round_up(s->Li, 4);
   s->plane = (int64_t)s->Lj * s->Pa;
   if (s->lite) return MLF_OK;  // batch member: geometry now, filter plan and scratch on first solve
-  s->tilesA = ceil_div(s->Li, 4);
-  s->tilesB = ceil_div(s->Lj, 8);
+  s->tilesA = ceil_div(s->Li, VW_TX);
+  s->tilesB = ceil_div(s->Lj, VW_TY);
   s->tps = s->tilesA * s->tilesB;
   if (s->tps > 256)
     return fail(MLF_ERR_UNSUPPORTED, "patch of " + std::to_string(s->Li) + " x " +
                                          std::to_string(s->Lj) +
                                          " lenslets exceeds the 128 x 64 per-solve limit; tile the field of view");
-  const int NW = view_nw(s->T);
-  s->RP = round_up(4 * (s->tilesA - 1) + 4 * NW, 4);
-  s->RProws = s->tilesB * 8 + s->T + 1;
+  const int NW = view_nw8(s->T);
+  s->RP = round_up(VW_TX * (s->tilesA - 1) + 4 * NW, 4);
+  s->RProws = s->tilesB * VW_TY + s->T + 1;
   s->XP = s->RP;
-  s->XProws = s->tilesB * 8 + s->T - 1;
+  s->XProws = s->tilesB * VW_TY + s->T - 1;
 
   std::vector<int> clsA, clsB;
   std::vector<std::pair<int, int>> rngA[3], rngB[3];

@@ -11,9 +11,10 @@
 //   update   (:130-137)  X <- w*clean(X*C/D) + (1-w)*X, clamped at 0
 //
 // with sa = floor((alpha-u+h)/N), sb = floor((beta-v+h)/N).  One CTA owns one or more
-// channel slots; each thread of a slot owns an 8 (b) x 4 (a) output tile.  Inputs are
+// channel slots; each thread of a slot owns a 4 (b) x 8 (a) output tile.  Inputs are
 // staged in shared memory with zero halos, so the tap loops need no bounds checks; the
-// sliding windows are read with aligned 128-bit shared loads.  The X tile of a channel is
+// sliding windows are read with aligned 128-bit shared loads, each input row once per
+// tile (conv_rows).  The X tile of a channel is
 // copied with cp.async straight into the forward-input plane and updated there in place.
 // The forward partial sums of a CTA stay in registers across all its channels and are
 // written once (a second kernel reduces them in a fixed order).
@@ -25,6 +26,8 @@
 
 namespace mlf {
 
+// Tile of conv_tile (8 b x 4 a), used by the allocation-free forward projection
+// (mlf_noalloc.cu).
 constexpr int VT_TY = 8;  // tile rows (b direction)
 constexpr int VT_TX = 4;  // tile cols (a direction)
 
@@ -77,6 +80,53 @@ __device__ __forceinline__ void conv_tile(const float* __restrict__ in, int pitc
   }
 }
 
+// acc[ty][tx] += sum_{dy<T, dx<T} in[(ty+dy)*pitch + OFF + tx + dx] * w[dy*WP+dx]
+// for the 4 x 8 tile of the view kernel.  Walks the VW_TY + T - 1 input rows once: row r
+// is loaded into registers once and serves every output row ty with a tap row dy = r - ty
+// (tap rows come from shared memory as broadcast 16-byte loads), so the input window is
+// read once per tile instead of once per tap row.  Per output the products are still
+// added in the order dy, then dx -- the order of conv_tile -- so the results are the
+// same bit for bit.  `in` 16-byte aligned, pitch a multiple of 4, WP a multiple of 4.
+template <int T, int OFF, int WP>
+__device__ __forceinline__ void conv_rows(const float* __restrict__ in, int pitch, const float* __restrict__ w,
+                                          float (&acc)[VW_TY][VW_TX]) {
+  constexpr int NW = view_nw8(T);
+  static_assert(OFF + VW_TX + T - 1 <= 4 * NW, "window too short");
+  static_assert(WP % 4 == 0, "tap rows must be 16-byte aligned");
+#pragma unroll 1
+  for (int r = 0; r < VW_TY + T - 1; ++r) {
+    float win[4 * NW];
+    const float4* r4 = reinterpret_cast<const float4*>(in + r * pitch);
+#pragma unroll
+    for (int k = 0; k < NW; ++k) {
+      const float4 t4 = r4[k];
+      win[4 * k + 0] = t4.x;
+      win[4 * k + 1] = t4.y;
+      win[4 * k + 2] = t4.z;
+      win[4 * k + 3] = t4.w;
+    }
+#pragma unroll
+    for (int ty = 0; ty < VW_TY; ++ty) {
+      const int dy = r - ty;
+      if (dy < 0 || dy >= T) continue;
+      float wr[T];
+      const float4* w4 = reinterpret_cast<const float4*>(w + dy * WP);
+#pragma unroll
+      for (int k = 0; k < (T + 3) / 4; ++k) {
+        const float4 t4 = w4[k];
+        wr[4 * k] = t4.x;
+        if (4 * k + 1 < T) wr[4 * k + 1] = t4.y;
+        if (4 * k + 2 < T) wr[4 * k + 2] = t4.z;
+        if (4 * k + 3 < T) wr[4 * k + 3] = t4.w;
+      }
+#pragma unroll
+      for (int dx = 0; dx < T; ++dx)
+#pragma unroll
+        for (int tx = 0; tx < VW_TX; ++tx) acc[ty][tx] = fmaf(win[OFF + tx + dx], wr[dx], acc[ty][tx]);
+    }
+  }
+}
+
 __device__ __forceinline__ int floor_div(int a, int b) {
   int q = a / b;
   return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
@@ -107,7 +157,7 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
   const bool tile_ok = slot_ok && lt < A.tps;
   const int ta = lt % A.tilesA;
   const int tb = lt / A.tilesA;
-  const int a0 = ta * VT_TX, b0 = tb * VT_TY;
+  const int a0 = ta * VW_TX, b0 = tb * VW_TY;
 
   // ---- shared memory carve-up
   float* rs = sm;                                              // [RProws][RP] (BWD only)
@@ -130,11 +180,11 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
   }
   __syncthreads();
 
-  float hx[VT_TY][VT_TX];
+  float hx[VW_TY][VW_TX];
 #pragma unroll
-  for (int y = 0; y < VT_TY; ++y)
+  for (int y = 0; y < VW_TY; ++y)
 #pragma unroll
-    for (int x = 0; x < VT_TX; ++x) hx[y][x] = 0.f;
+    for (int x = 0; x < VW_TX; ++x) hx[y][x] = 0.f;
 
   const int h = (A.N - 1) / 2;
   const int64_t step = (int64_t)gridDim.x * A.slots;
@@ -158,13 +208,17 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
     const float* wbs = taps + buf * 2 * TTW;
     const float* wfs = wbs + TTW;
 
-    // ---- X tile -> forward-input plane (interior at rows +Q, cols +QP), asynchronously
+    // ---- X tile -> forward-input plane (interior at rows +Q, cols +QP), asynchronously.
+    // A plane row has Pa (a multiple of 4) floats: the second 16-byte half of the last tile
+    // may lie past it and is then not copied (its shared-memory cells stay zero).
     if (XIN && active && lt < A.tps) {
       const float* Xch = A.X + ch * A.plane;
 #pragma unroll
-      for (int y = 0; y < VT_TY; ++y) {
+      for (int y = 0; y < VW_TY; ++y) {
         const int b = b0 + y;
-        if (b < A.Lj) cp_async16(xin + (b + Q) * A.XP + a0 + QP, Xch + (int64_t)b * A.Pa + a0);
+        if (b >= A.Lj) continue;
+        cp_async16(xin + (b + Q) * A.XP + a0 + QP, Xch + (int64_t)b * A.Pa + a0);
+        if (a0 + 4 < A.Pa) cp_async16(xin + (b + Q) * A.XP + a0 + QP + 4, Xch + (int64_t)b * A.Pa + a0 + 4);
       }
     }
 
@@ -201,30 +255,30 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
       if (active && lt < A.tps && ph == 0 && !BWD) {
         cp_async_wait_all();  // forward only: this thread's X tile has landed in xin
       } else if (active && lt < A.tps) {
-        float acc[VT_TY][VT_TX];
+        float acc[VW_TY][VW_TX];
 #pragma unroll
-        for (int y = 0; y < VT_TY; ++y)
+        for (int y = 0; y < VW_TY; ++y)
 #pragma unroll
-          for (int x = 0; x < VT_TX; ++x) acc[y][x] = 0.f;
+          for (int x = 0; x < VW_TX; ++x) acc[y][x] = 0.f;
         const float* in = ph == 0 ? rs + (b0 + sb + 1) * A.RP + a0 : xin + b0 * A.XP + a0;
         const int pitch = ph == 0 ? A.RP : A.XP;
         const float* wsel = ph == 0 ? wbs : wfs;
         switch (ph == 0 ? sa + 1 : QP - Q) {
-          case 0: conv_tile<T, 0, TW>(in, pitch, wsel, acc); break;
-          case 1: conv_tile<T, 1, TW>(in, pitch, wsel, acc); break;
-          case 2: conv_tile<T, 2, TW>(in, pitch, wsel, acc); break;
+          case 0: conv_rows<T, 0, TW>(in, pitch, wsel, acc); break;
+          case 1: conv_rows<T, 1, TW>(in, pitch, wsel, acc); break;
+          case 2: conv_rows<T, 2, TW>(in, pitch, wsel, acc); break;
           default:
-            if constexpr (QP - Q == 3) conv_tile<T, 3, TW>(in, pitch, wsel, acc);
+            if constexpr (QP - Q == 3) conv_rows<T, 3, TW>(in, pitch, wsel, acc);
             break;
         }
         if (ph == 0) {
           if (MODE == MODE_BWDC) {
 #pragma unroll
-            for (int y = 0; y < VT_TY; ++y) {
+            for (int y = 0; y < VW_TY; ++y) {
               const int b = b0 + y;
               if (b >= A.Lj) continue;
 #pragma unroll
-              for (int x = 0; x < VT_TX; ++x)
+              for (int x = 0; x < VW_TX; ++x)
                 if (a0 + x < A.Li) A.Cout[ch * A.plane + (int64_t)b * A.Pa + a0 + x] = acc[y][x];
             }
           } else {
@@ -233,13 +287,13 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
             const int* cB = A.clsB + (sb + 1) * A.Lj;
             float* Xch = A.X + ch * A.plane;
 #pragma unroll
-            for (int y = 0; y < VT_TY; ++y) {
+            for (int y = 0; y < VW_TY; ++y) {
               const int b = b0 + y;
               if (b >= A.Lj) continue;
               const int cb = __ldg(cB + b);
               float* xrow = xin + (b + Q) * A.XP + a0 + QP;
 #pragma unroll
-              for (int x = 0; x < VT_TX; ++x) {
+              for (int x = 0; x < VW_TX; ++x) {
                 const int a = a0 + x;
                 if (a >= A.Li) continue;
                 const float c = acc[y][x];
@@ -256,9 +310,9 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
           }
         } else {
 #pragma unroll
-          for (int y = 0; y < VT_TY; ++y)
+          for (int y = 0; y < VW_TY; ++y)
 #pragma unroll
-            for (int x = 0; x < VT_TX; ++x) hx[y][x] += acc[y][x];
+            for (int x = 0; x < VW_TX; ++x) hx[y][x] += acc[y][x];
         }
       }
       if (ph == 0) __syncthreads();
@@ -285,11 +339,11 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
   __syncthreads();
   if (tile_ok) {
 #pragma unroll
-    for (int y = 0; y < VT_TY; ++y) {
+    for (int y = 0; y < VW_TY; ++y) {
       const int b = b0 + y;
       if (b >= A.Lj) continue;
 #pragma unroll
-      for (int x = 0; x < VT_TX; ++x) {
+      for (int x = 0; x < VW_TX; ++x) {
         const int a = a0 + x;
         if (a < A.Li) red[slot * LL + b * A.Li + a] = hx[y][x];
       }
