@@ -254,8 +254,29 @@ int mlf_batch_destroy(mlf_batch* b);
 int mlf_batch_plan_bytes(const mlf_psf* psf, int32_t npatch, const int64_t* Xr, const int64_t* Xc,
                          const int32_t* z0, const int32_t* nz, int64_t* bytes);
 int64_t mlf_batch_device_bytes(const mlf_batch* b);
+/* A run may leave patches out: lfimg[k] == NULL means patch k sits this run out (its
+ * weights are 0 for every view, so its tiles are skipped; warm[k] and vol_out[k] are not
+ * touched and may be NULL).  A serving loop sizes one work set for all its patches once and
+ * runs any subset of them, so no work set is created on the request path.  At least one
+ * patch must have an image. */
 int mlf_batch_run(mlf_batch* b, const float* const* lfimg, int32_t max_iter, int32_t precision,
                   const float* const* warm, float* const* vol_out, mlf_stats* stats, void* stream);
+
+/* Cancellation (failure handling of a serving loop: a request withdrawn while its solve
+ * runs).  mlf_batch_cancel / mlf_solver_cancel may be called from any host thread while a
+ * run of that work set is in progress: they set a word in mapped pinned host memory that
+ * the first CTA of every view-step kernel reads; from the next view step on, every kernel
+ * of the run returns at entry (before any barrier or TMEM allocation), and the run's output
+ * volumes are left unwritten (a warm-start volume passed as both warm and output keeps the
+ * previous frame).  A run with stats (synchronous) then returns MLF_ERR_CANCELLED; for a
+ * stream-ordered run, mlf_batch_cancelled / mlf_solver_cancelled tell, once the stream has
+ * been synchronised, whether the last run stopped early.  The next run clears the request
+ * when it starts.  No counterpart in the reference (its MATLAB loop has none; the peeling
+ * variant's retry loop, …_simple_peeling.m:122-178, restarts a failed solve instead). */
+int mlf_batch_cancel(mlf_batch* b);
+int mlf_batch_cancelled(const mlf_batch* b);
+int mlf_solver_cancel(mlf_solver* s);
+int mlf_solver_cancelled(const mlf_solver* s);
 
 /* One-shot form with the reference's argument order (H, Ht raw PSFs).  Builds the PSF
  * and a solver, runs, frees.  Synchronous. */

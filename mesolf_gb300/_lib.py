@@ -61,6 +61,10 @@ SIGNATURES = {
     "mlf_batch_destroy": (ctypes.c_int, [_vp]),
     "mlf_batch_device_bytes": (_i64, [_vp]),
     "mlf_batch_run": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp]),
+    "mlf_batch_cancel": (ctypes.c_int, [_vp]),
+    "mlf_batch_cancelled": (ctypes.c_int, [_vp]),
+    "mlf_solver_cancel": (ctypes.c_int, [_vp]),
+    "mlf_solver_cancelled": (ctypes.c_int, [_vp]),
     "mlf_solver_create_variant": (ctypes.c_int, [_vp, _i64, _i64, _i32, _vp]),
     "mlf_solver_run_peeling": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp]),
     "mlf_batch_plan_bytes": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, ctypes.POINTER(_i64)]),

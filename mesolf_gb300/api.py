@@ -360,6 +360,16 @@ class RLSolver:
         check(_lib.load().mlf_sample_filter(self._h, vol.data_ptr(), _stream_of(vol, stream)))
         return vol
 
+    def cancel(self):
+        """Ask the solve in progress (from another thread) to stop between view steps; its
+        output is left unwritten and a synchronous run raises MesoLFError (MLF_ERR_CANCELLED)."""
+        check(_lib.load().mlf_solver_cancel(self._h))
+
+    @property
+    def cancelled(self):
+        """True if the last solve stopped early (read after its stream was synchronised)."""
+        return bool(_lib.load().mlf_solver_cancelled(self._h))
+
     def close(self):
         if getattr(self, "_h", None):
             _lib.load().mlf_solver_destroy(self._h)
@@ -414,13 +424,20 @@ class BatchSolver:
         return int(out.value)
 
     def run(self, lfimgs, max_iter, precision="bf16x2", warm=None, outs=None, stream=None, want_stats=True):
-        """Device (torch CUDA) images in, list of (Xr, Xc, nz) device volumes out."""
+        """Device (torch CUDA) images in, list of (Xr, Xc, nz) device volumes out.  A None
+        image leaves that patch out of this run (its output entry is returned as given, or
+        None); at least one patch needs an image."""
         import torch
         lib = _lib.load()
         P = len(self.shapes)
         keep = []
         lp = (ctypes.c_void_p * P)()
+        first = next((im for im in lfimgs if im is not None), None)
+        if first is None:
+            raise ValueError("BatchSolver.run: no patch has an image")
         for k, im in enumerate(lfimgs):
+            if im is None:
+                continue
             t, ptr = _fortran(im)
             keep.append(t)
             lp[k] = ptr
@@ -433,15 +450,27 @@ class BatchSolver:
                     keep.append(t)
                     wp[k] = ptr
         if outs is None:
-            outs = [_empty_like_kind(lfimgs[k], (self.shapes[k][0], self.shapes[k][1], self.planes[k][1]))[0]
+            outs = [None if lfimgs[k] is None else
+                    _empty_like_kind(lfimgs[k], (self.shapes[k][0], self.shapes[k][1], self.planes[k][1]))[0]
                     for k in range(P)]
-        op = (ctypes.c_void_p * P)(*[o.data_ptr() for o in outs])
+        op = (ctypes.c_void_p * P)(*[(o.data_ptr() if (o is not None and lfimgs[k] is not None) else None)
+                                     for k, o in enumerate(outs)])
         st = MLFStats()
         check(lib.mlf_batch_run(self._h, lp, int(max_iter), PRECISIONS[precision], wp, op,
-                                ctypes.byref(st) if want_stats else None, _stream_of(lfimgs[0], stream)))
+                                ctypes.byref(st) if want_stats else None, _stream_of(first, stream)))
         self.last_stats = st.as_dict() if want_stats else None
         del keep
         return outs
+
+    def cancel(self):
+        """Ask the run in progress on this work set (from another thread) to stop between
+        view steps; its outputs are left unwritten (see mlf_batch_cancel)."""
+        check(_lib.load().mlf_batch_cancel(self._h))
+
+    @property
+    def cancelled(self):
+        """True if the last run stopped early (read after its stream was synchronised)."""
+        return bool(_lib.load().mlf_batch_cancelled(self._h))
 
     def forward_project(self, vols, raw_psf=True, precision="bf16x3", stream=None):
         """Full light-field images of device volumes (patch k: (Xr, Xc, nz) with the PSF

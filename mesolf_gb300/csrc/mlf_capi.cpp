@@ -678,16 +678,43 @@ int mlf_batch_run(mlf_batch* b, const float* const* lfimg, int32_t max_iter, int
   std::vector<const float*> lf(P), wm(P);
   std::vector<float*> out(P);
   std::vector<mlf::Solver*> ms;
+  size_t active = 0;
   for (size_t k = 0; k < P; ++k) {
     lf[k] = lfimg[k];
+    ms.push_back(b->members[k].get());
+    if (!lf[k]) continue;  // patch k sits this run out
+    ++active;
     wm[k] = warm ? warm[k] : nullptr;
     out[k] = vol_out[k];
-    if (!lf[k] || !out[k]) return fail(MLF_ERR_INVALID, "mlf_batch_run: null image or output pointer");
+    if (!out[k]) return fail(MLF_ERR_INVALID, "mlf_batch_run: null output pointer for a patch with an image");
     if (!is_device_ptr(lf[k]) || !is_device_ptr(out[k]) || (wm[k] && !is_device_ptr(wm[k])))
       return fail(MLF_ERR_INVALID, "mlf_batch_run: device pointers required");
-    ms.push_back(b->members[k].get());
   }
+  if (active == 0) return fail(MLF_ERR_INVALID, "mlf_batch_run: no patch has an image");
   return tc_run(b->work, ms, lf, wm, out, max_iter, precision, stats, ms[0], static_cast<cudaStream_t>(stream));
+}
+
+int mlf_batch_cancel(mlf_batch* b) {
+  if (!b) return fail(MLF_ERR_INVALID, "mlf_batch_cancel: null batch");
+  tc_cancel_state(b->work).request();
+  return MLF_OK;
+}
+
+int mlf_batch_cancelled(const mlf_batch* b) {
+  return (b && tc_cancel_state(b->work).stopped()) ? 1 : 0;
+}
+
+int mlf_solver_cancel(mlf_solver* s) {
+  if (!s) return fail(MLF_ERR_INVALID, "mlf_solver_cancel: null solver");
+  s->cancel.request();
+  if (s->tc) tc_cancel_state(s->tc).request();
+  return MLF_OK;
+}
+
+int mlf_solver_cancelled(const mlf_solver* s) {
+  if (!s) return 0;
+  if (s->last_run_tc) return (s->tc && tc_cancel_state(s->tc).stopped()) ? 1 : 0;
+  return s->cancel.stopped() ? 1 : 0;
 }
 
 int mlf_rl_solve(const float* lfimg, int64_t Xr, int64_t Xc, const float* H, const float* Ht,

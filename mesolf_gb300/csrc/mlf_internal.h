@@ -58,6 +58,36 @@ struct DevBuf {
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
+// Cancellation of a run in progress (mlf_solver_cancel / mlf_batch_cancel).  `req` is a
+// word of mapped pinned host memory that the host sets; thread 0 of the first CTA of every
+// view-step kernel (k_view, k_tc_bwd) reads it and, when set, raises `stop` (device memory,
+// which every CTA of every later kernel checks at entry before any barrier, so the rest of
+// the run's view steps return at once) and `stopped_host` (mapped, read by the host after
+// the stream is synchronised).  The kernels that write a run's outputs skip them when `stop`
+// is set, so a cancelled run leaves its outputs (e.g. a warm-start volume) as they were.
+// begin() clears the request on the host and both stop words in stream order.
+struct CancelState {
+  int* host = nullptr;      // [0] request (host writes), [1] stopped (device writes), mapped
+  int* req_dev = nullptr;   // device addresses of host[0] and host[1]
+  int* stopped_dev = nullptr;
+  DevBuf stop;              // int on the device: the kernels' entry check
+  CancelState() = default;
+  CancelState(const CancelState&) = delete;
+  CancelState& operator=(const CancelState&) = delete;
+  ~CancelState();
+  int init();                 // allocates: outside any stream capture
+  int begin(cudaStream_t st);
+  void request() const;       // any thread
+  bool stopped() const;       // after the run's stream has been synchronised
+};
+// the kernels' view of a CancelState (all null: not cancellable)
+struct CancelRef {
+  const int* req;
+  int* stopped_host;
+  int* stop;
+};
+inline CancelRef cancel_ref(const CancelState& c) { return CancelRef{c.req_dev, c.stopped_dev, c.stop.as<int>()}; }
+
 // Serialises CUDA graph captures against device memory allocation and release in this
 // library (cudaFree synchronises the device, which would invalidate a capture running
 // on another thread).  Recursive: releases can nest inside locked regions.
@@ -166,6 +196,8 @@ struct Solver {
   bool lite = false;            // batch member: geometry, filter plan and filter scratch only
   bool lite_ready = false;      // ... the latter two built by lite_prepare on the first solve
   int z0 = 0;                   // first PSF plane of this patch (batch members)
+  CancelState cancel;           // cancellation of the solver's plain FP32 runs
+  bool last_run_tc = false;     // the last run took the tensor-core path (its work set's CancelState)
   TcSolverState* tc = nullptr;  // built on the first tensor-core solve
   ~Solver();
   size_t bytes() const;
@@ -193,7 +225,8 @@ int forward_project(Solver* s, const float* d_vol, float* d_lf, const float* d_z
 int peel_solve(Solver* s, const float* d_lf, int max_iter, int precision, float* d_out, float* d_lf_peeled,
                float* d_proj, mlf_stats* stats, cudaStream_t st);
 inline float solver_d_eps(const Solver* s) { return s->variant == MLF_VARIANT_PEELING ? 1e-10f : 0.f; }
-int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st);
+// skip (nullable): a device word; the copy is skipped when it is non-zero (a cancelled run)
+int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st, const int* skip = nullptr);
 // flat initial guess sum(lf)/(Xr*Xc*Z) on the patch's planes, 0 on the other channels
 int launch_init_flat(const float* d_lf, const PatchGeo& g, float* X, double* scratch, cudaStream_t st);
 // Convergence monitor: rel = ||X - Xprev||_2 / ||X||_2 over n floats, both sums in FP64
@@ -228,6 +261,8 @@ int tc_forward_project(TcSolverState* w, const std::vector<Solver*>& members, co
                        const std::vector<float*>& lf_out, int precision, const float* zscale, cudaStream_t st);
 int tc_view_step(Solver* s, int precision, const float* d_lf, float* d_vol, int view, float w, cudaStream_t st);
 int tc_check_error(TcSolverState* w);
+// the work set's cancellation state (created with the work set)
+CancelState& tc_cancel_state(TcSolverState* w);
 size_t tc_psf_bytes(const Psf* p);
 size_t tc_solver_bytes(const Solver* s);
 size_t tc_work_bytes(const TcSolverState* w);
@@ -251,6 +286,20 @@ int launch_mex_pad_add(const float* src, int64_t W, int64_t H, int64_t Wp, int64
 int launch_mex_crop(const float* src, int64_t Wp, int64_t Hq, int64_t W, int64_t H, int64_t n, float* out,
                     cudaStream_t st);
 
+// Entry check of the cancellable kernels, by thread 0 (the caller broadcasts the result to
+// its CTA before any barrier): CTA 0 turns a host request into the stop words; every CTA
+// then returns when the device stop word is set.
+#ifdef __CUDACC__
+__device__ __forceinline__ int cancel_entry(const CancelRef& c) {
+  if (!c.stop) return 0;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && c.req && *reinterpret_cast<const volatile int*>(c.req) != 0) {
+    *reinterpret_cast<volatile int*>(c.stop) = 1;
+    *reinterpret_cast<volatile int*>(c.stopped_host) = 1;
+  }
+  return *reinterpret_cast<const volatile int*>(c.stop);
+}
+#endif
+
 // view kernels (instantiated per tap count T in mlf_view_T*.cu)
 struct ViewArgs {
   float* X;            // phase-major volume (read; written when updating)
@@ -271,6 +320,7 @@ struct ViewArgs {
   int64_t plane, nch;
   int tilesA, tilesB, tps, slots;
   int RP, RProws, XP, XProws, maxc, slot_floats;
+  CancelRef cancel;    // all null: not cancellable
 };
 enum ViewMode { MODE_FWD = 0, MODE_STEP = 1, MODE_BWDC = 2 };
 

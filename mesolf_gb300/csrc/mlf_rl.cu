@@ -84,7 +84,9 @@ __global__ void k_to_phase(const float* __restrict__ vol, PatchGeo g, float* __r
     X[phase_index(g, e)] = zscale ? vol[e] * zscale[e / (g.Xr * g.Xc)] : vol[e];
 }
 
-__global__ void k_from_phase(const float* __restrict__ X, PatchGeo g, float* __restrict__ vol) {
+__global__ void k_from_phase(const float* __restrict__ X, PatchGeo g, float* __restrict__ vol,
+                             const int* __restrict__ skip) {
+  if (skip && *reinterpret_cast<const volatile int*>(skip)) return;  // cancelled run: leave vol as it is
   const int64_t n = g.Xr * g.Xc * g.Z;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x)
@@ -276,6 +278,7 @@ ViewArgs view_args(Solver* s) {
   a.plane = s->plane; a.nch = s->nch;
   a.tilesA = s->tilesA; a.tilesB = s->tilesB; a.tps = s->tps; a.slots = s->slots;
   a.RP = s->RP; a.RProws = s->RProws; a.XP = s->XP; a.XProws = s->XProws; a.maxc = s->maxc;
+  a.cancel = CancelRef{nullptr, nullptr, nullptr};  // solves set it (enqueue_iteration)
   a.slot_floats = round_up(s->XProws * s->XP + 4 * s->T * view_tap_pitch(s->T) + s->maxc * s->maxc + s->T * s->maxc, 4);
   return a;
 }
@@ -340,9 +343,10 @@ int timing_mark(Solver* s, cudaStream_t st) {
 namespace {
 
 int run_view(Solver* s, int mode, int view_cur, int view_next, float w, bool do_fwd,
-             cudaStream_t st) {
+             cudaStream_t st, bool cancellable = false) {
   MLF_TRY(timing_mark(s, st));
   ViewArgs a = view_args(s);
+  if (cancellable) a.cancel = cancel_ref(s->cancel);
   const int N = s->N;
   a.u = view_cur % N;
   a.v = view_cur / N;
@@ -370,14 +374,14 @@ int enqueue_iteration(Solver* s, int64_t* launches, cudaStream_t st) {
   const int V = (int)views.size();
   int64_t n = 0;
   if (V > 0) {
-    MLF_TRY(run_view(s, MODE_FWD, views[0], views[0], 0.f, true, st));
+    MLF_TRY(run_view(s, MODE_FWD, views[0], views[0], 0.f, true, st, true));
     MLF_TRY(run_reduce(s, views[0], nullptr, true, st));
     n += 2;
     for (int k = 0; k < V; ++k) {
       const int cur = views[k];
       const bool more = k + 1 < V;
       const float w = (float)s->psf->weights[cur];
-      MLF_TRY(run_view(s, MODE_STEP, cur, more ? views[k + 1] : -1, w, more, st));
+      MLF_TRY(run_view(s, MODE_STEP, cur, more ? views[k + 1] : -1, w, more, st, true));
       ++n;
       if (more) {
         MLF_TRY(run_reduce(s, views[k + 1], nullptr, true, st));
@@ -392,6 +396,41 @@ int enqueue_iteration(Solver* s, int64_t* launches, cudaStream_t st) {
 }
 
 }  // namespace
+
+// ------------------------------------------------------------------ cancellation
+namespace {
+__global__ void k_cancel_begin(int* stop, int* stopped_host) {
+  *stop = 0;
+  *reinterpret_cast<volatile int*>(stopped_host) = 0;
+}
+}  // namespace
+
+CancelState::~CancelState() {
+  if (host) cudaFreeHost(host);
+}
+int CancelState::init() {
+  if (host) return MLF_OK;
+  MLF_CUDA(cudaHostAlloc((void**)&host, 64, cudaHostAllocMapped));
+  host[0] = host[1] = 0;
+  int* d = nullptr;
+  MLF_CUDA(cudaHostGetDevicePointer((void**)&d, host, 0));
+  req_dev = d;
+  stopped_dev = d + 1;
+  MLF_TRY(stop.alloc(sizeof(int), "cancellation word"));
+  MLF_CUDA(cudaMemset(stop.p, 0, sizeof(int)));
+  return MLF_OK;
+}
+int CancelState::begin(cudaStream_t st) {
+  MLF_TRY(init());
+  reinterpret_cast<volatile int*>(host)[0] = 0;
+  k_cancel_begin<<<1, 1, 0, st>>>(stop.as<int>(), stopped_dev);
+  MLF_LAUNCHED();
+  return MLF_OK;
+}
+void CancelState::request() const {
+  if (host) reinterpret_cast<volatile int*>(host)[0] = 1;
+}
+bool CancelState::stopped() const { return host && reinterpret_cast<const volatile int*>(host)[1] != 0; }
 
 Solver::~Solver() {
   for (cudaEvent_t e : tev) cudaEventDestroy(e);
@@ -429,8 +468,8 @@ int launch_scatter_views(const float* lfs, const PatchGeo& g, float* d_lf, int64
   MLF_LAUNCHED();
   return MLF_OK;
 }
-int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st) {
-  k_from_phase<<<grid_for(g.Xr * g.Xc * g.Z), 256, 0, st>>>(X, g, d_vol);
+int launch_from_phase(const float* X, const PatchGeo& g, float* d_vol, cudaStream_t st, const int* skip) {
+  k_from_phase<<<grid_for(g.Xr * g.Xc * g.Z), 256, 0, st>>>(X, g, d_vol, skip);
   MLF_LAUNCHED();
   return MLF_OK;
 }
@@ -636,8 +675,10 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
                float* d_out, mlf_stats* stats, cudaStream_t st) {
   if (precision != MLF_PREC_FP32) {
     MLF_TRY(tc_solver_prepare(s, st));
+    s->last_run_tc = true;
     return tc_run(s->tc, {s}, {d_lf}, {d_warm}, {d_out}, max_iter, precision, stats, s, st);
   }
+  s->last_run_tc = false;
   const PatchGeo g = solver_geo(s);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (stats) {
@@ -648,6 +689,8 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
   int64_t launches = 0;
   s->timing = stats != nullptr;
   s->tev_used = 0;
+  MLF_TRY(s->cancel.begin(st));
+  ++launches;
   MLF_TRY(launch_extract_views(d_lf, g, s->lfs.as<float>(), (int64_t)s->Li * s->Lj, 0, st));
   ++launches;
   if (d_warm) {
@@ -674,7 +717,7 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
       launches += 2;
     }
   }
-  MLF_TRY(launch_from_phase(s->X.as<float>(), g, d_out, st));
+  MLF_TRY(launch_from_phase(s->X.as<float>(), g, d_out, st, s->cancel.stop.as<int>()));
   ++launches;
   if (stats) {
     MLF_CUDA(cudaEventRecord(e1, st));
@@ -699,6 +742,11 @@ int solver_run(Solver* s, const float* d_lf, int max_iter, int precision, const 
     stats->fwd_splits = stats->fwd_stages = stats->bwd_xbufs = stats->tuned = 0;
     stats->rel_change = 0.0;
     if (monitor) MLF_TRY(rel_change_read(s->relbuf.as<double>(), &stats->rel_change));
+    if (s->cancel.stopped()) {
+      s->timing = false;
+      s->tev_used = 0;
+      return fail(MLF_ERR_CANCELLED, "solve cancelled between view steps; outputs left unwritten");
+    }
   }
   s->timing = false;
   s->tev_used = 0;

@@ -121,6 +121,7 @@ struct TcBwdArgs {
   float* rmax_next;     // the next view's slot, reset to 0 here for its col2im
   float* xmax;          // running maximum of X (the forward GEMM's scale), raised by the update
   const float* bscale;  // scale of each tap row of this view [CHP] (to scale d_eps with D)
+  CancelRef cancel;     // solves: stop between view steps when cancelled (null otherwise)
 };
 
 constexpr int BWD_BN = 128;                            // channels per tile
@@ -265,6 +266,12 @@ k_tc_bwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtens
          const __grid_constant__ CUtensorMap mA1, const __grid_constant__ CUtensorMap mBh,
          const __grid_constant__ CUtensorMap mBl, const __grid_constant__ CUtensorMap mX, TcBwdArgs a,
          int mtiles, int ntiles) {
+  {  // a cancelled solve: the rest of its view steps return at once (CTA-uniform, before TMEM)
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) s_stop = cancel_entry(a.cancel);
+    __syncthreads();
+    if (s_stop) return;
+  }
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull[XB][2], hdone[2][2], mdone;
@@ -556,6 +563,7 @@ struct TcFwdArgs {
   // FP16 modes only (null otherwise)
   const float* xmax;       // running maximum of X: the operand is X * f16_scale(xmax)
   const float* fsinv;      // inverse scales of the view's tap columns [NB]
+  CancelRef cancel;        // solves: stop between view steps when cancelled (null otherwise)
 };
 
 // The forward GEMM reads the FP32 volume directly: each stage's 32 KB region receives the
@@ -575,6 +583,12 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtenso
   // a patch that does not use this view needs no projection for it (whole CTA, before any
   // barrier or TMEM allocation)
   if (a.wview && __ldg(a.wview + __ldg(a.tile_patch + blockIdx.x)) == 0.f) return;
+  {  // a cancelled solve: the rest of its view steps return at once (CTA-uniform, before TMEM)
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) s_stop = cancel_entry(a.cancel);
+    __syncthreads();
+    if (s_stop) return;
+  }
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   __shared__ __align__(8) uint64_t full[FWD_MAX_STAGES], rdone[FWD_MAX_STAGES], conv[FWD_MAX_STAGES],
@@ -1043,6 +1057,10 @@ struct TcSolverState {
   // FP16 modes: the im2col of ones in FP16, and the operand scales' state: [0] running
   // maximum of X, [1], [2] max |R| of the even / odd view steps of an iteration
   DevBuf a1h, f16s;
+  CancelState cancel;       // cancellation of the work set's solves
+  // patches taking part in the weights now on the device (a run may leave patches out)
+  std::vector<char> active_dev;
+  std::vector<float> wtab_cur;  // the uploaded weights ([views][P], left-out patches 0)
   CUtensorMap mARh, mARl, mA1, mA1h, mXv;
   // One RL iteration (view loop + filters of every patch) as an instantiated CUDA graph,
   // per precision and with / without per-view timing nodes.  All buffers above are fixed
@@ -1257,6 +1275,8 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_TRY(t->a1.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->a1h.alloc((size_t)t->MP * tp->KB * 2, "tc im2col"));
   MLF_TRY(t->f16s.alloc(4 * sizeof(float), "tc FP16 operand scales"));
+  MLF_TRY(t->cancel.init());
+  t->active_dev.assign(t->P, 1);
   MLF_TRY(t->ypart.alloc((size_t)t->splits_max * t->MP * tp->NB * 4, "tc forward partials"));
   MLF_TRY(t->err.alloc(sizeof(int), "tc error flag"));
   t->dtab_ok = true;
@@ -1333,7 +1353,7 @@ PatchGeo work_geo(const TcSolverState* t, const Solver* m, int p) {
 
 // wview (nullable): per-patch weights of `view`; patches with weight 0 are not projected.
 int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cudaStream_t st,
-                  const float* wview = nullptr) {
+                  const float* wview = nullptr, bool cancellable = false) {
   const TcPsfState* tp = psf->tc;
   int alo, blo;
   splits_of(precision, &alo, &blo);
@@ -1353,6 +1373,7 @@ int tc_fwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, cud
   a.tile_patch = t->tile_patch.as<int>();
   a.pinfo = t->pinfo.as<int>();
   a.NN = psf->N * psf->N;
+  if (cancellable) a.cancel = cancel_ref(t->cancel);
   const bool use16 = prec_f16(precision);
   if (use16) {
     a.xmax = t->f16s.as<float>();
@@ -1420,7 +1441,7 @@ int tc_dtab_prepare(const Psf* psf, int precision, cudaStream_t st) {
 }
 
 int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, const float* wrow, cudaStream_t st,
-                  int slot = 0) {
+                  int slot = 0, bool cancellable = false) {
   const TcPsfState* tp = psf->tc;
   int alo, blo;
   splits_of(precision, &alo, &blo);
@@ -1441,6 +1462,7 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
   a.dtab = dgemm ? nullptr : dt.as<float>() + (int64_t)view * nc * nc * tp->CHP;
   a.q = q;
   a.ncls = nc;
+  if (cancellable) a.cancel = cancel_ref(t->cancel);
   if (use16) {
     a.rmax = t->f16s.as<float>() + 1 + slot;
     a.rmax_next = t->f16s.as<float>() + 1 + (slot ^ 1);
@@ -1485,17 +1507,18 @@ int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* ti
   int64_t n = 0;
   MLF_TRY(tc_f16_begin(t, precision, st, &n));
   MLF_TRY(timing_mark(timer, st));
-  MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[0], st, t->wtab_dev.as<float>()));
+  MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[0], st, t->wtab_dev.as<float>(), true));
   MLF_TRY(timing_mark(timer, st));
   MLF_TRY(tc_col2im(psf, t, t->views[0], true, nullptr, st, precision, 0));
   MLF_TRY(tc_im2col_ratio(psf, t, precision, st, 0));
   n += 3;
   for (int k = 0; k < V; ++k) {
     MLF_TRY(timing_mark(timer, st));
-    MLF_TRY(tc_bwd_launch(psf, t, precision, t->views[k], t->wtab_dev.as<float>() + (size_t)k * t->P, st, k & 1));
+    MLF_TRY(tc_bwd_launch(psf, t, precision, t->views[k], t->wtab_dev.as<float>() + (size_t)k * t->P, st, k & 1, true));
     ++n;
     if (k + 1 < V) {
-      MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[k + 1], st, t->wtab_dev.as<float>() + (size_t)(k + 1) * t->P));
+      MLF_TRY(tc_fwd_launch(psf, t, precision, t->views[k + 1], st, t->wtab_dev.as<float>() + (size_t)(k + 1) * t->P,
+                            true));
       MLF_TRY(timing_mark(timer, st));
       MLF_TRY(tc_col2im(psf, t, t->views[k + 1], true, nullptr, st, precision, (k + 1) & 1));
       MLF_TRY(tc_im2col_ratio(psf, t, precision, st, (k + 1) & 1));
@@ -1660,9 +1683,29 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
   timer->timing = stats != nullptr;
   timer->tev_used = 0;
   int64_t launches = 0;
+  // patches without an image sit this run out: their weights are 0 for every view (their
+  // tiles are skipped, their X left as it is) and nothing of theirs is read or written
+  {
+    std::vector<char> active(t->P);
+    for (int p = 0; p < t->P; ++p) active[p] = lf[p] != nullptr;
+    if (active != t->active_dev) {
+      const size_t V = t->views.size();
+      t->wtab_cur.assign(t->wtab.begin(), t->wtab.end());
+      for (size_t k = 0; k < V; ++k)
+        for (int p = 0; p < t->P; ++p)
+          if (!active[p]) t->wtab_cur[k * t->P + p] = 0.f;
+      if (!t->wtab_cur.empty())
+        MLF_CUDA(cudaMemcpyAsync(t->wtab_dev.p, t->wtab_cur.data(), t->wtab_cur.size() * sizeof(float),
+                                 cudaMemcpyHostToDevice, st));
+      t->active_dev = active;
+    }
+  }
+  MLF_TRY(t->cancel.begin(st));
+  ++launches;
   if (prec_f16(precision)) MLF_TRY(tc_f16_prepare(psf, st));
   if (t->dtab_ok) MLF_TRY(tc_dtab_prepare(psf, precision, st));
   for (int p = 0; p < t->P; ++p) {
+    if (!lf[p]) continue;
     const PatchGeo g = work_geo(t, members[p], p);
     float* Xp = t->X.as<float>() + t->pos0[p];
     MLF_TRY(launch_extract_views(lf[p], g, t->lfs.as<float>(), t->MP, t->pos0[p], st));
@@ -1695,7 +1738,9 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
     launches += g.launches * max_iter;
   }
   for (int p = 0; p < t->P; ++p) {
-    MLF_TRY(launch_from_phase(t->X.as<float>() + t->pos0[p], work_geo(t, members[p], p), out[p], st));
+    if (!lf[p]) continue;
+    MLF_TRY(launch_from_phase(t->X.as<float>() + t->pos0[p], work_geo(t, members[p], p), out[p], st,
+                              t->cancel.stop.as<int>()));
     ++launches;
   }
   if (stats) {
@@ -1725,11 +1770,18 @@ int tc_run(TcSolverState* t, const std::vector<Solver*>& members, const std::vec
     stats->rel_change = 0.0;
     if (monitor) MLF_TRY(rel_change_read(t->relbuf.as<double>(), &stats->rel_change));
     MLF_TRY(tc_check_error(t));
+    if (t->cancel.stopped()) {
+      timer->timing = false;
+      timer->tev_used = 0;
+      return fail(MLF_ERR_CANCELLED, "solve cancelled between view steps; outputs left unwritten");
+    }
   }
   timer->timing = false;
   timer->tev_used = 0;
   return MLF_OK;
 }
+
+CancelState& tc_cancel_state(TcSolverState* t) { return t->cancel; }
 
 // Forward projection of one view with the tensor cores (parity tests), single solver.
 int tc_forward_view(Solver* s, int precision, const float* d_vol, int view, float* hx_out, cudaStream_t st) {

@@ -159,6 +159,14 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
   const int tb = lt / A.tilesA;
   const int a0 = ta * VW_TX, b0 = tb * VW_TY;
 
+  // ---- a cancelled solve: the rest of its view steps return at once (CTA-uniform)
+  {
+    __shared__ int s_stop;
+    if (tid == 0) s_stop = cancel_entry(A.cancel);
+    __syncthreads();
+    if (s_stop) return;
+  }
+
   // ---- shared memory carve-up
   float* rs = sm;                                              // [RProws][RP] (BWD only)
   float* slot_base = rs + (BWD ? A.RProws * A.RP : 0);

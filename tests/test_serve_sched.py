@@ -87,3 +87,25 @@ def test_simulated_lanes_process_everything_once_in_order():
             inflight.append(reqs)
         assert len({r.patch for b in inflight for r in b}) == sum(len(b) for b in inflight)
     assert all(v == list(range(5)) for v in seen.values())
+
+
+def test_drop_stale_takes_the_newest_frame():
+    s = Scheduler(2, 2, lambda key: 0, lambda: 1, lambda: False, drop_stale=True)
+    for f in range(3):
+        s.add(Request(0, f, None, float(f)))
+    s.add(Request(1, 0, None, 0.5))
+    reqs = s.pick(lambda k: True)
+    assert [(r.patch, r.frame) for r in reqs] == [(0, 2), (1, 0)]
+    assert [(r.patch, r.frame) for r in s.dropped] == [(0, 0), (0, 1)]
+    assert s.pending() == 0
+
+
+def test_remove_queued_request():
+    s = make()
+    s.add(Request(0, 0, None, 0.0))
+    s.add(Request(0, 1, None, 0.1))
+    r = s.remove(0, 1)
+    assert r is not None and r.frame == 1
+    assert s.remove(0, 5) is None
+    assert [(x.patch, x.frame) for x in s.pick(lambda k: True)] == [(0, 0)]
+    assert s.pending() == 0
