@@ -214,11 +214,11 @@ def test_server_cancel_queued_and_running(cuda):
     H, Ht = synth.make_psf(61, 15, np.arange(7) - 3, seed=1)
     psf = PhaseSpacePSF(H, Ht)
     lfs = frames(H, n_frames=3)
-    srv = SolveServer(psf, GEO, iters=40, precision="bf16x2", lanes=1, max_batch=len(GEO))
+    srv = SolveServer(psf, GEO, iters=400, precision="bf16x2", lanes=1, max_batch=len(GEO))
     f0 = [srv.submit(p, 0, lfs[p, 0]) for p in range(len(GEO))]
     first = [np.array(f.result(timeout=300)) for f in f0]
     f1 = [srv.submit(p, 1, lfs[p, 1]) for p in range(len(GEO))]
-    time.sleep(0.05)
+    time.sleep(0.25)                                          # well inside the 400-iteration batch
     assert all(srv.cancel(p, 1) for p in range(len(GEO)))     # running (or still queued)
     f2q = srv.submit(0, 2, lfs[0, 2])
     for f in f1:
@@ -236,6 +236,6 @@ def test_server_cancel_queued_and_running(cuda):
         return _fortran(torch.as_tensor(np.ascontiguousarray(x)).cuda())[0]
     (xr, xc), planes = GEO[0]
     alone = BatchSolver(psf, [(xr, xc)], [planes])
-    want = alone.run([dev(lfs[0, 2])], 40, precision="bf16x2", warm=[dev(first[0])])[0].cpu().numpy()
+    want = alone.run([dev(lfs[0, 2])], 400, precision="bf16x2", warm=[dev(first[0])])[0].cpu().numpy()
     assert rel_l2(res2, want) <= 1e-5
     alone.close()
