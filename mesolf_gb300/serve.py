@@ -270,6 +270,11 @@ class SolveServer:
             "lanes": self.lanes,
         }
 
+    def latencies_ms(self):
+        """Latencies (ms) of the requests served since the last reset, in completion order."""
+        with self._lock:
+            return [1e3 * x for x in self._lat]
+
     def reset_stats(self):
         """Forget the latencies and throughput recorded so far (e.g. after a warm-up)."""
         with self._lock:
