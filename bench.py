@@ -178,6 +178,16 @@ def cpu_fft_sample(Xr, Xc, S, calls=3):
     return (time.perf_counter() - t0) / calls, E
 
 
+def progress(what):
+    """One line per finished block on stderr: elapsed time and the process's peak host memory."""
+    import resource
+    rss = resource.getrusage(resource.RUSAGE_SELF).ru_maxrss / 1024.0
+    print(f"[bench {time.perf_counter() - _T0:7.1f} s] {what} (peak RSS {rss:.0f} MB)", file=sys.stderr, flush=True)
+
+
+_T0 = time.perf_counter()
+
+
 def workload_config(ws, n_views):
     """The `config` of both arms' lines (the workload, not the implementation)."""
     return {"workload": WORKLOAD, "desc": WORKLOAD_DESC, "views_per_iteration": int(n_views),
@@ -448,24 +458,33 @@ def main():
     # the single-GPU extras (error table, MEX projector, serving stream, batched workload) run
     # at N = 1 only
     if ws == 1:
+        progress("main solve, mixed, e2e, CPU baseline")
         line["config1"] = config1_block(dev, cpu=not args.no_cpu_baseline)
+        progress("config1")
         line["mex_projector"] = mex_block(dev, peak)
+        progress("mex_projector")
         line["seed_library"] = seed_block(Ht, dev)
+        progress("seed_library")
         line["summary_image"] = summary_block(dev, cpu=not args.no_cpu_baseline)
+        progress("summary_image")
         line["rectification"] = rectify_block(dev, cpu=not args.no_cpu_baseline)
+        progress("rectification")
         solver.close()
         torch.cuda.empty_cache()
         line["precision_vs_fp64_oracle"] = precision_block(psf, dev)
+        progress("precision_vs_fp64_oracle")
     if ws == 1 and args.serve_seconds > 0 and args.mixed:
         solver.close()
         del out_dev, lf_dev
         torch.cuda.empty_cache()
         line["serving"] = serve_block(psf, args.serve_seconds, args.mixed, dev)
+        progress("serving")
     if ws == 1 and args.batched_steps > 0 and args.mixed:
         solver.close()
         psf.close()
         torch.cuda.empty_cache()
         line["batched"] = batched_block(args.mixed, dev, steps=args.batched_steps)
+        progress("batched")
     if rank == 0:
         print(json.dumps(line), flush=True)
     solver.close()
@@ -535,7 +554,6 @@ def serve_block(psf, seconds, precision, dev, pool=12, rate_hz=18.0, paced_frac=
 
     def stream(period_s, jitter, seconds_):
         rng_j = np.random.default_rng(3 + fno[0])
-        futs = []
         t0 = time.perf_counter() + 0.01
         t_next, n = t0, 0
         while t_next < t0 + seconds_:
@@ -543,21 +561,21 @@ def serve_block(psf, seconds, precision, dev, pool=12, rate_hz=18.0, paced_frac=
                 time.sleep(max(0.0, min(0.002, t_next - time.perf_counter())))
             fr = frames[fno[0] % pool]
             for p in range(P):
-                futs.append((t_next - t0, srv.submit(p, fno[0], fr[p], t_arrival=t_next)))
+                # the futures are not kept: a served volume is freed once its lane is done with it
+                srv.submit(p, fno[0], fr[p], t_arrival=t_next)
             fno[0] += 1
             n += 1
             t_next += period_s * (1.0 + (rng_j.uniform(-jitter, jitter) if jitter else 0.0))
         srv.drain()
-        return n, futs
+        return n
 
-    n_over, _ = stream(1.0 / rate_hz, 0.1, seconds)
+    n_over = stream(1.0 / rate_hz, 0.1, seconds)
     rep = srv.report()
     sustained = rep["voxels_per_s"] / frame_vox
     srv.reset_stats()
     slow_period = 1.0 / (paced_frac * sustained)
-    n_paced, futs = stream(slow_period, 0.0, seconds)
+    n_paced = stream(slow_period, 0.0, seconds)
     rep_slow = srv.report()
-    del futs
     # latencies of the paced leg in completion order: first and second half
     srv_lat = np.array(srv.latencies_ms())
     half = len(srv_lat) // 2

@@ -197,7 +197,8 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
   const int h = (A.N - 1) / 2;
   const int64_t step = (int64_t)gridDim.x * A.slots;
   const int64_t first = (int64_t)blockIdx.x * A.slots + slot;
-  // taps of the first channel into buffer 0
+  // taps of the first channel into buffer 0; the D row sums below read taps that other
+  // threads stored, so the barrier is needed before the first channel
   if (slot_ok && first < A.nch) {
     for (int i = lt; i < TT; i += A.tps) {
       const int j = (i / T) * TW + i % T;
@@ -205,6 +206,7 @@ __global__ void __launch_bounds__(256, 2) k_view(ViewArgs A) {
       if (XIN) taps[TTW + j] = __ldg(A.wf + first * TT + i);
     }
   }
+  __syncthreads();
   int buf = 0;
   for (int64_t base = (int64_t)blockIdx.x * A.slots; base < A.nch; base += step, buf ^= 1) {
     const int64_t ch = base + slot;
