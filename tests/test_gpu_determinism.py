@@ -18,7 +18,7 @@ def test_async_fp32_solves_are_bit_identical(cuda):
     H, Ht = w.psf()
     psf = PhaseSpacePSF(H, Ht)
     s = RLSolver(psf, w.image_shape)
-    lf = _fortran(torch.as_tensor(np.ascontiguousarray(w.measured(H, w.volume()))).cuda())[0]
+    lf = _fortran(torch.as_tensor(np.ascontiguousarray(w.measured(H, w.volume(), device="cuda"))).cuda())[0]
     base = s.run(lf, 2, want_stats=False).cpu().numpy()
     torch.cuda.synchronize()
     outs = [s.run(lf, 2, want_stats=False) for _ in range(8)]
