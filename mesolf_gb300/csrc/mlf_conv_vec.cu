@@ -9,57 +9,137 @@
 // (bitmap_end = x + kw/2 + 1) never reaches the last input column / row, so those are
 // treated as zero here too.
 //
-// All slices and output phases run in one launch (the reference issues one launch per
-// slice on 16 streams, :396-405).  Each CTA computes a 32 x 8 output tile of one slice
-// from a shared-memory input tile (tile + kernel halo, staged in row strips).
+// Direct kernel (k_conv_vec_rows).  The outputs of one row phase b = y % 15 share one set
+// of 15 kernels (one per x phase), so a CTA takes rows y = b + 15 j of one slice and a
+// thread owns a segment of 15 consecutive outputs x = 15 i + a, a = 0..14 -- one per x
+// phase.  Per kernel row ky the CTA stages its input rows and the 15 kernels' row ky
+// ([kx][a], padded to 16) in shared memory with zero-filling cp.async, double buffered so
+// that row ky + 1 loads while row ky is computed.  Along kx the thread slides a window of
+// 15 inputs in registers (one new shared load per step) and reads the step's 15 taps as
+// broadcast 16-byte loads shared by the whole CTA; kw is padded to a multiple of 15 with
+// zero taps so that the 15-step rotation of the window needs no tail.  Every output still adds its products in
+// the reference's order -- kernel rows in order, each row left to right, one FP32 FMA chain
+// (mex_lfm_convolution_vec.cu:147-251) -- and the products it adds beyond the reference's
+// clipped window multiply zero-filled inputs, which adds exactly 0 for finite kernels; so
+// the output equals the reference kernel's bit for bit (tests/test_gpu_ref_mex.py).
+#include <algorithm>
+
 #include "mlf_internal.h"
 
 namespace mlf {
 
 namespace {
 
-constexpr int CV_TX = 32, CV_TY = 8;   // output tile per CTA
-constexpr int CV_STRIP = 16;           // input rows staged per step
+constexpr int CV_NN = 15;            // kernels per axis (the reference's num_kernels)
+constexpr int CV_MAX_THREADS = 768;  // 85 registers a thread: no spills
 
-__global__ void __launch_bounds__(CV_TX * CV_TY)
-k_conv_vec(const float* __restrict__ in, int W, int H, const float* __restrict__ K, int kw, int nn,
-           float* __restrict__ out) {
-  extern __shared__ float tile[];  // [CV_STRIP + CV_TY - 1][CV_TX + kw - 1]
-  const int hk = kw / 2;
-  const int x0 = blockIdx.x * CV_TX, y0 = blockIdx.y * CV_TY;
-  const int i = blockIdx.z;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int x = x0 + tx, y = y0 + ty;
-  const int tw = CV_TX + kw - 1;
-  const int Wv = (kw % 2 == 0) ? W - 1 : W;  // even kw: last column / row never used
-  const int Hv = (kw % 2 == 0) ? H - 1 : H;
-  const float* src = in + (int64_t)i * W * H;
-  const float* Kp = K + (int64_t)((y % nn) * nn + (x % nn)) * kw * kw;
-  const int nthr = CV_TX * CV_TY, tid = ty * CV_TX + tx;
-  float acc = 0.f;
-  // input row for kernel row ky of output row y: y + ky - hk
-  for (int ky0 = 0; ky0 < kw; ky0 += CV_STRIP) {
-    const int nk = min(CV_STRIP, kw - ky0);
-    const int rows = nk + CV_TY - 1;
-    __syncthreads();
-    for (int e = tid; e < rows * tw; e += nthr) {
-      const int r = e / tw, c = e - r * tw;
-      const int gy = y0 + ky0 + r - hk, gx = x0 + c - hk;
-      float v = 0.f;
-      if (gy >= 0 && gy < Hv && gx >= 0 && gx < Wv) v = __ldg(src + (int64_t)gy * W + gx);
-      tile[e] = v;
-    }
-    __syncthreads();
-    if (x < W && y < H) {
-      for (int k = 0; k < nk; ++k) {
-        const float* trow = tile + (ty + k) * tw + tx;
-        const float* krow = Kp + (int64_t)(ky0 + k) * kw;
-#pragma unroll 8
-        for (int kx = 0; kx < kw; ++kx) acc = fmaf(trow[kx], __ldg(krow + kx), acc);
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+struct ConvRowsArgs {
+  const float* in;   // W x H x n slices (x fastest)
+  const float* K;    // kw x kw x 15 x 15 (kx fastest; kernel (a, b) at kw*kw*(a + 15 b))
+  float* out;
+  int W, H, kw, hk, Wv, Hv;  // Wv, Hv: columns / rows that can contribute (even kw: W-1, H-1)
+  int kwp;                   // kw rounded up to a multiple of 15 (the extra taps are zero)
+  int sx, sy, tilesX;        // CTA tile: sx segments of 15 outputs x sy rows of one row phase
+  int width, pitch;          // staged input row: 15 sx + kw - 1 floats, pitch odd
+  int64_t slice0;            // first slice of this launch
+};
+
+// Stage input rows (row phase b, rows j0.., kernel row ky) and the 15 kernels' row ky into
+// buffer sel (zero where the reference reads nothing), then commit the copies.
+__device__ __forceinline__ void conv_rows_stage(const ConvRowsArgs& A, float* sm, float* rows0, int rowbuf,
+                                                const float* src, const float* kb, int64_t kplane, int b,
+                                                int j0, int nJ, int cstart, int ky, int sel) {
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  float* rb = rows0 + sel * rowbuf;
+  for (int e = tid; e < A.sy * A.width; e += nthr) {
+    const int r_l = e / A.width, c = e - r_l * A.width;
+    const int r = b + CV_NN * (j0 + r_l) + ky - A.hk, col = cstart + c;
+    const bool ok = (j0 + r_l) < nJ && r >= 0 && r < A.Hv && col >= 0 && col < A.Wv;
+    cp_async4(rb + r_l * A.pitch + c, ok ? src + (int64_t)r * A.W + col : src, ok);
+  }
+  float* tb = sm + sel * 16 * A.kwp;
+  const float* krow = kb + (int64_t)A.kw * ky;
+  for (int e = tid; e < 16 * A.kwp; e += nthr) {
+    const int kx = e >> 4, a = e & 15;
+    const bool ok = a < CV_NN && kx < A.kw;
+    cp_async4(tb + e, ok ? krow + kplane * a + kx : kb, ok);
+  }
+  cp_async_commit();
+}
+
+__global__ void __launch_bounds__(CV_MAX_THREADS, 1) k_conv_vec_rows(ConvRowsArgs A) {
+  extern __shared__ __align__(16) float sm[];
+  const int b = blockIdx.y;                      // row phase
+  const int64_t slice = A.slice0 + blockIdx.z;
+  const int i0 = (blockIdx.x % A.tilesX) * A.sx; // first segment
+  const int j0 = (blockIdx.x / A.tilesX) * A.sy; // first row index of phase b
+  const int nJ = b < A.H ? (A.H - b + CV_NN - 1) / CV_NN : 0;
+  if (j0 >= nJ) return;                           // CTA-uniform
+  const int tid = threadIdx.x;
+  const int il = tid % A.sx, jl = tid / A.sx;
+  const int x_seg = CV_NN * (i0 + il);
+  const int y = b + CV_NN * (j0 + jl);
+  const bool mine = jl < A.sy && x_seg < A.W && y < A.H;
+  const int cstart = CV_NN * i0 - A.hk;          // input column of staged column 0
+  // taps first (16-byte aligned for the float4 loads), then the two row buffers
+  const int rowbuf = A.sy * A.pitch;
+  float* const rows0 = sm + 32 * A.kwp;  // buffer sel: taps sm + sel*16*kwp, rows rows0 + sel*rowbuf
+  const float* src = A.in + slice * (int64_t)A.W * A.H;
+  const int64_t kplane = (int64_t)A.kw * A.kw;
+  const float* kb = A.K + kplane * CV_NN * b;    // kernels (a, b), a = 0..14
+
+
+  float acc[CV_NN];
+#pragma unroll
+  for (int a = 0; a < CV_NN; ++a) acc[a] = 0.f;
+  conv_rows_stage(A, sm, rows0, rowbuf, src, kb, kplane, b, j0, nJ, cstart, 0, 0);
+  cp_async_wait0();
+  __syncthreads();
+  for (int ky = 0; ky < A.kw; ++ky) {
+    const int sel = ky & 1;
+    if (ky + 1 < A.kw) conv_rows_stage(A, sm, rows0, rowbuf, src, kb, kplane, b, j0, nJ, cstart, ky + 1, sel ^ 1);
+    if (mine) {
+      const float* rowp = rows0 + sel * rowbuf + jl * A.pitch + CV_NN * il;
+      const float* tp = sm + sel * 16 * A.kwp;
+      float w[CV_NN];  // w[(m + a) % 15] holds rowp[kx0 + m + a]
+#pragma unroll
+      for (int a = 0; a < CV_NN - 1; ++a) w[a] = rowp[a];
+      for (int kx0 = 0; kx0 < A.kwp; kx0 += CV_NN) {
+#pragma unroll
+        for (int m = 0; m < CV_NN; ++m) {
+          w[(m + CV_NN - 1) % CV_NN] = rowp[kx0 + m + CV_NN - 1];
+          const float4* t4 = reinterpret_cast<const float4*>(tp + 16 * (kx0 + m));
+          float t[16];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float4 v = t4[q];
+            t[4 * q] = v.x;
+            t[4 * q + 1] = v.y;
+            t[4 * q + 2] = v.z;
+            t[4 * q + 3] = v.w;
+          }
+#pragma unroll
+          for (int a = 0; a < CV_NN; ++a) acc[a] = fmaf(w[(m + a) % CV_NN], t[a], acc[a]);
+        }
       }
     }
+    cp_async_wait0();
+    __syncthreads();
   }
-  if (x < W && y < H) out[(int64_t)i * W * H + (int64_t)y * W + x] = acc;
+  if (mine) {
+    float* o = A.out + slice * (int64_t)A.W * A.H + (int64_t)y * A.W;
+#pragma unroll
+    for (int a = 0; a < CV_NN; ++a)
+      if (x_seg + a < A.W) o[x_seg + a] = acc[a];
+  }
 }
 
 // ---- tensor-core route: the correlation above (kernel slot from the OUTPUT pixel's phase)
@@ -146,12 +226,43 @@ int launch_mex_crop(const float* src, int64_t Wp, int64_t Hq, int64_t W, int64_t
 
 int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const float* d_kernels,
                  int64_t kw, int nnum, float* d_out, cudaStream_t st) {
-  const size_t smem = sizeof(float) * (size_t)(CV_STRIP + CV_TY - 1) * (CV_TX + kw - 1);
-  MLF_TRY(allow_max_dyn_smem((const void*)k_conv_vec));
-  const dim3 grid((unsigned)((W + CV_TX - 1) / CV_TX), (unsigned)((H + CV_TY - 1) / CV_TY), (unsigned)n);
-  k_conv_vec<<<grid, dim3(CV_TX, CV_TY), smem, st>>>(d_bitmap, (int)W, (int)H, d_kernels, (int)kw,
-                                                     nnum, d_out);
-  MLF_LAUNCHED();
+  if (nnum != CV_NN) return fail(MLF_ERR_INVALID, "direct MEX projector: the kernel grid must be 15 x 15");
+  if (W > (1 << 24) || H > (1 << 24) || W * H > ((int64_t)1 << 31))
+    return fail(MLF_ERR_UNSUPPORTED, "direct MEX projector: slice larger than 2^31 pixels");
+  int dev = 0, optin = 0;
+  MLF_CUDA(cudaGetDevice(&dev));
+  MLF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  MLF_TRY(allow_max_dyn_smem((const void*)k_conv_vec_rows));
+  ConvRowsArgs a{};
+  a.in = d_bitmap;
+  a.K = d_kernels;
+  a.out = d_out;
+  a.W = (int)W;
+  a.H = (int)H;
+  a.kw = (int)kw;
+  a.hk = (int)(kw / 2);
+  a.kwp = (a.kw + CV_NN - 1) / CV_NN * CV_NN;
+  a.Wv = (kw % 2 == 0) ? a.W - 1 : a.W;  // even kw: the reference's clip never reaches the last column / row
+  a.Hv = (kw % 2 == 0) ? a.H - 1 : a.H;
+  const int nI = (a.W + CV_NN - 1) / CV_NN, nJ = (a.H + CV_NN - 1) / CV_NN;
+  a.sx = std::min(nI, 32);
+  a.width = CV_NN * a.sx + a.kwp - 1;
+  a.pitch = a.width | 1;  // odd: rows of a warp fall on different banks
+  const size_t tap_bytes = sizeof(float) * 2 * 16 * (size_t)a.kwp;
+  const size_t budget = (size_t)optin - 1024;
+  a.sy = std::max(1, std::min(nJ, CV_MAX_THREADS / a.sx));
+  while (a.sy > 1 && sizeof(float) * 2 * (size_t)a.sy * a.pitch + tap_bytes > budget) --a.sy;
+  const size_t smem = sizeof(float) * 2 * (size_t)a.sy * a.pitch + tap_bytes;
+  if (smem > budget) return fail(MLF_ERR_UNSUPPORTED, "direct MEX projector: kernel row does not fit in shared memory");
+  a.tilesX = (nI + a.sx - 1) / a.sx;
+  const int tilesY = (nJ + a.sy - 1) / a.sy;
+  const int threads = (a.sx * a.sy + 31) / 32 * 32;
+  for (int64_t s0 = 0; s0 < n; s0 += 65535) {
+    a.slice0 = s0;
+    const dim3 grid((unsigned)(a.tilesX * tilesY), CV_NN, (unsigned)std::min<int64_t>(65535, n - s0));
+    k_conv_vec_rows<<<grid, threads, smem, st>>>(a);
+    MLF_LAUNCHED();
+  }
   return MLF_OK;
 }
 
