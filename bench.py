@@ -461,6 +461,8 @@ def main():
         progress("main solve, mixed, e2e, CPU baseline")
         line["config1"] = config1_block(dev, cpu=not args.no_cpu_baseline)
         progress("config1")
+        line["fft_formulation"] = fft_formulation_block(H, Ht, lf, psf, dev)
+        progress("fft_formulation")
         line["mex_projector"] = mex_block(dev, peak)
         progress("mex_projector")
         line["seed_library"] = seed_block(Ht, dev)
@@ -825,6 +827,120 @@ def precision_block(psf, dev):
             rows.append(row)
     s.close()
     return {"available": True, "sample_voxels": int(g["idx"].size), "vs": "FP64 oracle", "rows": rows}
+
+
+def fft_formulation_block(H, Ht, lf, psf, dev, steps=5):
+    """The reference's GPU-branch formulation of one RL view step (recon_..._with_filter.m:
+    109-137 with conv2FFT.m:1-22 on the exsize grid) on this GPU with cuFFT (torch.fft) and
+    the PSF spectra of the view precomputed (the reference recomputes them every call):
+    forward = Z R2C transforms of the volume planes, the spectral product summed over z, one
+    C2R; back projection = one R2C of the sparse ratio image, Z C2R for C and Z for D
+    (= bwd(ones), recomputed per view as the reference does).  A comparison measurement, not a
+    product path: the FP32 time per view, the bytes its transforms and spectra move, and the
+    error of its updated volume against the FP32 direct view step (mlf_rl_view_step) from the
+    same start -- in FP32 and, as a check of the formulation, in FP64, over all voxels and
+    over those where D is not round-off -- for the active view nearest the centre and for the
+    view of largest weight (a corner view, where D is exactly 0 near the image edge).
+    Spectra of all views would need 2 x 225 x Z x E x (E/2+1) x 8 B of HBM."""
+    import torch
+    from mesolf_gb300 import RLSolver
+    from mesolf_gb300.api import _fortran
+    from oracle import mesolf_ref as R
+    N = psf.N
+    Xr, Xc = lf.shape
+    Z = H.shape[4]
+    S = psf.S
+    E = R.ex_size((Xr, Xc), S)
+    m = S // 2
+    c0 = (N + 1) // 2 - 1
+    lf64 = torch.as_tensor(np.ascontiguousarray(lf), dtype=torch.float64, device=dev)
+    X0 = torch.full((Z, Xr, Xc), float(lf.sum()) / (lf.size * Z), dtype=torch.float64, device=dev)
+    X0 *= 1.0 + 0.1 * torch.rand(X0.shape, generator=torch.Generator(device=dev).manual_seed(3), device=dev,
+                                 dtype=torch.float64)
+    X0 = X0.float().double()                         # the same start, representable in FP32
+    s = RLSolver(psf, (Xr, Xc))
+    lf_d = _fortran(torch.as_tensor(np.ascontiguousarray(lf), dtype=torch.float32).to(dev))[0]
+
+    def view_case(u, v, timed):
+        h, t = R.phasespace_view(H, Ht, u, v)
+        w_uv = float(psf.weights[u, v])
+        kp = np.zeros((2, Z) + E)
+        kp[0, :, :S, :S] = np.moveaxis(h, 2, 0)
+        kp[1, :, :S, :S] = np.moveaxis(t, 2, 0)
+        kp = np.roll(kp, (-m, -m), axis=(2, 3))     # conv2FFT's circular re-centring
+        res = {"view": [u, v], "weight": w_uv}
+        ref = s.view_step(lf_d, _fortran(X0.float().permute(1, 2, 0).contiguous())[0], u, v, w_uv)
+        ref = ref.permute(2, 0, 1).double()
+        for dt, name in ((torch.float32, "fp32"), (torch.float64, "fp64")):
+            spec = torch.fft.rfft2(torch.as_tensor(kp, dtype=dt, device=dev))
+            Hs, Ts = spec[0], spec[1]
+            Xp = torch.zeros((Z,) + E, dtype=dt, device=dev)
+            Bp = torch.zeros(E, dtype=dt, device=dev)
+            Op = torch.zeros(E, dtype=dt, device=dev)
+            Op[u:Xr:N, v:Xc:N] = 1.0
+            ones_s = torch.fft.rfft2(Op)
+            X = X0.to(dt)
+            lft = lf64.to(dt)
+
+            def step():
+                Xp[:, :Xr, :Xc] = X
+                P = torch.fft.irfft2((torch.fft.rfft2(Xp) * Hs).sum(0), s=E)[:Xr, :Xc]
+                Rr = lft[u::N, v::N] / P[c0::N, c0::N]
+                Rr = torch.where(torch.isfinite(Rr), Rr, torch.zeros_like(Rr))
+                Bp.zero_()
+                Bp[u:Xr:N, v:Xc:N] = Rr
+                C = torch.fft.irfft2(torch.fft.rfft2(Bp) * Ts, s=E)[:, :Xr, :Xc]
+                D = torch.fft.irfft2(ones_s * Ts, s=E)[:, :Xr, :Xc]
+                Xn = X * C / D
+                Xn = torch.where(torch.isfinite(Xn) & (Xn >= 0), Xn, torch.zeros_like(Xn))
+                return torch.clamp(w_uv * Xn + (1 - w_uv) * X, min=0), D
+
+            out, D = step()
+            if name == "fp64":
+                # where the exact D is 0 (no sampled lenslet's kernel reaches the voxel) the
+                # transforms leave round-off of ~1e-16 of the peak, and C/D is a ratio of two
+                # round-off values; the direct form has exact zeros there (0/0 -> 0)
+                keep = D.abs() > 1e-9 * float(D.abs().max())
+                res["voxels_with_D_roundoff_only"] = float(1.0 - keep.double().mean())
+            if timed and name == "fp32":
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(steps):
+                    out, D = step()
+                e1.record()
+                torch.cuda.synchronize()
+                res["ms_per_view_fp32"] = e0.elapsed_time(e1) / steps
+            res[f"rel_l2_{name}_vs_fp32_direct"] = float((out.double() - ref).norm() / ref.norm())
+            if name == "fp64":
+                for nm, o in (("fp64", out.double()), ("fp32", out32.double())):
+                    d = torch.where(keep, o - ref, torch.zeros_like(ref))
+                    r = torch.where(keep, ref, torch.zeros_like(ref))
+                    res[f"rel_l2_{nm}_vs_fp32_direct_where_D_nonzero"] = float(d.norm() / r.norm())
+            else:
+                out32 = out
+            del spec, Hs, Ts, Xp, out, D
+            torch.cuda.empty_cache()
+        return res
+
+    W = psf.weights
+    h0 = (N - 1) // 2
+    act = [(abs(a - h0) + abs(b - h0), a, b) for a in range(N) for b in range(N) if W[a, b] != 0]
+    _, ua, va = min(act)                             # the active view nearest the centre
+    cases = [view_case(ua, va, True)]
+    uc, vc = (int(k) for k in np.unravel_index(int(np.argmax(W)), W.shape))
+    if (uc, vc) != (ua, va):
+        cases.append(view_case(uc, vc, False))
+    s.close()
+    spec_bytes = 2 * Z * E[0] * (E[1] // 2 + 1) * 8
+    ntrans = 3 * Z + 2
+    trans_bytes = ntrans * E[0] * (E[1] // 2 + 1) * 8 * 2
+    return {"exsize": list(E), "views": cases, "transforms_per_view": ntrans,
+            "spectra_bytes_per_view": spec_bytes, "transform_bytes_per_view_min": trans_bytes,
+            "hbm_bound_ms_per_view": (spec_bytes + trans_bytes + 8 * Xr * Xc * Z) / (_measured_hbm() or 6800) / 1e6,
+            "spectra_bytes_all_views": 225 * spec_bytes,
+            "note": "cuFFT (torch.fft) on this GPU, spectra of the view precomputed; comparison only"}
 
 
 def mex_block(dev, fp32_peak, steps=2):
