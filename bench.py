@@ -276,9 +276,10 @@ def main():
                     help="seconds of each leg of the 36-patch 18 Hz serving stream (0 to skip)")
     ap.add_argument("--batched-steps", type=int, default=1,
                     help="timed steps of the 64-patch batched workload (0 to skip)")
-    ap.add_argument("--only", choices=["summary", "rectify"], default=None,
-                    help="run only that block (summary image / frame rectification) on --frames frames, "
-                         "2 timed calls, no CPU or host leg, and exit (for ncu captures)")
+    ap.add_argument("--only", choices=["summary", "rectify", "mex"], default=None,
+                    help="run only that block (summary image / frame rectification on --frames frames; the "
+                         "direct MEX projector on --frames slices of the fixture shape), 2 timed calls, no CPU "
+                         "or host leg, and exit (for ncu captures)")
     ap.add_argument("--frames", type=int, default=2000)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -290,6 +291,8 @@ def main():
         dev0 = torch.device("cuda", 0)
         if args.only == "summary":
             blk = summary_block(dev0, T=args.frames, steps=2, cpu=False, e2e=False)
+        elif args.only == "mex":
+            blk = mex_direct_block(dev0, n=args.frames)
         else:
             blk = rectify_block(dev0, T=args.frames, steps=2, cpu=False, e2e=False)
         print(json.dumps({"only": args.only, "block": blk}), flush=True)
@@ -941,6 +944,29 @@ def fft_formulation_block(H, Ht, lf, psf, dev, steps=5):
             "hbm_bound_ms_per_view": (spec_bytes + trans_bytes + 8 * Xr * Xc * Z) / (_measured_hbm() or 6800) / 1e6,
             "spectra_bytes_all_views": 225 * spec_bytes,
             "note": "cuFFT (torch.fft) on this GPU, spectra of the view precomputed; comparison only"}
+
+
+def mex_direct_block(dev, n=8, kw=241, steps=2):
+    """The direct MEX kernel alone on n slices of the fixture shape (376 x 376, kw 241):
+    time per call and TFLOP/s (algorithmic 2*W*H*n*kw^2); for ncu captures."""
+    import torch
+    from mesolf_gb300 import mex_lfm_convolution_vec
+    W = Hh = 376
+    g = torch.Generator(device=dev)
+    g.manual_seed(9)
+    bm = torch.rand((n, Hh, W), generator=g, device=dev).permute(2, 1, 0)
+    K = torch.rand((15, 15, kw, kw), generator=g, device=dev).permute(3, 2, 1, 0)
+    mex_lfm_convolution_vec(bm, K, method="direct")
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        mex_lfm_convolution_vec(bm, K, method="direct")
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"W": W, "H": Hh, "n": n, "kw": kw, "ms_per_call": ms, "tflops": 2.0 * W * Hh * n * kw * kw / ms / 1e9}
 
 
 def mex_block(dev, fp32_peak, steps=2):
