@@ -181,7 +181,7 @@ struct Solver {
   DevBuf Xtmp;       // float [nch][plane]      scratch volume (back-projection output, filter)
   DevBuf lfs;        // float [N*N][Lj*Li]      sub-aperture images
   DevBuf rpad;       // float [RProws][RP]      halo-padded ratio image
-  DevBuf part;       // float [grid][Lj*Li]     per-CTA forward partials
+  DevBuf part;       // float [grid*slots][tilesB*VW_TY][tilesA*VW_TX] per-slot forward partials
   DevBuf hx;         // float [Lj*Li]           last forward projection
   DevBuf cls;        // int tables: clsA[3][Li], clsB[3][Lj], rngA[3][maxc][2], rngB[3][maxc][2]
   DevBuf red;        // double scratch for reductions
@@ -307,7 +307,7 @@ struct ViewArgs {
   const float* rpad;   // halo-padded ratio image
   const float* wb;     // backward taps of the current view [nch][T*T]
   const float* wf;     // forward taps of the view being projected [nch][T*T]
-  float* part;         // [gridDim.x][Lj*Li]
+  float* part;         // [gridDim.x * slots][tilesB*VW_TY][tilesA*VW_TX] forward partials
   const int* clsA;     // [3][Li]
   const int* clsB;     // [3][Lj]
   const int* rngA;     // [3][maxc][2]
@@ -339,6 +339,19 @@ constexpr int view_nw(int T) { return (4 + T - 1 + view_offmax((T - 1) / 2) + 3)
 // above (8 b x 4 a) is the allocation-free forward projection's.
 constexpr int VW_TY = 4;
 constexpr int VW_TX = 8;
+// threads per view-kernel CTA at most (two slots of up to 160 tiles)
+constexpr int kViewMaxThreads = 320;
+// Staged planes of the view kernel (ratio image, forward input) are stored with their
+// 16-byte column chunks swizzled: in every other 32-float block the chunks of each pair
+// trade places (column c lives at c ^ 4 when bit 5 of c is set), except a last chunk whose
+// partner lies past the row.  With a row pitch of 4 mod 8 floats and the lane order of the
+// view kernel, the 16-byte window loads of a warp meet 1.3 distinct rows per bank on
+// average (2.6 unswizzled) at the 67 x 67 lenslet patch.
+__host__ __device__ inline int view_pcol(int c, int pitch) {
+  return ((c & 32) && (c | 4) < pitch) ? (c ^ 4) : c;
+}
+// Smallest pitch >= need (floats) that is 4 mod 8.
+__host__ __device__ constexpr int view_plane_pitch(int need) { return ((need + 3) & ~7) + 4; }
 constexpr int view_nw8(int T) { return (VW_TX + T - 1 + view_offmax((T - 1) / 2) + 3) / 4; }
 int prepare_view_kernels(int T, size_t smem);
 int occupancy_view_kernel(int T, int threads, size_t smem, int* blocks);

@@ -202,31 +202,35 @@ __global__ void k_scatter_views(const float* __restrict__ lfs, PatchGeo g, float
   }
 }
 
-// HX = sum of the per-CTA forward partials (fixed order).  Optionally writes HX and the
+// HX = sum of the per-slot forward partials (fixed order).  Optionally writes HX and the
 // ratio image R = LF_sub ./ HX with non-finite -> 0 (recon_…_with_filter.m:116-117) into
-// the halo-padded buffer read by the next view kernel.
-// One block covers 32 positions (lanes); its 8 warps take the partials k = w, w+8, ... with
-// four accumulators each, and the warps' sums are added in a fixed order (deterministic).
+// the halo-padded buffer read by the next view kernel.  A partial plane holds row b of the
+// lenslet grid at b * HP (HP >= Li, the view kernel's tile-padded width), planes PPL floats
+// apart.  One block covers 32 positions (lanes); its 8 warps take the partials k = w, w+8,
+// ... with four accumulators each, and the warps' sums are added in a fixed order
+// (deterministic).
 constexpr int kReduceGroups = 8;
 __global__ void __launch_bounds__(32 * kReduceGroups)
-k_reduce_ratio(const float* __restrict__ part, int nparts, int Li, int Lj,
+k_reduce_ratio(const float* __restrict__ part, int nparts, int Li, int Lj, int HP, int64_t PPL,
                const float* __restrict__ lfsub, float* __restrict__ hx_out,
                float* __restrict__ rpad, int RP, int off) {
   __shared__ float sh[kReduceGroups][32];
   const int LL = Li * Lj;
   const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
   const int i = blockIdx.x * 32 + lane;
+  const int a = i % Li, b = i / Li;
+  const float* pp = part + (int64_t)b * HP + a;
   float s = 0.f;
   if (i < LL) {
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
     int k = grp;
     for (; k + 3 * kReduceGroups < nparts; k += 4 * kReduceGroups) {
-      s0 += part[(int64_t)k * LL + i];
-      s1 += part[(int64_t)(k + kReduceGroups) * LL + i];
-      s2 += part[(int64_t)(k + 2 * kReduceGroups) * LL + i];
-      s3 += part[(int64_t)(k + 3 * kReduceGroups) * LL + i];
+      s0 += pp[k * PPL];
+      s1 += pp[(k + kReduceGroups) * PPL];
+      s2 += pp[(k + 2 * kReduceGroups) * PPL];
+      s3 += pp[(k + 3 * kReduceGroups) * PPL];
     }
-    for (; k < nparts; k += kReduceGroups) s0 += part[(int64_t)k * LL + i];
+    for (; k < nparts; k += kReduceGroups) s0 += pp[k * PPL];
     s = (s0 + s1) + (s2 + s3);
   }
   sh[grp][lane] = s;
@@ -239,8 +243,7 @@ k_reduce_ratio(const float* __restrict__ part, int nparts, int Li, int Lj,
   if (rpad) {
     float r = lfsub[i] / hx;
     if (!isfinite(r)) r = 0.f;
-    const int a = i % Li, b = i / Li;
-    rpad[(b + off) * RP + a + off] = r;
+    rpad[(b + off) * RP + view_pcol(a + off, RP)] = r;  // swizzled plane columns
   }
 }
 
@@ -250,7 +253,7 @@ __global__ void k_fill_rpad(const float* __restrict__ proj, int Li, int Lj, floa
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= Li * Lj) return;
   const int a = i % Li, b = i / Li;
-  rpad[(b + off) * RP + a + off] = proj[i];
+  rpad[(b + off) * RP + view_pcol(a + off, RP)] = proj[i];  // swizzled plane columns
 }
 
 inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
@@ -361,8 +364,9 @@ int run_view(Solver* s, int mode, int view_cur, int view_next, float w, bool do_
 int run_reduce(Solver* s, int view, float* hx_out, bool ratio, cudaStream_t st) {
   const int LL = s->Li * s->Lj;
   const float* lfsub = s->lfs.as<float>() + (int64_t)view * LL;
+  const int HP = s->tilesA * VW_TX;
   k_reduce_ratio<<<ceil_div(LL, 32), 32 * kReduceGroups, 0, st>>>(
-      s->part.as<float>(), s->grid, s->Li, s->Lj, lfsub, hx_out,
+      s->part.as<float>(), s->grid * s->slots, s->Li, s->Lj, HP, (int64_t)s->tilesB * VW_TY * HP, lfsub, hx_out,
       ratio ? s->rpad.as<float>() : nullptr, s->RP, s->q + 1);
   MLF_LAUNCHED();
   return MLF_OK;
@@ -601,7 +605,7 @@ int solver_init(Solver* s) {
                                          std::to_string(s->Lj) +
                                          " lenslets exceeds the 128 x 64 per-solve limit; tile the field of view");
   const int NW = view_nw8(s->T);
-  s->RP = round_up(VW_TX * (s->tilesA - 1) + 4 * NW, 4);
+  s->RP = view_plane_pitch(VW_TX * (s->tilesA - 1) + 4 * NW);
   s->RProws = s->tilesB * VW_TY + s->T + 1;
   s->XP = s->RP;
   s->XProws = s->tilesB * VW_TY + s->T - 1;
@@ -633,9 +637,18 @@ int solver_init(Solver* s) {
   int dev_smem = 0, nsm = 0;
   MLF_CUDA(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
   MLF_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device));
-  // small patches: several channel slots per CTA, as many as the shared memory holds
-  const int64_t fit = ((int64_t)dev_smem / (int64_t)sizeof(float) - (int64_t)s->RProws * s->RP) / slot_floats;
-  s->slots = s->tps >= 128 ? 1 : std::max(1, std::min({32, 192 / s->tps, (int)std::max<int64_t>(1, fit)}));
+  // Channel slots per CTA (they share the staged ratio image).  Small patches: as many as
+  // the shared memory holds, up to 192 threads.  Patches of 128..160 tiles: two slots when
+  // two such CTAs fit an SM's shared memory (20 warps per SM instead of 15); larger: one.
+  const int64_t R_floats = (int64_t)s->RProws * s->RP;
+  const int64_t fit = ((int64_t)dev_smem / (int64_t)sizeof(float) - R_floats) / slot_floats;
+  int sm_per_sm = 0;
+  MLF_CUDA(cudaDeviceGetAttribute(&sm_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->device));
+  const int64_t two_slot_bytes = (int64_t)sizeof(float) * (R_floats + 2 * (int64_t)slot_floats);
+  if (s->tps < 128)
+    s->slots = std::max(1, std::min({32, 192 / s->tps, (int)std::max<int64_t>(1, fit)}));
+  else
+    s->slots = (2 * s->tps <= kViewMaxThreads && 2 * (two_slot_bytes + 1024) <= sm_per_sm) ? 2 : 1;
   s->threads = round_up(s->slots * s->tps, 32);
   s->smem = sizeof(float) * ((size_t)s->RProws * s->RP + (size_t)s->slots * slot_floats);
   if ((int)s->smem > dev_smem) return fail(MLF_ERR_UNSUPPORTED, "view kernel shared memory exceeds the device limit");
@@ -652,7 +665,8 @@ int solver_init(Solver* s) {
   MLF_TRY(s->Xtmp.alloc(vol * sizeof(float), "scratch volume"));
   MLF_TRY(s->lfs.alloc((size_t)s->N * s->N * LL * sizeof(float), "sub-aperture images"));
   MLF_TRY(s->rpad.alloc((size_t)s->RProws * s->RP * sizeof(float), "ratio image"));
-  MLF_TRY(s->part.alloc((size_t)s->grid * LL * sizeof(float), "forward partials"));
+  MLF_TRY(s->part.alloc((size_t)s->grid * s->slots * (s->tilesB * VW_TY) * (s->tilesA * VW_TX) * sizeof(float),
+                        "forward partials"));
   MLF_TRY(s->hx.alloc(LL * sizeof(float), "forward projection"));
   MLF_TRY(s->red.alloc(4096 * sizeof(double), "reduction scratch"));
   MLF_CUDA(cudaMemset(s->X.p, 0, s->X.bytes));
