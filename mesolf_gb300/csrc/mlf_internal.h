@@ -173,7 +173,7 @@ struct Solver {
   int64_t plane = 0;   // floats per plane (Lj * Pa)
   int64_t nch = 0;
   // view-kernel geometry
-  int tilesA = 0, tilesB = 0, tps = 0, slots = 0, threads = 0, grid = 0;
+  int tilesA = 0, tilesB = 0, tps = 0, slots = 0, tstride = 0, threads = 0, grid = 0;
   int RP = 0, RProws = 0, XP = 0, XProws = 0, maxc = 0;
   size_t smem = 0;
   int ncA[3] = {0, 0, 0}, ncB[3] = {0, 0, 0};
@@ -318,7 +318,7 @@ struct ViewArgs {
   int do_fwd;          // MODE_STEP: also project with wf
   int N, Z, Li, Lj, Pa, q;
   int64_t plane, nch;
-  int tilesA, tilesB, tps, slots;
+  int tilesA, tilesB, tps, slots, tstride;  // tstride: threads per slot (>= tps)
   int RP, RProws, XP, XProws, maxc, slot_floats;
   CancelRef cancel;    // all null: not cancellable
 };

@@ -279,7 +279,7 @@ ViewArgs view_args(Solver* s) {
   a.d_eps = solver_d_eps(s);
   a.N = s->N; a.Z = s->Z; a.Li = s->Li; a.Lj = s->Lj; a.Pa = s->Pa; a.q = s->q;
   a.plane = s->plane; a.nch = s->nch;
-  a.tilesA = s->tilesA; a.tilesB = s->tilesB; a.tps = s->tps; a.slots = s->slots;
+  a.tilesA = s->tilesA; a.tilesB = s->tilesB; a.tps = s->tps; a.slots = s->slots; a.tstride = s->tstride;
   a.RP = s->RP; a.RProws = s->RProws; a.XP = s->XP; a.XProws = s->XProws; a.maxc = s->maxc;
   a.cancel = CancelRef{nullptr, nullptr, nullptr};  // solves set it (enqueue_iteration)
   a.slot_floats = round_up(s->XProws * s->XP + 4 * s->T * view_tap_pitch(s->T) + s->maxc * s->maxc + s->T * s->maxc, 4);
@@ -649,7 +649,10 @@ int solver_init(Solver* s) {
     s->slots = std::max(1, std::min({32, 192 / s->tps, (int)std::max<int64_t>(1, fit)}));
   else
     s->slots = (2 * s->tps <= kViewMaxThreads && 2 * (two_slot_bytes + 1024) <= sm_per_sm) ? 2 : 1;
-  s->threads = round_up(s->slots * s->tps, 32);
+  // several slots: each starts on a warp boundary when that costs no extra warp
+  s->tstride = (s->slots > 1 && round_up(s->slots * round_up(s->tps, 32), 32) == round_up(s->slots * s->tps, 32))
+                   ? round_up(s->tps, 32) : s->tps;
+  s->threads = round_up(s->slots * s->tstride, 32);
   s->smem = sizeof(float) * ((size_t)s->RProws * s->RP + (size_t)s->slots * slot_floats);
   if ((int)s->smem > dev_smem) return fail(MLF_ERR_UNSUPPORTED, "view kernel shared memory exceeds the device limit");
   MLF_TRY(prepare_view_kernels(s->T, s->smem));

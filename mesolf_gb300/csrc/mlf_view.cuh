@@ -89,18 +89,21 @@ __device__ __forceinline__ void conv_tile(const float* __restrict__ in, int pitc
 // acc[ty][tx] += sum_{dy<T, dx<T} in[(ty+dy)*pitch + col(OFF + tx + dx)] * w[dy*WP+dx]
 // for the 4 x 8 tile of the view kernel, on a plane whose columns are swizzled in 16-byte
 // chunks: chunk k of this thread's window (columns a0 + 4k .. a0 + 4k + 3) starts at column
-// off[k] of a row (view_pcol).  Walks the VW_TY + T - 1 input rows once: row r is loaded
+// view_pcol(a0 + 4k, pitch) of a row.  Walks the VW_TY + T - 1 input rows once: row r is loaded
 // into registers once and serves every output row ty with a tap row dy = r - ty (tap rows
 // come from shared memory as broadcast 16-byte loads), so the input window is read once
 // per tile instead of once per tap row.  Per output the products are added in the order
 // dy, then dx -- the order of conv_tile -- so the results are the same bit for bit.
-// `in` and every in + off[k] 16-byte aligned, pitch a multiple of 4, WP a multiple of 4.
+// `in` 16-byte aligned, a0 and pitch multiples of 4, WP a multiple of 4.
 template <int T, int OFF, int WP>
-__device__ __forceinline__ void conv_rows(const float* __restrict__ in, int pitch, const int (&off)[view_nw8(T)],
+__device__ __forceinline__ void conv_rows(const float* __restrict__ in, int pitch, int a0,
                                           const float* __restrict__ w, float (&acc)[VW_TY][VW_TX]) {
   constexpr int NW = view_nw8(T);
   static_assert(OFF + VW_TX + T - 1 <= 4 * NW, "window too short");
   static_assert(WP % 4 == 0, "tap rows must be 16-byte aligned");
+  int off[NW];
+#pragma unroll
+  for (int k = 0; k < NW; ++k) off[k] = view_pcol(a0 + 4 * k, pitch);
 #pragma unroll 1
   for (int r = 0; r < VW_TY + T - 1; ++r) {
     float win[4 * NW];
@@ -155,7 +158,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
 //   dtab[cb][ca] = sum_{dj in rngB[sb][cb]} rowp[dj][ca]
 // Both add in index order, so the values do not depend on the launch shape.
 template <int T>
-__device__ __forceinline__ void view_d_rows(const ViewArgs& A, int64_t ch, int lt, float* rowp) {
+__device__ __forceinline__ void view_d_rows(const ViewArgs& A, int ch, int lt, float* rowp) {
   const int h = (A.N - 1) / 2;
   const int alpha = (int)((ch / A.Z) % A.N);
   const int sa = floor_div(alpha - A.u + h, A.N);
@@ -164,22 +167,33 @@ __device__ __forceinline__ void view_d_rows(const ViewArgs& A, int64_t ch, int l
   for (int i = lt; i < T * A.maxc; i += A.tps) {
     const int dj = i / A.maxc, ca = i - dj * A.maxc;
     const int lo = __ldg(rA + 2 * ca), hi = __ldg(rA + 2 * ca + 1);
+    float v[T];  // the whole tap row in flight at once; the sum takes [lo, hi] in order
+#pragma unroll
+    for (int di = 0; di < T; ++di) v[di] = __ldg(w + dj * T + di);
     float s = 0.f;
-    for (int di = lo; di <= hi; ++di) s += __ldg(w + dj * T + di);
+#pragma unroll
+    for (int di = 0; di < T; ++di)
+      if (di >= lo && di <= hi) s += v[di];
     rowp[i] = s;
   }
 }
-__device__ __forceinline__ void view_d_table(const ViewArgs& A, int64_t ch, int lt, const float* rowp,
+template <int T>
+__device__ __forceinline__ void view_d_table(const ViewArgs& A, int ch, int lt, const float* rowp,
                                              float* dtab) {
   const int h = (A.N - 1) / 2;
-  const int beta = (int)(ch / ((int64_t)A.Z * A.N));
+  const int beta = ch / (A.Z * A.N);
   const int sb = floor_div(beta - A.v + h, A.N);
   const int* rB = A.rngB + (sb + 1) * A.maxc * 2;
   for (int i = lt; i < A.maxc * A.maxc; i += A.tps) {
     const int cb = i / A.maxc, ca = i - cb * A.maxc;
     const int lo = __ldg(rB + 2 * cb), hi = __ldg(rB + 2 * cb + 1);
+    float v[T];
+#pragma unroll
+    for (int dj = 0; dj < T; ++dj) v[dj] = rowp[dj * A.maxc + ca];
     float s = 0.f;
-    for (int dj = lo; dj <= hi; ++dj) s += rowp[dj * A.maxc + ca];
+#pragma unroll
+    for (int dj = 0; dj < T; ++dj)
+      if (dj >= lo && dj <= hi) s += v[dj];
     dtab[i] = s;
   }
 }
@@ -196,9 +210,9 @@ __global__ void __launch_bounds__(kViewMaxThreads, 2) k_view(ViewArgs A) {
   constexpr bool BWD = (MODE != MODE_FWD);
   constexpr bool XIN = (MODE != MODE_BWDC);
   const int tid = threadIdx.x;
-  const int slot = tid / A.tps;
-  const int lt = tid - slot * A.tps;  // thread index within slot
-  const bool slot_ok = slot < A.slots;
+  const int slot = tid / A.tstride;          // slots start at multiples of tstride >= tps
+  const int lt = tid - slot * A.tstride;     // thread index within slot
+  const bool slot_ok = slot < A.slots && lt < A.tps;
   // tile of this thread: with more than 8 tile columns, lanes 8k .. 8k+7 take columns 0..7
   // of one tile row (a 64-float span, so a warp's window loads spread over all banks) and
   // the remaining columns follow; fewer columns: row-major
@@ -215,13 +229,8 @@ __global__ void __launch_bounds__(kViewMaxThreads, 2) k_view(ViewArgs A) {
     tb = lt / A.tilesA;
   }
   const int a0 = ta * VW_TX, b0 = tb * VW_TY;
-  // swizzled start columns of the 16-byte chunks of this thread's window (both staged
-  // planes have pitch RP == XP)
-  constexpr int NWIN = view_nw8(T);
-  int woff[NWIN];
-#pragma unroll
-  for (int k = 0; k < NWIN; ++k) woff[k] = view_pcol(a0 + 4 * k, A.RP);
-  const int xc0 = view_pcol(a0 + QP, A.XP), xc1 = view_pcol(a0 + QP + 4, A.XP);  // this tile's X chunks
+  // swizzled columns of this tile's two X chunks in the forward-input plane
+  const int xc0 = view_pcol(a0 + QP, A.XP), xc1 = view_pcol(a0 + QP + 4, A.XP);
 
   // ---- a cancelled solve: the rest of its view steps return at once (CTA-uniform)
   {
@@ -253,8 +262,10 @@ __global__ void __launch_bounds__(kViewMaxThreads, 2) k_view(ViewArgs A) {
 
   constexpr bool DT = (MODE == MODE_STEP);  // the update needs D
   const int h = (A.N - 1) / 2;
-  const int64_t step = (int64_t)gridDim.x * A.slots;
-  const int64_t first = (int64_t)blockIdx.x * A.slots + slot;
+  // channel indices fit in 32 bits (N*N*Z <= 225 * 4096)
+  const int nch = (int)A.nch;
+  const int step = (int)gridDim.x * A.slots;
+  const int first = (int)blockIdx.x * A.slots + slot;
   // this thread's tile in its slot's forward partial plane [tilesB*VW_TY][tilesA*VW_TX]
   // (tile rows 32-byte aligned); recomputed where used rather than held across the loop
   auto hx_tile = [&]() {
@@ -266,7 +277,7 @@ __global__ void __launch_bounds__(kViewMaxThreads, 2) k_view(ViewArgs A) {
 
   // taps of the first channel into buffer 0, its D row sums; the table after the barrier
   // (the row sums come from other threads)
-  if (slot_ok && first < A.nch) {
+  if (slot_ok && first < nch) {
     for (int i = lt; i < TT; i += A.tps) {
       const int j = (i / T) * TW + i % T;
       if (BWD) taps[j] = __ldg(A.wb + first * TT + i);
@@ -275,17 +286,17 @@ __global__ void __launch_bounds__(kViewMaxThreads, 2) k_view(ViewArgs A) {
     if (DT) view_d_rows<T>(A, first, lt, rowp);
   }
   __syncthreads();
-  if (DT && slot_ok && first < A.nch) view_d_table(A, first, lt, rowp, dtab);
+  if (DT && slot_ok && first < nch) view_d_table<T>(A, first, lt, rowp, dtab);
   __syncthreads();
 
   int buf = 0;
-  for (int64_t base = (int64_t)blockIdx.x * A.slots; base < A.nch; base += step, buf ^= 1) {
-    const int64_t ch = base + slot;
-    const int64_t nxt = ch + step;
-    const bool active = slot_ok && ch < A.nch;
-    const bool more = slot_ok && nxt < A.nch;
+  for (int base = (int)blockIdx.x * A.slots; base < nch; base += step, buf ^= 1) {
+    const int ch = base + slot;
+    const int nxt = ch + step;
+    const bool active = slot_ok && ch < nch;
+    const bool more = slot_ok && nxt < nch;
     const int alpha = active ? (int)((ch / A.Z) % A.N) : 0;
-    const int beta = active ? (int)(ch / ((int64_t)A.Z * A.N)) : 0;
+    const int beta = active ? ch / (A.Z * A.N) : 0;
     const int sa = floor_div(alpha - A.u + h, A.N);
     const int sb = floor_div(beta - A.v + h, A.N);
     const float* wbs = taps + buf * 2 * TTW;
@@ -318,15 +329,21 @@ __global__ void __launch_bounds__(kViewMaxThreads, 2) k_view(ViewArgs A) {
         for (int y = 0; y < VW_TY; ++y)
 #pragma unroll
           for (int x = 0; x < VW_TX; ++x) acc[y][x] = 0.f;
+        if (ph == 1 && hx_written) {  // this tile's forward partials into L1 for the add below
+          const float* hxp = hx_tile();
+#pragma unroll
+          for (int y = 0; y < VW_TY; ++y)
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(hxp + y * A.tilesA * VW_TX));
+        }
         const float* in = ph == 0 ? rs + (b0 + sb + 1) * A.RP : xin + b0 * A.XP;
         const int pitch = ph == 0 ? A.RP : A.XP;
         const float* wsel = ph == 0 ? wbs : wfs;
         switch (ph == 0 ? sa + 1 : QP - Q) {
-          case 0: conv_rows<T, 0, TW>(in, pitch, woff, wsel, acc); break;
-          case 1: conv_rows<T, 1, TW>(in, pitch, woff, wsel, acc); break;
-          case 2: conv_rows<T, 2, TW>(in, pitch, woff, wsel, acc); break;
+          case 0: conv_rows<T, 0, TW>(in, pitch, a0, wsel, acc); break;
+          case 1: conv_rows<T, 1, TW>(in, pitch, a0, wsel, acc); break;
+          case 2: conv_rows<T, 2, TW>(in, pitch, a0, wsel, acc); break;
           default:
-            if constexpr (QP - Q == 3) conv_rows<T, 3, TW>(in, pitch, woff, wsel, acc);
+            if constexpr (QP - Q == 3) conv_rows<T, 3, TW>(in, pitch, a0, wsel, acc);
             break;
         }
         if (ph == 0) {
@@ -337,7 +354,7 @@ __global__ void __launch_bounds__(kViewMaxThreads, 2) k_view(ViewArgs A) {
               if (b >= A.Lj) continue;
 #pragma unroll
               for (int x = 0; x < VW_TX; ++x)
-                if (a0 + x < A.Li) A.Cout[ch * A.plane + (int64_t)b * A.Pa + a0 + x] = acc[y][x];
+                if (a0 + x < A.Li) A.Cout[(int64_t)ch * A.plane + (int64_t)b * A.Pa + a0 + x] = acc[y][x];
             }
           } else {
             cp_async_wait_all();  // this thread's X tile has landed in xin
@@ -408,7 +425,7 @@ __global__ void __launch_bounds__(kViewMaxThreads, 2) k_view(ViewArgs A) {
     }
     // the next channel: its D table and its taps (into the other buffer)
     if (more) {
-      if (DT) view_d_table(A, nxt, lt, rowp, dtab);
+      if (DT) view_d_table<T>(A, nxt, lt, rowp, dtab);
       float* nb = taps + (buf ^ 1) * 2 * TTW;
       for (int i = lt; i < TT; i += A.tps) {
         const int j = (i / T) * TW + i % T;
