@@ -47,7 +47,7 @@ WORKLOAD_DESC = ("Nnum 15, 67x67 lenslets (1005x1005 px), 51 planes (0-200 um at
                  "PSF 231 px (phase-space 225), 2000 somas, 2000-photon Poisson image, 3 RL iterations")
 
 
-KVIEW_DRAM_BYTES = 386.4e6     # k_view MODE_STEP launch, 1005x1005x51, FP32
+KVIEW_DRAM_BYTES = 393.3e6     # k_view MODE_STEP launch, 1005x1005x51, FP32 (ncu, 2 launches: 229.9 + 163.4 MB)
 KTC_DRAM_BYTES = {"k_tc_bwd": 390.7e6, "k_tc_fwd": 220.5e6}   # per launch, same workload, bf16x2
 
 
