@@ -31,7 +31,8 @@ namespace mlf {
 namespace {
 
 constexpr int CV_NN = 15;            // kernels per axis (the reference's num_kernels)
-constexpr int CV_MAX_THREADS = 768;  // 85 registers a thread: no spills
+constexpr int CV_MAX_THREADS = 768;  // rows a CTA's threads own at most (RPT rows per thread)
+constexpr int CV_RPT = 2;            // output rows per thread
 
 __device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
   const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
@@ -75,7 +76,10 @@ __device__ __forceinline__ void conv_rows_stage(const ConvRowsArgs& A, float* sm
   cp_async_commit();
 }
 
-__global__ void __launch_bounds__(CV_MAX_THREADS, 1) k_conv_vec_rows(ConvRowsArgs A) {
+// RPT output rows per thread (rows jl*RPT .. jl*RPT + RPT-1 of the CTA's tile): the taps
+// of a step, loaded once, serve RPT rows.
+template <int RPT>
+__global__ void __launch_bounds__(CV_MAX_THREADS / RPT, 1) k_conv_vec_rows(ConvRowsArgs A) {
   extern __shared__ __align__(16) float sm[];
   const int b = blockIdx.y;                      // row phase
   const int64_t slice = A.slice0 + blockIdx.z;
@@ -84,10 +88,15 @@ __global__ void __launch_bounds__(CV_MAX_THREADS, 1) k_conv_vec_rows(ConvRowsArg
   const int nJ = b < A.H ? (A.H - b + CV_NN - 1) / CV_NN : 0;
   if (j0 >= nJ) return;                           // CTA-uniform
   const int tid = threadIdx.x;
-  const int il = tid % A.sx, jl = tid / A.sx;
+  const int il = tid % A.sx, jl = (tid / A.sx) * RPT;
   const int x_seg = CV_NN * (i0 + il);
-  const int y = b + CV_NN * (j0 + jl);
-  const bool mine = jl < A.sy && x_seg < A.W && y < A.H;
+  bool mine[RPT];
+  int yr[RPT];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    yr[r] = b + CV_NN * (j0 + jl + r);
+    mine[r] = jl + r < A.sy && x_seg < A.W && yr[r] < A.H;
+  }
   const int cstart = CV_NN * i0 - A.hk;          // input column of staged column 0
   // taps first (16-byte aligned for the float4 loads), then the two row buffers
   const int rowbuf = A.sy * A.pitch;
@@ -96,26 +105,34 @@ __global__ void __launch_bounds__(CV_MAX_THREADS, 1) k_conv_vec_rows(ConvRowsArg
   const int64_t kplane = (int64_t)A.kw * A.kw;
   const float* kb = A.K + kplane * CV_NN * b;    // kernels (a, b), a = 0..14
 
-
-  float acc[CV_NN];
+  float acc[RPT][CV_NN];
 #pragma unroll
-  for (int a = 0; a < CV_NN; ++a) acc[a] = 0.f;
+  for (int r = 0; r < RPT; ++r)
+#pragma unroll
+    for (int a = 0; a < CV_NN; ++a) acc[r][a] = 0.f;
   conv_rows_stage(A, sm, rows0, rowbuf, src, kb, kplane, b, j0, nJ, cstart, 0, 0);
   cp_async_wait0();
   __syncthreads();
   for (int ky = 0; ky < A.kw; ++ky) {
     const int sel = ky & 1;
     if (ky + 1 < A.kw) conv_rows_stage(A, sm, rows0, rowbuf, src, kb, kplane, b, j0, nJ, cstart, ky + 1, sel ^ 1);
-    if (mine) {
-      const float* rowp = rows0 + sel * rowbuf + jl * A.pitch + CV_NN * il;
-      const float* tp = sm + sel * 16 * A.kwp;
-      float w[CV_NN];  // w[(m + a) % 15] holds rowp[kx0 + m + a]
+    if (mine[0]) {
+      // rows past the tile read staged rows that exist (jl + r < sy is not required for the
+      // read: the buffer holds sy rows, so clamp) and are not stored
+      const float* rowp[RPT];
 #pragma unroll
-      for (int a = 0; a < CV_NN - 1; ++a) w[a] = rowp[a];
+      for (int r = 0; r < RPT; ++r) rowp[r] = rows0 + sel * rowbuf + min(jl + r, A.sy - 1) * A.pitch + CV_NN * il;
+      const float* tp = sm + sel * 16 * A.kwp;
+      float w[RPT][CV_NN];  // w[r][(m + a) % 15] holds rowp[r][kx0 + m + a]
+#pragma unroll
+      for (int r = 0; r < RPT; ++r)
+#pragma unroll
+        for (int a = 0; a < CV_NN - 1; ++a) w[r][a] = rowp[r][a];
       for (int kx0 = 0; kx0 < A.kwp; kx0 += CV_NN) {
 #pragma unroll
         for (int m = 0; m < CV_NN; ++m) {
-          w[(m + CV_NN - 1) % CV_NN] = rowp[kx0 + m + CV_NN - 1];
+#pragma unroll
+          for (int r = 0; r < RPT; ++r) w[r][(m + CV_NN - 1) % CV_NN] = rowp[r][kx0 + m + CV_NN - 1];
           const float4* t4 = reinterpret_cast<const float4*>(tp + 16 * (kx0 + m));
           float t[16];
 #pragma unroll
@@ -127,18 +144,22 @@ __global__ void __launch_bounds__(CV_MAX_THREADS, 1) k_conv_vec_rows(ConvRowsArg
             t[4 * q + 3] = v.w;
           }
 #pragma unroll
-          for (int a = 0; a < CV_NN; ++a) acc[a] = fmaf(w[(m + a) % CV_NN], t[a], acc[a]);
+          for (int r = 0; r < RPT; ++r)
+#pragma unroll
+            for (int a = 0; a < CV_NN; ++a) acc[r][a] = fmaf(w[r][(m + a) % CV_NN], t[a], acc[r][a]);
         }
       }
     }
     cp_async_wait0();
     __syncthreads();
   }
-  if (mine) {
-    float* o = A.out + slice * (int64_t)A.W * A.H + (int64_t)y * A.W;
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    if (!mine[r]) continue;
+    float* o = A.out + slice * (int64_t)A.W * A.H + (int64_t)yr[r] * A.W;
 #pragma unroll
     for (int a = 0; a < CV_NN; ++a)
-      if (x_seg + a < A.W) o[x_seg + a] = acc[a];
+      if (x_seg + a < A.W) o[x_seg + a] = acc[r][a];
   }
 }
 
@@ -232,7 +253,7 @@ int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const f
   int dev = 0, optin = 0;
   MLF_CUDA(cudaGetDevice(&dev));
   MLF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  MLF_TRY(allow_max_dyn_smem((const void*)k_conv_vec_rows));
+  MLF_TRY(allow_max_dyn_smem((const void*)k_conv_vec_rows<CV_RPT>));
   ConvRowsArgs a{};
   a.in = d_bitmap;
   a.K = d_kernels;
@@ -250,17 +271,17 @@ int conv_vec_run(const float* d_bitmap, int64_t W, int64_t H, int64_t n, const f
   a.pitch = a.width | 1;  // odd: rows of a warp fall on different banks
   const size_t tap_bytes = sizeof(float) * 2 * 16 * (size_t)a.kwp;
   const size_t budget = (size_t)optin - 1024;
-  a.sy = std::max(1, std::min(nJ, CV_MAX_THREADS / a.sx));
+  a.sy = std::max(1, std::min(nJ, CV_RPT * (CV_MAX_THREADS / CV_RPT / a.sx)));
   while (a.sy > 1 && sizeof(float) * 2 * (size_t)a.sy * a.pitch + tap_bytes > budget) --a.sy;
   const size_t smem = sizeof(float) * 2 * (size_t)a.sy * a.pitch + tap_bytes;
   if (smem > budget) return fail(MLF_ERR_UNSUPPORTED, "direct MEX projector: kernel row does not fit in shared memory");
   a.tilesX = (nI + a.sx - 1) / a.sx;
   const int tilesY = (nJ + a.sy - 1) / a.sy;
-  const int threads = (a.sx * a.sy + 31) / 32 * 32;
+  const int threads = (a.sx * ((a.sy + CV_RPT - 1) / CV_RPT) + 31) / 32 * 32;
   for (int64_t s0 = 0; s0 < n; s0 += 65535) {
     a.slice0 = s0;
     const dim3 grid((unsigned)(a.tilesX * tilesY), CV_NN, (unsigned)std::min<int64_t>(65535, n - s0));
-    k_conv_vec_rows<<<grid, threads, smem, st>>>(a);
+    k_conv_vec_rows<CV_RPT><<<grid, threads, smem, st>>>(a);
     MLF_LAUNCHED();
   }
   return MLF_OK;
