@@ -22,11 +22,13 @@
 // calls whose kernels overlap on the GPU (different streams, or different host threads)
 // race on the array and must be serialised by the caller.
 //
-// The projection itself is the MODE_FWD correlation of k_view (mlf_view.cuh), restaged:
-// the plane is gathered from the MATLAB-layout volume and the taps have pitch T.  A change
-// to k_view's tile geometry (VT_TX x VT_TY tiles, view_nw, view_qpad, conv_tile) must be
-// carried into k_fwd_static; tests/test_zz_no_alloc.py compares the two on every tap count
-// it covers.
+// The projection is the per-channel forward correlation of k_view's MODE_FWD (mlf_view.cuh)
+// with a tiling of its own: 8 x 4 tiles (VT_TY x VT_TX) through conv_tile on unswizzled
+// planes, the plane gathered from the MATLAB-layout volume, taps at pitch T, partials
+// reduced per CTA in shared memory.  It shares view_nw, view_qpad and conv_tile with
+// mlf_view.cuh, not k_view's 4 x 8 tile, swizzled planes or slot partial planes; both add
+// each output's products in the order (tap row, tap column), and tests/test_zz_no_alloc.py
+// compares the two on every tap count it covers.
 #include <cuda_runtime.h>
 
 #include <algorithm>
