@@ -117,8 +117,9 @@ __global__ void __launch_bounds__(RC_ROWS * RC_COLS, 4)
 k_rectify_staged(const TIn* __restrict__ raw, int64_t total, int64_t fstride, int64_t cstride, int64_t row0,
                  int64_t col0, const int* __restrict__ iy, const float* __restrict__ wy, int oh,
                  const int* __restrict__ ix, const float* __restrict__ wx, int ow, int64_t f0, int64_t fstep,
-                 int64_t n_out, int slot, int maxc, float* __restrict__ out) {
+                 int64_t n_out, int slot, int maxc, int same_align, float* __restrict__ out) {
   constexpr int VEC = 16 / sizeof(TIn);
+  constexpr int NT = RC_ROWS * RC_COLS;
   extern __shared__ __align__(16) unsigned char rc_smem[];
   TIn* tile = reinterpret_cast<TIn*>(rc_smem);  // [SF][maxc][slot]
   __shared__ int off[SF][8];
@@ -130,20 +131,29 @@ k_rectify_staged(const TIn* __restrict__ raw, int64_t total, int64_t fstride, in
   const int nv = (nrow + 2 * VEC - 2) / VEC;                         // vectors per column segment
   const int64_t ib = (int64_t)blockIdx.z * SF;
   const int nf = (int)(n_out - ib < SF ? n_out - ib : SF);
-  const int nload = nf * ncol * nv;
-  for (int idx = tid; idx < nload; idx += RC_ROWS * RC_COLS) {
-    const int q = idx / (ncol * nv), rem = idx - q * (ncol * nv);
+  // staging: a thread keeps one (column k, vector v) of the footprint and walks the frames
+  // q = g, g + G, ... (G groups of ncol * nv threads), so the index split is done once
+  {
+    const int cnv = ncol * nv;
+    const int G = NT / cnv;  // >= 1: the host bounds nrow and maxc
+    const int g = tid / cnv, rem = tid - g * cnv;
     const int k = rem / nv, v = rem - k * nv;
-    const int64_t e = (f0 + (ib + q) * fstep) * fstride + (row0 + rlo) + cstride * (col0 + clo + k);
-    const int64_t ea = e & ~(int64_t)(VEC - 1);
-    if (v == 0) off[q][k] = (int)(e - ea);
-    TIn* dst = tile + ((int64_t)q * maxc + k) * slot + (int64_t)v * VEC;
-    const int64_t src = ea + (int64_t)v * VEC;
-    if (src + VEC <= total) {
-      *reinterpret_cast<uint4*>(dst) = __ldcs(reinterpret_cast<const uint4*>(raw + src));
-    } else {
+    if (g < G) {
+      const int64_t colbase = (row0 + rlo) + cstride * (col0 + clo + k);
+      const int64_t fdelta = (int64_t)G * fstep * fstride;
+      int64_t e = (f0 + (ib + g) * fstep) * fstride + colbase;
+      for (int q = g; q < nf; q += G, e += fdelta) {
+        const int64_t ea = e & ~(int64_t)(VEC - 1);
+        if (v == 0) off[q][k] = (int)(e - ea);
+        TIn* dst = tile + ((int64_t)q * maxc + k) * slot + (int64_t)v * VEC;
+        const int64_t src = ea + (int64_t)v * VEC;
+        if (src + VEC <= total) {
+          *reinterpret_cast<uint4*>(dst) = __ldcs(reinterpret_cast<const uint4*>(raw + src));
+        } else {
 #pragma unroll
-      for (int u = 0; u < VEC; ++u) dst[u] = src + u < total ? raw[src + u] : TIn(0);
+          for (int u = 0; u < VEC; ++u) dst[u] = src + u < total ? raw[src + u] : TIn(0);
+        }
+      }
     }
   }
   __syncthreads();
@@ -154,10 +164,26 @@ k_rectify_staged(const TIn* __restrict__ raw, int64_t total, int64_t fstride, in
   const int64_t P = (int64_t)oh * ow;
   float* op = out + r + (int64_t)oh * c + P * ib;
   const TIn* base = tile + (int64_t)lc * slot + lr;
+  const int fs = maxc * slot;  // elements per staged frame
+  if (same_align) {
+    // every frame has the same 16-byte alignment: the column offsets of frame 0 serve all
+    const TIn* ca = base + off[0][lc];
+    const TIn* cb = base + slot + off[0][lc + 1];
+#pragma unroll
+    for (int q = 0; q < SF; ++q) {
+      if (q < nf) {
+        const float v00 = to_f(ca[q * fs]), v10 = to_f(ca[q * fs + 1]);
+        const float v01 = to_f(cb[q * fs]), v11 = to_f(cb[q * fs + 1]);
+        const float a = fmaf(fx, v01 - v00, v00), b = fmaf(fx, v11 - v10, v10);
+        __stcs(op + P * q, fmaf(fy, b - a, a));
+      }
+    }
+    return;
+  }
 #pragma unroll 4
   for (int q = 0; q < nf; ++q) {
-    const TIn* ca = base + (int64_t)q * maxc * slot + off[q][lc];
-    const TIn* cb = base + (int64_t)q * maxc * slot + slot + off[q][lc + 1];
+    const TIn* ca = base + (int64_t)q * fs + off[q][lc];
+    const TIn* cb = base + (int64_t)q * fs + slot + off[q][lc + 1];
     const float v00 = to_f(ca[0]), v10 = to_f(ca[1]), v01 = to_f(cb[0]), v11 = to_f(cb[1]);
     const float a = fmaf(fx, v01 - v00, v00), b = fmaf(fx, v11 - v10, v10);
     __stcs(op + P * q, fmaf(fy, b - a, a));
@@ -268,17 +294,20 @@ int rectify_run(const void* d_raw, int dtype, int64_t total, int64_t fstride, in
     const void* kf = dtype == MLF_DTYPE_U16 ? (const void*)k_rectify_staged<uint16_t> : (const void*)k_rectify_staged<float>;
     MLF_TRY(allow_max_dyn_smem(kf));
     const int64_t chunks = (n_out + SF - 1) / SF;
+    // frames whose starts differ by multiples of 16 bytes share the staged column offsets
+    const int same_align = ((fstep * fstride) % vec == 0) ? 1 : 0;
     if (chunks > 65535) return fail(MLF_ERR_UNSUPPORTED, "mlf_rectify_frames: more than 1048560 output frames");
     const dim3 grid((unsigned)((out_h + RC_ROWS - 1) / RC_ROWS), (unsigned)((out_w + RC_COLS - 1) / RC_COLS),
                     (unsigned)chunks);
     if (dtype == MLF_DTYPE_U16)
       k_rectify_staged<uint16_t><<<grid, block, smem, st>>>(static_cast<const uint16_t*>(d_raw), total, fstride,
                                                             cstride, row0, col0, d_iy, d_wy, (int)out_h, d_ix, d_wx,
-                                                            (int)out_w, f0, fstep, n_out, slot, maxc, d_out);
+                                                            (int)out_w, f0, fstep, n_out, slot, maxc, same_align,
+                                                            d_out);
     else
       k_rectify_staged<float><<<grid, block, smem, st>>>(static_cast<const float*>(d_raw), total, fstride, cstride,
                                                          row0, col0, d_iy, d_wy, (int)out_h, d_ix, d_wx, (int)out_w,
-                                                         f0, fstep, n_out, slot, maxc, d_out);
+                                                         f0, fstep, n_out, slot, maxc, same_align, d_out);
     MLF_LAUNCHED();
   } else {
   const int64_t per_block = (int64_t)RC_FCH * RC_NCH;

@@ -31,9 +31,10 @@ def frames_u16(shape, n, seed):
     dict(frames_start=1, frames_step=2, frames_average=False),
 ])
 @pytest.mark.parametrize("dtype", ["u16", "f32"])
-def test_image_load_matches_oracle(cuda, sel, dtype):
+@pytest.mark.parametrize("shape", [(1024, 1040), (1023, 1041)])  # frames 16-byte aligned, or not
+def test_image_load_matches_oracle(cuda, sel, dtype, shape):
     SI = dict(SI0, **sel)
-    frames = frames_u16((1024, 1040), 12, seed=3)
+    frames = frames_u16(shape, 12, seed=3)
     if dtype == "f32":
         frames = frames.astype(np.float32) * np.float32(0.37)
     infos = RC.determine_patch_info_aug(SI, frames.shape[:2])
