@@ -757,6 +757,536 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtenso
   if (warp == 2) tc::tmem_dealloc(tmem_base, tcols);
 }
 
+// ------------------------------------------------------------------ fused back projection + next forward
+// One launch per view step for the BF16 modes (bf16, bf16x2) when D comes from the class
+// tables and the forward taps fit one MMA (N <= 256): back projection + update of view k as
+// in k_tc_bwd, and the forward GEMM of view k+1 on each updated X tile while it is still in
+// shared memory, so the volume is read and written once per view (k_tc_fwd re-reads it).
+// Work items are (position tile m, split s): the channel tiles of split s -- the split
+// boundaries of k_tc_fwd, so Y accumulates over the same K-steps in the same order (the
+// results are bit for bit those of k_tc_bwd + k_tc_fwd).  Per tile:
+//   producer:  the 5 AR / Wb stages of tile i, then the 1-2 Wf half stages of tile i-1
+//   MMA:       back projection of tile i into C[i & 1], then the forward of tile i-1 into Y
+//   epilogue:  update of tile i (as k_tc_bwd); after the I/O warp has stored the FP32 half
+//              (its TMA store has read the buffer), every warp of the half reads its values,
+//              meets the others on an mbarrier, and writes the BF16 hi / lo operand back into
+//              the same 32 KB in the K-major 128-byte-swizzled layout; after the item's last
+//              forward MMA it drains Y (TMEM) into the split's partials
+//   X I/O:     loads, stores, and reloads a buffer only after the forward MMAs that read it
+// TMEM: C buffers at columns 0 and 128, Y at 256 (NB <= 256 columns).  Every wait is
+// bounded; a timeout sets the device status word and the abort flag.
+struct TcFusedArgs {
+  TcBwdArgs b;
+  float* ypart;        // [splits][NB][MP]
+  const float* wview;  // per patch weight of the projected (next) view
+  int MP, NB, splits, ks_per_split, KS, frow0, ntiles;
+};
+
+struct FusedItem {
+  int m, s, n_lo, n_hi, ks0, ks1, c0, c1;
+  bool wcur, wnext;
+};
+__device__ __forceinline__ FusedItem fused_item(const TcFusedArgs& a, int item) {
+  FusedItem f;
+  f.m = item / a.splits;
+  f.s = item - f.m * a.splits;
+  const int pp = __ldg(a.b.tile_patch + f.m);
+  const int* pi = a.b.pinfo + 8 * pp;
+  const int z0 = __ldg(pi + 4), nz = __ldg(pi + 5);
+  f.c0 = z0 * a.b.NN;                 // channel range of the patch (as bwd_skip)
+  f.c1 = f.c0 + nz * a.b.NN;
+  const int klo = z0 * a.b.NN / BK;   // K-steps of the forward (as k_tc_fwd)
+  const int khi = ((z0 + nz) * a.b.NN + BK - 1) / BK;
+  f.ks0 = max(f.s * a.ks_per_split, klo);
+  f.ks1 = min(min(a.KS, f.s * a.ks_per_split + a.ks_per_split), khi);
+  f.n_lo = f.s * (a.ks_per_split / 2);
+  f.n_hi = min(a.ntiles, (f.s + 1) * (a.ks_per_split / 2));
+  f.wcur = __ldg(a.b.wrow + pp) != 0.f;
+  f.wnext = a.wview ? __ldg(a.wview + pp) != 0.f : true;
+  return f;
+}
+// flags of channel tile n of an item: bit 0 back projection, bits 1-2 forward halves
+__device__ __forceinline__ int fused_tile(const FusedItem& f, int n) {
+  const int n0 = n * BWD_BN;
+  const bool b = f.wcur && !(n0 + BWD_BN <= f.c0 || n0 >= f.c1);
+  const bool h0 = f.wnext && 2 * n >= f.ks0 && 2 * n < f.ks1;
+  const bool h1 = f.wnext && 2 * n + 1 >= f.ks0 && 2 * n + 1 < f.ks1;
+  return (b ? 1 : 0) | (h0 ? 2 : 0) | (h1 ? 4 : 0);
+}
+__device__ __forceinline__ int fused_nfwd(const FusedItem& f) {
+  int c = 0;
+  for (int n = f.n_lo; n < f.n_hi; ++n) {
+    const int fl = fused_tile(f, n);
+    c += ((fl >> 1) & 1) + ((fl >> 2) & 1);
+  }
+  return c;
+}
+
+template <int XB>
+__global__ void __launch_bounds__(BWD_THREADS, 1)
+k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+            const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mX,
+            const __grid_constant__ CUtensorMap mF, TcFusedArgs a, int nitems) {
+  {  // a cancelled solve: the rest of its view steps return at once (CTA-uniform, before TMEM)
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) s_stop = cancel_entry(a.b.cancel);
+    __syncthreads();
+    if (s_stop) return;
+  }
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull[XB][2], hdone[2][2],
+      xstored[XB][2], rdone[XB][2], aready[XB][2], afree[XB][2], yfull, ydone, mdone;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int KS = a.b.KB / BK;
+  const bool need_alo = a.b.use_alo != 0;
+  const BwdLayout L = bwd_layout(a.b.use_alo, 0, false);
+  float* xs = reinterpret_cast<float*>(smem + STAGES * L.stage);  // [XB][2 halves][64 ch][128 pos]
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&tfull[b], 1);
+      tc::mbar_init(&tempty[b], BWD_EPI_WARPS);
+      tc::mbar_init(&hdone[b][0], BWD_EPI_WARPS / 2);
+      tc::mbar_init(&hdone[b][1], BWD_EPI_WARPS / 2);
+    }
+    for (int b = 0; b < XB; ++b)
+      for (int h = 0; h < 2; ++h) {
+        tc::mbar_init(&xfull[b][h], 1);
+        tc::mbar_init(&xstored[b][h], 1);
+        tc::mbar_init(&rdone[b][h], BWD_EPI_WARPS / 2);
+        tc::mbar_init(&aready[b][h], BWD_EPI_WARPS / 2);
+        tc::mbar_init(&afree[b][h], 1);
+      }
+    tc::mbar_init(&yfull, 1);
+    tc::mbar_init(&ydone, BWD_EPI_WARPS);
+    tc::mbar_init(&mdone, 1);
+    tc::fence_mbar_init();
+    abort_flag = 0;
+    tc::tma_prefetch_desc(&mAh);
+    tc::tma_prefetch_desc(&mBh);
+    tc::tma_prefetch_desc(&mX);
+    tc::tma_prefetch_desc(&mF);
+  }
+  if (warp == 1) tc::tmem_alloc(&tmem_base, 512);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer: bwd stages of tile i, then the Wf halves of tile i-1
+      const uint32_t bbytes = 2 * TILE_A + (need_alo ? TILE_A : 0);
+      const uint32_t fbytes = (uint32_t)a.NB * 128;
+      int it = 0;
+      bool ok = true;
+      int pn = -1, pfl = 0;  // previous active tile
+      auto stage = [&](bool fwd, int ks, int m0, int n0) {
+        const int s = it % STAGES;
+        const uint32_t ph = (it / STAGES) & 1;
+        if (!tc::mbar_wait(&empty[s], ph ^ 1, WAIT_LIMIT)) {
+          set_abort(&abort_flag);
+          atomicExch(a.b.err, TC_ERR_TIMEOUT_PRODUCER);
+          ok = false;
+          return;
+        }
+        uint8_t* st = smem + s * L.stage;
+        if (fwd) {
+          tc::mbar_arrive_expect_tx(&full[s], fbytes);
+          tc::tma_load_2d(st, &mF, &full[s], ks * BK, a.frow0);
+        } else {
+          tc::mbar_arrive_expect_tx(&full[s], bbytes);
+          tc::tma_load_2d(st, &mAh, &full[s], ks * BK, m0);
+          if (need_alo) tc::tma_load_2d(st + L.offAl, &mAl, &full[s], ks * BK, m0);
+          tc::tma_load_2d(st + L.offBh, &mBh, &full[s], ks * BK, a.b.brow0 + n0);
+        }
+        ++it;
+      };
+      for (int item = blockIdx.x; item < nitems && ok && !aborted(&abort_flag); item += gridDim.x) {
+        const FusedItem f = fused_item(a, item);
+        for (int n = f.n_lo; n < f.n_hi && ok; ++n) {
+          const int fl = fused_tile(f, n);
+          if (!fl) continue;
+          if (fl & 1)
+            for (int ks = 0; ks < KS && ok; ++ks) stage(false, ks, f.m * BM, n * BWD_BN);
+          if (pn >= 0)
+            for (int h = 0; h < 2 && ok; ++h)
+              if (pfl & (2 << h)) stage(true, 2 * pn + h, 0, 0);
+          pn = n;
+          pfl = fl;
+        }
+      }
+      if (pn >= 0 && ok)
+        for (int h = 0; h < 2 && ok; ++h)
+          if (pfl & (2 << h)) stage(true, 2 * pn + h, 0, 0);
+      // drain: every issued copy must have landed before the CTA can exit
+      for (int i = std::max(0, it - STAGES); i < it; ++i)
+        if (!tc::mbar_wait(&full[i % STAGES], (i / STAGES) & 1, WAIT_LIMIT)) atomicExch(a.b.err, TC_ERR_TIMEOUT_DRAIN);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      const uint32_t bdesc_i = tc::idesc_bf16_f32(BM, BWD_BN);
+      const uint32_t fdesc_i = tc::idesc_bf16_f32(BM, a.NB);
+      const uint32_t tY = tmem_base + 256;
+      int it = 0, bt = 0, ti = 0, yitems = 0;
+      int cnt_ready[XB][2] = {};  // forward uses of each buffer half (aready phases)
+      bool ok = true;
+      int pn = -1, pfl = 0, pxb = 0;  // previous active tile and its X buffer
+      int pleft = 0;                  // forward halves of the previous tile's item still to issue
+      bool pfirst = false;            // the previous tile's item has issued no forward MMA yet
+      int cur_left = 0;
+      bool cur_first = false;
+      auto wait_stage = [&]() -> uint32_t {
+        const int s = it % STAGES;
+        const uint32_t ph = (it / STAGES) & 1;
+        if (!tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
+          set_abort(&abort_flag);
+          atomicExch(a.b.err, TC_ERR_TIMEOUT_MMA);
+          ok = false;
+        }
+        tc::tc_fence_after();
+        return tc::smem_u32(smem + s * L.stage);
+      };
+      // forward halves of a tile whose update has been converted into its X buffer
+      auto forward = [&](int fl, int xb, int& left, bool& first) {
+        for (int h = 0; h < 2 && ok; ++h) {
+          if (!(fl & (2 << h))) continue;
+          if (first && yitems > 0 && !tc::mbar_wait(&ydone, (yitems - 1) & 1, WAIT_LIMIT)) {
+            set_abort(&abort_flag);
+            atomicExch(a.b.err, TC_ERR_TIMEOUT_MMA);
+            ok = false;
+            break;
+          }
+          if (!tc::mbar_wait(&aready[xb][h], cnt_ready[xb][h] & 1, WAIT_LIMIT)) {
+            set_abort(&abort_flag);
+            atomicExch(a.b.err, TC_ERR_TIMEOUT_MMA);
+            ok = false;
+            break;
+          }
+          ++cnt_ready[xb][h];
+          const uint32_t st = wait_stage();
+          if (!ok) break;
+          const uint32_t xa = tc::smem_u32(xs + (xb * 2 + h) * (XHALF / 4));
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k) {
+            const uint32_t acc = (first && k == 0) ? 0u : 1u;
+            const uint64_t dah = tc::desc_kmajor_sw128(xa + 32 * k);
+            const uint64_t dbh = tc::desc_kmajor_sw128(st + 32 * k);
+            tc::mma_bf16(tY, dah, dbh, fdesc_i, acc);
+            if (need_alo) tc::mma_bf16(tY, tc::desc_kmajor_sw128(xa + TILE_A + 32 * k), dbh, fdesc_i, 1u);
+          }
+          first = false;
+          tc::mma_commit(&empty[it % STAGES]);
+          tc::mma_commit(&afree[xb][h]);
+          ++it;
+          if (--left == 0) {
+            tc::mma_commit(&yfull);
+            ++yitems;
+          }
+        }
+      };
+      for (int item = blockIdx.x; item < nitems && ok && !aborted(&abort_flag); item += gridDim.x) {
+        const FusedItem f = fused_item(a, item);
+        cur_left = fused_nfwd(f);
+        cur_first = true;
+        for (int n = f.n_lo; n < f.n_hi && ok; ++n) {
+          const int fl = fused_tile(f, n);
+          if (!fl) continue;
+          if (fl & 1) {
+            const int buf = bt & 1;
+            if (!tc::mbar_wait(&tempty[buf], ((bt >> 1) & 1) ^ 1, WAIT_LIMIT)) {
+              set_abort(&abort_flag);
+              atomicExch(a.b.err, TC_ERR_TIMEOUT_MMA);
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint32_t tC = tmem_base + buf * 128;
+            for (int ks = 0; ks < KS && ok; ++ks) {
+              const uint32_t st = wait_stage();
+              if (!ok) break;
+#pragma unroll
+              for (int k = 0; k < BK / 16; ++k) {
+                const uint32_t acc = (ks > 0 || k > 0) ? 1u : 0u;
+                const uint64_t dah = tc::desc_kmajor_sw128(st + 32 * k);
+                const uint64_t dbh = tc::desc_kmajor_sw128(st + L.offBh + 32 * k);
+                tc::mma_bf16(tC, dah, dbh, bdesc_i, acc);
+                if (need_alo) tc::mma_bf16(tC, tc::desc_kmajor_sw128(st + L.offAl + 32 * k), dbh, bdesc_i, 1u);
+              }
+              tc::mma_commit(&empty[it % STAGES]);
+              ++it;
+            }
+            if (!ok) break;
+            tc::mma_commit(&tfull[buf]);
+            ++bt;
+          }
+          if (pn >= 0) forward(pfl, pxb, pleft, pfirst);
+          if (!ok) break;
+          // this tile becomes the previous one: its forward runs after the next tile's back
+          // projection, with its item's count of forward halves still to issue (pleft) and
+          // whether it opens the item's Y accumulation (pfirst)
+          pn = n;
+          pfl = fl;
+          pxb = ti % XB;
+          pleft = cur_left;
+          pfirst = cur_first;
+          cur_left -= ((fl >> 1) & 1) + ((fl >> 2) & 1);
+          if (((fl >> 1) & 1) + ((fl >> 2) & 1)) cur_first = false;
+          ++ti;
+        }
+      }
+      if (pn >= 0 && ok) forward(pfl, pxb, pleft, pfirst);
+      // every issued MMA must have completed before TMEM is released
+      tc::mma_commit(&mdone);
+      if (!tc::mbar_wait(&mdone, 0, WAIT_LIMIT)) atomicExch(a.b.err, TC_ERR_TIMEOUT_DRAIN);
+    }
+  } else if (warp < BWD_IO_WARP) {
+    // ---------------- epilogue: update X (as k_tc_bwd), then the forward operand, then Y
+    const int e = warp - 2;
+    const int half = e >> 3;
+    const int sub = (e & 7) >> 2;
+    const int quad = warp & 3;
+    const int row = quad * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    int bt = 0, ti = 0, yitems = 0;
+    int cnt_use[XB] = {};  // loads into each buffer
+    int cnt_fwd[XB] = {};  // forward uses of this warp's half of each buffer
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      const FusedItem f = fused_item(a, item);
+      const int pp = __ldg(a.b.tile_patch + f.m);
+      const int* pi = a.b.pinfo + 8 * pp;
+      const int m0 = f.m * BM;
+      const int local = m0 + row - __ldg(pi + 3);
+      const bool pos_ok = local < __ldg(pi + 2);
+      int cls = 0;
+      {
+        const int Li = __ldg(pi + 0), Lj = __ldg(pi + 1);
+        const int jj = local / Li, ii = local - jj * Li;
+        if (pos_ok) cls = dtab_class(jj, Lj, a.b.q) * a.b.ncls + dtab_class(ii, Li, a.b.q);
+      }
+      const int ch_lo = __ldg(pi + 4) * a.b.NN;
+      const unsigned ch_n = (unsigned)(min(a.b.nch, (__ldg(pi + 4) + __ldg(pi + 5)) * a.b.NN) - ch_lo);
+      const float wv = __ldg(a.b.wrow + pp);
+      const int nf = fused_nfwd(f);
+      for (int n = f.n_lo; n < f.n_hi && ok; ++n) {
+        const int fl = fused_tile(f, n);
+        if (!fl) continue;
+        const int xb = ti % XB, use = cnt_use[xb]++;
+        float* xh = xs + (xb * 2 + half) * (XHALF / 4);  // [64 ch][128 pos]
+        const int n0 = n * BWD_BN;
+        if (aborted(&abort_flag) || !tc::mbar_wait(&xfull[xb][half], use & 1, WAIT_LIMIT)) {
+          ok = false;
+          break;
+        }
+        if (fl & 1) {
+          const int buf = bt & 1;
+          float dpre[16];
+          load_dtab16(a.b.dtab + (int64_t)cls * a.b.CHP + n0 + (half * 4 + sub * 2) * 16, dpre);
+          if (!tc::mbar_wait(&tfull[buf], (bt >> 1) & 1, WAIT_LIMIT)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t tC = tmem_base + buf * 128 + lane_off;
+#pragma unroll
+          for (int cc = 0; cc < 2; ++cc) {
+            const int c = half * 4 + sub * 2 + cc;
+            const int chb = n0 + c * 16;
+            float cv[16], dv[16];
+            if (cc == 0) {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) dv[j] = dpre[j];
+            } else {
+              load_dtab16(a.b.dtab + (int64_t)cls * a.b.CHP + chb, dv);
+            }
+            tc::tmem_ld16(tC + c * 16, cv);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              float* xp = xh + ((sub * 2 + cc) * 16 + j) * BM + row;
+              if (pos_ok && (unsigned)(chb + j - ch_lo) < ch_n) {
+                const float xo = *xp;
+                float xc = __fdividef(xo * cv[j], dv[j] + a.b.d_eps);  // :130  X .* C ./ D
+                if (!(xc >= 0.f) || isinf(xc)) xc = 0.f;               // :132-134
+                float xn = __fmaf_rn(xc, wv, __fmul_rn(1.f - wv, xo));  // :136
+                if (xn < 0.f) xn = 0.f;                                // :137
+                *xp = xn;
+              }
+            }
+          }
+          tc::tc_fence_before();
+          ++bt;
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&tempty[buf]);
+        }
+        // this warp's part of the half written (or read only): the I/O warp may store it
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&hdone[ti & 1][half]);
+        if (fl & (2 << half)) {
+          // the stored FP32 half -> BF16 hi / lo forward operand, in place
+          if (!tc::mbar_wait(&xstored[xb][half], use & 1, WAIT_LIMIT)) {
+            ok = false;
+            break;
+          }
+          float x[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) x[j] = xh[(sub * 32 + j) * BM + row];
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&rdone[xb][half]);
+          if (!tc::mbar_wait(&rdone[xb][half], cnt_fwd[xb]++ & 1, WAIT_LIMIT)) {
+            ok = false;
+            break;
+          }
+          uint8_t* xb8 = reinterpret_cast<uint8_t*>(xh);
+#pragma unroll
+          for (int q8 = 0; q8 < 4; ++q8) {
+            const int c8 = sub * 4 + q8;
+            __align__(16) bf16 hi[8];
+            __align__(16) bf16 lo[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) split_bf16(x[q8 * 8 + j], hi[j], lo[j]);
+            const int off = row * 128 + ((c8 ^ (row & 7)) << 4);
+            *reinterpret_cast<uint4*>(xb8 + off) = *reinterpret_cast<const uint4*>(hi);
+            if (need_alo) *reinterpret_cast<uint4*>(xb8 + TILE_A + off) = *reinterpret_cast<const uint4*>(lo);
+          }
+          tc::fence_proxy_async_smem();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&aready[xb][half]);
+        }
+        ++ti;
+      }
+      if (!ok || !f.wnext) continue;
+      // the split's partial Y of this position tile: 15 16-column chunks over the 4 warps of
+      // this TMEM quadrant (an item without forward K-steps writes zeros, as k_tc_fwd does)
+      float* out = a.ypart + (int64_t)f.s * a.NB * a.MP + m0 + row;
+      const int wq = e >> 2;  // 0..3: warp within the quadrant
+      if (nf > 0) {
+        if (!tc::mbar_wait(&yfull, yitems & 1, WAIT_LIMIT)) {
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        for (int c = wq; c < a.NB / 16; c += 4) {
+          float v[16];
+          tc::tmem_ld16(tmem_base + 256 + lane_off + c * 16, v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) out[(int64_t)(c * 16 + j) * a.MP] = v[j];
+        }
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&ydone);
+        ++yitems;
+      } else {
+        for (int c = wq; c < a.NB / 16; c += 4)
+#pragma unroll
+          for (int j = 0; j < 16; ++j) out[(int64_t)(c * 16 + j) * a.MP] = 0.f;
+      }
+    }
+    if (!ok) {
+      if (lane == 0) atomicExch(a.b.err, TC_ERR_TIMEOUT_EPILOGUE);
+      set_abort(&abort_flag);
+    }
+  } else if (warp == BWD_IO_WARP) {
+    if (lane == 0) {
+      // ---------------- X I/O: first XB active tiles in; per tile store the updated halves,
+      // tell the epilogue they are stored, and refill the buffer once the forward MMAs of
+      // both halves have read it
+      int ti = 0, loaded = 0;
+      int cnt_free[XB][2] = {};
+      bool ok = true;
+      // the active tiles of this CTA in order; next_tile yields the next one not yet loaded
+      int li_item = blockIdx.x, li_n = -1;
+      FusedItem li_f;
+      bool li_valid = false;
+      auto next_tile = [&](int& m_out, int& n_out) -> bool {
+        while (li_item < nitems) {
+          if (!li_valid) {
+            li_f = fused_item(a, li_item);
+            li_n = li_f.n_lo - 1;
+            li_valid = true;
+          }
+          for (++li_n; li_n < li_f.n_hi; ++li_n)
+            if (fused_tile(li_f, li_n)) {
+              m_out = li_f.m;
+              n_out = li_n;
+              return true;
+            }
+          li_item += gridDim.x;
+          li_valid = false;
+        }
+        return false;
+      };
+      auto load = [&](int xb, int m, int n) {
+        for (int h = 0; h < 2; ++h) {
+          tc::mbar_arrive_expect_tx(&xfull[xb][h], XHALF);
+          tc::tma_load_2d(xs + (xb * 2 + h) * (XHALF / 4), &mX, &xfull[xb][h], m * BM, n * BWD_BN + 64 * h);
+        }
+        ++loaded;
+      };
+      for (int b = 0; b < XB; ++b) {
+        int m, n;
+        if (!next_tile(m, n)) break;
+        load(b, m, n);
+      }
+      for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+        const FusedItem f = fused_item(a, item);
+        for (int n = f.n_lo; n < f.n_hi && ok; ++n) {
+          const int fl = fused_tile(f, n);
+          if (!fl) continue;
+          const int xb = ti % XB;
+          for (int h = 0; h < 2 && ok; ++h) {
+            if (aborted(&abort_flag) || !tc::mbar_wait(&hdone[ti & 1][h], (ti >> 1) & 1, WAIT_LIMIT)) {
+              ok = false;
+              break;
+            }
+            if (fl & 1) {
+              tc::tma_store_2d(&mX, xs + (xb * 2 + h) * (XHALF / 4), f.m * BM, n * BWD_BN + 64 * h);
+              tc::bulk_commit();
+            }
+          }
+          if (!ok) break;
+          tc::bulk_wait_read0();
+          for (int h = 0; h < 2; ++h) tc::mbar_arrive(&xstored[xb][h]);
+          int m2, n2;
+          if (next_tile(m2, n2)) {  // tile ti + XB, into this buffer
+            // the buffer is free once the forward MMAs that read its halves are done
+            for (int h = 0; h < 2 && ok; ++h) {
+              if (!(fl & (2 << h))) continue;
+              if (!tc::mbar_wait(&afree[xb][h], cnt_free[xb][h] & 1, WAIT_LIMIT)) ok = false;
+              ++cnt_free[xb][h];
+            }
+            if (!ok) break;
+            load(xb, m2, n2);
+          } else {
+            for (int h = 0; h < 2; ++h)
+              if (fl & (2 << h)) ++cnt_free[xb][h];
+          }
+          ++ti;
+        }
+      }
+      if (!ok) {
+        if (!aborted(&abort_flag)) atomicExch(a.b.err, TC_ERR_TIMEOUT_EPILOGUE);
+        set_abort(&abort_flag);
+      }
+      tc::bulk_wait0();
+      // loads not consumed (after an abort) must land before the CTA exits
+      for (int k = ti; k < loaded; ++k)
+        for (int h = 0; h < 2; ++h)
+          if (!tc::mbar_wait(&xfull[k % XB][h], (k / XB) & 1, WAIT_LIMIT)) atomicExch(a.b.err, TC_ERR_TIMEOUT_DRAIN);
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) tc::tmem_dealloc(tmem_base, 512);
+}
+
 // ------------------------------------------------------------------ small kernels
 // Tensor-core channels are plane-major (ch = z*N*N + beta*N + alpha); the FP32 tap tables
 // are indexed by the channel-major (beta*N + alpha)*Z + z.
@@ -1023,6 +1553,7 @@ struct TcPsfState {
   int KB = 0, NB = 0, NH = 0, nparts = 1, CHP = 0;
   int fwd_dyn_max = 0;  // dynamic shared memory available to the forward GEMM
   int bwd_dyn_max = 0;  // ... and to the back projection (smallest of its instantiations)
+  int fused_dyn_max = 0;  // ... and to the fused back projection + forward
   DevBuf dtab[2];       // D class tables of every view, [view][ncls][ncls][CHP]; taps hi / hi + lo
   DevBuf wbx_hi, wbx_lo, wft_hi, wft_lo;
   CUtensorMap mBh, mBl, mFh, mFl;
@@ -1132,6 +1663,13 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
     MLF_TRY(allow_max_dyn_smem((const void*)k_tc_dtab<bf16>));
     MLF_TRY(allow_max_dyn_smem((const void*)k_tc_dtab<f16>));
     t->bwd_dyn_max = bmax;
+    int fmx = optin;
+    for (const void* f : {(const void*)k_tc_bwdfwd<1>, (const void*)k_tc_bwdfwd<2>}) {
+      MLF_CUDA(cudaFuncGetAttributes(&fb, f));
+      MLF_TRY(allow_max_dyn_smem(f));
+      fmx = std::min(fmx, optin - (int)fb.sharedSizeBytes);
+    }
+    t->fused_dyn_max = fmx;
     if (bwd_smem_bytes(1, 1, true, 1) > (size_t)bmax)
       return fail(MLF_ERR_UNSUPPORTED, "tensor-core back projection needs more shared memory than the device offers");
     for (const void* f : {(const void*)k_tc_fwd<false>, (const void*)k_tc_fwd<true>}) {
@@ -1257,7 +1795,9 @@ int tc_work_create(Psf* psf, const std::vector<Solver*>& members, TcSolverState*
   MLF_CUDA(cudaDeviceGetAttribute(&t->nsm, cudaDevAttrMultiProcessorCount, members[0]->device));
   const int mt = t->MP / BM;
   t->splits = std::max(1, std::min(t->KSF, t->nsm / std::max(1, mt)));
-  t->ks_per_split = (t->KSF + t->splits - 1) / t->splits;
+  // even K-steps per split: a split then covers whole 128-channel tiles (the fused kernel's
+  // work items keep the forward GEMM's split boundaries)
+  t->ks_per_split = (((t->KSF + t->splits - 1) / t->splits) + 1) & ~1;
   t->splits = (t->KSF + t->ks_per_split - 1) / t->ks_per_split;
   t->splits_def = t->splits;
   t->ksp_def = t->ks_per_split;
@@ -1499,6 +2039,63 @@ int tc_bwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, con
 }
 
 
+// The fused back projection + next forward applies to the BF16 modes with D from the class
+// tables, a forward taps tile of one MMA (N <= 256) and even split sizes; MLF_FUSED=0 keeps
+// the two kernels.
+bool tc_fused_ok(const Psf* psf, const TcSolverState* t, int precision) {
+  if (precision != MLF_PREC_BF16 && precision != MLF_PREC_BF16X2) return false;
+  const TcPsfState* tp = psf->tc;
+  if (!t->dtab_ok || tp->nparts != 1 || tp->NB > 256 || t->ks_per_split % 2 != 0) return false;
+  const char* env = std::getenv("MLF_FUSED");
+  if (env && std::strcmp(env, "0") == 0) return false;
+  int alo, blo;
+  splits_of(precision, &alo, &blo);
+  return !blo && bwd_smem_bytes(alo, 0, false, 1) <= (size_t)tp->fused_dyn_max;
+}
+
+int tc_bwdfwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, int view_next, const float* wrow,
+                     const float* wnext, cudaStream_t st, bool cancellable = false) {
+  const TcPsfState* tp = psf->tc;
+  int alo, blo;
+  splits_of(precision, &alo, &blo);
+  const int q = psf->q, nc = 2 * q + 3;
+  const DevBuf& dt = tp->dtab[0];
+  if (!dt.p) return fail(MLF_ERR_INVALID, "tensor-core D class tables not prepared");
+  TcFusedArgs a{};
+  a.b.err = t->err.as<int>();
+  a.b.tile_patch = t->tile_patch.as<int>();
+  a.b.pinfo = t->pinfo.as<int>();
+  a.b.wrow = wrow;
+  a.b.CHP = tp->CHP; a.b.nch = (int)psf->nch; a.b.KB = tp->KB; a.b.brow0 = view * tp->CHP; a.b.NN = psf->N * psf->N;
+  a.b.use_alo = alo;
+  a.b.use_blo = 0;
+  a.b.d_eps = t->d_eps;
+  a.b.dtab = dt.as<float>() + (int64_t)view * nc * nc * tp->CHP;
+  a.b.q = q;
+  a.b.ncls = nc;
+  if (cancellable) a.b.cancel = cancel_ref(t->cancel);
+  a.ypart = t->ypart.as<float>();
+  a.wview = wnext;
+  a.MP = t->MP;
+  a.NB = tp->NB;
+  a.splits = t->splits;
+  a.ks_per_split = t->ks_per_split;
+  a.KS = t->KSF;
+  a.frow0 = view_next * tp->NB;
+  a.ntiles = tp->CHP / BWD_BN;
+  const int nitems = (t->MP / BM) * t->splits;
+  const int grid = std::min(nitems, t->nsm);
+  int xbufs = bwd_smem_bytes(alo, 0, false, 2) <= (size_t)tp->fused_dyn_max ? 2 : 1;
+  if (t->xbufs == 1) xbufs = 1;
+  const size_t smem = bwd_smem_bytes(alo, 0, false, xbufs);
+  if (xbufs == 2)
+    k_tc_bwdfwd<2><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, tp->mBh, t->mXv, tp->mFh, a, nitems);
+  else
+    k_tc_bwdfwd<1><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, tp->mBh, t->mXv, tp->mFh, a, nitems);
+  MLF_LAUNCHED();
+  return MLF_OK;
+}
+
 // The view loop of one iteration over all patches of the work set.
 int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* timer, int64_t* launches,
                      cudaStream_t st) {
@@ -1512,8 +2109,20 @@ int tc_enqueue_views(const Psf* psf, TcSolverState* t, int precision, Solver* ti
   MLF_TRY(tc_col2im(psf, t, t->views[0], true, nullptr, st, precision, 0));
   MLF_TRY(tc_im2col_ratio(psf, t, precision, st, 0));
   n += 3;
+  const bool fused = tc_fused_ok(psf, t, precision);
   for (int k = 0; k < V; ++k) {
     MLF_TRY(timing_mark(timer, st));
+    if (fused && k + 1 < V) {
+      // back projection of view k and forward projection of view k+1 in one launch
+      MLF_TRY(tc_bwdfwd_launch(psf, t, precision, t->views[k], t->views[k + 1],
+                               t->wtab_dev.as<float>() + (size_t)k * t->P,
+                               t->wtab_dev.as<float>() + (size_t)(k + 1) * t->P, st, true));
+      MLF_TRY(timing_mark(timer, st));
+      MLF_TRY(tc_col2im(psf, t, t->views[k + 1], true, nullptr, st, precision, (k + 1) & 1));
+      MLF_TRY(tc_im2col_ratio(psf, t, precision, st, (k + 1) & 1));
+      n += 3;
+      continue;
+    }
     MLF_TRY(tc_bwd_launch(psf, t, precision, t->views[k], t->wtab_dev.as<float>() + (size_t)k * t->P, st, k & 1, true));
     ++n;
     if (k + 1 < V) {
@@ -1622,7 +2231,7 @@ int tc_autotune(const Psf* psf, TcSolverState* t, int precision, cudaStream_t st
   const float* w0 = t->wtab_dev.as<float>();
   float best = 1e30f;
   for (int s : {std::max(1, t->splits_def / 2), t->splits_def, t->splits_max}) {
-    const int ksp = (t->KSF + s - 1) / s;
+    const int ksp = (((t->KSF + s - 1) / s) + 1) & ~1;
     const int sp = (t->KSF + ksp - 1) / ksp;
     if (sp > t->splits_max) continue;
     for (int stg = 2; stg <= FWD_MAX_STAGES; ++stg) {
