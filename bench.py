@@ -48,7 +48,9 @@ WORKLOAD_DESC = ("Nnum 15, 67x67 lenslets (1005x1005 px), 51 planes (0-200 um at
 
 
 KVIEW_DRAM_BYTES = 393.3e6     # k_view MODE_STEP launch, 1005x1005x51, FP32 (ncu, 2 launches: 229.9 + 163.4 MB)
-KTC_DRAM_BYTES = {"k_tc_bwd": 390.7e6, "k_tc_fwd": 220.5e6}   # per launch, same workload, bf16x2
+# per launch, same workload, bf16x2 (ncu): the fused view step (back projection + next forward),
+# and the two-kernel form it replaces (MLF_FUSED=0)
+KTC_DRAM_BYTES = {"k_tc_bwdfwd": 412.4e6, "two_kernel_form": {"k_tc_bwd": 390.7e6, "k_tc_fwd": 220.5e6}}
 
 
 def max_over_ranks(x, ws, dev=None):
@@ -396,8 +398,9 @@ def main():
                               "traffic": KTC_DRAM_BYTES if (Xr, Xc, Z) == (1005, 1005, 51) else None,
                               "peak": _measured_bf16(), "unit": "TFLOP/s",
                               "frac": (mflop / (mk_ms * 1e-3) / 1e12) / _measured_bf16() if _measured_bf16() else None,
-                              "note": "algorithmic flop of the projections / time of the two GEMM kernels "
-                                      "(back projection + update, next-view forward); peak = measured bf16 burst"}}
+                              "note": "algorithmic flop of the projections / time of the view-step GEMM kernels "
+                                      "(fused back projection + update + next-view forward, k_tc_bwdfwd); "
+                                      "peak = measured bf16 burst"}}
 
     # e2e: pinned host image in, pinned host volume out, through mlf_solver_run
     lf_host = torch.empty((Xc, Xr), dtype=torch.float32, pin_memory=True).t()

@@ -773,7 +773,8 @@ k_tc_fwd(const __grid_constant__ CUtensorMap mX, const __grid_constant__ CUtenso
 //              the same 32 KB in the K-major 128-byte-swizzled layout; after the item's last
 //              forward MMA it drains Y (TMEM) into the split's partials
 //   X I/O:     loads, stores, and reloads a buffer only after the forward MMAs that read it
-// TMEM: C buffers at columns 0 and 128, Y at 256 (NB <= 256 columns).  Every wait is
+// TMEM: C buffers at columns 0 and 128, Y at 256 (NB <= 256 columns).  XB X buffers per
+// half and an NS-stage operand ring: (2, 2) or (1, 3) fit the shared memory.  Every wait is
 // bounded; a timeout sets the device status word and the abort flag.
 struct TcFusedArgs {
   TcBwdArgs b;
@@ -822,7 +823,7 @@ __device__ __forceinline__ int fused_nfwd(const FusedItem& f) {
   return c;
 }
 
-template <int XB>
+template <int XB, int NS>
 __global__ void __launch_bounds__(BWD_THREADS, 1)
 k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
             const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mX,
@@ -835,7 +836,7 @@ k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUt
   }
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
-  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], xfull[XB][2], hdone[2][2],
+  __shared__ __align__(8) uint64_t full[NS], empty[NS], tfull[2], tempty[2], xfull[XB][2], hdone[2][2],
       xstored[XB][2], rdone[XB][2], aready[XB][2], afree[XB][2], yfull, ydone, mdone;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
@@ -843,9 +844,9 @@ k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUt
   const int KS = a.b.KB / BK;
   const bool need_alo = a.b.use_alo != 0;
   const BwdLayout L = bwd_layout(a.b.use_alo, 0, false);
-  float* xs = reinterpret_cast<float*>(smem + STAGES * L.stage);  // [XB][2 halves][64 ch][128 pos]
+  float* xs = reinterpret_cast<float*>(smem + NS * L.stage);  // [XB][2 halves][64 ch][128 pos]
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
+    for (int s = 0; s < NS; ++s) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
@@ -887,8 +888,8 @@ k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUt
       bool ok = true;
       int pn = -1, pfl = 0;  // previous active tile
       auto stage = [&](bool fwd, int ks, int m0, int n0) {
-        const int s = it % STAGES;
-        const uint32_t ph = (it / STAGES) & 1;
+        const int s = it % NS;
+        const uint32_t ph = (it / NS) & 1;
         if (!tc::mbar_wait(&empty[s], ph ^ 1, WAIT_LIMIT)) {
           set_abort(&abort_flag);
           atomicExch(a.b.err, TC_ERR_TIMEOUT_PRODUCER);
@@ -925,8 +926,8 @@ k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUt
         for (int h = 0; h < 2 && ok; ++h)
           if (pfl & (2 << h)) stage(true, 2 * pn + h, 0, 0);
       // drain: every issued copy must have landed before the CTA can exit
-      for (int i = std::max(0, it - STAGES); i < it; ++i)
-        if (!tc::mbar_wait(&full[i % STAGES], (i / STAGES) & 1, WAIT_LIMIT)) atomicExch(a.b.err, TC_ERR_TIMEOUT_DRAIN);
+      for (int i = std::max(0, it - NS); i < it; ++i)
+        if (!tc::mbar_wait(&full[i % NS], (i / NS) & 1, WAIT_LIMIT)) atomicExch(a.b.err, TC_ERR_TIMEOUT_DRAIN);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -943,8 +944,8 @@ k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUt
       int cur_left = 0;
       bool cur_first = false;
       auto wait_stage = [&]() -> uint32_t {
-        const int s = it % STAGES;
-        const uint32_t ph = (it / STAGES) & 1;
+        const int s = it % NS;
+        const uint32_t ph = (it / NS) & 1;
         if (!tc::mbar_wait(&full[s], ph, WAIT_LIMIT)) {
           set_abort(&abort_flag);
           atomicExch(a.b.err, TC_ERR_TIMEOUT_MMA);
@@ -982,7 +983,7 @@ k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUt
             if (need_alo) tc::mma_bf16(tY, tc::desc_kmajor_sw128(xa + TILE_A + 32 * k), dbh, fdesc_i, 1u);
           }
           first = false;
-          tc::mma_commit(&empty[it % STAGES]);
+          tc::mma_commit(&empty[it % NS]);
           tc::mma_commit(&afree[xb][h]);
           ++it;
           if (--left == 0) {
@@ -1019,7 +1020,7 @@ k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUt
                 tc::mma_bf16(tC, dah, dbh, bdesc_i, acc);
                 if (need_alo) tc::mma_bf16(tC, tc::desc_kmajor_sw128(st + L.offAl + 32 * k), dbh, bdesc_i, 1u);
               }
-              tc::mma_commit(&empty[it % STAGES]);
+              tc::mma_commit(&empty[it % NS]);
               ++it;
             }
             if (!ok) break;
@@ -1664,7 +1665,7 @@ int tc_psf_prepare(Psf* p, cudaStream_t st) {
     MLF_TRY(allow_max_dyn_smem((const void*)k_tc_dtab<f16>));
     t->bwd_dyn_max = bmax;
     int fmx = optin;
-    for (const void* f : {(const void*)k_tc_bwdfwd<1>, (const void*)k_tc_bwdfwd<2>}) {
+    for (const void* f : {(const void*)k_tc_bwdfwd<1, 3>, (const void*)k_tc_bwdfwd<2, 2>}) {
       MLF_CUDA(cudaFuncGetAttributes(&fb, f));
       MLF_TRY(allow_max_dyn_smem(f));
       fmx = std::min(fmx, optin - (int)fb.sharedSizeBytes);
@@ -2050,7 +2051,7 @@ bool tc_fused_ok(const Psf* psf, const TcSolverState* t, int precision) {
   if (env && std::strcmp(env, "0") == 0) return false;
   int alo, blo;
   splits_of(precision, &alo, &blo);
-  return !blo && bwd_smem_bytes(alo, 0, false, 1) <= (size_t)tp->fused_dyn_max;
+  return !blo && 3 * (size_t)bwd_layout(alo, 0, false).stage + XTILE + 1024 <= (size_t)tp->fused_dyn_max;
 }
 
 int tc_bwdfwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, int view_next, const float* wrow,
@@ -2085,13 +2086,19 @@ int tc_bwdfwd_launch(const Psf* psf, TcSolverState* t, int precision, int view, 
   a.ntiles = tp->CHP / BWD_BN;
   const int nitems = (t->MP / BM) * t->splits;
   const int grid = std::min(nitems, t->nsm);
-  int xbufs = bwd_smem_bytes(alo, 0, false, 2) <= (size_t)tp->fused_dyn_max ? 2 : 1;
-  if (t->xbufs == 1) xbufs = 1;
-  const size_t smem = bwd_smem_bytes(alo, 0, false, xbufs);
-  if (xbufs == 2)
-    k_tc_bwdfwd<2><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, tp->mBh, t->mXv, tp->mFh, a, nitems);
+  // (X buffers, ring stages): (2, 2), or (1, 3) where two X buffers do not fit or the
+  // environment sets MLF_FUSED_XB=1 (slower on the 1005 x 1005 x 51 workload: 0.218 vs
+  // 0.189 ms per view, the single X buffer serialises the tiles)
+  const size_t stage = (size_t)bwd_layout(alo, 0, false).stage;
+  const size_t smem22 = 2 * stage + 2 * (size_t)XTILE + 1024, smem13 = 3 * stage + (size_t)XTILE + 1024;
+  const char* env = std::getenv("MLF_FUSED_XB");
+  bool one = env && std::strcmp(env, "1") == 0;
+  if (smem22 > (size_t)tp->fused_dyn_max) one = true;
+  if (one && smem13 > (size_t)tp->fused_dyn_max) return fail(MLF_ERR_UNSUPPORTED, "fused view step: shared memory");
+  if (one)
+    k_tc_bwdfwd<1, 3><<<grid, BWD_THREADS, smem13, st>>>(t->mARh, t->mARl, tp->mBh, t->mXv, tp->mFh, a, nitems);
   else
-    k_tc_bwdfwd<1><<<grid, BWD_THREADS, smem, st>>>(t->mARh, t->mARl, tp->mBh, t->mXv, tp->mFh, a, nitems);
+    k_tc_bwdfwd<2, 2><<<grid, BWD_THREADS, smem22, st>>>(t->mARh, t->mARl, tp->mBh, t->mXv, tp->mFh, a, nitems);
   MLF_LAUNCHED();
   return MLF_OK;
 }
