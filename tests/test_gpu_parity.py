@@ -137,6 +137,35 @@ def test_view_step_matches_oracle(cuda, lenslets, K0, Z):
         assert rel_l2(got, ref) <= 1e-5, (u, v, rel_l2(got, ref))
 
 
+# Patches with 128..160 output tiles run two channel slots per CTA (slots on warp
+# boundaries), more than 8 tile columns take the bank-spreading lane order, and the staged
+# planes use the swizzled column layout at a pitch of 4 mod 8 floats; 72 x 80 lenslets
+# (180 tiles) run one slot.
+@pytest.mark.parametrize("lenslets,K0,Z", [((64, 64), 61, 2), ((67, 61), 61, 2), ((61, 67), 91, 2),
+                                           ((72, 80), 61, 1)])
+def test_view_step_large_patches_match_oracle(cuda, lenslets, K0, Z):
+    from mesolf_gb300 import PhaseSpacePSF, RLSolver
+    w = synth.small_config(lenslets=lenslets, K0=K0, Z=Z)
+    H, Ht = w.psf()
+    Hn, Htn = R.normalize_psf(H, Ht)
+    Hps, Htc = R.gen_phasespace_psf(Hn, Htn)
+    Xr, Xc = w.image_shape
+    rng = np.random.default_rng(K0 + Z)
+    LF = rng.uniform(50.0, 150.0, (Xr, Xc)).astype(np.float32)
+    X = rng.uniform(0.5, 1.5, (Xr, Xc, Z)).astype(np.float32)
+    psf = PhaseSpacePSF(H, Ht)
+    s = RLSolver(psf, LF.shape)
+    for (u, v) in [(7, 7), (0, 0), (14, 3)]:
+        ref = R.rl_view_step(X.astype(np.float64), LF.astype(np.float64), Hps, Htc, u, v, 0.3, 15)
+        got = to_host(s.view_step(to_dev(LF), to_dev(X), u, v, 0.3))
+        assert rel_l2(got, ref) <= 1e-5, (u, v, rel_l2(got, ref))
+        hx = to_host(s.forward_view(to_dev(X), u, v))
+        refh = R.forward_ps(Hps[:, :, u, v, :], X.astype(np.float64), 15)
+        assert rel_l2(hx, refh) <= 1e-5, (u, v)
+    s.close()
+    psf.close()
+
+
 @pytest.mark.parametrize("shape,Z", [((60, 45), 5), ((165, 165), 21), ((45, 90), 3)])
 def test_sample_filter_matches_oracle(cuda, shape, Z):
     from mesolf_gb300 import PhaseSpacePSF, RLSolver
