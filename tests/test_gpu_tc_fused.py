@@ -2,7 +2,8 @@
 of view k+1 in one launch, k_tc_bwdfwd) against the two-kernel form (k_tc_bwd + k_tc_fwd,
 selected with MLF_FUSED=0).  The fused kernel keeps the forward GEMM's split boundaries and
 K-step order, so the solves are bit-identical; it launches one kernel fewer per view step.
-The autotuner is off (MLF_TUNE=0) so that both solves use the same launch configuration.
+The autotuner is off (MLF_TUNE=0) so that both solves use the same launch configuration;
+both buffer layouts of the fused kernel are covered (MLF_FUSED_XB).
 Shapes: one 128-channel tile per split (9 x 8 lenslets, 7 planes), several tiles per split
 and several position tiles (20 x 18, 6 planes), and the 67 x 67 lenslet patch (3 planes)."""
 import numpy as np
@@ -29,9 +30,11 @@ def rel_l2(a, b):
 
 @pytest.mark.parametrize("lenslets,K0,Z", CASES)
 @pytest.mark.parametrize("prec", ["bf16x2", "bf16"])
-def test_fused_solve_equals_two_kernel_solve(cuda, monkeypatch, lenslets, K0, Z, prec):
+@pytest.mark.parametrize("xb", ["2", "1"])  # two X buffers and a 2-stage ring, or one and three
+def test_fused_solve_equals_two_kernel_solve(cuda, monkeypatch, lenslets, K0, Z, prec, xb):
     from mesolf_gb300 import PhaseSpacePSF, RLSolver
     monkeypatch.setenv("MLF_TUNE", "0")
+    monkeypatch.setenv("MLF_FUSED_XB", xb)
     w = synth.small_config(lenslets=lenslets, K0=K0, Z=Z)
     H, Ht = w.psf()
     Xr, Xc = w.image_shape
