@@ -324,9 +324,9 @@ struct ViewArgs {
 };
 enum ViewMode { MODE_FWD = 0, MODE_STEP = 1, MODE_BWDC = 2 };
 
-// View-kernel tiling shared by host and device.  Each thread owns an 8 (b) x 4 (a)
-// output tile; the forward-input plane keeps its interior at column offset
-// tap-row pitch of the view kernel's shared tap buffers
+// View-kernel geometry shared by host and device (the tiles: VW_TY x VW_TX below for
+// k_view, VT_TY x VT_TX in mlf_view.cuh for the allocation-free forward projection).
+// Tap-row pitch of the view kernels' shared tap buffers:
 constexpr int view_tap_pitch(int T) { return (T + 3) & ~3; }
 // view_qpad(q) = round_up(q, 4) (16-byte aligned for cp.async), so the window offset of the
 // forward correlation is view_qpad(q) - q; the back projection's is s_alpha + 1 in {0,1,2}.

@@ -112,8 +112,16 @@ constexpr int SF = 16;
 __device__ __forceinline__ float to_f(uint16_t x) { return __uint_as_float(0x4B000000u | x) - 8388608.f; }
 __device__ __forceinline__ float to_f(float x) { return x; }
 
+__device__ __forceinline__ void rc_cp_async16(void* smem, const void* gmem, int src_bytes) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem), "r"(src_bytes) : "memory");
+}
+
+// Persistent over frame chunks z = blockIdx.z, blockIdx.z + gridDim.z, ...: the raw tile of
+// chunk z+1 is copied into the second buffer (16-byte zero-filling cp.async, no register
+// round trip) while chunk z is interpolated, so DRAM loads stay in flight.
 template <typename TIn>
-__global__ void __launch_bounds__(RC_ROWS * RC_COLS, 4)
+__global__ void __launch_bounds__(RC_ROWS * RC_COLS, 3)
 k_rectify_staged(const TIn* __restrict__ raw, int64_t total, int64_t fstride, int64_t cstride, int64_t row0,
                  int64_t col0, const int* __restrict__ iy, const float* __restrict__ wy, int oh,
                  const int* __restrict__ ix, const float* __restrict__ wx, int ow, int64_t f0, int64_t fstep,
@@ -121,73 +129,84 @@ k_rectify_staged(const TIn* __restrict__ raw, int64_t total, int64_t fstride, in
   constexpr int VEC = 16 / sizeof(TIn);
   constexpr int NT = RC_ROWS * RC_COLS;
   extern __shared__ __align__(16) unsigned char rc_smem[];
-  TIn* tile = reinterpret_cast<TIn*>(rc_smem);  // [SF][maxc][slot]
-  __shared__ int off[SF][8];
+  TIn* tiles = reinterpret_cast<TIn*>(rc_smem);  // [2 buffers][SF][maxc][slot]
+  __shared__ int off[2][SF][8];
   const int tid = threadIdx.y * RC_ROWS + threadIdx.x;
   const int r0 = blockIdx.x * RC_ROWS, c0 = blockIdx.y * RC_COLS;
   const int r1 = min(r0 + RC_ROWS, oh) - 1, c1 = min(c0 + RC_COLS, ow) - 1;
   const int rlo = __ldg(iy + r0), nrow = __ldg(iy + r1) + 2 - rlo;
   const int clo = __ldg(ix + c0), ncol = __ldg(ix + c1) + 2 - clo;  // <= maxc (host bound)
   const int nv = (nrow + 2 * VEC - 2) / VEC;                         // vectors per column segment
-  const int64_t ib = (int64_t)blockIdx.z * SF;
-  const int nf = (int)(n_out - ib < SF ? n_out - ib : SF);
-  // staging: a thread keeps one (column k, vector v) of the footprint and walks the frames
-  // q = g, g + G, ... (G groups of ncol * nv threads), so the index split is done once
-  {
-    const int cnv = ncol * nv;
-    const int G = NT / cnv;  // >= 1: the host bounds nrow and maxc
-    const int g = tid / cnv, rem = tid - g * cnv;
-    const int k = rem / nv, v = rem - k * nv;
-    if (g < G) {
-      const int64_t colbase = (row0 + rlo) + cstride * (col0 + clo + k);
-      const int64_t fdelta = (int64_t)G * fstep * fstride;
-      int64_t e = (f0 + (ib + g) * fstep) * fstride + colbase;
-      for (int q = g; q < nf; q += G, e += fdelta) {
-        const int64_t ea = e & ~(int64_t)(VEC - 1);
-        if (v == 0) off[q][k] = (int)(e - ea);
-        TIn* dst = tile + ((int64_t)q * maxc + k) * slot + (int64_t)v * VEC;
-        const int64_t src = ea + (int64_t)v * VEC;
-        if (src + VEC <= total) {
-          *reinterpret_cast<uint4*>(dst) = __ldcs(reinterpret_cast<const uint4*>(raw + src));
-        } else {
+  const int64_t chunks = (n_out + SF - 1) / SF;
+  const int64_t fs = (int64_t)SF * maxc * slot;                    // elements per buffer
+  // staging role of this thread: one (column k, vector v) of the footprint, frames q = g, g+G, ...
+  const int cnv = ncol * nv;
+  const int G = NT / cnv;  // >= 1: the host bounds nrow and maxc
+  const int sg = tid / cnv, srem = tid - sg * cnv;
+  const int sk = srem / nv, sv = srem - sk * nv;
+  const int64_t colbase = (row0 + rlo) + cstride * (col0 + clo + sk);
+  auto stage = [&](int64_t z, int b) {
+    if (sg >= G) return;
+    const int64_t ib = z * SF;
+    const int nf = (int)(n_out - ib < SF ? n_out - ib : SF);
+    const int64_t fdelta = (int64_t)G * fstep * fstride;
+    int64_t e = (f0 + (ib + sg) * fstep) * fstride + colbase;
+    for (int q = sg; q < nf; q += G, e += fdelta) {
+      const int64_t ea = e & ~(int64_t)(VEC - 1);
+      if (sv == 0) off[b][q][sk] = (int)(e - ea);
+      TIn* dst = tiles + b * fs + ((int64_t)q * maxc + sk) * slot + (int64_t)sv * VEC;
+      const int64_t src = ea + (int64_t)sv * VEC;
+      const int64_t avail = total - src;  // elements of the frame buffer left from src
+      const int nbytes = avail >= VEC ? 16 : (avail > 0 ? (int)avail * (int)sizeof(TIn) : 0);
+      rc_cp_async16(dst, nbytes > 0 ? (const void*)(raw + src) : (const void*)raw, nbytes);
+    }
+  };
+  const int r = r0 + threadIdx.x, c = c0 + threadIdx.y;
+  const bool mine = r < oh && c < ow;
+  const int lr = mine ? __ldg(iy + r) - rlo : 0, lc = mine ? __ldg(ix + c) - clo : 0;
+  const float fy = mine ? __ldg(wy + r) : 0.f, fx = mine ? __ldg(wx + c) : 0.f;
+  const int64_t P = (int64_t)oh * ow;
+  const int per = maxc * slot;  // elements per staged frame
+  int b = 0;
+  if (blockIdx.z < chunks) stage(blockIdx.z, 0);
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  for (int64_t z = blockIdx.z; z < chunks; z += gridDim.z, b ^= 1) {
+    const int64_t zn = z + gridDim.z;
+    if (zn < chunks) stage(zn, b ^ 1);  // the other buffer was last read before the barrier below
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 1;\n" ::: "memory");
+    __syncthreads();  // chunk z staged by every thread
+    if (mine) {
+      const int64_t ib = z * SF;
+      const int nf = (int)(n_out - ib < SF ? n_out - ib : SF);
+      float* op = out + r + (int64_t)oh * c + P * ib;
+      const TIn* base = tiles + b * fs + (int64_t)lc * slot + lr;
+      if (same_align) {
+        // every frame has the same 16-byte alignment: the column offsets of frame 0 serve all
+        const TIn* ca = base + off[b][0][lc];
+        const TIn* cb = base + slot + off[b][0][lc + 1];
 #pragma unroll
-          for (int u = 0; u < VEC; ++u) dst[u] = src + u < total ? raw[src + u] : TIn(0);
+        for (int q = 0; q < SF; ++q) {
+          if (q < nf) {
+            const float v00 = to_f(ca[q * per]), v10 = to_f(ca[q * per + 1]);
+            const float v01 = to_f(cb[q * per]), v11 = to_f(cb[q * per + 1]);
+            const float a = fmaf(fx, v01 - v00, v00), bb = fmaf(fx, v11 - v10, v10);
+            __stcs(op + P * q, fmaf(fy, bb - a, a));
+          }
+        }
+      } else {
+#pragma unroll 4
+        for (int q = 0; q < nf; ++q) {
+          const TIn* ca = base + (int64_t)q * per + off[b][q][lc];
+          const TIn* cb = base + (int64_t)q * per + slot + off[b][q][lc + 1];
+          const float v00 = to_f(ca[0]), v10 = to_f(ca[1]), v01 = to_f(cb[0]), v11 = to_f(cb[1]);
+          const float a = fmaf(fx, v01 - v00, v00), bb = fmaf(fx, v11 - v10, v10);
+          __stcs(op + P * q, fmaf(fy, bb - a, a));
         }
       }
     }
+    __syncthreads();  // buffer b is read: the next iteration may stage into it
   }
-  __syncthreads();
-  const int r = r0 + threadIdx.x, c = c0 + threadIdx.y;
-  if (r >= oh || c >= ow) return;
-  const int lr = __ldg(iy + r) - rlo, lc = __ldg(ix + c) - clo;
-  const float fy = __ldg(wy + r), fx = __ldg(wx + c);
-  const int64_t P = (int64_t)oh * ow;
-  float* op = out + r + (int64_t)oh * c + P * ib;
-  const TIn* base = tile + (int64_t)lc * slot + lr;
-  const int fs = maxc * slot;  // elements per staged frame
-  if (same_align) {
-    // every frame has the same 16-byte alignment: the column offsets of frame 0 serve all
-    const TIn* ca = base + off[0][lc];
-    const TIn* cb = base + slot + off[0][lc + 1];
-#pragma unroll
-    for (int q = 0; q < SF; ++q) {
-      if (q < nf) {
-        const float v00 = to_f(ca[q * fs]), v10 = to_f(ca[q * fs + 1]);
-        const float v01 = to_f(cb[q * fs]), v11 = to_f(cb[q * fs + 1]);
-        const float a = fmaf(fx, v01 - v00, v00), b = fmaf(fx, v11 - v10, v10);
-        __stcs(op + P * q, fmaf(fy, b - a, a));
-      }
-    }
-    return;
-  }
-#pragma unroll 4
-  for (int q = 0; q < nf; ++q) {
-    const TIn* ca = base + (int64_t)q * fs + off[q][lc];
-    const TIn* cb = base + (int64_t)q * fs + slot + off[q][lc + 1];
-    const float v00 = to_f(ca[0]), v10 = to_f(ca[1]), v01 = to_f(cb[0]), v11 = to_f(cb[1]);
-    const float a = fmaf(fx, v01 - v00, v00), b = fmaf(fx, v11 - v10, v10);
-    __stcs(op + P * q, fmaf(fy, b - a, a));
-  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
 __global__ void k_rc_max(const float* __restrict__ a, int64_t n, float* __restrict__ part) {
@@ -286,9 +305,9 @@ int rectify_run(const void* d_raw, int dtype, int64_t total, int64_t fstride, in
     maxc = std::max(maxc, ix[std::min<int64_t>(c0 + RC_COLS, out_w) - 1] + 2 - ix[c0]);
   const int es = dtype == MLF_DTYPE_U16 ? 2 : 4, vec = 16 / es;
   const int slot = ((maxr + 2 * vec - 2) / vec) * vec;
-  const size_t smem = (size_t)SF * maxc * slot * es;
+  const size_t smem = 2 * (size_t)SF * maxc * slot * es;  // two chunk buffers
   const bool staged = navg == 1 && reinterpret_cast<uintptr_t>(d_raw) % 16 == 0 && maxc <= 8 &&
-                      smem <= 96 * 1024 && (out_w + RC_COLS - 1) / RC_COLS <= 65535;
+                      smem <= 112 * 1024 && (out_w + RC_COLS - 1) / RC_COLS <= 65535;
   const dim3 block(RC_ROWS, RC_COLS);
   if (staged) {
     const void* kf = dtype == MLF_DTYPE_U16 ? (const void*)k_rectify_staged<uint16_t> : (const void*)k_rectify_staged<float>;
@@ -297,8 +316,15 @@ int rectify_run(const void* d_raw, int dtype, int64_t total, int64_t fstride, in
     // frames whose starts differ by multiples of 16 bytes share the staged column offsets
     const int same_align = ((fstep * fstride) % vec == 0) ? 1 : 0;
     if (chunks > 65535) return fail(MLF_ERR_UNSUPPORTED, "mlf_rectify_frames: more than 1048560 output frames");
+    // blocks loop over frame chunks (prefetching the next one): enough z-slices for about
+    // sixteen waves of resident blocks (a short last wave), each slice walking its chunks
+    int dev = 0, nsm = 0;
+    MLF_CUDA(cudaGetDevice(&dev));
+    MLF_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t gxy = ((out_h + RC_ROWS - 1) / RC_ROWS) * ((out_w + RC_COLS - 1) / RC_COLS);
+    const int64_t zb = std::max<int64_t>(1, std::min<int64_t>(chunks, (16 * 3 * (int64_t)nsm + gxy - 1) / gxy));
     const dim3 grid((unsigned)((out_h + RC_ROWS - 1) / RC_ROWS), (unsigned)((out_w + RC_COLS - 1) / RC_COLS),
-                    (unsigned)chunks);
+                    (unsigned)zb);
     if (dtype == MLF_DTYPE_U16)
       k_rectify_staged<uint16_t><<<grid, block, smem, st>>>(static_cast<const uint16_t*>(d_raw), total, fstride,
                                                             cstride, row0, col0, d_iy, d_wy, (int)out_h, d_ix, d_wx,
