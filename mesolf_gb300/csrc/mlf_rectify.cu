@@ -12,10 +12,13 @@
 // every output pixel of every output frame, averaging the selected input frames first (the
 // interpolation is linear, so this is the reference's mean-then-rectify).
 //
-// One launch covers all output frames: thread per output row of one column (coalesced along
-// the fast axis of the output, which maps to near-consecutive raw rows) and 8 output frames,
-// with all 32 neighbour loads of the 8 frames in flight before the interpolation.  The raw
-// data is read once from HBM; the four-neighbour reuse is served by L1/L2.  HBM-bound.
+// One launch covers all output frames.  Frame averaging (k_rectify): thread per output row
+// of one column (coalesced along the fast axis of the output, which maps to
+// near-consecutive raw rows) and 8 output frames, with all 32 neighbour loads of the 8
+// frames in flight before the interpolation.  One input frame per output frame
+// (k_rectify_staged): the raw tile of a block is staged in shared memory by 16-byte copies
+// and the next frame chunk is prefetched while the current one is interpolated.  The raw
+// data is read once from HBM.
 #include "mlf_internal.h"
 
 #include <algorithm>
