@@ -596,6 +596,9 @@ int solver_init(Solver* s) {
                                          " not in {3,5,...,17} (K0 up to 255 at N = 15)");
   s->Pa = round_up(s->Li, 4);
   s->plane = (int64_t)s->Lj * s->Pa;
+  // the view kernel indexes channels and per-channel tap blocks in 32 bits
+  if (s->nch * (int64_t)s->T * s->T >= (int64_t)INT32_MAX)
+    return fail(MLF_ERR_UNSUPPORTED, "too many depth planes for the view kernel's 32-bit channel indices");
   if (s->lite) return MLF_OK;  // batch member: geometry now, filter plan and scratch on first solve
   s->tilesA = ceil_div(s->Li, VW_TX);
   s->tilesB = ceil_div(s->Lj, VW_TY);

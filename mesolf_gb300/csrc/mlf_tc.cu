@@ -1191,7 +1191,8 @@ k_tc_bwdfwd(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUt
       }
     }
     if (!ok) {
-      if (lane == 0) atomicExch(a.b.err, TC_ERR_TIMEOUT_EPILOGUE);
+      // a wait of this warp gave up (or another role aborted first: keep its status)
+      if (lane == 0 && !aborted(&abort_flag)) atomicExch(a.b.err, TC_ERR_TIMEOUT_EPILOGUE);
       set_abort(&abort_flag);
     }
   } else if (warp == BWD_IO_WARP) {

@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kViewMaxThreads, 2) k_view(ViewArgs A) {
 
   constexpr bool DT = (MODE == MODE_STEP);  // the update needs D
   const int h = (A.N - 1) / 2;
-  // channel indices fit in 32 bits (N*N*Z <= 225 * 4096)
+  // channel indices and tap offsets (nch * T * T) fit in 32 bits: checked by the solver
   const int nch = (int)A.nch;
   const int step = (int)gridDim.x * A.slots;
   const int first = (int)blockIdx.x * A.slots + slot;
