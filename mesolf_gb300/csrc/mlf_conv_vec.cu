@@ -60,11 +60,17 @@ __device__ __forceinline__ void conv_rows_stage(const ConvRowsArgs& A, float* sm
                                                 int j0, int nJ, int cstart, int ky, int sel) {
   const int tid = threadIdx.x, nthr = blockDim.x;
   float* rb = rows0 + sel * rowbuf;
+  // element e = r_l * width + c, advanced by nthr per step without a division
+  int r_l = tid / A.width, c = tid - r_l * A.width;
   for (int e = tid; e < A.sy * A.width; e += nthr) {
-    const int r_l = e / A.width, c = e - r_l * A.width;
     const int r = b + CV_NN * (j0 + r_l) + ky - A.hk, col = cstart + c;
     const bool ok = (j0 + r_l) < nJ && r >= 0 && r < A.Hv && col >= 0 && col < A.Wv;
     cp_async4(rb + r_l * A.pitch + c, ok ? src + (int64_t)r * A.W + col : src, ok);
+    c += nthr;
+    while (c >= A.width) {
+      c -= A.width;
+      ++r_l;
+    }
   }
   float* tb = sm + sel * 16 * A.kwp;
   const float* krow = kb + (int64_t)A.kw * ky;
