@@ -45,6 +45,23 @@ def test_conv_vec_matches_oracle(cuda, W, H, n, kw):
     assert rel_l2(out, ref) <= 1e-5
 
 
+# The direct kernel's edges: two segment tiles along x (W > 480), one or two rows per row
+# phase (a thread's second row absent), one row or one column in all, even kernel widths
+# (the last row / column never read), and the widest kernel the MEX accepts.
+@pytest.mark.parametrize("W,H,n,kw", [(500, 16, 2, 9), (37, 1, 1, 5), (1, 29, 1, 3), (64, 47, 1, 2),
+                                      (120, 61, 1, 341)])
+def test_conv_vec_direct_edges_match_oracle(cuda, W, H, n, kw):
+    from mesolf_gb300 import mex_lfm_convolution_vec
+    rng = np.random.default_rng(W * 11 + H + kw)
+    bm = rng.random((W, H, n)).astype(np.float32)
+    K = rng.random((kw, kw, 15, 15)).astype(np.float32)
+    out = to_host(mex_lfm_convolution_vec(to_dev(bm), to_dev(K), method="direct"))
+    ref = R.lfm_conv_vec(bm, K)
+    assert out.shape == (W, H, n)
+    assert np.isfinite(out).all()
+    assert rel_l2(out, ref) <= 1e-5, rel_l2(out, ref)
+
+
 def test_conv_vec_2d_bitmap_and_host_arrays(cuda):
     from mesolf_gb300 import mex_lfm_convolution_vec
     rng = np.random.default_rng(11)
