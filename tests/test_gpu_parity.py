@@ -157,9 +157,9 @@ def test_view_step_matches_oracle(cuda, lenslets, K0, Z):
 # Patches with 128..160 output tiles run two channel slots per CTA (slots on warp
 # boundaries), more than 8 tile columns take the bank-spreading lane order, and the staged
 # planes use the swizzled column layout at a pitch of 4 mod 8 floats; 72 x 80 lenslets
-# (180 tiles) run one slot.
+# (180 tiles) run one slot; K0 255 gives the widest tap count, T = 17 (7 window chunks).
 @pytest.mark.parametrize("lenslets,K0,Z", [((64, 64), 61, 2), ((67, 61), 61, 2), ((61, 67), 91, 2),
-                                           ((72, 80), 61, 1)])
+                                           ((72, 80), 61, 1), ((64, 64), 255, 1)])
 def test_view_step_large_patches_match_oracle(cuda, lenslets, K0, Z):
     from mesolf_gb300 import PhaseSpacePSF, RLSolver
     w = synth.small_config(lenslets=lenslets, K0=K0, Z=Z)
